@@ -1,0 +1,173 @@
+"""Host-side mirror of the FV3 tracer-path interface, backed by libfv3g.so.
+
+The functions keep the Fortran names, argument order and meaning of
+``tracer_2d`` (fv_tracer2d.F90), ``fv_tp_2d`` (tp_core.F90) and
+``map_scalar`` / ``map1_ppm`` (fv_mapz.F90) of GFDL_atmos_cubed_sphere.
+Arrays are numpy float64 in C order with the Fortran shape reversed (a
+Fortran ``q(isd:ied, jsd:jed, npz, nq)`` is a numpy ``(nq, npz, njd, nid)``),
+so memory order is identical.  ``inout`` arguments are updated in place and a
+failing call raises ``Fv3gError`` (the Fortran shim maps it to FATAL).
+
+``CubeState`` is the batched, device-resident six-tile path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import DP, Bounds, Grid, StateDesc
+
+__all__ = ["Bounds", "GridStruct", "fv_tp_2d", "tracer_2d", "map_scalar", "map1_ppm", "map_scalar_3d", "CubeState",
+           "bounds_for"]
+
+
+def _p(a):
+    if a is None:
+        return None
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+        raise TypeError("arrays must be C-contiguous float64 numpy arrays")
+    return a.ctypes.data_as(DP)
+
+
+def bounds_for(n: int, ng: int = 3, is_: int = 1, ie: int | None = None, js: int = 1, je: int | None = None) -> Bounds:
+    ie = n if ie is None else ie
+    je = n if je is None else je
+    return Bounds(is_, ie, js, je, is_ - ng, ie + ng, js - ng, je + ng, ng)
+
+
+class GridStruct:
+    """fv3g_grid built from a tile geometry (keeps its arrays alive)."""
+
+    def __init__(self, geom, corners=(1, 1, 1, 1), nested: int = 0):
+        self.arrays = [np.ascontiguousarray(a, dtype=np.float64)
+                       for a in (geom.dx, geom.dy, geom.dxa, geom.dya, geom.area, geom.rarea, geom.sin_sg)]
+        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested)
+
+
+def fv_tp_2d(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, gridstruct: GridStruct, bd: Bounds, ra_x, ra_y,
+             lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+    _lib.call("fv3g_fv_tp_2d", _p(q), _p(crx), _p(cry), npx, npy, hord, _p(fx), _p(fy), _p(xfx), _p(yfx),
+              C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y), C.c_double(lim_fac), _p(mfx), _p(mfy),
+              nord, C.c_double(damp_c))
+
+
+def tracer_2d(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, npx, npy, npz, nq, hord, q_split, dt,
+              nord_tr=0, trdm=0.0, lim_fac=1.0, halo_update=None) -> int:
+    """Returns nsplt.  halo_update(q) (numpy view of q) refreshes halos per substep."""
+    shape = q.shape
+    cb = _lib.HALO_FN()
+    if halo_update is not None:
+        def _cb(ptr, nq_, npz_, ctx):
+            arr = np.ctypeslib.as_array(ptr, shape=shape)
+            halo_update(arr)
+        cb = _lib.HALO_FN(_cb)
+    nsplt = C.c_int(0)
+    _lib.call("fv3g_tracer_2d", _p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(gridstruct.struct),
+              C.byref(bd), npx, npy, npz, nq, hord, q_split, C.c_double(dt), nord_tr, C.c_double(trdm),
+              C.c_double(lim_fac), cb, None, C.byref(nsplt))
+    return nsplt.value
+
+
+def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min) -> None:
+    _lib.call("fv3g_map_scalar", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j, ibeg, iend, jbeg, jend,
+              iv, kord, C.c_double(q_min))
+
+
+def map1_ppm(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord) -> None:
+    _lib.call("fv3g_map1_ppm", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j, ibeg, iend, jbeg, jend,
+              iv, kord)
+
+
+def map_scalar_3d(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j1, j2, ibeg, iend, jbeg, jend, nq, iv, kord, q_min) -> None:
+    _lib.call("fv3g_map_scalar_3d", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j1, j2, ibeg, iend,
+              jbeg, jend, nq, iv, kord, C.c_double(q_min))
+
+
+class CubeState:
+    """Six tiles x npz levels x nq tracers resident in HBM (fv3g_state)."""
+
+    def __init__(self, n: int, npz: int, nq: int, *, precision: str = "fp64", hord: int = 8, kord: int = 9,
+                 iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0):
+        L = _lib.load()
+        self.n, self.npz, self.nq = n, npz, nq
+        self.nd = n + 6
+        self.precision = precision
+        prec = _lib.FV3G_FP64 if precision == "fp64" else _lib.FV3G_MIXED
+        desc = StateDesc(n, 6, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta)
+        self._h = C.c_void_p()
+        _lib.check(L.fv3g_state_create(C.byref(desc), C.byref(self._h)), "fv3g_state_create")
+        self._grids = []
+
+    def close(self):
+        if self._h:
+            _lib.load().fv3g_state_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------- setup
+    def set_grid(self, geoms) -> None:
+        for t, g in enumerate(geoms):
+            gs = GridStruct(g)
+            self._grids.append(gs)
+            _lib.call("fv3g_state_set_grid", self._h, t, C.byref(gs.struct))
+
+    def set_levels(self, ak, bk) -> None:
+        self._ak = np.ascontiguousarray(ak, dtype=np.float64)
+        self._bk = np.ascontiguousarray(bk, dtype=np.float64)
+        _lib.call("fv3g_state_set_levels", self._h, _p(self._ak), _p(self._bk))
+
+    def upload(self, field: str, host) -> None:
+        a = np.ascontiguousarray(host, dtype=np.float64)
+        _lib.call("fv3g_upload", self._h, _lib.FIELDS[field], _p(a))
+
+    def download(self, field: str) -> np.ndarray:
+        out = np.empty(self.field_shape(field), dtype=np.float64)
+        _lib.call("fv3g_download", self._h, _lib.FIELDS[field], _p(out))
+        return out
+
+    def upload_device(self, field: str, dptr: int, stream=None) -> None:
+        _lib.call("fv3g_upload_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), C.c_void_p(stream or 0))
+
+    def download_device(self, field: str, dptr: int, stream=None) -> None:
+        _lib.call("fv3g_download_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), C.c_void_p(stream or 0))
+
+    def field_shape(self, field: str) -> tuple:
+        n, nd, npz, nq = self.n, self.nd, self.npz, self.nq
+        return {"Q": (6, nq, npz, nd, nd), "Q_REMAPPED": (6, nq, npz, nd, nd), "DELP": (6, npz, nd, nd),
+                "DELP_OUT": (6, npz, nd, nd), "CX": (6, npz, nd, n + 1), "CY": (6, npz, n + 1, nd),
+                "MFX": (6, npz, n, n + 1), "MFY": (6, npz, n + 1, n)}[field]
+
+    def load_problem(self, prob) -> None:
+        """Upload a synth.Problem (grid, levels and every input field)."""
+        self.set_grid(prob.geoms)
+        self.set_levels(prob.ak, prob.bk)
+        for name, val in (("Q", prob.q), ("DELP", prob.dp), ("CX", prob.cx), ("CY", prob.cy), ("MFX", prob.mfx),
+                          ("MFY", prob.mfy)):
+            self.upload(name, val.detach().cpu().numpy() if hasattr(val, "detach") else val)
+
+    # ------------------------------------------------------------ compute
+    def tracer_2d(self, q_split: int, stream=None) -> None:
+        _lib.call("fv3g_tracer_2d_batched", self._h, q_split, C.c_void_p(stream or 0))
+
+    def remap(self, stream=None) -> None:
+        _lib.call("fv3g_remap_batched", self._h, C.c_void_p(stream or 0))
+
+    def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
+        _lib.call("fv3g_step", self._h, q_split, int(use_graph), C.c_void_p(stream or 0))
+
+    def mass(self, field: str = "Q", stream=None) -> np.ndarray:
+        out = np.zeros(self.nq, dtype=np.float64)
+        _lib.call("fv3g_mass_sum", self._h, _lib.FIELDS[field], _p(out), C.c_void_p(stream or 0))
+        return out
+
+    def error_code(self) -> int:
+        code = C.c_int(0)
+        _lib.call("fv3g_state_error", self._h, C.byref(code))
+        return code.value

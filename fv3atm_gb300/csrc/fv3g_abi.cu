@@ -1,0 +1,658 @@
+// fv3g_abi.cu -- the extern "C" boundary declared in include/fv3g.h.
+//
+// Exact-shape entries take the caller's HOST arrays in Fortran order with
+// explicit bounds (drop-in for tracer_2d / fv_tp_2d / map_scalar / map1_ppm
+// of GFDL_atmos_cubed_sphere, called in fv3atm from atmosphere_dynamics,
+// atmos_model.F90:879), copy them into the device plane layout, run the same
+// kernels as the batched path, and copy the results back.  Batched entries
+// keep all six tiles and all tracers resident in HBM inside an opaque state.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "fv3g_internal.cuh"
+#include "fv3g_mass.cuh"
+#include "fv3g_remap.cuh"
+
+namespace fv3g {
+
+// --------------------------------------------------------------- errors ---
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  set_error(FV3G_E_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+  return e == cudaErrorMemoryAllocation ? FV3G_E_NOMEM : FV3G_E_CUDA;
+}
+
+#define CHECK(expr)            \
+  do {                         \
+    int rc__ = (expr);         \
+    if (rc__ != 0) return rc__; \
+  } while (0)
+
+// ----------------------------------------------------- small kernels -------
+// Scatter/convert stacked host-order planes (ni x nj each, contiguous) into
+// device planes with an (i, j) offset; FP64 source, T destination.
+template <typename T>
+__global__ void k_to_planes(const double* src, T* dst, int ni, int nj, long long nplanes, int pitch,
+                            long long dplane, int ioff, int joff, long long sstride) {
+  const long long tot = (long long)ni * nj * nplanes;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % ni);
+    const long long r = e / ni;
+    const int j = (int)(r % nj);
+    const long long p = r / nj;
+    dst[p * dplane + (long long)(j + joff) * pitch + (i + ioff)] = (T)src[p * sstride + (long long)j * ni + i];
+  }
+}
+
+template <typename T>
+__global__ void k_from_planes(const T* src, double* dst, int ni, int nj, long long nplanes, int pitch,
+                              long long splane, int ioff, int joff, long long dstride) {
+  const long long tot = (long long)ni * nj * nplanes;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % ni);
+    const long long r = e / ni;
+    const int j = (int)(r % nj);
+    const long long p = r / nj;
+    dst[p * dstride + (long long)j * ni + i] = (double)src[p * splane + (long long)(j + joff) * pitch + (i + ioff)];
+  }
+}
+
+template <typename T>
+__global__ void k_scale(T* x, long long n, T f) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    x[e] *= f;
+}
+
+template <typename T>
+__global__ void k_copy_corners(T* q, PlaneGeom pg, int npx, int npy, int corners, int dir, long long nplanes,
+                               long long plane) {
+  // 4 corners x 9 cells per plane, rotation of the strip beside the corner
+  const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nplanes * 36) return;
+  const long long p = id / 36;
+  const int c = (int)(id % 36) / 9, a = (int)(id % 9) / 3 + 1, b = (int)(id % 3) + 1;
+  if (!(corners & (1 << c))) return;
+  const int su = (c & 1) ? 1 : -1, sv = (c & 2) ? 1 : -1;
+  const int cx2 = su < 0 ? 1 : 2 * npx - 1, cy2 = sv < 0 ? 1 : 2 * npy - 1;
+  const int U = su * (2 * a - 1), V = sv * (2 * b - 1);
+  const bool plus = (dir == 1) ? (su == -sv) : (su == sv);
+  const int U2 = plus ? -V : V, V2 = plus ? U : -U;
+  const int i = (U + cx2) / 2, j = (V + cy2) / 2, is = (U2 + cx2) / 2, js = (V2 + cy2) / 2;
+  q[p * plane + pg.at(i, j)] = q[p * plane + pg.at(is, js)];
+}
+
+static unsigned grid_for(long long n, int block = 256) {
+  long long g = (n + block - 1) / block;
+  return (unsigned)std::max<long long>(1, std::min<long long>(g, 152LL * 16));
+}
+
+}  // namespace fv3g
+
+using namespace fv3g;
+
+// ================================================================ state ====
+struct fv3g_state {
+  fv3g_state_desc d{};
+  bool fp64 = true;
+  int n = 0, nd = 0, npz = 0, nq = 0;
+  PlaneGeom pg{};
+  long long plane = 0;
+  size_t esz = 8;
+  void* q[3] = {nullptr, nullptr, nullptr};  // home, work B, work C
+  void* dp[3] = {nullptr, nullptr, nullptr};  // home (call start), work B, work C
+  void* cx = nullptr; void* cy = nullptr; void* mfx = nullptr; void* mfy = nullptr;  // inputs (unscaled)
+  void* cxs = nullptr; void* cys = nullptr; void* mfxs = nullptr; void* mfys = nullptr;  // scaled copies
+  void* xfx = nullptr; void* yfx = nullptr;
+  void* dp_eul = nullptr;
+  void* area = nullptr; void* rarea = nullptr; void* dxa = nullptr; void* dya = nullptr;
+  void* dx = nullptr; void* dy = nullptr; void* sin4 = nullptr;
+  void* eflux = nullptr;
+  double* ak = nullptr; double* bk = nullptr;
+  void* rscratch = nullptr; unsigned char* sched = nullptr;
+  double* partials = nullptr; double* mass_out = nullptr;
+  unsigned int* cmax = nullptr;
+  int* err = nullptr;
+  double* stage = nullptr; size_t stage_bytes = 0;  // FP64 staging for uploads
+  cudaStream_t stream = nullptr;
+  int q_cur = 0;      // buffer holding the latest tracer field
+  int dp_start = 0;   // buffer holding dp at the start of the last substep
+  int dp_end = 0;     // buffer holding dp at the end of the last substep
+  bool remapped = false;  // q[0] holds a remapped field (thickness dp_eul)
+  bool levels_set = false;
+  cudaGraphExec_t gexec = nullptr;
+  int g_qsplit = -1;
+  Topo topo{};
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int dalloc(fv3g_state* st, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMalloc");
+  st->allocs.push_back(*p);
+  e = cudaMemsetAsync(*p, 0, bytes, st->stream);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+  return 0;
+}
+
+// Six-tile topology of the face convention used by the grid generator
+// (fv3atm_gb300/grid.py): faces (centre, i axis, j axis).
+void build_topo(Topo& tp) {
+  const int F[6][3][3] = {{{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},  {{0, 1, 0}, {-1, 0, 0}, {0, 0, 1}},
+                          {{-1, 0, 0}, {0, -1, 0}, {0, 0, 1}}, {{0, -1, 0}, {1, 0, 0}, {0, 0, 1}},
+                          {{0, 0, 1}, {0, 1, 0}, {-1, 0, 0}},  {{0, 0, -1}, {0, 1, 0}, {1, 0, 0}}};
+  const int ends[4][2][2] = {{{-1, -1}, {-1, 1}}, {{1, -1}, {1, 1}}, {{-1, -1}, {1, -1}}, {{-1, 1}, {1, 1}}};
+  auto pt = [&](int f, int sx, int sy, int* o) {
+    for (int c = 0; c < 3; ++c) o[c] = F[f][0][c] + sx * F[f][1][c] + sy * F[f][2][c];
+  };
+  for (int t = 0; t < 6; ++t)
+    for (int e = 0; e < 4; ++e) {
+      int p0[3], p1[3];
+      pt(t, ends[e][0][0], ends[e][0][1], p0);
+      pt(t, ends[e][1][0], ends[e][1][1], p1);
+      for (int u = 0; u < 6; ++u) {
+        if (u == t) continue;
+        for (int f = 0; f < 4; ++f) {
+          int q0[3], q1[3];
+          pt(u, ends[f][0][0], ends[f][0][1], q0);
+          pt(u, ends[f][1][0], ends[f][1][1], q1);
+          const bool same = !memcmp(q0, p0, sizeof p0) && !memcmp(q1, p1, sizeof p1);
+          const bool flip = !memcmp(q0, p1, sizeof p0) && !memcmp(q1, p0, sizeof p1);
+          if (same || flip) {
+            tp.nbr[t][e] = (signed char)u;
+            tp.nedge[t][e] = (signed char)f;
+            tp.rev[t][e] = flip ? 1 : 0;
+          }
+        }
+      }
+    }
+}
+
+template <typename T>
+AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
+  AdvArgs<T> a{};
+  a.q_in = (const T*)st->q[src];
+  a.q_out = (T*)st->q[dst];
+  a.sQk = st->plane;
+  a.sQq = st->plane * st->npz;
+  a.sQt = a.sQq * st->nq;
+  a.cx = (const T*)st->cxs;
+  a.cy = (const T*)st->cys;
+  a.xfx = (const T*)st->xfx;
+  a.yfx = (const T*)st->yfx;
+  a.mfx = (const T*)st->mfxs;
+  a.mfy = (const T*)st->mfys;
+  a.dp1 = (const T*)st->dp[dp_in];
+  a.dp2 = (T*)st->dp[dp_out];
+  a.sFk = st->plane;
+  a.sFt = st->plane * st->npz;
+  a.area = (const T*)st->area;
+  a.rarea = (const T*)st->rarea;
+  a.dxa = (const T*)st->dxa;
+  a.dya = (const T*)st->dya;
+  a.sMt = st->plane;
+  a.pg = st->pg;
+  a.is = 1; a.ie = st->n; a.js = 1; a.je = st->n;
+  a.npx = st->n + 1; a.npy = st->n + 1;
+  a.nq = st->nq;
+  a.npz = st->npz;
+  a.corners = 15;
+  a.nested = 0;
+  a.cube = 1;
+  a.topo = st->topo;
+  a.eflux = (T*)st->eflux;
+  return a;
+}
+
+// Shape of a field in the host (Fortran) layout: (nplanes, nj, ni) and the
+// (i, j) offset of its first element in the device plane.
+struct FieldShape {
+  long long nplanes;
+  int ni, nj, ioff, joff;
+  void* dev;
+};
+
+int field_shape(fv3g_state* st, int field, FieldShape& fs, bool for_upload) {
+  const int n = st->n, nd = st->nd;
+  const long long t = 6;
+  switch (field) {
+    case FV3G_FIELD_Q:
+      fs = {t * st->nq * st->npz, nd, nd, 0, 0, for_upload ? st->q[0] : st->q[st->q_cur]};
+      return 0;
+    case FV3G_FIELD_Q_REMAPPED:
+      fs = {t * st->nq * st->npz, nd, nd, 0, 0, st->q[0]};
+      return 0;
+    case FV3G_FIELD_DELP: fs = {t * st->npz, nd, nd, 0, 0, st->dp[0]}; return 0;
+    case FV3G_FIELD_DELP_OUT: fs = {t * st->npz, nd, nd, 0, 0, st->dp[st->dp_end]}; return 0;
+    case FV3G_FIELD_CX: fs = {t * st->npz, n + 1, nd, NG, 0, st->cx}; return 0;
+    case FV3G_FIELD_CY: fs = {t * st->npz, nd, n + 1, 0, NG, st->cy}; return 0;
+    case FV3G_FIELD_MFX: fs = {t * st->npz, n + 1, n, NG, NG, st->mfx}; return 0;
+    case FV3G_FIELD_MFY: fs = {t * st->npz, n, n + 1, NG, NG, st->mfy}; return 0;
+    default: return set_error(FV3G_E_ARG, "unknown field %d", field);
+  }
+}
+
+int ensure_stage(fv3g_state* st, size_t bytes) {
+  if (st->stage_bytes >= bytes) return 0;
+  if (st->stage) cudaFree(st->stage);
+  st->stage = nullptr;
+  st->stage_bytes = 0;
+  FV3G_CUDA(cudaMalloc((void**)&st->stage, bytes));
+  st->stage_bytes = bytes;
+  return 0;
+}
+
+template <typename T>
+int upload_t(fv3g_state* st, const FieldShape& fs, const double* host, cudaStream_t s) {
+  const size_t bytes = (size_t)fs.nplanes * fs.ni * fs.nj * sizeof(double);
+  CHECK(ensure_stage(st, bytes));
+  FV3G_CUDA(cudaMemcpyAsync(st->stage, host, bytes, cudaMemcpyHostToDevice, s));
+  k_to_planes<T><<<grid_for((long long)fs.nplanes * fs.ni * fs.nj), 256, 0, s>>>(
+      st->stage, (T*)fs.dev, fs.ni, fs.nj, fs.nplanes, st->pg.pitch, st->plane, fs.ioff, fs.joff,
+      (long long)fs.ni * fs.nj);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <typename T>
+int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t s) {
+  const size_t bytes = (size_t)fs.nplanes * fs.ni * fs.nj * sizeof(double);
+  CHECK(ensure_stage(st, bytes));
+  k_from_planes<T><<<grid_for((long long)fs.nplanes * fs.ni * fs.nj), 256, 0, s>>>(
+      (const T*)fs.dev, st->stage, fs.ni, fs.nj, fs.nplanes, st->pg.pitch, st->plane, fs.ioff, fs.joff,
+      (long long)fs.ni * fs.nj);
+  FV3G_CUDA(cudaGetLastError());
+  FV3G_CUDA(cudaMemcpyAsync(host, st->stage, bytes, cudaMemcpyDeviceToHost, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+template <typename T>
+int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
+  const long long fsz = st->plane * st->npz * 6;
+  const size_t fb = (size_t)fsz * sizeof(T);
+  // scaled work copies and area fluxes
+  FV3G_CUDA(cudaMemcpyAsync(st->cxs, st->cx, fb, cudaMemcpyDeviceToDevice, s));
+  FV3G_CUDA(cudaMemcpyAsync(st->cys, st->cy, fb, cudaMemcpyDeviceToDevice, s));
+  FV3G_CUDA(cudaMemcpyAsync(st->mfxs, st->mfx, fb, cudaMemcpyDeviceToDevice, s));
+  FV3G_CUDA(cudaMemcpyAsync(st->mfys, st->mfy, fb, cudaMemcpyDeviceToDevice, s));
+  const T frac = (nsplt == 1) ? T(1) : T(1.0 / nsplt);
+  CHECK(launch_area_flux<T>((T*)st->cxs, (T*)st->cys, (T*)st->xfx, (T*)st->yfx, (T*)st->mfxs, (T*)st->mfys,
+                            (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
+                            (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
+                            st->n, 1, st->n, 6, st->npz, frac, s));
+  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 4);
+  int src = 0, dpi = 0;
+  for (int it = 0; it < nsplt; ++it) {
+    const int dst = (src == 1) ? 2 : 1;
+    const int dpo = (dpi == 1) ? 2 : 1;
+    AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
+    CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
+    CHECK(launch_edge_fix<T>(a, st->n, s));
+    st->dp_start = dpi;
+    src = dst;
+    dpi = dpo;
+  }
+  st->q_cur = src;
+  st->dp_end = dpi;
+  return 0;
+}
+
+template <typename T>
+int remap_t(fv3g_state* st, cudaStream_t s) {
+  if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  RemapArgs<T> r{};
+  r.q_in = (const T*)st->q[st->q_cur];
+  r.q_out = (T*)st->q[0];
+  if (st->q_cur == 0) return set_error(FV3G_E_ARG, "remap needs an advected field (run tracer_2d first)");
+  r.sQk = st->plane;
+  r.sQq = st->plane * st->npz;
+  r.sQt = r.sQq * st->nq;
+  r.sQqo = r.sQq;
+  r.nfield = st->nq;
+  r.dp = (const T*)st->dp[st->dp_end];
+  r.dp_out = (T*)st->dp_eul;
+  r.sFk = st->plane;
+  r.sFt = st->plane * st->npz;
+  r.ak = st->ak;
+  r.bk = st->bk;
+  r.pg = st->pg;
+  r.i1 = 1; r.j1 = 1; r.ni = st->n; r.nj = st->n;
+  r.ncol = 6LL * st->n * st->n;
+  r.km = st->npz; r.kn = st->npz;
+  r.iv = st->d.iv;
+  r.q_min = st->d.q_min;
+  r.scratch = (T*)st->rscratch;
+  r.sched = st->sched;
+  CHECK(launch_remap<T>(r, st->d.kord, s));
+  st->q_cur = 0;
+  st->remapped = true;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fv3g_version(void) { return 100; }
+
+int fv3g_last_error(char* buf, int len) {
+  if (!buf || len <= 0) return FV3G_E_ARG;
+  snprintf(buf, (size_t)len, "%s", g_last_error);
+  return 0;
+}
+
+int fv3g_device_info(char* buf, int len) {
+  int dev = 0;
+  cudaDeviceProp p;
+  FV3G_CUDA(cudaGetDevice(&dev));
+  FV3G_CUDA(cudaGetDeviceProperties(&p, dev));
+  if (buf && len > 0) snprintf(buf, (size_t)len, "%s sm_%d%d SMs=%d", p.name, p.major, p.minor, p.multiProcessorCount);
+  return 0;
+}
+
+int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
+  if (!desc || !out) return set_error(FV3G_E_ARG, "null argument");
+  *out = nullptr;
+  const fv3g_state_desc& d = *desc;
+  if (d.ntiles != 6) return set_error(FV3G_E_UNSUPPORTED, "batched state supports the six-tile cube (ntiles=6)");
+  if (d.n < 12 || d.npz < 2 || d.npz > KMAX || d.nq < 1)
+    return set_error(FV3G_E_ARG, "bad sizes n=%d npz=%d nq=%d (n>=12, 2<=npz<=%d, nq>=1)", d.n, d.npz, d.nq, KMAX);
+  if (d.precision != FV3G_FP64 && d.precision != FV3G_MIXED) return set_error(FV3G_E_ARG, "bad precision %d", d.precision);
+  if (d.hord != 5 && d.hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented", d.hord);
+  if (d.kord != 4 && d.kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented", d.kord);
+  if (d.iv < -2 || d.iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", d.iv);
+  fv3g_state* st = new (std::nothrow) fv3g_state();
+  if (!st) return set_error(FV3G_E_NOMEM, "host allocation failed");
+  st->d = d;
+  st->fp64 = d.precision == FV3G_FP64;
+  st->esz = st->fp64 ? 8 : 4;
+  st->n = d.n;
+  st->nd = d.n + 2 * NG;
+  st->npz = d.npz;
+  st->nq = d.nq;
+  st->pg.pitch = ((st->nd + 1 + 7) / 8) * 8;
+  st->pg.rows = st->nd + 1;
+  st->pg.isd = 1 - NG;
+  st->pg.jsd = 1 - NG;
+  st->plane = st->pg.plane();
+  build_topo(st->topo);
+  {
+    int prc = prepare_kernels();
+    if (prc) {
+      delete st;
+      return prc;
+    }
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete st;
+    return cuda_error(e, "cudaStreamCreate");
+  }
+  const size_t P = (size_t)st->plane * st->esz;
+  const size_t qb = P * 6 * d.nq * d.npz, fb = P * 6 * d.npz;
+  int rc = 0;
+  for (int b = 0; b < 3 && !rc; ++b) rc = dalloc(st, &st->q[b], qb);
+  for (int b = 0; b < 3 && !rc; ++b) rc = dalloc(st, &st->dp[b], fb);
+  void** fields[] = {&st->cx, &st->cy, &st->mfx, &st->mfy, &st->cxs, &st->cys, &st->mfxs, &st->mfys,
+                     &st->xfx, &st->yfx, &st->dp_eul};
+  for (void** f : fields)
+    if (!rc) rc = dalloc(st, f, fb);
+  void** metrics[] = {&st->area, &st->rarea, &st->dxa, &st->dya, &st->dx, &st->dy};
+  for (void** m : metrics)
+    if (!rc) rc = dalloc(st, m, P * 6);
+  if (!rc) rc = dalloc(st, &st->sin4, P * 6 * 4);
+  if (!rc) rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
+  if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
+  if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
+  const long long ncol = 6LL * d.n * d.n;
+  if (!rc) rc = dalloc(st, &st->rscratch, (size_t)ncol * (KMAX + 1) * 6 * st->esz);
+  if (!rc) rc = dalloc(st, (void**)&st->sched, (size_t)ncol * (KMAX + 1));
+  if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);
+  if (!rc) rc = dalloc(st, (void**)&st->mass_out, sizeof(double) * d.nq);
+  if (!rc) rc = dalloc(st, (void**)&st->cmax, sizeof(unsigned));
+  if (!rc) rc = dalloc(st, (void**)&st->err, sizeof(int));
+  if (!rc) {
+    e = cudaStreamSynchronize(st->stream);
+    if (e != cudaSuccess) rc = cuda_error(e, "cudaStreamSynchronize");
+  }
+  if (rc) {
+    fv3g_state_destroy(st);
+    return rc;
+  }
+  *out = st;
+  return 0;
+}
+
+int fv3g_state_destroy(fv3g_state* st) {
+  if (!st) return 0;
+  if (st->stream) cudaStreamSynchronize(st->stream);
+  if (st->gexec) cudaGraphExecDestroy(st->gexec);
+  for (void* p : st->allocs) cudaFree(p);
+  if (st->stage) cudaFree(st->stage);
+  if (st->stream) cudaStreamDestroy(st->stream);
+  delete st;
+  return 0;
+}
+
+int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* g) {
+  if (!st || !g || tile < 0 || tile > 5) return set_error(FV3G_E_ARG, "bad state/grid/tile");
+  const int nd = st->nd;
+  struct M { const double* src; void* dst; int ni, nj; long long off; };
+  const size_t P = (size_t)st->plane;
+  auto at = [&](void* base, long long plane_index) { return (char*)base + plane_index * P * st->esz; };
+  M ms[] = {{g->dx, at(st->dx, tile), nd, nd + 1, 0},    {g->dy, at(st->dy, tile), nd + 1, nd, 0},
+            {g->dxa, at(st->dxa, tile), nd, nd, 0},      {g->dya, at(st->dya, tile), nd, nd, 0},
+            {g->area, at(st->area, tile), nd, nd, 0},    {g->rarea, at(st->rarea, tile), nd, nd, 0}};
+  for (const M& m : ms) {
+    if (!m.src) return set_error(FV3G_E_ARG, "null metric pointer");
+    FieldShape fs{1, m.ni, m.nj, 0, 0, m.dst};
+    int rc = st->fp64 ? upload_t<double>(st, fs, m.src, st->stream) : upload_t<float>(st, fs, m.src, st->stream);
+    if (rc) return rc;
+  }
+  if (!g->sin_sg) return set_error(FV3G_E_ARG, "null sin_sg");
+  for (int sl = 0; sl < 4; ++sl) {
+    FieldShape fs{1, nd, nd, 0, 0, at(st->sin4, (long long)tile * 4 + sl)};
+    const double* src = g->sin_sg + (size_t)sl * nd * nd;
+    int rc = st->fp64 ? upload_t<double>(st, fs, src, st->stream) : upload_t<float>(st, fs, src, st->stream);
+    if (rc) return rc;
+  }
+  FV3G_CUDA(cudaStreamSynchronize(st->stream));
+  return 0;
+}
+
+int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk) {
+  if (!st || !ak || !bk) return set_error(FV3G_E_ARG, "null argument");
+  FV3G_CUDA(cudaMemcpyAsync(st->ak, ak, sizeof(double) * (st->npz + 1), cudaMemcpyHostToDevice, st->stream));
+  FV3G_CUDA(cudaMemcpyAsync(st->bk, bk, sizeof(double) * (st->npz + 1), cudaMemcpyHostToDevice, st->stream));
+  FV3G_CUDA(cudaStreamSynchronize(st->stream));
+  st->levels_set = true;
+  return 0;
+}
+
+int fv3g_upload(fv3g_state* st, int field, const double* host) {
+  if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, true));
+  if (field == FV3G_FIELD_Q_REMAPPED || field == FV3G_FIELD_DELP_OUT)
+    return set_error(FV3G_E_ARG, "field %d is an output", field);
+  int rc = st->fp64 ? upload_t<double>(st, fs, host, st->stream) : upload_t<float>(st, fs, host, st->stream);
+  if (rc) return rc;
+  if (field == FV3G_FIELD_Q) {
+    st->q_cur = 0;
+    st->remapped = false;
+  }
+  FV3G_CUDA(cudaStreamSynchronize(st->stream));
+  return 0;
+}
+
+int fv3g_download(fv3g_state* st, int field, double* host) {
+  if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, false));
+  return st->fp64 ? download_t<double>(st, fs, host, st->stream) : download_t<float>(st, fs, host, st->stream);
+}
+
+int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream) {
+  if (!st || !dptr) return set_error(FV3G_E_ARG, "null argument");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, true));
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  const size_t es = st->esz;
+  {
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)dptr, fs.ni * es, fs.ni, fs.nj);
+    p.dstPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
+                                   st->pg.pitch, st->pg.rows);
+    p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
+    p.kind = cudaMemcpyDeviceToDevice;
+    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  }
+  if (field == FV3G_FIELD_Q) {
+    st->q_cur = 0;
+    st->remapped = false;
+  }
+  return 0;
+}
+
+int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream) {
+  if (!st || !dptr) return set_error(FV3G_E_ARG, "null argument");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, false));
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  const size_t es = st->esz;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
+                                 st->pg.pitch, st->pg.rows);
+  p.dstPtr = make_cudaPitchedPtr(dptr, fs.ni * es, fs.ni, fs.nj);
+  p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
+  p.kind = cudaMemcpyDeviceToDevice;
+  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  return 0;
+}
+
+int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, false));
+  if (dptr) *dptr = fs.dev;
+  if (pitch) *pitch = st->pg.pitch;
+  if (strides4) {
+    strides4[0] = st->plane;  // level / plane stride
+    strides4[1] = st->plane * st->npz;  // tracer (q) or tile (per-level fields)
+    strides4[2] = st->plane * st->npz * st->nq;  // tile stride of q
+    strides4[3] = st->pg.rows;
+  }
+  return 0;
+}
+
+int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (q_split < 1 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 1..64 on the batched path");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  return st->fp64 ? tracer_2d_t<double>(st, q_split, s) : tracer_2d_t<float>(st, q_split, s);
+}
+
+int fv3g_remap_batched(fv3g_state* st, void* stream) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  return st->fp64 ? remap_t<double>(st, s) : remap_t<float>(st, s);
+}
+
+int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  if (!use_graph) {
+    CHECK(fv3g_tracer_2d_batched(st, q_split, s));
+    return fv3g_remap_batched(st, s);
+  }
+  if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  if (st->gexec == nullptr || st->g_qsplit != q_split) {
+    if (st->gexec) {
+      cudaGraphExecDestroy(st->gexec);
+      st->gexec = nullptr;
+    }
+    cudaStream_t cs;
+    FV3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    FV3G_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    int rc = fv3g_tracer_2d_batched(st, q_split, cs);
+    if (!rc) rc = fv3g_remap_batched(st, cs);
+    cudaError_t e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&st->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphInstantiate");
+    st->g_qsplit = q_split;
+  }
+  FV3G_CUDA(cudaGraphLaunch(st->gexec, s));
+  st->q_cur = 0;
+  st->remapped = true;
+  return 0;
+}
+
+int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream) {
+  if (!st || !host_out) return set_error(FV3G_E_ARG, "null argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  const void* qf;
+  const void* dpf;
+  if (which == FV3G_FIELD_Q) {
+    qf = st->q[st->q_cur];
+    dpf = (st->q_cur != 0) ? st->dp[st->dp_end] : (st->remapped ? st->dp_eul : st->dp[0]);
+  }
+  else if (which == FV3G_FIELD_Q_REMAPPED) { qf = st->q[0]; dpf = st->dp_eul; }
+  else return set_error(FV3G_E_ARG, "mass sum of field %d is not defined", which);
+  auto run = [&](auto tag) -> int {
+    using T = decltype(tag);
+    MassArgs<T> m{};
+    m.q = (const T*)qf;
+    m.sQk = st->plane;
+    m.sQq = st->plane * st->npz;
+    m.sQt = m.sQq * st->nq;
+    m.dp = (const T*)dpf;
+    m.sFk = st->plane;
+    m.sFt = st->plane * st->npz;
+    m.area = (const T*)st->area;
+    m.sMt = st->plane;
+    m.pg = st->pg;
+    m.i1 = 1; m.j1 = 1; m.ni = st->n; m.nj = st->n;
+    m.npz = st->npz;
+    m.ntiles = 6;
+    m.partials = st->partials;
+    return launch_mass<T>(m, st->nq, st->mass_out, s);
+  };
+  int rc = st->fp64 ? run(double{}) : run(float{});
+  if (rc) return rc;
+  FV3G_CUDA(cudaMemcpyAsync(host_out, st->mass_out, sizeof(double) * st->nq, cudaMemcpyDeviceToHost, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int fv3g_state_error(fv3g_state* st, int* code) {
+  if (!st || !code) return set_error(FV3G_E_ARG, "null argument");
+  FV3G_CUDA(cudaMemcpy(code, st->err, sizeof(int), cudaMemcpyDeviceToHost));
+  FV3G_CUDA(cudaMemset(st->err, 0, sizeof(int)));
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,439 @@
+// fv3g_dropin.cu -- exact-shape (host-array) entries: fv3g_fv_tp_2d,
+// fv3g_tracer_2d, fv3g_map_scalar, fv3g_map1_ppm, fv3g_map_scalar_3d.
+//
+// Each entry keeps the upstream Fortran argument list (fv_tp_2d / tracer_2d
+// of tp_core.F90 / fv_tracer2d.F90, map_scalar / map1_ppm of fv_mapz.F90 in
+// GFDL_atmos_cubed_sphere) with the array bounds passed explicitly, copies the
+// caller's column-major host arrays into a device plane layout with one
+// cudaMemcpy2D/3D per array, runs the batched kernels on that one domain and
+// copies the results back.  Work buffers and the stream are per calling host
+// thread, so the row-wise remap entries may be called from OpenMP threads.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fv3g_internal.cuh"
+#include "fv3g_remap.cuh"
+
+using namespace fv3g;
+
+namespace {
+
+#define CHECK(expr)             \
+  do {                          \
+    int rc__ = (expr);          \
+    if (rc__ != 0) return rc__; \
+  } while (0)
+
+// Per-thread stream and a grow-only device arena, released at thread exit.
+struct ThreadCtx {
+  cudaStream_t stream = nullptr;
+  char* arena = nullptr;
+  size_t cap = 0, used = 0;
+  ~ThreadCtx() {
+    if (arena) cudaFree(arena);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  int begin(size_t bytes) {
+    if (!stream) FV3G_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    bytes += 64 * 256;
+    if (cap < bytes) {
+      if (arena) cudaFree(arena);
+      arena = nullptr;
+      cap = 0;
+      FV3G_CUDA(cudaMalloc((void**)&arena, bytes));
+      cap = bytes;
+    }
+    used = 0;
+    return 0;
+  }
+  template <typename T>
+  T* take(size_t count) {
+    T* p = (T*)(arena + used);
+    used += ((count * sizeof(T) + 255) / 256) * 256;
+    return p;
+  }
+};
+thread_local ThreadCtx g_ctx;
+
+size_t padded(size_t count, size_t es) { return ((count * es + 255) / 256) * 256; }
+
+// Copy a host Fortran array with bounds (ilo:ihi, jlo:jhi, nplanes) into
+// device planes of geometry pg (which must contain those bounds).
+int h2d_planes(double* dev, const PlaneGeom& pg, const double* host, int ilo, int ihi, int jlo, int jhi,
+               long long nplanes, cudaStream_t s) {
+  const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((void*)host, (size_t)ni * 8, ni, nj);
+  p.dstPtr = make_cudaPitchedPtr(dev + pg.at(ilo, jlo), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
+  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
+  p.kind = cudaMemcpyHostToDevice;
+  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  return 0;
+}
+
+int d2h_planes(double* host, const double* dev, const PlaneGeom& pg, int ilo, int ihi, int jlo, int jhi,
+               long long nplanes, cudaStream_t s) {
+  const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((void*)(dev + pg.at(ilo, jlo)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
+  p.dstPtr = make_cudaPitchedPtr(host, (size_t)ni * 8, ni, nj);
+  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
+  p.kind = cudaMemcpyDeviceToHost;
+  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  return 0;
+}
+
+int d2d_planes(double* dst, const double* src, const PlaneGeom& pg, int ilo, int ihi, int jlo, int jhi,
+               long long nplanes, cudaStream_t s) {
+  const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((void*)(src + pg.at(ilo, jlo)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
+  p.dstPtr = make_cudaPitchedPtr(dst + pg.at(ilo, jlo), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
+  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
+  p.kind = cudaMemcpyDeviceToDevice;
+  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  return 0;
+}
+
+__global__ void k_corners(double* q, PlaneGeom pg, int npx, int npy, int corners, int dir, long long nplanes) {
+  const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nplanes * 36) return;
+  const long long p = id / 36;
+  const int c = (int)(id % 36) / 9, a = (int)(id % 9) / 3 + 1, b = (int)(id % 3) + 1;
+  if (!(corners & (1 << c))) return;
+  const int su = (c & 1) ? 1 : -1, sv = (c & 2) ? 1 : -1;
+  const int cx2 = su < 0 ? 1 : 2 * npx - 1, cy2 = sv < 0 ? 1 : 2 * npy - 1;
+  const int U = su * (2 * a - 1), V = sv * (2 * b - 1);
+  const bool plus = (dir == 1) ? (su == -sv) : (su == sv);
+  const int U2 = plus ? -V : V, V2 = plus ? U : -U;
+  const int i = (U + cx2) / 2, j = (V + cy2) / 2, is = (U2 + cx2) / 2, js = (V2 + cy2) / 2;
+  if (i < pg.isd || j < pg.jsd || is < pg.isd || js < pg.jsd || i >= pg.isd + pg.pitch || is >= pg.isd + pg.pitch ||
+      j >= pg.jsd + pg.rows || js >= pg.jsd + pg.rows)
+    return;
+  q[p * pg.plane() + pg.at(i, j)] = q[p * pg.plane() + pg.at(is, js)];
+}
+
+__global__ void k_max_abs2(const double* cx, const double* cy, PlaneGeom pg, int is, int ie, int js, int je, int npz,
+                           unsigned long long* out) {
+  const long long per = (long long)(ie - is + 1) * (je - js + 1);
+  double m = 0.0;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < per * npz; e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e / per);
+    const long long r = e % per;
+    const int i = is + (int)(r % (ie - is + 1)), j = js + (int)(r / (ie - is + 1));
+    const long long p = (long long)k * pg.plane() + pg.at(i, j);
+    m = fmax(m, fmax(fabs(cx[p]), fabs(cy[p])));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+int check_bounds(const fv3g_bounds* bd, int npx, int npy) {
+  if (!bd) return set_error(FV3G_E_ARG, "null bounds");
+  if (bd->ng != 3) return set_error(FV3G_E_ARG, "halo width ng must be 3 (got %d)", bd->ng);
+  if (bd->isd != bd->is - 3 || bd->ied != bd->ie + 3 || bd->jsd != bd->js - 3 || bd->jed != bd->je + 3)
+    return set_error(FV3G_E_ARG, "data domain must be the compute domain plus a 3-cell halo");
+  if (bd->ie < bd->is || bd->je < bd->js) return set_error(FV3G_E_ARG, "empty compute domain");
+  if (bd->is < 1 || bd->js < 1 || bd->ie > npx - 1 || bd->je > npy - 1)
+    return set_error(FV3G_E_ARG, "compute domain outside the tile (npx=%d, npy=%d)", npx, npy);
+  return 0;
+}
+
+PlaneGeom plane_for(const fv3g_bounds* bd) {
+  PlaneGeom pg;
+  pg.isd = bd->isd;
+  pg.jsd = bd->jsd;
+  pg.pitch = ((bd->ied - bd->isd + 2 + 7) / 8) * 8;
+  pg.rows = bd->jed - bd->jsd + 2;
+  return pg;
+}
+
+int corner_mask(const fv3g_grid* g) {
+  return (g->sw_corner ? 1 : 0) | (g->se_corner ? 2 : 0) | (g->nw_corner ? 4 : 0) | (g->ne_corner ? 8 : 0);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord, double* fx, double* fy,
+                  const double* xfx, const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd,
+                  const double* ra_x, const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
+                  int nord, double damp_c) {
+  (void)damp_c;
+  CHECK(check_bounds(bd, npx, npy));
+  if (!q || !crx || !cry || !fx || !fy || !xfx || !yfx || !grid || !ra_x || !ra_y)
+    return set_error(FV3G_E_ARG, "null array argument");
+  if (!grid->dxa || !grid->dya || !grid->area) return set_error(FV3G_E_ARG, "grid needs dxa, dya, area");
+  if (hord != 5 && hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
+  if (nord != 0) return set_error(FV3G_E_UNSUPPORTED, "tracer diffusion (nord=%d) is not implemented", nord);
+  if (lim_fac != 1.0) return set_error(FV3G_E_UNSUPPORTED, "lim_fac must be 1 (got %g)", lim_fac);
+  const PlaneGeom pg = plane_for(bd);
+  const size_t P = (size_t)pg.plane();
+  CHECK(g_ctx.begin(14 * padded(P, 8)));
+  cudaStream_t s = g_ctx.stream;
+  double *dq = g_ctx.take<double>(P), *dcx = g_ctx.take<double>(P), *dcy = g_ctx.take<double>(P);
+  double *dxf = g_ctx.take<double>(P), *dyf = g_ctx.take<double>(P), *drx = g_ctx.take<double>(P);
+  double *dry = g_ctx.take<double>(P), *dmx = g_ctx.take<double>(P), *dmy = g_ctx.take<double>(P);
+  double *ddxa = g_ctx.take<double>(P), *ddya = g_ctx.take<double>(P), *dar = g_ctx.take<double>(P);
+  double *dfx = g_ctx.take<double>(P), *dfy = g_ctx.take<double>(P);
+  FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
+  const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
+            jed = bd->jed;
+  CHECK(h2d_planes(dq, pg, q, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(dcx, pg, crx, is, ie + 1, jsd, jed, 1, s));
+  CHECK(h2d_planes(dcy, pg, cry, isd, ied, js, je + 1, 1, s));
+  CHECK(h2d_planes(dxf, pg, xfx, is, ie + 1, jsd, jed, 1, s));
+  CHECK(h2d_planes(dyf, pg, yfx, isd, ied, js, je + 1, 1, s));
+  CHECK(h2d_planes(drx, pg, ra_x, is, ie, jsd, jed, 1, s));
+  CHECK(h2d_planes(dry, pg, ra_y, isd, ied, js, je, 1, s));
+  if (mfx) CHECK(h2d_planes(dmx, pg, mfx, is, ie + 1, js, je, 1, s));
+  if (mfy) CHECK(h2d_planes(dmy, pg, mfy, is, ie, js, je + 1, 1, s));
+  CHECK(h2d_planes(ddxa, pg, grid->dxa, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(ddya, pg, grid->dya, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(dar, pg, grid->area, isd, ied, jsd, jed, 1, s));
+  AdvArgs<double> a{};
+  a.q_in = dq;
+  a.q_out = nullptr;
+  a.cx = dcx; a.cy = dcy; a.xfx = dxf; a.yfx = dyf;
+  // without mass fluxes the area fluxes weight the result, as upstream
+  a.mfx = mfx ? dmx : dxf;
+  a.mfy = mfy ? dmy : dyf;
+  a.dp1 = nullptr; a.dp2 = nullptr;
+  a.area = dar; a.rarea = dar; a.dxa = ddxa; a.dya = ddya;
+  a.ra_x = drx; a.ra_y = dry;
+  a.pg = pg;
+  a.is = is; a.ie = ie; a.js = js; a.je = je;
+  a.npx = npx; a.npy = npy;
+  a.nq = 1; a.npz = 1;
+  a.corners = corner_mask(grid);
+  a.nested = grid->nested;
+  a.cube = 0;
+  a.fx_out = dfx; a.fy_out = dfy; a.sFlux = (long long)P;
+  CHECK(launch_substep<double>(a, hord, true, 1, s));
+  if (!grid->nested && a.corners) {
+    k_corners<<<1, 64, 0, s>>>(dq, pg, npx, npy, a.corners, 1, 1);
+    FV3G_CUDA(cudaGetLastError());
+  }
+  CHECK(d2h_planes(fx, dfx, pg, is, ie + 1, js, je, 1, s));
+  CHECK(d2h_planes(fy, dfy, pg, is, ie, js, je + 1, 1, s));
+  CHECK(d2h_planes(q, dq, pg, isd, ied, jsd, jed, 1, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const fv3g_grid* grid,
+                   const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
+                   int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out) {
+  (void)dt;
+  (void)trdm;
+  CHECK(check_bounds(bd, npx, npy));
+  if (!q || !dp1 || !mfx || !mfy || !cx || !cy || !grid) return set_error(FV3G_E_ARG, "null array argument");
+  if (!grid->dx || !grid->dy || !grid->dxa || !grid->dya || !grid->area || !grid->rarea || !grid->sin_sg)
+    return set_error(FV3G_E_ARG, "incomplete grid");
+  if (npz < 1 || nq < 1) return set_error(FV3G_E_ARG, "npz and nq must be positive");
+  if (hord != 5 && hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
+  if (nord_tr != 0) return set_error(FV3G_E_UNSUPPORTED, "tracer diffusion (nord_tr=%d) is not implemented", nord_tr);
+  if (lim_fac != 1.0) return set_error(FV3G_E_UNSUPPORTED, "lim_fac must be 1 (got %g)", lim_fac);
+  const PlaneGeom pg = plane_for(bd);
+  const size_t P = (size_t)pg.plane();
+  const size_t nqp = (size_t)nq * npz;
+  CHECK(g_ctx.begin(padded(P * nqp, 8) * 2 + padded(P * npz, 8) * 9 + padded(P, 8) * 12 + 256));
+  cudaStream_t s = g_ctx.stream;
+  double* qa = g_ctx.take<double>(P * nqp);
+  double* qb = g_ctx.take<double>(P * nqp);
+  double* dpb[3] = {g_ctx.take<double>(P * npz), g_ctx.take<double>(P * npz), g_ctx.take<double>(P * npz)};
+  double *dcx = g_ctx.take<double>(P * npz), *dcy = g_ctx.take<double>(P * npz);
+  double *dmx = g_ctx.take<double>(P * npz), *dmy = g_ctx.take<double>(P * npz);
+  double *dxf = g_ctx.take<double>(P * npz), *dyf = g_ctx.take<double>(P * npz);
+  double *ddx = g_ctx.take<double>(P), *ddy = g_ctx.take<double>(P), *ddxa = g_ctx.take<double>(P);
+  double *ddya = g_ctx.take<double>(P), *dar = g_ctx.take<double>(P), *drar = g_ctx.take<double>(P);
+  double* dsin = g_ctx.take<double>(4 * P);
+  unsigned long long* dmax = g_ctx.take<unsigned long long>(1);
+  FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
+  const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
+            jed = bd->jed;
+  CHECK(h2d_planes(qa, pg, q, isd, ied, jsd, jed, (long long)nqp, s));
+  CHECK(h2d_planes(dpb[0], pg, dp1, isd, ied, jsd, jed, npz, s));
+  CHECK(h2d_planes(dcx, pg, cx, is, ie + 1, jsd, jed, npz, s));
+  CHECK(h2d_planes(dcy, pg, cy, isd, ied, js, je + 1, npz, s));
+  CHECK(h2d_planes(dmx, pg, mfx, is, ie + 1, js, je, npz, s));
+  CHECK(h2d_planes(dmy, pg, mfy, is, ie, js, je + 1, npz, s));
+  CHECK(h2d_planes(ddx, pg, grid->dx, isd, ied, jsd, jed + 1, 1, s));
+  CHECK(h2d_planes(ddy, pg, grid->dy, isd, ied + 1, jsd, jed, 1, s));
+  CHECK(h2d_planes(ddxa, pg, grid->dxa, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(ddya, pg, grid->dya, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(dar, pg, grid->area, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(drar, pg, grid->rarea, isd, ied, jsd, jed, 1, s));
+  CHECK(h2d_planes(dsin, pg, grid->sin_sg, isd, ied, jsd, jed, 4, s));  // slots 1..4 of sin_sg(:,:,9)
+
+  int nsplt = q_split;
+  if (q_split <= 0) {
+    k_max_abs2<<<64, 256, 0, s>>>(dcx, dcy, pg, is, ie, js, je, npz, dmax);
+    FV3G_CUDA(cudaGetLastError());
+    unsigned long long bits = 0;
+    FV3G_CUDA(cudaMemcpyAsync(&bits, dmax, 8, cudaMemcpyDeviceToHost, s));
+    FV3G_CUDA(cudaStreamSynchronize(s));
+    double cmax;
+    memcpy(&cmax, &bits, 8);
+    if (!std::isfinite(cmax)) return set_error(FV3G_E_NONFINITE, "non-finite Courant number");
+    nsplt = (int)(1.0 + cmax);
+  }
+  if (nsplt > 64) return set_error(FV3G_E_COURANT, "Courant number too large (nsplt=%d > 64)", nsplt);
+  if (nsplt_out) *nsplt_out = nsplt;
+  const double frac = (nsplt == 1) ? 1.0 : 1.0 / nsplt;
+  CHECK(launch_area_flux<double>(dcx, dcy, dxf, dyf, dmx, dmy, ddxa, ddya, ddx, ddy, dsin, 0, (long long)P, 0,
+                                 (long long)P, pg, is, ie, js, je, 1, npz, frac, s));
+  int dpi = 0;
+  int dp_start = 0;
+  for (int it = 0; it < nsplt; ++it) {
+    if (halo_fn) {
+      // refresh halos through the caller (FMS mpp_update_domains upstream)
+      CHECK(d2h_planes(q, qa, pg, isd, ied, jsd, jed, (long long)nqp, s));
+      FV3G_CUDA(cudaStreamSynchronize(s));
+      halo_fn(q, nq, npz, halo_ctx);
+      CHECK(h2d_planes(qa, pg, q, isd, ied, jsd, jed, (long long)nqp, s));
+    }
+    const int dpo = (dpi == 1) ? 2 : 1;
+    AdvArgs<double> a{};
+    a.q_in = qa; a.q_out = qb;
+    a.sQk = (long long)P; a.sQq = (long long)P * npz; a.sQt = 0;
+    a.cx = dcx; a.cy = dcy; a.xfx = dxf; a.yfx = dyf; a.mfx = dmx; a.mfy = dmy;
+    a.dp1 = dpb[dpi]; a.dp2 = dpb[dpo];
+    a.sFk = (long long)P; a.sFt = 0;
+    a.area = dar; a.rarea = drar; a.dxa = ddxa; a.dya = ddya; a.sMt = 0;
+    a.pg = pg;
+    a.is = is; a.ie = ie; a.js = js; a.je = je;
+    a.npx = npx; a.npy = npy;
+    a.nq = nq; a.npz = npz;
+    a.corners = corner_mask(grid);
+    a.nested = grid->nested;
+    a.cube = 0;
+    CHECK(launch_substep<double>(a, hord, false, std::min(nq, 4), s));
+    // the updated compute domain goes back into the halo-carrying buffer
+    CHECK(d2d_planes(qa, qb, pg, is, ie, js, je, (long long)nqp, s));
+    dp_start = dpi;
+    dpi = dpo;
+  }
+  if (!grid->nested && corner_mask(grid)) {
+    const long long np = (long long)nqp;
+    k_corners<<<(unsigned)((np * 36 + 255) / 256), 256, 0, s>>>(qa, pg, npx, npy, corner_mask(grid), 1, np);
+    FV3G_CUDA(cudaGetLastError());
+  }
+  // upstream leaves dp1 at the thickness of the start of the last substep
+  CHECK(d2h_planes(q, qa, pg, isd, ied, jsd, jed, (long long)nqp, s));
+  {
+    // dp1 compute domain of every level (halo of dp1 is left untouched)
+    const int ni = ie - is + 1, nj = je - js + 1, nid = ied - isd + 1, njd = jed - jsd + 1;
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)(dpb[dp_start] + pg.at(is, js)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
+    p.dstPtr = make_cudaPitchedPtr(dp1 + (is - isd) + (size_t)(js - jsd) * nid, (size_t)nid * 8, nid, njd);
+    p.extent = make_cudaExtent((size_t)ni * 8, nj, npz);
+    p.kind = cudaMemcpyDeviceToHost;
+    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  }
+  CHECK(d2h_planes(cx, dcx, pg, is, ie + 1, jsd, jed, npz, s));
+  CHECK(d2h_planes(cy, dcy, pg, isd, ied, js, je + 1, npz, s));
+  CHECK(d2h_planes(mfx, dmx, pg, is, ie + 1, js, je, npz, s));
+  CHECK(d2h_planes(mfy, dmy, pg, is, ie, js, je + 1, npz, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+static int map_common(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                      double* q2, int i1, int i2, int j1, int j2, int ibeg, int iend, int jbeg, int jend, int nq,
+                      int iv, int kord, double q_min) {
+  if (!pe1 || !q1 || !pe2 || !q2) return set_error(FV3G_E_ARG, "null array argument");
+  if (km < 1 || km > KMAX || kn < 1 || kn > KMAX)
+    return set_error(FV3G_E_ARG, "remap supports 1..%d layers (km=%d, kn=%d)", KMAX, km, kn);
+  if (i1 < ibeg || i2 > iend || i2 < i1 || j1 < jbeg || j2 > jend || j2 < j1)
+    return set_error(FV3G_E_ARG, "row/column range outside the array bounds");
+  if (kord != 4 && kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
+  if (iv < -2 || iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", iv);
+  const int ni = i2 - i1 + 1, nj = j2 - j1 + 1;
+  const long long ncol = (long long)ni * nj;
+  // device copy of the selected columns, planes of ni x nj per (field, level)
+  PlaneGeom pg;
+  pg.isd = i1;
+  pg.jsd = j1;
+  pg.pitch = ni;
+  pg.rows = nj;
+  const size_t P = (size_t)ni * nj;
+  CHECK(g_ctx.begin(padded(P * km * nq, 8) + padded(P * kn * nq, 8) + padded(P * (km + 1), 8) +
+                    padded(P * (kn + 1), 8) + padded(P, 8) + remap_scratch_bytes(ncol, true) + 1024));
+  cudaStream_t s = g_ctx.stream;
+  double* d1 = g_ctx.take<double>(P * km * nq);
+  double* d2 = g_ctx.take<double>(P * kn * nq);
+  double* dpe1 = g_ctx.take<double>(P * (km + 1));
+  double* dpe2 = g_ctx.take<double>(P * (kn + 1));
+  double* dqs = g_ctx.take<double>(P);
+  double* scr = g_ctx.take<double>((size_t)ncol * (KMAX + 1) * 6);
+  unsigned char* sch = g_ctx.take<unsigned char>((size_t)ncol * (KMAX + 1));
+  const int nib = iend - ibeg + 1, njb = jend - jbeg + 1;
+  // q1(ibeg:iend, jbeg:jend, km*nq): the (i1:i2, j1:j2) block of every plane
+  {
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)(q1 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib), (size_t)nib * 8, nib, njb);
+    p.dstPtr = make_cudaPitchedPtr(d1, (size_t)ni * 8, ni, nj);
+    p.extent = make_cudaExtent((size_t)ni * 8, nj, (size_t)km * nq);
+    p.kind = cudaMemcpyHostToDevice;
+    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  }
+  FV3G_CUDA(cudaMemcpyAsync(dpe1, pe1, sizeof(double) * P * (km + 1), cudaMemcpyHostToDevice, s));
+  FV3G_CUDA(cudaMemcpyAsync(dpe2, pe2, sizeof(double) * P * (kn + 1), cudaMemcpyHostToDevice, s));
+  if (qs) FV3G_CUDA(cudaMemcpyAsync(dqs, qs, sizeof(double) * P, cudaMemcpyHostToDevice, s));
+  RemapArgs<double> r{};
+  r.q_in = d1;
+  r.q_out = d2;
+  r.sQk = (long long)P;
+  r.sQq = (long long)P * km;
+  r.sQt = 0;
+  r.sQqo = (long long)P * kn;
+  r.nfield = nq;
+  r.dp = nullptr;
+  r.dp_out = nullptr;
+  r.pe1 = dpe1;
+  r.pe2 = dpe2;
+  r.qs = qs ? dqs : nullptr;
+  r.pg = pg;
+  r.i1 = i1; r.j1 = j1; r.ni = ni; r.nj = nj;
+  r.ncol = ncol;
+  r.km = km; r.kn = kn; r.iv = iv; r.q_min = q_min;
+  r.scratch = scr;
+  r.sched = sch;
+  CHECK(launch_remap<double>(r, kord, s));
+  {
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr(d2, (size_t)ni * 8, ni, nj);
+    p.dstPtr = make_cudaPitchedPtr(q2 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib, (size_t)nib * 8, nib, njb);
+    p.extent = make_cudaExtent((size_t)ni * 8, nj, (size_t)kn * nq);
+    p.kind = cudaMemcpyDeviceToHost;
+    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  }
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int fv3g_map_scalar(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                    double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord,
+                    double q_min) {
+  return map_common(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, j, ibeg, iend, jbeg, jend, 1, iv, kord, q_min);
+}
+
+int fv3g_map1_ppm(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                  double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord) {
+  return map_common(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, j, ibeg, iend, jbeg, jend, 1, iv, kord, 0.0);
+}
+
+int fv3g_map_scalar_3d(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                       double* q2, int i1, int i2, int j1, int j2, int ibeg, int iend, int jbeg, int jend, int nq,
+                       int iv, int kord, double q_min) {
+  if (nq < 1) return set_error(FV3G_E_ARG, "nq must be positive");
+  return map_common(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j1, j2, ibeg, iend, jbeg, jend, nq, iv, kord, q_min);
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// fv3g_internal.cuh -- shared device/host definitions of the fv3g library.
+//
+// Device layout ("plane layout"): every 2-D field of a tile lives in a plane
+// of `rows` rows of `pitch` elements; element (i, j) of the tile (1-based
+// Fortran indices, halo included) sits at (j - jsd) * pitch + (i - isd).
+// Cell fields use rows jsd..jed, face fields use up to jed+1 / ied+1, so one
+// plane geometry (rows = nd+1, pitch >= nd+1) serves all of them.  Planes are
+// stacked [tile][tracer][level] for tracers and [tile][level] for per-level
+// fields, matching the Fortran (i, j, k, iq) order inside a tile.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/fv3g.h"
+
+namespace fv3g {
+
+constexpr int NG = 3;    // halo width
+constexpr int TW = 26;   // output cells per CTA tile edge
+constexpr int WIN = 32;  // window = TW + 2*NG cells (one warp lane per line)
+constexpr int NF = 27;   // faces per line of a CTA tile
+constexpr int PQ = 33;   // odd pitch of 32-wide shared arrays
+constexpr int PF = 27;   // odd pitch of 27/26-wide shared arrays
+constexpr int NO_EDGE = -1000;
+
+// Tile-edge ordinals used by the cube topology and the edge-flux buffers.
+enum { EW = 0, EE = 1, ES = 2, EN = 3 };
+
+// Six-tile connectivity: for tile t and edge e the neighbour tile, its edge,
+// and whether the along-edge index runs the opposite way there.
+struct Topo {
+  signed char nbr[6][4];
+  signed char nedge[6][4];
+  signed char rev[6][4];
+};
+
+struct PlaneGeom {
+  int pitch;  // elements per row
+  int rows;   // rows per plane
+  int isd, jsd;
+  __host__ __device__ __forceinline__ long long at(int i, int j) const {
+    return (long long)(j - jsd) * pitch + (i - isd);
+  }
+  __host__ __device__ __forceinline__ long long plane() const { return (long long)pitch * rows; }
+};
+
+// Arguments of one advection substep (tracer_2d inner loop body).
+template <typename T>
+struct AdvArgs {
+  const T* q_in;  // [tile][tracer][level] planes
+  T* q_out;
+  long long sQt, sQq, sQk;  // plane strides in elements (tile, tracer, level)
+  const T* cx;              // [tile][level] planes (scaled by 1/nsplt)
+  const T* cy;
+  const T* xfx;
+  const T* yfx;
+  const T* mfx;
+  const T* mfy;
+  const T* dp1;  // layer thickness at the start of the substep
+  T* dp2;        // written: thickness at its end
+  long long sFt, sFk;
+  const T* area;  // [tile] planes
+  const T* rarea;
+  const T* dxa;
+  const T* dya;
+  long long sMt;
+  PlaneGeom pg;
+  int is, ie, js, je;  // compute domain (tile indices)
+  int npx, npy;        // tile size + 1
+  int nq;
+  int corners;  // bit 0 sw, 1 se, 2 nw, 3 ne: tile corner is a cube corner
+  int nested;
+  int cube;     // 1: halo gathered from neighbour tiles through topo
+  Topo topo;
+  T* eflux;     // cube: outward tile-edge fluxes [tile][edge][level][tracer][n]
+  int npz;
+  const T* ra_x;  // optional caller-supplied ra_x / ra_y planes (single level)
+  const T* ra_y;
+  T* fx_out;    // flux mode: planes [level*nq + tracer] of the tile
+  T* fy_out;
+  long long sFlux;
+};
+
+// ------------------------------------------------------------- helpers ----
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T tabs(T a) { return a < T(0) ? -a : a; }
+// |a| with the sign of b, b == 0 counted positive
+template <typename T> __device__ __forceinline__ T tsign(T a, T b) {
+  T m = tabs(a);
+  return b < T(0) ? -m : m;
+}
+template <typename T> __device__ __forceinline__ T clamp2(T a, T x0, T x1) {
+  return tmin(tmax(a, tmin(x0, x1)), tmax(x0, x1));
+}
+
+// Colella & Woodward (1984) eq. 1.10 in perturbation form (bl = aL - q, br = aR - q).
+template <typename T> __device__ __forceinline__ void cw84(T& bl, T& br) {
+  if (bl * br >= T(0)) {
+    bl = T(0);
+    br = T(0);
+    return;
+  }
+  T d = br - bl;
+  T t = T(3) * d * (bl + br);
+  T d2 = d * d;
+  if (-t > d2) bl = T(-2) * br;
+  else if (t > d2) br = T(-2) * bl;
+}
+
+// Monotonized central slope in half-increment form.
+template <typename T> __device__ __forceinline__ T vl_slope(T xm, T x0, T xp) {
+  T xt = T(0.25) * (xp - xm);
+  T smax = tmax(tmax(xm, x0), xp) - x0;
+  T smin = x0 - tmin(tmin(xm, x0), xp);
+  return tsign(tmin(tmin(tabs(xt), smax), smin), xt);
+}
+
+// Upwind integral of the sub-grid parabola over the swept fraction.
+template <typename T>
+__device__ __forceinline__ T ppm_flux(T c, T xl, T bll, T brl, T xr, T blr, T brr) {
+  if (c > T(0)) return xl + (T(1) - c) * (brl - c * (bll + brl));
+  return xr + (T(1) + c) * (blr + c * (blr + brr));
+}
+
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define FV3G_CUDA(call)                                         \
+  do {                                                          \
+    cudaError_t e__ = (call);                                   \
+    if (e__ != cudaSuccess) return ::fv3g::cuda_error(e__, #call); \
+  } while (0)
+
+// Host launchers (fv3g_advect.cu)
+template <typename T>
+int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s);
+template <typename T>
+int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s);
+template <typename T>
+int launch_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa, const T* dya,
+                     const T* dx, const T* dy, const T* sin_sg, long long sFt, long long sFk,
+                     long long sMt, long long sSin, PlaneGeom pg, int is, int ie, int js, int je,
+                     int ntiles, int npz, T frac, cudaStream_t s);
+template <typename T>
+int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is,
+                       int ie, int js, int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s);
+
+size_t substep_smem_bytes(bool fp64, int warps);
+int prepare_kernels();
+
+}  // namespace fv3g

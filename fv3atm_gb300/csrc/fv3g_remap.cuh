@@ -1,0 +1,38 @@
+// fv3g_remap.cuh -- arguments of the column remap kernel.
+#pragma once
+
+#include "fv3g_internal.cuh"
+
+namespace fv3g {
+
+constexpr int KMAX = 128;  // most layers per column (source or target)
+
+template <typename T>
+struct RemapArgs {
+  const T* q_in;  // field planes, [tile][field][level]
+  T* q_out;
+  long long sQt, sQq, sQk;
+  long long sQqo;  // field stride of q_out (kn levels)
+  int nfield;
+  const T* dp;  // Lagrangian thickness planes [tile][level] (batched mode)
+  T* dp_out;    // target thickness (may be null)
+  long long sFt, sFk;
+  const double* ak;  // device, km+1 / kn+1 (batched mode)
+  const double* bk;
+  const double* pe1;  // drop-in mode: [k][col] interface pressures (null in batched mode)
+  const double* pe2;
+  const double* qs;  // [col] surface value for iv == -2 (may be null)
+  PlaneGeom pg;
+  int i1, j1, ni, nj;  // column block: i1..i1+ni-1, j1..j1+nj-1 on every tile
+  long long ncol;      // ntiles * ni * nj
+  int km, kn, iv;
+  double q_min;
+  T* scratch;             // 6 * (KMAX+1) * ncol elements
+  unsigned char* sched;   // (KMAX+1) * ncol bytes
+};
+
+template <typename T>
+int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s);
+size_t remap_scratch_bytes(long long ncol, bool fp64);
+
+}  // namespace fv3g

@@ -1,0 +1,184 @@
+"""Equiangular gnomonic cubed-sphere geometry, tile topology and hybrid levels.
+
+This module generates the grid metrics that FV3's ``fv_grid_type`` carries into
+the tracer path (dx, dy, dxa, dya, area, rarea, sin_sg, corner flags; upstream
+``fv_grid_tools`` / ``fv_grid_utils``, absent from the reference tree, whose only
+in-tree users are ``atmos_model.F90:578-614``) and the six-tile connectivity that
+the on-device halo gather and the tile-edge flux reconciliation use.
+
+Arrays are numpy float64 with shape ``(nj, ni)`` in C order, so memory is
+i-fastest exactly like a Fortran ``(i, j)`` array.  Halo metrics are those of the
+extended gnomonic grid of the same face (the synthetic problem does not need
+them to equal the neighbour's), which requires ``n >= 12`` with a 3-cell halo.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+RADIUS = 6.371e6  # m
+
+# Face definitions: (centre, i axis, j axis).  e_i x e_j = centre on every face.
+FACES = (
+    ((1, 0, 0), (0, 1, 0), (0, 0, 1)),
+    ((0, 1, 0), (-1, 0, 0), (0, 0, 1)),
+    ((-1, 0, 0), (0, -1, 0), (0, 0, 1)),
+    ((0, -1, 0), (1, 0, 0), (0, 0, 1)),
+    ((0, 0, 1), (0, 1, 0), (-1, 0, 0)),
+    ((0, 0, -1), (0, 1, 0), (1, 0, 0)),
+)
+W, E, S, N = 0, 1, 2, 3
+# endpoints of each edge in face coordinates (sx, sy); "along" runs first -> second
+_EDGE_ENDS = {W: ((-1, -1), (-1, 1)), E: ((1, -1), (1, 1)), S: ((-1, -1), (1, -1)), N: ((-1, 1), (1, 1))}
+
+
+def _cube_point(face: int, sx: int, sy: int) -> tuple:
+    c, e1, e2 = (np.array(v) for v in FACES[face])
+    return tuple(int(v) for v in (c + sx * e1 + sy * e2))
+
+
+def cube_topology() -> np.ndarray:
+    """(6, 4, 3) int32: neighbour tile, neighbour edge, reversed-along flag."""
+    topo = np.zeros((6, 4, 3), dtype=np.int32)
+    for t in range(6):
+        for e in range(4):
+            p0 = _cube_point(t, *_EDGE_ENDS[e][0])
+            p1 = _cube_point(t, *_EDGE_ENDS[e][1])
+            found = None
+            for u in range(6):
+                if u == t:
+                    continue
+                for f in range(4):
+                    q0 = _cube_point(u, *_EDGE_ENDS[f][0])
+                    q1 = _cube_point(u, *_EDGE_ENDS[f][1])
+                    if {q0, q1} == {p0, p1}:
+                        found = (u, f, 0 if q0 == p0 else 1)
+            assert found is not None
+            topo[t, e] = found
+    return topo
+
+
+def halo_source(topo: np.ndarray, n: int, t: int, i: int, j: int) -> tuple:
+    """Tile-local 1-based halo cell (i, j) of tile t -> (tile, i, j) interior cell."""
+    if i < 1:
+        e, d, s = W, 1 - i, j - 1
+    elif i > n:
+        e, d, s = E, i - n, j - 1
+    elif j < 1:
+        e, d, s = S, 1 - j, i - 1
+    else:
+        e, d, s = N, j - n, i - 1
+    nt, ne, rev = (int(v) for v in topo[t, e])
+    sb = n - 1 - s if rev else s
+    if ne == W:
+        return nt, d, sb + 1
+    if ne == E:
+        return nt, n + 1 - d, sb + 1
+    if ne == S:
+        return nt, sb + 1, d
+    return nt, sb + 1, n + 1 - d
+
+
+def _gnomonic(face: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Unit vectors of equiangular face coordinates (a, b) in radians."""
+    c, e1, e2 = (np.array(v, dtype=np.float64) for v in FACES[face])
+    x, y = np.tan(a), np.tan(b)
+    p = c[None, None, :] + x[..., None] * e1 + y[..., None] * e2
+    return p / np.linalg.norm(p, axis=-1, keepdims=True)
+
+
+def _arc(p: np.ndarray, q: np.ndarray) -> np.ndarray:
+    """Great-circle angle between unit vectors (numerically robust form)."""
+    return 2.0 * np.arcsin(np.clip(0.5 * np.linalg.norm(p - q, axis=-1), 0.0, 1.0))
+
+
+def _tri_area(a: np.ndarray, b: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """Solid angle of spherical triangles (Van Oosterom & Strackee 1983)."""
+    num = np.abs(np.einsum("...k,...k->...", a, np.cross(b, c)))
+    den = 1.0 + np.einsum("...k,...k->...", a, b) + np.einsum("...k,...k->...", b, c) + np.einsum(
+        "...k,...k->...", c, a)
+    return 2.0 * np.arctan2(num, den)
+
+
+def _sin_angle(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Sine of the angle between the equiangular coordinate lines at (a, b)."""
+    x, y = np.tan(a), np.tan(b)
+    cos = -x * y / np.sqrt((1.0 + x * x) * (1.0 + y * y))
+    return np.sqrt(1.0 - cos * cos)
+
+
+@dataclasses.dataclass
+class TileGeom:
+    """Metrics of one tile on the data domain (isd:ied, jsd:jed), shape (nj, ni)."""
+
+    n: int
+    ng: int
+    tile: int
+    dx: np.ndarray      # (n+2ng+1, n+2ng)   south-edge length, rows jsd..jed+1
+    dy: np.ndarray      # (n+2ng, n+2ng+1)   west-edge length, cols isd..ied+1
+    dxa: np.ndarray
+    dya: np.ndarray
+    area: np.ndarray
+    rarea: np.ndarray
+    sin_sg: np.ndarray  # (9, n+2ng, n+2ng); slots 0..3 = W, S, E, N edges
+    corners: np.ndarray  # (n+2ng+1, n+2ng+1, 3) unit vectors of cell corners
+    centers: np.ndarray  # (n+2ng, n+2ng, 3)
+    sw_corner: int = 1
+    se_corner: int = 1
+    nw_corner: int = 1
+    ne_corner: int = 1
+
+
+def tile_geometry(n: int, tile: int, ng: int = 3, radius: float = RADIUS) -> TileGeom:
+    if n < 12:
+        raise ValueError("tile size n must be >= 12 for a 3-cell extended-gnomonic halo")
+    h = 0.5 * math.pi / n
+    ic = np.arange(1 - ng, n + 2 + ng)           # corner indices I = isd..ied+1
+    ac = -0.25 * math.pi + (ic - 1) * h           # corner angles
+    am = ac[:-1] + 0.5 * h                        # cell-centre angles
+    B, A = np.meshgrid(ac, ac, indexing="ij")     # [J, I]
+    corners = _gnomonic(tile, A, B)
+    Bm, Am = np.meshgrid(am, am, indexing="ij")
+    centers = _gnomonic(tile, Am, Bm)
+    # edge midpoints (equiangular midpoints)
+    Bw, Aw = np.meshgrid(am, ac, indexing="ij")   # x-faces: (J cell, I face)
+    xmid = _gnomonic(tile, Aw, Bw)                # (nd, nd+1)
+    Bs, As = np.meshgrid(ac, am, indexing="ij")   # y-faces: (J face, I cell)
+    ymid = _gnomonic(tile, As, Bs)                # (nd+1, nd)
+    dx = radius * _arc(corners[:, :-1], corners[:, 1:])     # (nd+1, nd)
+    dy = radius * _arc(corners[:-1, :], corners[1:, :])     # (nd, nd+1)
+    dxa = radius * _arc(xmid[:, :-1], xmid[:, 1:])          # (nd, nd)
+    dya = radius * _arc(ymid[:-1, :], ymid[1:, :])          # (nd, nd)
+    c00, c10, c01, c11 = corners[:-1, :-1], corners[:-1, 1:], corners[1:, :-1], corners[1:, 1:]
+    area = radius * radius * (_tri_area(c00, c10, c11) + _tri_area(c00, c11, c01))
+    nd = n + 2 * ng
+    sin_sg = np.empty((9, nd, nd))
+    sin_sg[0] = _sin_angle(Aw[:, :-1], Bw[:, :-1])   # west edge
+    sin_sg[1] = _sin_angle(As[:-1, :], Bs[:-1, :])   # south edge
+    sin_sg[2] = _sin_angle(Aw[:, 1:], Bw[:, 1:])     # east edge
+    sin_sg[3] = _sin_angle(As[1:, :], Bs[1:, :])     # north edge
+    sin_sg[4:] = _sin_angle(Am, Bm)[None]
+    return TileGeom(n=n, ng=ng, tile=tile, dx=dx, dy=dy, dxa=dxa, dya=dya, area=area, rarea=1.0 / area,
+                    sin_sg=sin_sg, corners=corners, centers=centers)
+
+
+def cube_geometry(n: int, ng: int = 3, radius: float = RADIUS) -> list:
+    return [tile_geometry(n, t, ng, radius) for t in range(6)]
+
+
+def hybrid_levels(km: int, ptop: float = 100.0, p0: float = 1.0e5, eta_c: float = 0.2) -> tuple:
+    """Synthetic monotone hybrid sigma-pressure coefficients (ak, bk), km+1 each.
+
+    The operational GFS L63/L127 tables live in the absent ``fv_eta.F90``; this
+    coordinate is pure pressure above eta_c and blends quadratically to sigma
+    at the surface.  Interfaces stay monotone for ps in [900, 1100] hPa.
+    """
+    eta = np.arange(km + 1, dtype=np.float64) / km
+    pref = ptop + (p0 - ptop) * eta ** 1.5
+    bk = np.where(eta > eta_c, ((eta - eta_c) / (1.0 - eta_c)) ** 2, 0.0)
+    ak = pref - bk * p0
+    ak[-1] = 0.0
+    bk[-1] = 1.0
+    return ak, bk

@@ -1,0 +1,209 @@
+/*
+ * fv3g.h -- C ABI of the GB300 (sm_103a) FV3 tracer-transport path.
+ *
+ * Drop-in for the FV3 dynamical core's tracer transport: horizontal PPM
+ * advection (tracer_2d / fv_tp_2d with xppm/yppm and copy_corners) and the
+ * Lagrangian-to-Eulerian vertical remap (map_scalar / map1_ppm / cs_profile).
+ * The upstream Fortran lives in the GFDL_atmos_cubed_sphere submodule
+ * (model/fv_tracer2d.F90, model/tp_core.F90, model/fv_mapz.F90), which is an
+ * empty directory in the fv3atm tree (.gitmodules:1-4; linked as CMake target
+ * fv3, CMakeLists.txt:43,149).  Its caller in fv3atm is
+ * atmosphere_dynamics (atmos_model.F90:879); tracers are stored
+ * q(isd:ied, jsd:jed, npz, nq) with i fastest (atmos_model.F90:1423).
+ *
+ * Conventions
+ *  - Everything is plain C: pointers, sizes and doubles/ints, callable from
+ *    Fortran through ISO_C_BINDING (bind(C) interfaces in INTEGRATION.md).
+ *  - Arrays passed to the exact-shape entries are HOST arrays in Fortran
+ *    (column-major, i fastest) order with the bounds documented per argument;
+ *    the library copies them to the GPU and back.
+ *  - Every entry returns 0 on success or a negative FV3G_E* code; the message
+ *    of the last error on the calling thread is available from
+ *    fv3g_last_error().  No entry aborts the process.
+ *  - The library never frees caller memory.  Device state is owned by the
+ *    opaque fv3g_state handle.
+ */
+#ifndef FV3G_H
+#define FV3G_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- error codes -- */
+#define FV3G_OK 0
+#define FV3G_E_ARG -1        /* bad argument (shape, option, null pointer) */
+#define FV3G_E_CUDA -2       /* a CUDA runtime call failed */
+#define FV3G_E_COURANT -3    /* Courant number above the supported limit */
+#define FV3G_E_NONFINITE -4  /* non-finite value in an input field */
+#define FV3G_E_DELP -5       /* a layer thickness became non-positive */
+#define FV3G_E_UNSUPPORTED -6 /* option outside the implemented set */
+#define FV3G_E_NOMEM -7      /* device allocation failed */
+
+/* ------------------------------------------------------------ precision -- */
+#define FV3G_FP64 0   /* FP64 throughout */
+#define FV3G_MIXED 1  /* FP32 stencils; FP64 pe/peln, remap cumulative mass, mass sums */
+
+/* Bounds of one rank's domain, as FV3's fv_grid_bounds_type. */
+typedef struct {
+  int is, ie, js, je;     /* compute domain */
+  int isd, ied, jsd, jed; /* data domain = compute domain + ng */
+  int ng;                 /* halo width; must be 3 */
+} fv3g_bounds;
+
+/* Grid metrics (host pointers, FP64), the fields of fv_grid_type on the path. */
+typedef struct {
+  const double* dx;     /* (isd:ied,   jsd:jed+1) */
+  const double* dy;     /* (isd:ied+1, jsd:jed)   */
+  const double* dxa;    /* (isd:ied,   jsd:jed)   */
+  const double* dya;    /* (isd:ied,   jsd:jed)   */
+  const double* area;   /* (isd:ied,   jsd:jed)   */
+  const double* rarea;  /* (isd:ied,   jsd:jed)   */
+  const double* sin_sg; /* (isd:ied,   jsd:jed, 9) */
+  int sw_corner, se_corner, nw_corner, ne_corner; /* tile corner is a cube corner */
+  int nested;           /* 1: no cube-edge treatment and no corner fill */
+} fv3g_grid;
+
+/* Halo refresh called by fv3g_tracer_2d before every substep with the HOST
+ * tracer array q(isd:ied,jsd:jed,npz,nq); the Fortran side wraps FMS
+ * mpp_update_domains here.  May be NULL when halos are valid and nsplt == 1. */
+typedef void (*fv3g_halo_fn)(double* q, int nq, int npz, void* ctx);
+
+/* ------------------------------------------------ library / diagnostics -- */
+int fv3g_version(void);                      /* 100*major + minor */
+int fv3g_last_error(char* buf, int len);     /* copies the calling thread's last message */
+int fv3g_device_info(char* buf, int len);    /* GPU name and SM count */
+
+/* ======================================================================== */
+/* Exact-shape drop-in entries (host arrays, one domain).                   */
+/* ======================================================================== */
+
+/* fv_tp_2d (tp_core.F90): fluxes of one level of one tracer.
+ *   q   (isd:ied, jsd:jed)      inout: cube-corner halo blocks are rewritten
+ *   crx (is:ie+1, jsd:jed)   cry (isd:ied, js:je+1)
+ *   fx  (is:ie+1, js:je)     fy  (is:ie, js:je+1)        out
+ *   xfx (is:ie+1, jsd:jed)   yfx (isd:ied, js:je+1)
+ *   ra_x (is:ie, jsd:jed)    ra_y (isd:ied, js:je)
+ *   mfx (is:ie+1, js:je)     mfy (is:ie, js:je+1)   may be NULL (then xfx/yfx weight the fluxes)
+ *   hord: 5 (unlimited PPM) or 8 (Lin 2004 monotone).  lim_fac must be 1.
+ *   nord must be 0 (tracer diffusion is not implemented); damp_c ignored.
+ * Replaces: fv_tp_2d(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, gridstruct,
+ *           bd, ra_x, ra_y, lim_fac, mfx, mfy, mass, nord, damp_c). */
+int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord,
+                  double* fx, double* fy, const double* xfx, const double* yfx,
+                  const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x,
+                  const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
+                  int nord, double damp_c);
+
+/* tracer_2d (fv_tracer2d.F90) on one domain, FP64.
+ *   q   (isd:ied, jsd:jed, npz, nq) inout     dp1 (isd:ied, jsd:jed, npz) inout
+ *   mfx (is:ie+1, js:je, npz)  mfy (is:ie, js:je+1, npz)                 inout (scaled by 1/nsplt)
+ *   cx  (is:ie+1, jsd:jed, npz) cy (isd:ied, js:je+1, npz)               inout (scaled by 1/nsplt)
+ *   q_split > 0 fixes the substep count, 0 derives it from the max Courant
+ *   number.  nord_tr must be 0; lim_fac must be 1.
+ * On return dp1 holds the layer thickness at the start of the last substep,
+ * as upstream.  nsplt_out (may be NULL) receives the substep count.
+ * Replaces: tracer_2d(q, dp1, mfx, mfy, cx, cy, gridstruct, bd, domain, npx,
+ *           npy, npz, nq, hord, q_split, dt, id_divg, q_pack, dp1_pack,
+ *           nord_tr, trdm, lim_fac). */
+int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                   const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq,
+                   int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
+                   fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out);
+
+/* map_scalar (fv_mapz.F90): remap row j of a 3-D field, FP64.
+ *   pe1 (i1:i2, km+1)  pe2 (i1:i2, kn+1)  qs (i1:i2)
+ *   q1 (ibeg:iend, jbeg:jend, km) in    q2 (ibeg:iend, jbeg:jend, kn) inout
+ *   iv: -2 (bottom value qs), -1, 0 (positive), 1 (floor q_min)
+ *   kord: 4 (C1 spline, CW84 limiter) or 9 (monotone)
+ *   pe2(1) must equal pe1(1) and pe2(kn+1) must equal pe1(km+1).
+ * Thread-safe: may be called concurrently from OpenMP threads (per-thread
+ * stream and scratch).
+ * Replaces: map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend,
+ *           jbeg, jend, iv, kord, q_min). */
+int fv3g_map_scalar(int km, const double* pe1, const double* q1, const double* qs, int kn,
+                    const double* pe2, double* q2, int i1, int i2, int j, int ibeg, int iend,
+                    int jbeg, int jend, int iv, int kord, double q_min);
+
+/* map1_ppm (fv_mapz.F90): as map_scalar without the floor argument.
+ * Replaces: map1_ppm(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend,
+ *           jbeg, jend, iv, kord). */
+int fv3g_map1_ppm(int km, const double* pe1, const double* q1, const double* qs, int kn,
+                  const double* pe2, double* q2, int i1, int i2, int j, int ibeg, int iend,
+                  int jbeg, int jend, int iv, int kord);
+
+/* Whole-domain remap of nq fields in one call (the loop over j rows and
+ * tracers of Lagrangian_to_Eulerian / mapn_tracer, fv_mapz.F90):
+ *   pe1 (i1:i2, j1:j2, km+1)  pe2 (i1:i2, j1:j2, kn+1)  qs (i1:i2, j1:j2) or NULL
+ *   q1 (ibeg:iend, jbeg:jend, km, nq) in    q2 (ibeg:iend, jbeg:jend, kn, nq) inout */
+int fv3g_map_scalar_3d(int km, const double* pe1, const double* q1, const double* qs, int kn,
+                       const double* pe2, double* q2, int i1, int i2, int j1, int j2, int ibeg,
+                       int iend, int jbeg, int jend, int nq, int iv, int kord, double q_min);
+
+/* ======================================================================== */
+/* Batched, device-resident entries (all six tiles, all tracers).           */
+/* ======================================================================== */
+
+typedef struct fv3g_state fv3g_state;
+
+typedef struct {
+  int n;          /* cells per tile edge (C_n) */
+  int ntiles;     /* 6 (cube) */
+  int npz;        /* Lagrangian levels */
+  int nq;         /* tracers */
+  int precision;  /* FV3G_FP64 or FV3G_MIXED */
+  int hord;       /* 5 or 8 */
+  int kord;       /* 4 or 9 */
+  int iv;         /* remap iv (see fv3g_map_scalar) */
+  double q_min;   /* remap floor for iv == 1 */
+  int warps_per_cta; /* advection CTA width in warps (0 = default) */
+} fv3g_state_desc;
+
+/* Which field an upload/download addresses. */
+enum {
+  FV3G_FIELD_Q = 0,    /* (6, nq, npz, nd, nd)    nd = n + 6, halo included */
+  FV3G_FIELD_DELP,     /* (6, npz, nd, nd)        Lagrangian thickness at call start */
+  FV3G_FIELD_CX,       /* (6, npz, nd, n+1)       Fortran (is:ie+1, jsd:jed) per level */
+  FV3G_FIELD_CY,       /* (6, npz, n+1, nd)       (isd:ied, js:je+1) */
+  FV3G_FIELD_MFX,      /* (6, npz, n, n+1)        (is:ie+1, js:je) */
+  FV3G_FIELD_MFY,      /* (6, npz, n+1, n)        (is:ie, js:je+1) */
+  FV3G_FIELD_Q_REMAPPED, /* (6, nq, npz, nd, nd) output of the remap */
+  FV3G_FIELD_DELP_OUT,   /* (6, npz, nd, nd)      thickness after the last substep */
+  FV3G_NFIELDS
+};
+
+/* Grid of one tile (host arrays with the fv3g_grid shapes, tile-local bounds). */
+int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out);
+int fv3g_state_destroy(fv3g_state* st);
+int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* grid);
+int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk); /* npz+1 each */
+/* Host <-> device copies (FP64 host data; converted to FP32 in MIXED mode).
+ * stream may be NULL (the state's stream). */
+int fv3g_upload(fv3g_state* st, int field, const double* host);
+int fv3g_download(fv3g_state* st, int field, double* host);
+/* Raw device copies with the state's storage type (float in MIXED). */
+int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream);
+int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream);
+
+/* One tracer_2d call on device data (nsplt = q_split; q_split must be > 0). */
+int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream);
+/* Remap every tracer from the Lagrangian levels of DELP_OUT to ak + bk*ps. */
+int fv3g_remap_batched(fv3g_state* st, void* stream);
+/* tracer_2d + remap; with use_graph the step is captured once as a CUDA graph
+ * and replayed on later calls with the same q_split. */
+int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream);
+/* Compensated FP64 global tracer mass sum(q*delp*area) over 6 tiles, per
+ * tracer, of the field (FV3G_FIELD_Q with DELP, or Q_REMAPPED with the
+ * remapped thickness).  Writes nq doubles to host_out. */
+int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream);
+/* Sticky device error word of the state (0 = none); cleared by reading. */
+int fv3g_state_error(fv3g_state* st, int* code);
+/* Device pointer and element strides of a field (for zero-copy harnesses). */
+int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FV3G_H */

@@ -1,0 +1,792 @@
+// fv3_oracle.cpp -- FP64 CPU restatement of the FV3 tracer-transport path.
+//
+// TEST INFRASTRUCTURE ONLY (the checker for the CUDA path).  See fv3_oracle.h
+// for the method references and the parity status (unpinned: the upstream
+// Fortran is an empty submodule in the reference tree, .gitmodules:1-4).
+//
+// The PPM core is a template on the tracer scalar type so that the same code,
+// instantiated with a dual number, yields the tangent-linear model with every
+// limiter branch frozen at the trajectory.
+#include "fv3_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- scalars ---
+struct Dual {  // value + tangent; comparisons act on the value only
+  double v, d;
+  Dual() : v(0), d(0) {}
+  Dual(double a) : v(a), d(0) {}
+  Dual(double a, double b) : v(a), d(b) {}
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline double val(double a) { return a; }
+inline double val(const Dual& a) { return a.v; }
+template <class T> inline T tmin(T a, T b) { return val(b) < val(a) ? b : a; }
+template <class T> inline T tmax(T a, T b) { return val(b) > val(a) ? b : a; }
+template <class T> inline T tabs(T a) { return val(a) < 0 ? -a : a; }
+// magnitude of a with the sign of b (b == 0 counts as positive)
+template <class T> inline T tsign(T a, T b) {
+  T m = tabs(a);
+  return val(b) < 0 ? -m : m;
+}
+
+// ------------------------------------------------------------ array views ---
+template <class T>
+struct View2 {  // Fortran-style (i,j) view with explicit lower bounds, i fastest
+  T* p;
+  int ilo, jlo, ni;
+  T& operator()(int i, int j) const { return p[(ptrdiff_t)(i - ilo) + (ptrdiff_t)(j - jlo) * ni]; }
+};
+template <class T> View2<T> v2(T* p, int ilo, int ihi, int jlo) { return View2<T>{p, ilo, jlo, ihi - ilo + 1}; }
+
+// ------------------------------------------------------------ PPM on a line ---
+// Colella & Woodward (1984) eq. 1.10 in perturbation form: bl = aL - q,
+// br = aR - q.  Flatten a cell that is a local extremum; otherwise move the
+// edge value on the overshooting side so that the parabola's extremum sits on
+// the opposite edge.
+template <class T> inline void cw84(T& bl, T& br) {
+  if (val(bl) * val(br) >= 0.0) {
+    bl = T(0.0);
+    br = T(0.0);
+    return;
+  }
+  double t = 3.0 * (val(br) - val(bl)) * (val(bl) + val(br));
+  double d2 = (val(br) - val(bl)) * (val(br) - val(bl));
+  if (-t > d2) {
+    bl = T(-2.0) * br;
+  } else if (t > d2) {
+    br = T(-2.0) * bl;
+  }
+}
+
+template <class T> inline T clamp2(T a, T x0, T x1) {  // a into [min(x0,x1), max(x0,x1)]
+  T lo = tmin(x0, x1), hi = tmax(x0, x1);
+  return tmin(tmax(a, lo), hi);
+}
+
+// Fluxes at faces f in [flo, fhi] (face f separates cells f-1 and f).
+// x(m) for m in [flo-3, fhi+2] via xs(m) = x[m - (flo-3)]; c[f - flo];
+// dxa(m) in the same indexing as x.  eW / eE: tile-edge faces in range, or
+// INT_MIN when the line has none.
+constexpr int kNoEdge = -1000000;
+
+template <class T>
+void ppm_line(int hord, const T* x, const double* c, const double* dxa, int flo, int fhi, int eW,
+              int eE, T* flux) {
+  const int m0 = flo - 3;  // first cell index held in x
+  const int ncell = fhi - flo + 6;
+  auto X = [&](int m) -> const T& { return x[m - m0]; };
+  auto DX = [&](int m) -> double { return dxa[m - m0]; };
+  std::vector<T> bl(ncell), br(ncell);
+  auto BL = [&](int m) -> T& { return bl[m - m0]; };
+  auto BR = [&](int m) -> T& { return br[m - m0]; };
+
+  if (hord == 8) {
+    std::vector<T> dm(ncell), al(ncell + 1);
+    auto DM = [&](int m) -> T& { return dm[m - m0]; };
+    auto AL = [&](int f) -> T& { return al[f - m0]; };
+    for (int m = flo - 2; m <= fhi + 1; ++m) {
+      // monotonized central slope in half-increment form (Lin et al. 1994)
+      T xt = T(0.25) * (X(m + 1) - X(m - 1));
+      T smax = tmax(tmax(X(m - 1), X(m)), X(m + 1)) - X(m);
+      T smin = X(m) - tmin(tmin(X(m - 1), X(m)), X(m + 1));
+      DM(m) = tsign(tmin(tmin(tabs(xt), smax), smin), xt);
+    }
+    for (int f = flo - 1; f <= fhi + 1; ++f)
+      AL(f) = T(0.5) * (X(f - 1) + X(f)) + (DM(f - 1) - DM(f)) * T(1.0 / 3.0);
+    for (int m = flo - 1; m <= fhi; ++m) {
+      // Lin (2004) constraint: |edge deviation| <= |2 dm|, same sign as dm
+      T xt = T(2.0) * DM(m);
+      BL(m) = -tsign(tmin(tabs(xt), tabs(AL(m) - X(m))), xt);
+      BR(m) = tsign(tmin(tabs(xt), tabs(AL(m + 1) - X(m))), xt);
+    }
+  } else {  // hord 5: unlimited fourth-order PPM (linear in x)
+    for (int m = flo - 1; m <= fhi; ++m) {
+      T aL = T(7.0 / 12.0) * (X(m - 1) + X(m)) - T(1.0 / 12.0) * (X(m - 2) + X(m + 1));
+      T aR = T(7.0 / 12.0) * (X(m) + X(m + 1)) - T(1.0 / 12.0) * (X(m - 1) + X(m + 2));
+      BL(m) = aL - X(m);
+      BR(m) = aR - X(m);
+    }
+  }
+
+  // Cube-face edge at face e (Putman & Lin 2007): the edge value is the mean of
+  // the two one-sided linear extrapolations (dxa-weighted) from either face;
+  // the two neighbouring interfaces use one-sided third-order values that do
+  // not reach across the edge.
+  auto edge = [&](int e) {
+    T extL = ((2.0 * DX(e - 1) + DX(e - 2)) * X(e - 1) - DX(e - 1) * X(e - 2)) / (DX(e - 2) + DX(e - 1));
+    T extR = ((2.0 * DX(e) + DX(e + 1)) * X(e) - DX(e) * X(e + 1)) / (DX(e) + DX(e + 1));
+    T a0 = T(0.5) * (extL + extR);
+    T aM = T(-1.0 / 6.0) * X(e - 3) + T(5.0 / 6.0) * X(e - 2) + T(1.0 / 3.0) * X(e - 1);
+    T aP = T(1.0 / 3.0) * X(e) + T(5.0 / 6.0) * X(e + 1) - T(1.0 / 6.0) * X(e + 2);
+    if (hord == 8) {
+      aM = clamp2(aM, X(e - 2), X(e - 1));
+      a0 = clamp2(a0, X(e - 1), X(e));
+      aP = clamp2(aP, X(e), X(e + 1));
+    }
+    int lo = flo - 1, hi = fhi;  // cells whose bl/br feed a flux
+    if (e - 2 >= lo && e - 2 <= hi) BR(e - 2) = aM - X(e - 2);
+    if (e - 1 >= lo && e - 1 <= hi) { BL(e - 1) = aM - X(e - 1); BR(e - 1) = a0 - X(e - 1); }
+    if (e >= lo && e <= hi) { BL(e) = a0 - X(e); BR(e) = aP - X(e); }
+    if (e + 1 >= lo && e + 1 <= hi) BL(e + 1) = aP - X(e + 1);
+    if (hord == 8)
+      for (int m = e - 2; m <= e + 1; ++m)
+        if (m >= lo && m <= hi) cw84(BL(m), BR(m));
+  };
+  if (eW != kNoEdge) edge(eW);
+  if (eE != kNoEdge) edge(eE);
+
+  // upwind integral of the sub-grid parabola over the swept fraction |c|
+  for (int f = flo; f <= fhi; ++f) {
+    double cf = c[f - flo];
+    if (cf > 0.0) {
+      T b0 = BL(f - 1) + BR(f - 1);
+      flux[f - flo] = X(f - 1) + T(1.0 - cf) * (BR(f - 1) - T(cf) * b0);
+    } else {
+      T b0 = BL(f) + BR(f);
+      flux[f - flo] = X(f) + T(1.0 + cf) * (BL(f) + T(cf) * b0);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- corners ---
+// The ng x ng halo block at a cube corner has no cells of its own (three faces
+// meet there).  For a sweep along x the block continues the rows of the halo
+// strip beside it in y; for a sweep along y it continues the columns of the
+// strip beside it in x.  Each corner cell takes the value found by rotating it
+// by +-90 degrees about the cube-corner point into that strip.
+template <class T>
+void copy_corners_t(T* q, int npx, int npy, int dir, const orc_grid* g, const orc_bounds* bd) {
+  if (g->nested) return;
+  View2<T> Q = v2(q, bd->isd, bd->ied, bd->jsd);
+  const int ng = bd->ng;
+  struct Corner { int on; double cx, cy; int su, sv; };  // corner point and quadrant signs
+  const Corner cs[4] = {
+      {g->sw_corner, 0.5, 0.5, -1, -1},
+      {g->se_corner, npx - 0.5, 0.5, +1, -1},
+      {g->nw_corner, 0.5, npy - 0.5, -1, +1},
+      {g->ne_corner, npx - 0.5, npy - 0.5, +1, +1},
+  };
+  for (const Corner& k : cs) {
+    if (!k.on) continue;
+    // source quadrant: same u-sign for x sweeps (the strip beside it in y),
+    // same v-sign for y sweeps (the strip beside it in x)
+    int tu = (dir == 1) ? k.su : -k.su;
+    int tv = (dir == 1) ? -k.sv : k.sv;
+    for (int a = 1; a <= ng; ++a)
+      for (int b = 1; b <= ng; ++b) {
+        double u = k.su * (a - 0.5), v = k.sv * (b - 0.5);
+        double uu, vv;
+        // rotation +90: (u,v)->(-v,u); rotation -90: (u,v)->(v,-u)
+        if ((-v > 0) == (tu > 0) && (u > 0) == (tv > 0)) { uu = -v; vv = u; }
+        else { uu = v; vv = -u; }
+        int i = (int)std::lround(k.cx + u), j = (int)std::lround(k.cy + v);
+        int is = (int)std::lround(k.cx + uu), js = (int)std::lround(k.cy + vv);
+        Q(i, j) = Q(is, js);
+      }
+  }
+}
+
+// ---------------------------------------------------------------- sweeps ---
+// x sweep: fluxes at faces [bd->is, bd->ie+1] for rows [j1, j2].
+template <class T>
+void xppm_t(T* flux /*(is:ie+1, j1:j2)*/, const T* q /*(isd:ied,jsd:jed)*/, const double* c /*(is:ie+1, clo..)*/,
+            int cjlo, int hord, int j1, int j2, int npx, const orc_grid* g, const orc_bounds* bd) {
+  const int is = bd->is, ie = bd->ie;
+  View2<const T> Q{q, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
+  View2<const double> C{c, is, cjlo, ie - is + 2};
+  View2<const double> DXA{g->dxa, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
+  View2<T> F{flux, is, j1, ie - is + 2};
+  int eW = (!g->nested && is == 1) ? 1 : kNoEdge;
+  int eE = (!g->nested && ie + 1 == npx) ? npx : kNoEdge;
+  std::vector<T> line(ie - is + 7), out(ie - is + 2);
+  std::vector<double> cl(ie - is + 2), dl(ie - is + 7);
+  for (int j = j1; j <= j2; ++j) {
+    for (int m = is - 3; m <= ie + 3; ++m) { line[m - is + 3] = Q(m, j); dl[m - is + 3] = DXA(m, j); }
+    for (int f = is; f <= ie + 1; ++f) cl[f - is] = C(f, j);
+    ppm_line<T>(hord, line.data(), cl.data(), dl.data(), is, ie + 1, eW, eE, out.data());
+    for (int f = is; f <= ie + 1; ++f) F(f, j) = out[f - is];
+  }
+}
+
+// y sweep: fluxes at faces [bd->js, bd->je+1] for columns [i1, i2].
+template <class T>
+void yppm_t(T* flux /*(i1:i2, js:je+1)*/, const T* q, const double* c /*(cilo.., js:je+1)*/, int cilo,
+            int cni, int hord, int i1, int i2, int npy, const orc_grid* g, const orc_bounds* bd) {
+  const int js = bd->js, je = bd->je;
+  View2<const T> Q{q, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
+  View2<const double> C{c, cilo, js, cni};
+  View2<const double> DYA{g->dya, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
+  View2<T> F{flux, i1, js, i2 - i1 + 1};
+  int eS = (!g->nested && js == 1) ? 1 : kNoEdge;
+  int eN = (!g->nested && je + 1 == npy) ? npy : kNoEdge;
+  std::vector<T> line(je - js + 7), out(je - js + 2);
+  std::vector<double> cl(je - js + 2), dl(je - js + 7);
+  for (int i = i1; i <= i2; ++i) {
+    for (int m = js - 3; m <= je + 3; ++m) { line[m - js + 3] = Q(i, m); dl[m - js + 3] = DYA(i, m); }
+    for (int f = js; f <= je + 1; ++f) cl[f - js] = C(i, f);
+    ppm_line<T>(hord, line.data(), cl.data(), dl.data(), js, je + 1, eS, eN, out.data());
+    for (int f = js; f <= je + 1; ++f) F(i, f) = out[f - js];
+  }
+}
+
+// fv_tp_2d: Lin & Rood inner/outer operators.  q's corner halo is modified.
+template <class T>
+void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, int hord, T* fx, T* fy,
+                const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
+                const double* ra_x, const double* ra_y, const double* mfx, const double* mfy) {
+  const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je;
+  const int isd = bd->isd, ied = bd->ied, jsd = bd->jsd, jed = bd->jed;
+  const int nid = ied - isd + 1;
+  View2<T> Q{q, isd, jsd, nid};
+  View2<const double> AREA{g->area, isd, jsd, nid};
+  View2<const double> XFX{xfx, is, jsd, ie - is + 2};
+  View2<const double> YFX{yfx, isd, js, nid};
+  View2<const double> RAX{ra_x, is, jsd, ie - is + 1};
+  View2<const double> RAY{ra_y, isd, js, nid};
+
+  // inner y operator on every column of the data domain, then outer x
+  copy_corners_t<T>(q, npx, npy, 2, g, bd);
+  std::vector<T> fy2((size_t)nid * (je - js + 2));
+  yppm_t<T>(fy2.data(), q, cry, isd, nid, hord, isd, ied, npy, g, bd);
+  View2<T> FY2{fy2.data(), isd, js, nid};
+  std::vector<T> qi((size_t)nid * (jed - jsd + 1));
+  View2<T> QI{qi.data(), isd, jsd, nid};
+  for (int j = js; j <= je; ++j)
+    for (int i = isd; i <= ied; ++i)
+      QI(i, j) = (Q(i, j) * T(AREA(i, j)) + T(YFX(i, j)) * FY2(i, j) - T(YFX(i, j + 1)) * FY2(i, j + 1)) /
+                 T(RAY(i, j));
+  xppm_t<T>(fx, qi.data(), crx, jsd, hord, js, je, npx, g, bd);
+
+  // inner x operator on every row of the data domain, then outer y
+  copy_corners_t<T>(q, npx, npy, 1, g, bd);
+  std::vector<T> fx2((size_t)(ie - is + 2) * (jed - jsd + 1));
+  xppm_t<T>(fx2.data(), q, crx, jsd, hord, jsd, jed, npx, g, bd);
+  View2<T> FX2{fx2.data(), is, jsd, ie - is + 2};
+  std::vector<T> qj((size_t)nid * (jed - jsd + 1));
+  View2<T> QJ{qj.data(), isd, jsd, nid};
+  for (int j = jsd; j <= jed; ++j)
+    for (int i = is; i <= ie; ++i)
+      QJ(i, j) = (Q(i, j) * T(AREA(i, j)) + T(XFX(i, j)) * FX2(i, j) - T(XFX(i + 1, j)) * FX2(i + 1, j)) /
+                 T(RAX(i, j));
+  yppm_t<T>(fy, qj.data(), cry, isd, nid, hord, is, ie, npy, g, bd);
+
+  View2<T> FX{fx, is, js, ie - is + 2};
+  View2<T> FY{fy, is, js, ie - is + 1};
+  for (int j = js; j <= je; ++j)
+    for (int i = is; i <= ie + 1; ++i) {
+      double w = mfx ? View2<const double>{mfx, is, js, ie - is + 2}(i, j) : XFX(i, j);
+      FX(i, j) = T(0.5) * (FX(i, j) + FX2(i, j)) * T(w);
+    }
+  for (int j = js; j <= je + 1; ++j)
+    for (int i = is; i <= ie; ++i) {
+      double w = mfy ? View2<const double>{mfy, is, js, ie - is + 1}(i, j) : YFX(i, j);
+      FY(i, j) = T(0.5) * (FY(i, j) + FY2(i, j)) * T(w);
+    }
+}
+
+// --------------------------------------------------------- tracer_2d parts ---
+struct Level {  // per-level work arrays of tracer_2d
+  std::vector<double> xfx, yfx, rax, ray, dp2;
+};
+
+// Area fluxes from Courant numbers (upwind metric), as tracer_2d does.
+void area_fluxes(const double* cx, const double* cy, double* xfx, double* yfx, const orc_grid* g,
+                 const orc_bounds* bd) {
+  const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je;
+  const int isd = bd->isd, ied = bd->ied, jsd = bd->jsd, jed = bd->jed;
+  const int nid = ied - isd + 1;
+  View2<const double> DXA{g->dxa, isd, jsd, nid}, DYA{g->dya, isd, jsd, nid};
+  View2<const double> DX{g->dx, isd, jsd, nid}, DY{g->dy, isd, jsd, nid + 1};
+  const size_t plane = (size_t)nid * (jed - jsd + 1);
+  auto SIN = [&](int i, int j, int s) { return g->sin_sg[(size_t)(s - 1) * plane + (i - isd) + (size_t)(j - jsd) * nid]; };
+  View2<const double> CX{cx, is, jsd, ie - is + 2}, CY{cy, isd, js, nid};
+  View2<double> XF{xfx, is, jsd, ie - is + 2}, YF{yfx, isd, js, nid};
+  for (int j = jsd; j <= jed; ++j)
+    for (int i = is; i <= ie + 1; ++i) {
+      double c = CX(i, j);
+      XF(i, j) = c > 0.0 ? c * DXA(i - 1, j) * DY(i, j) * SIN(i - 1, j, 3) : c * DXA(i, j) * DY(i, j) * SIN(i, j, 1);
+    }
+  for (int j = js; j <= je + 1; ++j)
+    for (int i = isd; i <= ied; ++i) {
+      double c = CY(i, j);
+      YF(i, j) = c > 0.0 ? c * DYA(i, j - 1) * DX(i, j) * SIN(i, j - 1, 4) : c * DYA(i, j) * DX(i, j) * SIN(i, j, 2);
+    }
+}
+
+struct Dom {  // convenience sizes of one domain
+  int is, ie, js, je, isd, ied, jsd, jed, nid, njd;
+  size_t plane, nxf, nyf, nmx, nmy;
+  explicit Dom(const orc_bounds* b)
+      : is(b->is), ie(b->ie), js(b->js), je(b->je), isd(b->isd), ied(b->ied), jsd(b->jsd), jed(b->jed) {
+    nid = ied - isd + 1;
+    njd = jed - jsd + 1;
+    plane = (size_t)nid * njd;
+    nxf = (size_t)(ie - is + 2) * njd;           // cx, xfx
+    nyf = (size_t)nid * (je - js + 2);           // cy, yfx
+    nmx = (size_t)(ie - is + 2) * (je - js + 1); // mfx, fx
+    nmy = (size_t)(ie - is + 1) * (je - js + 2); // mfy, fy
+  }
+};
+
+double max_courant(const double* cx, const double* cy, const Dom& d, int npz) {
+  double cmax = 0.0;
+  for (int k = 0; k < npz; ++k) {
+    View2<const double> CX{cx + k * d.nxf, d.is, d.jsd, d.ie - d.is + 2};
+    View2<const double> CY{cy + k * d.nyf, d.isd, d.js, d.nid};
+    for (int j = d.js; j <= d.je; ++j)
+      for (int i = d.is; i <= d.ie; ++i) cmax = std::max(cmax, std::max(std::fabs(CX(i, j)), std::fabs(CY(i, j))));
+  }
+  return cmax;
+}
+
+void scale_fluxes(double* mfx, double* mfy, double* cx, double* cy, const Dom& d, int npz, double frac) {
+  for (size_t n = 0; n < d.nxf * npz; ++n) cx[n] *= frac;
+  for (size_t n = 0; n < d.nyf * npz; ++n) cy[n] *= frac;
+  for (size_t n = 0; n < d.nmx * npz; ++n) mfx[n] *= frac;
+  for (size_t n = 0; n < d.nmy * npz; ++n) mfy[n] *= frac;
+}
+
+// dp2, ra_x, ra_y of level k
+void level_setup(Level& L, const double* dp1k, const double* mfxk, const double* mfyk, const orc_grid* g,
+                 const Dom& d) {
+  View2<const double> AREA{g->area, d.isd, d.jsd, d.nid}, RAREA{g->rarea, d.isd, d.jsd, d.nid};
+  View2<const double> XF{L.xfx.data(), d.is, d.jsd, d.ie - d.is + 2}, YF{L.yfx.data(), d.isd, d.js, d.nid};
+  View2<const double> MX{mfxk, d.is, d.js, d.ie - d.is + 2}, MY{mfyk, d.is, d.js, d.ie - d.is + 1};
+  View2<const double> DP{dp1k, d.isd, d.jsd, d.nid};
+  L.rax.assign((size_t)(d.ie - d.is + 1) * d.njd, 0.0);
+  L.ray.assign((size_t)d.nid * (d.je - d.js + 1), 0.0);
+  L.dp2.assign(d.plane, 0.0);
+  View2<double> RX{L.rax.data(), d.is, d.jsd, d.ie - d.is + 1}, RY{L.ray.data(), d.isd, d.js, d.nid};
+  View2<double> D2{L.dp2.data(), d.isd, d.jsd, d.nid};
+  for (int j = d.js; j <= d.je; ++j)
+    for (int i = d.is; i <= d.ie; ++i)
+      D2(i, j) = DP(i, j) + (MX(i, j) - MX(i + 1, j) + MY(i, j) - MY(i, j + 1)) * RAREA(i, j);
+  for (int j = d.jsd; j <= d.jed; ++j)
+    for (int i = d.is; i <= d.ie; ++i) RX(i, j) = AREA(i, j) + XF(i, j) - XF(i + 1, j);
+  for (int j = d.js; j <= d.je; ++j)
+    for (int i = d.isd; i <= d.ied; ++i) RY(i, j) = AREA(i, j) + YF(i, j) - YF(i, j + 1);
+}
+
+// flux-form update of the compute domain
+void flux_update(double* qk, const double* dp1k, const Level& L, const double* fx, const double* fy,
+                 const orc_grid* g, const Dom& d) {
+  View2<double> Q{qk, d.isd, d.jsd, d.nid};
+  View2<const double> DP{dp1k, d.isd, d.jsd, d.nid}, D2{L.dp2.data(), d.isd, d.jsd, d.nid};
+  View2<const double> RAREA{g->rarea, d.isd, d.jsd, d.nid};
+  View2<const double> FX{fx, d.is, d.js, d.ie - d.is + 2}, FY{fy, d.is, d.js, d.ie - d.is + 1};
+  for (int j = d.js; j <= d.je; ++j)
+    for (int i = d.is; i <= d.ie; ++i)
+      Q(i, j) = (Q(i, j) * DP(i, j) + (FX(i, j) - FX(i + 1, j) + FY(i, j) - FY(i, j + 1)) * RAREA(i, j)) / D2(i, j);
+}
+
+// ------------------------------------------------------------------ remap ---
+// Column reconstruction.  Interface values come from the C1 ("cubic-spline")
+// condition: the sub-grid parabolas of adjacent layers have equal slopes at
+// their shared interface, which on layers of thickness h_{k-1}, h_k gives
+//   a_{k-1} + 2(1+d) a_k + d a_{k+1} = 3 (q_{k-1} + d q_k),   d = h_{k-1}/h_k.
+// The top and bottom rows require the outermost interface pair to agree with
+// one parabola through the two outermost layer means (exact for quadratics).
+// iv == -2 replaces the bottom row by a_km = qs.  Constraints:
+//   kord 9: every interface value is clamped to the range of its two adjacent
+//           layer means (boundary interfaces: the two outermost means), then
+//           the CW84 cell constraint -- monotone, no new extrema;
+//   kord 4: no clamp; edge values floored at the iv floor (iv >= 0), then CW84.
+template <class T>
+void column_profile_t(const T* q, const double* dp, int km, int iv, int kord, double qs, double q_min,
+                      T* aL, T* aR, T* a6) {
+  std::vector<T> a(km + 1), rhs(km + 1);
+  std::vector<double> cp(km + 1), lo(km + 1), di(km + 1), up(km + 1);
+  if (km == 1) {
+    a[0] = q[0];
+    a[1] = q[0];
+  } else {
+    double g = dp[1] / dp[0];
+    di[0] = g; up[0] = g + 1.0; lo[0] = 0.0;
+    rhs[0] = (T(g * (2.0 * g + 3.0)) * q[0] + q[1]) / T(g + 1.0);
+    for (int k = 1; k < km; ++k) {
+      double d = dp[k - 1] / dp[k];
+      lo[k] = 1.0; di[k] = 2.0 * (1.0 + d); up[k] = d;
+      rhs[k] = T(3.0) * (q[k - 1] + T(d) * q[k]);
+    }
+    if (iv == -2) {
+      lo[km] = 0.0; di[km] = 1.0; up[km] = 0.0;
+      rhs[km] = T(qs);
+    } else {
+      double gb = dp[km - 2] / dp[km - 1];
+      lo[km] = gb + 1.0; di[km] = gb; up[km] = 0.0;
+      rhs[km] = (T(gb * (2.0 * gb + 3.0)) * q[km - 1] + q[km - 2]) / T(gb + 1.0);
+    }
+    // Thomas algorithm
+    cp[0] = up[0] / di[0];
+    a[0] = rhs[0] / T(di[0]);
+    for (int k = 1; k <= km; ++k) {
+      double den = di[k] - lo[k] * cp[k - 1];
+      cp[k] = up[k] / den;
+      a[k] = (rhs[k] - T(lo[k]) * a[k - 1]) / T(den);
+    }
+    for (int k = km - 1; k >= 0; --k) a[k] = a[k] - T(cp[k]) * a[k + 1];
+  }
+  const double floor_v = (iv == 1) ? q_min : 0.0;
+  if (kord == 9 && km > 1) {
+    a[0] = clamp2(a[0], q[0], q[1]);
+    for (int k = 1; k < km; ++k) a[k] = clamp2(a[k], q[k - 1], q[k]);
+    if (iv != -2) a[km] = clamp2(a[km], q[km - 2], q[km - 1]);
+  }
+  for (int k = 0; k < km; ++k) {
+    T l = a[k], r = a[k + 1];
+    if (kord != 9 && iv >= 0) {
+      l = tmax(l, T(floor_v));
+      r = tmax(r, T(floor_v));
+    }
+    T bl = l - q[k], br = r - q[k];
+    cw84(bl, br);
+    aL[k] = q[k] + bl;
+    aR[k] = q[k] + br;
+    a6[k] = T(-3.0) * (bl + br);
+  }
+}
+
+// mean of the parabola of layer k over [x1, x2] (fractions of the layer)
+template <class T> inline T pmean(const T& l, const T& r, const T& s6, double x1, double x2) {
+  return l + T(0.5 * (x1 + x2)) * ((r - l) + s6) - s6 * T((x2 * x2 + x1 * x2 + x1 * x1) / 3.0);
+}
+
+// Conservative remap of one column (merge of the two sorted interface lists).
+template <class T>
+void remap_column_t(int km, const double* pe1, const T* q1, double qs, int kn, const double* pe2, T* q2,
+                    int iv, int kord, double q_min) {
+  std::vector<double> dp(km);
+  for (int k = 0; k < km; ++k) dp[k] = pe1[k + 1] - pe1[k];
+  std::vector<T> aL(km), aR(km), a6(km);
+  column_profile_t<T>(q1, dp.data(), km, iv, kord, qs, q_min, aL.data(), aR.data(), a6.data());
+  int k1 = 0;
+  for (int k2 = 0; k2 < kn; ++k2) {
+    const double top = pe2[k2], bot = pe2[k2 + 1];
+    while (k1 < km - 1 && pe1[k1 + 1] <= top) ++k1;
+    if (bot <= pe1[k1 + 1]) {  // inside one source layer
+      if (top == pe1[k1] && bot == pe1[k1 + 1]) {
+        q2[k2] = q1[k1];
+      } else {
+        double x1 = (top - pe1[k1]) / dp[k1], x2 = (bot - pe1[k1]) / dp[k1];
+        q2[k2] = pmean(aL[k1], aR[k1], a6[k1], x1, x2);
+      }
+      continue;
+    }
+    T mass;
+    if (top == pe1[k1]) {
+      mass = q1[k1] * T(dp[k1]);
+    } else {
+      double x1 = (top - pe1[k1]) / dp[k1];
+      mass = T(dp[k1] * (1.0 - x1)) * pmean(aL[k1], aR[k1], a6[k1], x1, 1.0);
+    }
+    int m = k1 + 1;
+    while (m < km && pe1[m + 1] <= bot) {
+      mass = mass + q1[m] * T(dp[m]);
+      ++m;
+    }
+    if (m < km) {
+      if (bot > pe1[m]) {
+        double x2 = (bot - pe1[m]) / dp[m];
+        mass = mass + T(dp[m] * x2) * pmean(aL[m], aR[m], a6[m], 0.0, x2);
+      }
+    } else if (bot > pe1[km]) {  // below the source column: constant extension
+      mass = mass + q1[km - 1] * T(bot - pe1[km]);
+    }
+    q2[k2] = mass / T(bot - top);
+    k1 = std::min(m, km - 1);
+  }
+}
+
+}  // namespace
+
+// =================================================================== C ABI ===
+extern "C" {
+
+void orc_copy_corners(double* q, int npx, int npy, int dir, const orc_grid* g, const orc_bounds* bd) {
+  copy_corners_t<double>(q, npx, npy, dir, g, bd);
+}
+
+void orc_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord, double* fx,
+                  double* fy, const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
+                  const double* ra_x, const double* ra_y, const double* mfx, const double* mfy) {
+  fv_tp_2d_t<double>(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, g, bd, ra_x, ra_y, mfx, mfy);
+}
+
+void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const double* cry, int npx,
+                     int npy, int hord, double* dfx, double* dfy, const double* xfx, const double* yfx,
+                     const orc_grid* g, const orc_bounds* bd, const double* ra_x, const double* ra_y,
+                     const double* mfx, const double* mfy) {
+  Dom d(bd);
+  std::vector<Dual> qq(d.plane), fx(d.nmx), fy(d.nmy);
+  for (size_t n = 0; n < d.plane; ++n) qq[n] = Dual(q[n], dq[n]);
+  fv_tp_2d_t<Dual>(qq.data(), crx, cry, npx, npy, hord, fx.data(), fy.data(), xfx, yfx, g, bd, ra_x, ra_y, mfx,
+                   mfy);
+  for (size_t n = 0; n < d.nmx; ++n) dfx[n] = fx[n].d;
+  for (size_t n = 0; n < d.nmy; ++n) dfy[n] = fy[n].d;
+}
+
+int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
+                  const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
+                  orc_halo_fn halo_fn, void* halo_ctx) {
+  (void)dt;
+  Dom d(bd);
+  std::vector<double> xfx(d.nxf * npz), yfx(d.nyf * npz);
+  for (int k = 0; k < npz; ++k) area_fluxes(cx + k * d.nxf, cy + k * d.nyf, xfx.data() + k * d.nxf,
+                                            yfx.data() + k * d.nyf, g, bd);
+  int nsplt = q_split > 0 ? q_split : (int)(1.0 + max_courant(cx, cy, d, npz));
+  if (nsplt != 1) {
+    double frac = 1.0 / nsplt;
+    scale_fluxes(mfx, mfy, cx, cy, d, npz, frac);
+    for (auto& v : xfx) v *= frac;
+    for (auto& v : yfx) v *= frac;
+  }
+  std::vector<double> fx(d.nmx), fy(d.nmy);
+  for (int it = 0; it < nsplt; ++it) {
+    if (halo_fn) halo_fn(q, nq, npz, halo_ctx);
+#pragma omp parallel for schedule(dynamic) firstprivate(fx, fy)
+    for (int k = 0; k < npz; ++k) {
+      Level L;
+      L.xfx.assign(xfx.begin() + k * d.nxf, xfx.begin() + (k + 1) * d.nxf);
+      L.yfx.assign(yfx.begin() + k * d.nyf, yfx.begin() + (k + 1) * d.nyf);
+      level_setup(L, dp1 + k * d.plane, mfx + k * d.nmx, mfy + k * d.nmy, g, d);
+      for (int iq = 0; iq < nq; ++iq) {
+        double* qk = q + ((size_t)iq * npz + k) * d.plane;
+        fv_tp_2d_t<double>(qk, cx + k * d.nxf, cy + k * d.nyf, npx, npy, hord, fx.data(), fy.data(), L.xfx.data(),
+                           L.yfx.data(), g, bd, L.rax.data(), L.ray.data(), mfx + k * d.nmx, mfy + k * d.nmy);
+        flux_update(qk, dp1 + k * d.plane, L, fx.data(), fy.data(), g, d);
+      }
+      if (it < nsplt - 1) {
+        View2<double> DP{dp1 + k * d.plane, d.isd, d.jsd, d.nid};
+        View2<const double> D2{L.dp2.data(), d.isd, d.jsd, d.nid};
+        for (int j = d.js; j <= d.je; ++j)
+          for (int i = d.is; i <= d.ie; ++i) DP(i, j) = D2(i, j);
+      }
+    }
+  }
+  return nsplt;
+}
+
+// Edge halo strips of six tiles from their neighbours' interiors.
+void orc_cube_halo_fill(double* q, int n, int ng, int nplanes, const int* topo) {
+  const int nid = n + 2 * ng;
+  const size_t plane = (size_t)nid * nid;
+  auto at = [&](int t, int p, int i, int j) -> double& {  // i, j 1-based tile indices
+    return q[((size_t)t * nplanes + p) * plane + (size_t)(i - 1 + ng) + (size_t)(j - 1 + ng) * nid];
+  };
+#pragma omp parallel for schedule(static)
+  for (int p = 0; p < nplanes; ++p)
+    for (int t = 0; t < 6; ++t)
+      for (int e = 0; e < 4; ++e) {
+        const int nt = topo[(t * 4 + e) * 3 + 0], ne = topo[(t * 4 + e) * 3 + 1], rev = topo[(t * 4 + e) * 3 + 2];
+        for (int dpt = 1; dpt <= ng; ++dpt)
+          for (int s = 0; s < n; ++s) {
+            int i, j;  // halo cell on tile t
+            switch (e) {
+              case 0: i = 1 - dpt; j = s + 1; break;
+              case 1: i = n + dpt; j = s + 1; break;
+              case 2: i = s + 1; j = 1 - dpt; break;
+              default: i = s + 1; j = n + dpt; break;
+            }
+            int sb = rev ? n - 1 - s : s, ib, jb;  // interior cell on tile nt
+            switch (ne) {
+              case 0: ib = dpt; jb = sb + 1; break;
+              case 1: ib = n + 1 - dpt; jb = sb + 1; break;
+              case 2: ib = sb + 1; jb = dpt; break;
+              default: ib = sb + 1; jb = n + 1 - dpt; break;
+            }
+            at(t, p, i, j) = at(nt, p, ib, jb);
+          }
+      }
+}
+
+int orc_tracer_2d_cube(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                       const orc_grid* g6, int n, int npz, int nq, int hord, int q_split, const int* topo,
+                       int sync_edges) {
+  const int ng = 3;
+  orc_bounds bd{1, n, 1, n, 1 - ng, n + ng, 1 - ng, n + ng, ng};
+  Dom d(&bd);
+  const int npx = n + 1, npy = n + 1;
+  std::vector<double> xfx(6 * d.nxf * npz), yfx(6 * d.nyf * npz);
+  double cmax = 0.0;
+  for (int t = 0; t < 6; ++t) {
+    for (int k = 0; k < npz; ++k)
+      area_fluxes(cx + (t * npz + k) * d.nxf, cy + (t * npz + k) * d.nyf, xfx.data() + (t * npz + k) * d.nxf,
+                  yfx.data() + (t * npz + k) * d.nyf, &g6[t], &bd);
+    cmax = std::max(cmax, max_courant(cx + t * npz * d.nxf, cy + t * npz * d.nyf, d, npz));
+  }
+  int nsplt = q_split > 0 ? q_split : (int)(1.0 + cmax);
+  if (nsplt != 1) {
+    double frac = 1.0 / nsplt;
+    for (int t = 0; t < 6; ++t)
+      scale_fluxes(mfx + t * npz * d.nmx, mfy + t * npz * d.nmy, cx + t * npz * d.nxf, cy + t * npz * d.nyf, d,
+                   npz, frac);
+    for (auto& v : xfx) v *= frac;
+    for (auto& v : yfx) v *= frac;
+  }
+  // edge outflux of each tile-edge face: eflux[((t*4+e)*n + s)]
+  for (int it = 0; it < nsplt; ++it) {
+    orc_cube_halo_fill(q, n, ng, npz * nq, topo);
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < npz; ++k) {
+      Level L[6];
+      std::vector<double> fx(6 * d.nmx), fy(6 * d.nmy), ef(6 * 4 * n);
+      for (int t = 0; t < 6; ++t) {
+        L[t].xfx.assign(xfx.begin() + (t * npz + k) * d.nxf, xfx.begin() + (t * npz + k + 1) * d.nxf);
+        L[t].yfx.assign(yfx.begin() + (t * npz + k) * d.nyf, yfx.begin() + (t * npz + k + 1) * d.nyf);
+        level_setup(L[t], dp1 + (t * npz + k) * d.plane, mfx + (t * npz + k) * d.nmx, mfy + (t * npz + k) * d.nmy,
+                    &g6[t], d);
+      }
+      for (int iq = 0; iq < nq; ++iq) {
+        for (int t = 0; t < 6; ++t) {
+          double* qk = q + (((size_t)t * nq + iq) * npz + k) * d.plane;
+          fv_tp_2d_t<double>(qk, cx + (t * npz + k) * d.nxf, cy + (t * npz + k) * d.nyf, npx, npy, hord,
+                             fx.data() + t * d.nmx, fy.data() + t * d.nmy, L[t].xfx.data(), L[t].yfx.data(),
+                             &g6[t], &bd, L[t].rax.data(), L[t].ray.data(), mfx + (t * npz + k) * d.nmx,
+                             mfy + (t * npz + k) * d.nmy);
+        }
+        if (sync_edges) {
+          // outward flux of every tile-edge face, then adopt the owner's value
+          auto FX = [&](int t, int i, int j) -> double& { return fx[t * d.nmx + (i - 1) + (size_t)(j - 1) * (n + 1)]; };
+          auto FY = [&](int t, int i, int j) -> double& { return fy[t * d.nmy + (i - 1) + (size_t)(j - 1) * n]; };
+          auto out = [&](int t, int e, int s) -> double {
+            switch (e) {
+              case 0: return -FX(t, 1, s + 1);
+              case 1: return FX(t, n + 1, s + 1);
+              case 2: return -FY(t, s + 1, 1);
+              default: return FY(t, s + 1, n + 1);
+            }
+          };
+          for (int t = 0; t < 6; ++t)
+            for (int e = 0; e < 4; ++e)
+              for (int s = 0; s < n; ++s) ef[(t * 4 + e) * n + s] = out(t, e, s);
+          // the face flux is the one computed by the upwind tile (the tile the
+          // flow leaves), so every donor cell's outflow comes from its own
+          // monotone reconstruction; a face with zero Courant number belongs
+          // to the lower-numbered tile
+          for (int t = 0; t < 6; ++t)
+            for (int e = 0; e < 4; ++e) {
+              const int nt = topo[(t * 4 + e) * 3 + 0], ne = topo[(t * 4 + e) * 3 + 1], rev = topo[(t * 4 + e) * 3 + 2];
+              const double* cxt = cx + (t * npz + k) * d.nxf;
+              const double* cyt = cy + (t * npz + k) * d.nyf;
+              for (int s = 0; s < n; ++s) {
+                double cin;  // Courant number into tile t through this face
+                switch (e) {
+                  case 0: cin = cxt[0 + (size_t)(s + 1 - d.jsd) * (n + 1)]; break;
+                  case 1: cin = -cxt[n + (size_t)(s + 1 - d.jsd) * (n + 1)]; break;
+                  case 2: cin = cyt[(s + 1 - d.isd) + 0 * (size_t)d.nid]; break;
+                  default: cin = -cyt[(s + 1 - d.isd) + (size_t)n * d.nid]; break;
+                }
+                if (!(cin > 0.0 || (cin == 0.0 && nt < t))) continue;  // tile t is upwind: keeps its flux
+                double inflow = ef[(nt * 4 + ne) * n + (rev ? n - 1 - s : s)];  // upwind tile's outflux
+                switch (e) {
+                  case 0: FX(t, 1, s + 1) = inflow; break;
+                  case 1: FX(t, n + 1, s + 1) = -inflow; break;
+                  case 2: FY(t, s + 1, 1) = inflow; break;
+                  default: FY(t, s + 1, n + 1) = -inflow; break;
+                }
+              }
+            }
+        }
+        for (int t = 0; t < 6; ++t) {
+          double* qk = q + (((size_t)t * nq + iq) * npz + k) * d.plane;
+          flux_update(qk, dp1 + (t * npz + k) * d.plane, L[t], fx.data() + t * d.nmx, fy.data() + t * d.nmy,
+                      &g6[t], d);
+        }
+      }
+      if (it < nsplt - 1)
+        for (int t = 0; t < 6; ++t) {
+          View2<double> DP{dp1 + (t * npz + k) * d.plane, d.isd, d.jsd, d.nid};
+          View2<const double> D2{L[t].dp2.data(), d.isd, d.jsd, d.nid};
+          for (int j = 1; j <= n; ++j)
+            for (int i = 1; i <= n; ++i) DP(i, j) = D2(i, j);
+        }
+    }
+  }
+  return nsplt;
+}
+
+void orc_column_profile(const double* q, const double* delp, int km, int iv, int kord, double qs, double q_min,
+                        double* a4) {
+  std::vector<double> aL(km), aR(km), a6(km);
+  column_profile_t<double>(q, delp, km, iv, kord, qs, q_min, aL.data(), aR.data(), a6.data());
+  for (int k = 0; k < km; ++k) {
+    a4[4 * k + 0] = q[k];
+    a4[4 * k + 1] = aL[k];
+    a4[4 * k + 2] = aR[k];
+    a4[4 * k + 3] = a6[k];
+  }
+}
+
+void orc_remap_column(int km, const double* pe1, const double* q1, double qs, int kn, const double* pe2, double* q2,
+                      int iv, int kord, double q_min) {
+  remap_column_t<double>(km, pe1, q1, qs, kn, pe2, q2, iv, kord, q_min);
+}
+
+static void map_row(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                    double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord,
+                    double q_min) {
+  const int ni = i2 - i1 + 1;
+  const size_t nib = (size_t)(iend - ibeg + 1), plane = nib * (size_t)(jend - jbeg + 1);
+  std::vector<double> p1(km + 1), p2(kn + 1), c1(km), c2(kn);
+  for (int i = i1; i <= i2; ++i) {
+    for (int k = 0; k <= km; ++k) p1[k] = pe1[(i - i1) + (size_t)k * ni];
+    for (int k = 0; k <= kn; ++k) p2[k] = pe2[(i - i1) + (size_t)k * ni];
+    const size_t off = (size_t)(i - ibeg) + (size_t)(j - jbeg) * nib;
+    for (int k = 0; k < km; ++k) c1[k] = q1[off + k * plane];
+    remap_column_t<double>(km, p1.data(), c1.data(), qs ? qs[i - i1] : 0.0, kn, p2.data(), c2.data(), iv, kord,
+                           q_min);
+    for (int k = 0; k < kn; ++k) q2[off + k * plane] = c2[k];
+  }
+}
+
+void orc_map_scalar(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                    double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord,
+                    double q_min) {
+  map_row(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min);
+}
+
+void orc_map1_ppm(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
+                  double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord) {
+  map_row(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, 0.0);
+}
+
+void orc_remap_columns(int ncol, int km, const double* pe1, const double* q1, const double* qs, int kn,
+                       const double* pe2, double* q2, int iv, int kord, double q_min) {
+#pragma omp parallel
+  {
+    std::vector<double> p1(km + 1), p2(kn + 1), c1(km), c2(kn);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncol; ++c) {
+      for (int k = 0; k <= km; ++k) p1[k] = pe1[c + (size_t)k * ncol];
+      for (int k = 0; k <= kn; ++k) p2[k] = pe2[c + (size_t)k * ncol];
+      for (int k = 0; k < km; ++k) c1[k] = q1[c + (size_t)k * ncol];
+      remap_column_t<double>(km, p1.data(), c1.data(), qs ? qs[c] : 0.0, kn, p2.data(), c2.data(), iv, kord, q_min);
+      for (int k = 0; k < kn; ++k) q2[c + (size_t)k * ncol] = c2[k];
+    }
+  }
+}
+
+double orc_mass_sum(const double* q, const double* dp, const double* area, long n, long narea) {
+  double s = 0.0, comp = 0.0;  // Neumaier
+  for (long i = 0; i < n; ++i) {
+    double x = q[i] * dp[i] * area[i % narea];
+    double t = s + x;
+    if (std::fabs(s) >= std::fabs(x)) comp += (s - t) + x;
+    else comp += (x - t) + s;
+    s = t;
+  }
+  return s + comp;
+}
+
+}  // extern "C"

@@ -1,0 +1,198 @@
+"""ctypes bindings of the FP64 CPU oracle (oracle/fv3_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the checker that the CUDA path is compared against.
+The library is built by ``make -C oracle`` (``build()`` below does it).
+Parity against the upstream Fortran is unpinned (its source is absent).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libfv3oracle.so")
+_lib = None
+
+DP = C.POINTER(C.c_double)
+
+
+class Bounds(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("is_", "ie", "js", "je", "isd", "ied", "jsd", "jed", "ng")]
+
+
+class Grid(C.Structure):
+    _fields_ = [("dx", DP), ("dy", DP), ("dxa", DP), ("dya", DP), ("area", DP), ("rarea", DP), ("sin_sg", DP),
+                ("sw_corner", C.c_int), ("se_corner", C.c_int), ("nw_corner", C.c_int), ("ne_corner", C.c_int),
+                ("nested", C.c_int)]
+
+
+HALO_FN = C.CFUNCTYPE(None, DP, C.c_int, C.c_int, C.c_void_p)
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(
+            os.path.getmtime(os.path.join(_HERE, f)) for f in ("fv3_oracle.cpp", "fv3_oracle.h")):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        L.orc_fv_tp_2d.restype = None
+        L.orc_tracer_2d.restype = C.c_int
+        L.orc_tracer_2d_cube.restype = C.c_int
+        L.orc_mass_sum.restype = C.c_double
+        L.orc_mass_sum.argtypes = [DP, DP, DP, C.c_long, C.c_long]
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(DP)
+
+
+def _f64(a) -> np.ndarray:
+    if hasattr(a, "detach"):
+        a = a.detach().cpu().numpy()
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def bounds_for(n: int, ng: int = 3) -> Bounds:
+    return Bounds(1, n, 1, n, 1 - ng, n + ng, 1 - ng, n + ng, ng)
+
+
+class GridRef:
+    """An orc_grid plus the arrays it points to (kept alive)."""
+
+    def __init__(self, geom, corners=(1, 1, 1, 1), nested=0):
+        self.arrays = [_f64(geom.dx), _f64(geom.dy), _f64(geom.dxa), _f64(geom.dya), _f64(geom.area),
+                       _f64(geom.rarea), _f64(geom.sin_sg)]
+        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested)
+
+
+def copy_corners(q: np.ndarray, n: int, direction: int, geom, ng: int = 3) -> np.ndarray:
+    q = _f64(q).copy()
+    g = GridRef(geom)
+    lib().orc_copy_corners(_p(q), n + 1, n + 1, direction, C.byref(g.struct), C.byref(bounds_for(n, ng)))
+    return q
+
+
+def fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3):
+    """Returns (fx, fy, q_with_corners)."""
+    q = _f64(q).copy()
+    n = q.shape[-1] - 2 * ng
+    fx = np.zeros((n, n + 1))
+    fy = np.zeros((n + 1, n))
+    g = GridRef(geom)
+    arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y)]
+    mx = _f64(mfx) if mfx is not None else None
+    my = _f64(mfy) if mfy is not None else None
+    lib().orc_fv_tp_2d(_p(q), _p(arrs[0]), _p(arrs[1]), n + 1, n + 1, hord, _p(fx), _p(fy), _p(arrs[2]),
+                       _p(arrs[3]), C.byref(g.struct), C.byref(bounds_for(n, ng)), _p(arrs[4]), _p(arrs[5]),
+                       _p(mx) if mx is not None else None, _p(my) if my is not None else None)
+    return fx, fy, q
+
+
+def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3):
+    q = _f64(q)
+    dq = _f64(dq)
+    n = q.shape[-1] - 2 * ng
+    dfx = np.zeros((n, n + 1))
+    dfy = np.zeros((n + 1, n))
+    g = GridRef(geom)
+    arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y)]
+    mx = _f64(mfx) if mfx is not None else None
+    my = _f64(mfy) if mfy is not None else None
+    lib().orc_fv_tp_2d_tl(_p(q), _p(dq), _p(arrs[0]), _p(arrs[1]), n + 1, n + 1, hord, _p(dfx), _p(dfy),
+                          _p(arrs[2]), _p(arrs[3]), C.byref(g.struct), C.byref(bounds_for(n, ng)), _p(arrs[4]),
+                          _p(arrs[5]), _p(mx) if mx is not None else None, _p(my) if my is not None else None)
+    return dfx, dfy
+
+
+def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3):
+    """Single-domain tracer_2d.  q (nq, npz, nd, nd).  Returns (q, dp1, mfx, mfy, cx, cy, nsplt)."""
+    q = _f64(q).copy()
+    dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
+    nq, npz = q.shape[0], q.shape[1]
+    n = q.shape[-1] - 2 * ng
+    g = GridRef(geom)
+    cb = HALO_FN(halo_fn) if halo_fn is not None else HALO_FN()
+    nsplt = lib().orc_tracer_2d(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(g.struct),
+                                C.byref(bounds_for(n, ng)), n + 1, n + 1, npz, nq, hord, q_split, C.c_double(0.0),
+                                cb, None)
+    return q, dp1, mfx, mfy, cx, cy, nsplt
+
+
+def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=True, ng: int = 3):
+    """Six-tile tracer_2d.  q (6, nq, npz, nd, nd).  Returns (q, dp1, nsplt)."""
+    q = _f64(q).copy()
+    dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
+    nq, npz = q.shape[1], q.shape[2]
+    n = q.shape[-1] - 2 * ng
+    refs = [GridRef(g) for g in geoms]
+    arr = (Grid * 6)(*[r.struct for r in refs])
+    topo = np.ascontiguousarray(topo, dtype=np.int32)
+    nsplt = lib().orc_tracer_2d_cube(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), arr, n, npz, nq, hord,
+                                     q_split, topo.ctypes.data_as(C.POINTER(C.c_int)), int(sync_edges))
+    return q, dp1, nsplt
+
+
+def cube_halo_fill(q, n: int, topo, ng: int = 3) -> np.ndarray:
+    q = _f64(q).copy()
+    nplanes = int(np.prod(q.shape[1:-2]))
+    topo = np.ascontiguousarray(topo, dtype=np.int32)
+    lib().orc_cube_halo_fill(_p(q), n, ng, nplanes, topo.ctypes.data_as(C.POINTER(C.c_int)))
+    return q
+
+
+def column_profile(q, delp, iv=0, kord=9, qs=0.0, q_min=0.0) -> np.ndarray:
+    q = _f64(q)
+    delp = _f64(delp)
+    a4 = np.zeros((q.shape[0], 4))
+    lib().orc_column_profile(_p(q), _p(delp), q.shape[0], iv, kord, C.c_double(qs), C.c_double(q_min), _p(a4))
+    return a4
+
+
+def remap_column(pe1, q1, pe2, iv=0, kord=9, qs=0.0, q_min=0.0) -> np.ndarray:
+    pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
+    q2 = np.zeros(pe2.shape[0] - 1)
+    lib().orc_remap_column(q1.shape[0], _p(pe1), _p(q1), C.c_double(qs), q2.shape[0], _p(pe2), _p(q2), iv, kord,
+                           C.c_double(q_min))
+    return q2
+
+
+def remap_columns(pe1, q1, pe2, iv=0, kord=9, qs=None, q_min=0.0) -> np.ndarray:
+    """pe1 (km+1, ncol), q1 (km, ncol), pe2 (kn+1, ncol) -> q2 (kn, ncol)."""
+    pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
+    km, ncol = q1.shape
+    kn = pe2.shape[0] - 1
+    q2 = np.zeros((kn, ncol))
+    qsa = _f64(qs) if qs is not None else None
+    lib().orc_remap_columns(ncol, km, _p(pe1), _p(q1), _p(qsa) if qsa is not None else None, kn, _p(pe2), _p(q2),
+                            iv, kord, C.c_double(q_min))
+    return q2
+
+
+def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min):
+    """Row-wise map_scalar on Fortran-shaped arrays (q1 (km, jdim, idim) C-order == (i,j,k) Fortran)."""
+    pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
+    q2 = _f64(q2).copy()
+    qsa = _f64(qs) if qs is not None else None
+    lib().orc_map_scalar(km, _p(pe1), _p(q1), _p(qsa) if qsa is not None else None, kn, _p(pe2), _p(q2), i1, i2, j,
+                         ibeg, iend, jbeg, jend, iv, kord, C.c_double(q_min))
+    return q2
+
+
+def mass_sum(q, dp, area) -> float:
+    """Neumaier-compensated sum of q*dp*area; q, dp (..., ncell) broadcast area (ncell)."""
+    q, dp, area = _f64(q), _f64(dp), _f64(area)
+    q, dp = np.broadcast_arrays(q, dp)
+    q = np.ascontiguousarray(q)
+    dp = np.ascontiguousarray(dp)
+    return lib().orc_mass_sum(_p(q), _p(dp), _p(area), q.size, area.size)

@@ -1,0 +1,250 @@
+"""GPU parity of the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+Tolerances: FP64 path relative L2 <= 1e-12 per field (bit-for-bit agreement is
+not expected: the kernels multiply by reciprocals and contract FMAs where the
+oracle divides); FP32-mixed path relative L2 <= 1e-5 against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from fv3atm_gb300 import api
+from fv3atm_gb300 import synth as S
+
+from ._helpers import (area_fluxes, cube_mass, final_dp, interior, ra_xy, rel_l2, remap_reference)
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def cube_prob():
+    # n = 60: two full 26-cell CTA tiles plus a partial one per direction
+    return S.make_problem(60, 5, 3, seed=11, cmax=0.8)
+
+
+@pytest.fixture(scope="module")
+def cube_oracle(cube_prob):
+    P = cube_prob
+    q1, dp_last, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=8, q_split=3)
+    dpf = final_dp(dp_last, P.mfx.numpy(), P.mfy.numpy(), P.geoms, ns, P.n)
+    return q1, dpf
+
+
+def _run_cube(P, precision, hord=8, q_split=3, kord=9, remap=False, graph=False, warps=0):
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision, hord=hord, kord=kord, warps_per_cta=warps)
+    st.load_problem(P)
+    if graph:
+        st.step(q_split, use_graph=True)
+    else:
+        st.tracer_2d(q_split)
+        if remap:
+            st.remap()
+    return st
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_cube_tracer_2d_matches_oracle(cuda, cube_prob, cube_oracle, precision, tol):
+    P = cube_prob
+    q_ref, dp_ref = cube_oracle
+    st = _run_cube(P, precision)
+    q = st.download("Q")
+    dp = st.download("DELP_OUT")
+    n = P.n
+    for iq in range(P.nq):
+        e = rel_l2(interior(q[:, iq], n), interior(q_ref[:, iq], n))
+        assert e <= tol, (precision, iq, e)
+    assert rel_l2(interior(dp, n), interior(dp_ref, n)) <= tol
+
+
+@pytest.mark.parametrize("warps", [1, 3])
+def test_cube_warps_per_cta_do_not_change_results(cuda, cube_prob, warps):
+    P = cube_prob
+    a = _run_cube(P, "fp64", warps=warps).download("Q")
+    b = _run_cube(P, "fp64", warps=4).download("Q")
+    assert np.array_equal(interior(a, P.n), interior(b, P.n))
+
+
+def test_cube_hord5_matches_oracle(cuda, cube_prob):
+    P = cube_prob
+    q_ref, _, _ = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=5, q_split=2)
+    q = _run_cube(P, "fp64", hord=5, q_split=2).download("Q")
+    assert rel_l2(interior(q, P.n), interior(q_ref, P.n)) <= FP64_TOL
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_cube_remap_matches_oracle(cuda, cube_prob, cube_oracle, precision, tol):
+    P = cube_prob
+    q_adv, dpf = cube_oracle
+    q_ref, dp2_ref, _, _ = remap_reference(q_adv, dpf, P.ak, P.bk, P.n)
+    st = _run_cube(P, precision, remap=True)
+    q = st.download("Q_REMAPPED")
+    for iq in range(P.nq):
+        e = rel_l2(interior(q[:, iq], P.n), interior(q_ref[:, iq], P.n))
+        assert e <= tol, (precision, iq, e)
+
+
+def test_graph_step_equals_eager_step(cuda, cube_prob):
+    P = cube_prob
+    a = _run_cube(P, "mixed", remap=True).download("Q_REMAPPED")
+    st = _run_cube(P, "mixed", graph=True)
+    b = st.download("Q_REMAPPED")
+    assert np.array_equal(interior(a, P.n), interior(b, P.n))
+    st.step(3, use_graph=True)  # replay
+    assert np.isfinite(st.download("Q")).all()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+def test_cube_conserves_tracer_mass(cuda, cube_prob, precision, tol):
+    P = cube_prob
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    st.load_problem(P)
+    m0 = st.mass("Q")
+    ref0 = cube_mass(P.q.numpy(), P.dp.numpy(), P.geoms, P.n)
+    assert np.allclose(m0, ref0, rtol=1e-13 if precision == "fp64" else 1e-6)
+    st.tracer_2d(3)
+    m1 = st.mass("Q")
+    assert np.all(np.abs(m1 - m0) <= tol * np.abs(m0)), (m0, m1)
+    st.remap()
+    m2 = st.mass("Q_REMAPPED")
+    assert np.all(np.abs(m2 - m0) <= 10 * tol * np.abs(m0)), (m0, m2)
+
+
+def test_cube_monotone_no_new_extrema(cuda, cube_prob):
+    P = cube_prob
+    st = _run_cube(P, "fp64", remap=True)
+    q0 = interior(P.q.numpy(), P.n)
+    q = interior(st.download("Q_REMAPPED"), P.n)
+    for iq in range(P.nq):
+        assert q[:, iq].min() >= q0[:, iq].min() - 1e-14
+        assert q[:, iq].max() <= q0[:, iq].max() + 1e-14
+
+
+# ------------------------------------------------------------ drop-in entries
+def _tile_inputs(P, t=0, k=2, iq=1):
+    g = P.geoms[t]
+    cx, cy = P.cx[t, k].numpy(), P.cy[t, k].numpy()
+    xfx, yfx = area_fluxes(cx, cy, g)
+    rax, ray = ra_xy(xfx, yfx, g)
+    q = np.ascontiguousarray(P.q[t, iq, k].numpy())
+    return g, q, cx, cy, xfx, yfx, rax, ray, P.mfx[t, k].numpy(), P.mfy[t, k].numpy()
+
+
+@pytest.mark.parametrize("hord", [5, 8])
+@pytest.mark.parametrize("with_mass", [True, False])
+def test_fv_tp_2d_dropin_matches_oracle(cuda, cube_prob, hord, with_mass):
+    P = cube_prob
+    g, q, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_inputs(P)
+    mx, my = (mfx, mfy) if with_mass else (None, None)
+    fx_r, fy_r, q_r = O.fv_tp_2d(q, cx, cy, hord, xfx, yfx, g, rax, ray, mx, my)
+    n = P.n
+    fx = np.zeros((n, n + 1))
+    fy = np.zeros((n + 1, n))
+    qg = q.copy()
+    api.fv_tp_2d(qg, cx, cy, n + 1, n + 1, hord, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray,
+                 1.0, mx, my)
+    assert rel_l2(fx, fx_r) <= FP64_TOL
+    assert rel_l2(fy, fy_r) <= FP64_TOL
+    assert np.array_equal(qg, q_r)  # corner blocks rewritten exactly as copy_corners does
+
+
+def test_tracer_2d_dropin_matches_oracle_with_halo_callback(cuda, cube_prob):
+    P = cube_prob
+    t = 2
+    g = P.geoms[t]
+    q0 = np.ascontiguousarray(P.q[t].numpy())          # (nq, npz, nd, nd): halos from the neighbours
+    halo = q0.copy()
+
+    def refresh(qarr):  # stand-in for mpp_update_domains: restore the halo ring
+        n, ng = P.n, 3
+        keep = qarr[..., ng:ng + n, ng:ng + n].copy()
+        qarr[...] = halo
+        qarr[..., ng:ng + n, ng:ng + n] = keep
+
+    args = [np.ascontiguousarray(a[t].numpy()) for a in (P.dp, P.mfx, P.mfy, P.cx, P.cy)]
+    ref = O.tracer_2d(q0, *args, g, hord=8, q_split=3, halo_fn=lambda p, nq, npz, ctx: refresh(
+        np.ctypeslib.as_array(p, shape=q0.shape)))
+    qg = q0.copy()
+    dp, mfx, mfy, cx, cy = (a.copy() for a in args)
+    ns = api.tracer_2d(qg, dp, mfx, mfy, cx, cy, api.GridStruct(g), api.bounds_for(P.n), P.n + 1, P.n + 1, P.npz,
+                       P.nq, 8, 3, P.dt, halo_update=refresh)
+    assert ns == ref[6] == 3
+    assert rel_l2(interior(qg, P.n), interior(ref[0], P.n)) <= FP64_TOL
+    assert rel_l2(interior(dp, P.n), interior(ref[1], P.n)) <= FP64_TOL
+    for got, want in zip((mfx, mfy, cx, cy), ref[2:6]):
+        assert rel_l2(got, want) <= 1e-15
+
+
+def test_tracer_2d_dropin_derives_nsplt(cuda, cube_prob):
+    P = cube_prob
+    t = 0
+    g = P.geoms[t]
+    args = [np.ascontiguousarray(a[t].numpy()) for a in (P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy)]
+    ref = O.tracer_2d(*args, g, hord=8, q_split=0)
+    q, dp, mfx, mfy, cx, cy = (a.copy() for a in args)
+    ns = api.tracer_2d(q, dp, mfx, mfy, cx, cy, api.GridStruct(g), api.bounds_for(P.n), P.n + 1, P.n + 1, P.npz,
+                       P.nq, 8, 0, P.dt)
+    assert ns == ref[6] == 1
+    assert rel_l2(interior(q, P.n), interior(ref[0], P.n)) <= FP64_TOL
+
+
+@pytest.mark.parametrize("kord,iv", [(9, 0), (9, 1), (4, 0), (4, -1), (4, -2)])
+def test_map_scalar_dropin_matches_oracle(cuda, kord, iv):
+    rng = np.random.default_rng(5)
+    from fv3atm_gb300 import grid as G
+    km, ni, nj = 63, 20, 7
+    ak, bk = G.hybrid_levels(km)
+    ps = rng.uniform(95000, 103000, (nj, ni))
+    dref = np.diff(ak)[:, None, None] + np.diff(bk)[:, None, None] * ps[None]
+    dp = dref * (1 + 0.1 * rng.uniform(-1, 1, dref.shape))
+    dp *= dref.sum(0) / dp.sum(0)
+    q1 = np.ascontiguousarray(np.abs(rng.standard_normal((km, nj, ni))) + 0.1)
+    pe1 = np.concatenate([np.full((1, nj, ni), ak[0]), ak[0] + np.cumsum(dp, 0)])
+    pe2 = ak[:, None, None] + bk[:, None, None] * pe1[-1][None]
+    qs = rng.uniform(0, 1, (nj, ni))
+    j = 4
+    p1 = np.ascontiguousarray(pe1[:, j, 2:18])  # (km+1, i1:i2)
+    p2 = np.ascontiguousarray(pe2[:, j, 2:18])
+    qsr = np.ascontiguousarray(qs[j, 2:18])
+    # Fortran bounds: ibeg=1..ni, jbeg=1..nj, i1=3..i2=18, row j+1
+    ref = O.map_scalar(km, p1, q1, qsr, km, p2, np.zeros_like(q1), 3, 18, j + 1, 1, ni, 1, nj, iv, kord, 0.05)
+    got = np.zeros_like(q1)
+    api.map_scalar(km, p1, q1, qsr, km, p2, got, 3, 18, j + 1, 1, ni, 1, nj, iv, kord, 0.05)
+    assert rel_l2(got[:, j, 2:18], ref[:, j, 2:18]) <= FP64_TOL
+    assert np.count_nonzero(got[:, j, :2]) == 0 and np.count_nonzero(got[:, :j]) == 0
+
+
+def test_map_scalar_3d_matches_rows(cuda):
+    rng = np.random.default_rng(9)
+    from fv3atm_gb300 import grid as G
+    km, ni, nj, nq = 32, 12, 5, 2
+    ak, bk = G.hybrid_levels(km)
+    ps = rng.uniform(95000, 103000, (nj, ni))
+    dref = np.diff(ak)[:, None, None] + np.diff(bk)[:, None, None] * ps[None]
+    dp = dref * (1 + 0.1 * rng.uniform(-1, 1, dref.shape))
+    pe1 = np.ascontiguousarray(np.concatenate([np.full((1, nj, ni), ak[0]), ak[0] + np.cumsum(dp, 0)]))
+    pe2 = np.ascontiguousarray(ak[:, None, None] + bk[:, None, None] * pe1[-1][None])
+    q1 = np.ascontiguousarray(rng.uniform(0, 1, (nq, km, nj, ni)))
+    got = np.zeros_like(q1)
+    api.map_scalar_3d(km, pe1, q1, None, km, pe2, got, 1, ni, 1, nj, 1, ni, 1, nj, nq, 0, 9, 0.0)
+    for iq in range(nq):
+        r = O.remap_columns(pe1.reshape(km + 1, -1), q1[iq].reshape(km, -1), pe2.reshape(km + 1, -1), iv=0, kord=9)
+        assert rel_l2(got[iq].reshape(km, -1), r) <= FP64_TOL
+
+
+def test_errors_are_reported_not_fatal(cuda, cube_prob):
+    P = cube_prob
+    g, q, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_inputs(P)
+    n = P.n
+    fx = np.zeros((n, n + 1))
+    fy = np.zeros((n + 1, n))
+    from fv3atm_gb300._lib import Fv3gError
+    with pytest.raises(Fv3gError, match="hord 6"):
+        api.fv_tp_2d(q, cx, cy, n + 1, n + 1, 6, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray)
+    with pytest.raises(Fv3gError, match="nord"):
+        api.fv_tp_2d(q, cx, cy, n + 1, n + 1, 8, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray,
+                     1.0, None, None, 1)
+    with pytest.raises(Fv3gError, match="kord 7"):
+        api.CubeState(P.n, P.npz, P.nq, kord=7)
