@@ -1,0 +1,440 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FV3 tracer-transport path.
+
+Metric: tracer-cell-level updates/s, one update = one tracer value of one cell
+of one level advanced by a full step = tracer_2d (n_split substeps of
+fv_tp_2d + flux-form update) followed by the map_scalar kord=9 remap of every
+tracer onto the hybrid levels.  Workload: six C384 tiles, 127 levels,
+20 tracers, n_split=3, hord_tr=8, kord=9, seeded synthetic fields (no public
+dataset exists for this path): cosine bells / Gaussian blobs with 1 % noise,
+solid-body rotation tilted 45 deg plus a degree-20 spherical-harmonic stream
+function perturbation (10 m/s), max Courant 0.8, Lagrangian delp perturbed
++-10 % per layer with column mass kept, ps in 950-1030 hPa.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Legs (rank 0 prints ONE JSON line): the FP32-mixed path (headline, CUDA
+graph per step), the FP64 path, the mixed-vs-FP64 error per tracer and the
+global mass drift, the end-to-end C-ABI path with pinned host buffers, the
+roofline of the advection substep kernel, and the CPU oracle baseline.
+With N > 1 ranks each GPU advances an independent ensemble member (replicas,
+weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tracer-cell-level updates/s at C384L127: FP32-mix vs FP64 on 1 GB300; % HBM"
+UNIT = "tracer-cell-level updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fv3g", choices=["fv3g", "reference"])
+    ap.add_argument("--n", type=int, default=384)
+    ap.add_argument("--npz", type=int, default=127)
+    ap.add_argument("--nq", type=int, default=20)
+    ap.add_argument("--q-split", type=int, default=3)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def workload(a) -> dict:
+    return {"workload": f"6xC{a.n} L{a.npz} {a.nq} tracers: tracer_2d n_split={a.q_split} hord_tr=8 + map_scalar kord=9",
+            "tiles": 6, "n": a.n, "npz": a.npz, "nq": a.nq, "n_split": a.q_split, "hord": 8, "kord": 9,
+            "l2_policy": "inputs larger than L2 (q alone is 9.3 GB FP32 / 18.5 GB FP64 vs 129 MB L2)"}
+
+
+def alg_bytes(a, s_q: int, s_f: int) -> dict:
+    """Algorithmic HBM bytes (halo cells excluded): per substep launch and per step."""
+    cells = 6 * a.n * a.n * a.npz
+    sub = cells * (a.nq * 2 * s_q + 8 * s_f)      # q in/out + cx,cy,xfx,yfx,mfx,mfy,dp1 in, dp2 out
+    rem = cells * (a.nq * 2 * s_q + 2 * s_f)      # q in/out + delp in, delp out
+    return {"substep": sub, "remap": rem, "step": a.q_split * sub + rem,
+            "per_update": (a.q_split * sub + rem) / (cells * a.nq)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(precision: str):
+    """Per-launch DRAM bytes of the substep kernel at this workload from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "substep_kernel_C384L127x20.txt")
+    try:
+        with open(path) as f:
+            txt = f.read()
+    except OSError:
+        return None
+    m = re.search(rf"traffic_per_launch_{precision}_bytes\s*[:=]\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[2]) for r in rows if re.match(r"^[0-9.]+$", r[2])), default=None)}
+
+
+# ----------------------------------------------------------------- helpers --
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_state(P, precision, nq, npz, n):
+    import torch
+    from fv3atm_gb300 import api
+    st = api.CubeState(n, npz, nq, precision=precision, hord=8, kord=9)
+    st.set_grid(P.geoms)
+    st.set_levels(P.ak, P.bk)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    cur = torch.cuda.current_stream().cuda_stream  # copies are ordered after the conversions
+    for name, val in (("Q", P.q), ("DELP", P.dp), ("CX", P.cx), ("CY", P.cy), ("MFX", P.mfx), ("MFY", P.mfy)):
+        v = val.to(dt).contiguous()
+        st.upload_device(name, v.data_ptr(), stream=cur)
+        torch.cuda.synchronize()
+        del v
+    return st
+
+
+def timed_steps(st, a, world, steps, warmup, stream):
+    """Warm-up, then `steps` graph replays bracketed by barrier + synchronize; per-kernel event times."""
+    import torch
+    st.set_timing(True)
+    for _ in range(warmup):
+        st.step(a.q_split, use_graph=True, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    kern = {}
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            st.step(a.q_split, use_graph=True, stream=stream.cuda_stream)
+            for k, (ms, cnt) in st.kernel_times().items():
+                kms, kc = kern.get(k, (0.0, 0))
+                kern[k] = (kms + ms, kc + cnt)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return max_over_ranks(ms, world), kern
+
+
+def rel_err_per_tracer(x, ref, n):
+    import torch
+    s = slice(3, 3 + n)
+    out = []
+    for iq in range(x.shape[1]):
+        a = x[:, iq, :, s, s].double()
+        b = ref[:, iq, :, s, s].double()
+        out.append(float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b)))
+    return out
+
+
+# ------------------------------------------------------------- CPU oracle --
+def cpu_oracle_rate(n, npz, nq, q_split, seconds, steps=None, warmup=0):
+    """Updates/s of the FP64 C++ oracle (OpenMP, all host threads) on a bounded sample.
+
+    The sample keeps the six C{n} tiles and the workload's generator settings
+    and reduces levels/tracers; `steps` timed steps (or as many as fit in
+    `seconds`) follow `warmup` untimed ones."""
+    import numpy as np
+    import oracle as O
+    from fv3atm_gb300 import synth as S
+    P = S.make_problem(n, npz, nq, seed=4242, cmax=0.8, pert_amp=10.0, dp_noise=0.10, device="cpu")
+    q0, dp, mfx, mfy, cx, cy = (P.q.numpy(), P.dp.numpy(), P.mfx.numpy(), P.mfy.numpy(), P.cx.numpy(),
+                                P.cy.numpy())
+    sl = slice(3, 3 + n)
+
+    def one_step():
+        q1, dp_last, ns = O.tracer_2d_cube(q0, dp, mfx, mfy, cx, cy, P.geoms, P.topo, hord=8, q_split=q_split)
+        fr = 1.0 / ns
+        dpf = dp_last.copy()
+        for t, g in enumerate(P.geoms):
+            mx, my = mfx[t] * fr, mfy[t] * fr
+            dpf[t][:, sl, sl] = dp_last[t][:, sl, sl] + (mx[..., :-1] - mx[..., 1:] + my[..., :-1, :] -
+                                                         my[..., 1:, :]) * g.rarea[sl, sl]
+        dpi = dpf[:, :, sl, sl].transpose(1, 0, 2, 3).reshape(npz, -1)
+        pe1 = np.concatenate([np.full((1, dpi.shape[1]), P.ak[0]), P.ak[0] + np.cumsum(dpi, axis=0)])
+        pe2 = P.ak[:, None] + P.bk[:, None] * pe1[-1][None]
+        for iq in range(nq):
+            O.remap_columns(pe1, q1[:, iq][:, :, sl, sl].transpose(1, 0, 2, 3).reshape(npz, -1), pe2, kord=9)
+
+    for _ in range(warmup):
+        one_step()
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        one_step()
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and done >= steps) or (steps is None and el >= seconds):
+            break
+    upd = 6 * n * n * npz * nq * done
+    return upd / el, {"sample": f"6xC{n} L{npz} {nq} tracers, n_split={q_split}, {done} steps",
+                      "seconds": el, "threads": os.cpu_count()}
+
+
+# ------------------------------------------------------------------- main --
+def run_reference(a, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    npz_s, nq_s = 8, 2  # bounded sample per step: six C384 tiles, 8 levels, 2 tracers
+    rate, info = cpu_oracle_rate(a.n, npz_s, nq_s, a.q_split, 0.0, steps=a.steps, warmup=a.warmup)
+    cfg = workload(a)
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * info["seconds"] / max(a.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": info["sample"] + " (C++ FP64 oracle, OpenMP; the upstream Fortran is absent)"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_setup()
+    if a.impl == "reference":
+        run_reference(a, world, rank)
+        return
+    import numpy as np
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from fv3atm_gb300 import synth as S
+
+    units = 6 * a.n * a.n * a.npz * a.nq  # tracer-cell-levels per step
+    t_gen = time.perf_counter()
+    P = S.make_problem(a.n, a.npz, a.nq, seed=2000 + rank, cmax=0.8, pert_amp=10.0, dp_noise=0.10, device="cuda")
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
+    stream = torch.cuda.Stream()
+    peak, peak_kind = measured_peak()
+    out = {}
+
+    # ---------------------------------------------------- FP64 reference leg
+    ref_q = None
+    if not a.no_fp64:
+        st = build_state(P, "fp64", a.nq, a.npz, a.n)
+        st.step(a.q_split, use_graph=False)
+        ref_q = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float64, device="cuda")
+        st.download_device("Q_REMAPPED", ref_q.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        ms, kern = timed_steps(st, a, world, max(1, a.steps), max(1, min(a.warmup, 3)), stream)
+        out["fp64"] = {"value": world * units * a.steps / (ms / 1e3), "ms_per_step": ms / a.steps,
+                       "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern.items()}}
+        st.close()
+        del st
+        torch.cuda.empty_cache()
+
+    # --------------------------------------------------- mixed headline leg
+    st = build_state(P, "mixed", a.nq, a.npz, a.n)
+    m0 = st.mass("Q")
+    st.step(a.q_split, use_graph=False)
+    m1 = st.mass("Q_REMAPPED")
+    err = None
+    if ref_q is not None:
+        mq = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, device="cuda")
+        st.download_device("Q_REMAPPED", mq.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        err = rel_err_per_tracer(mq, ref_q, a.n)
+        del mq, ref_q
+        torch.cuda.empty_cache()
+    q32 = P.q.to(torch.float32).contiguous()
+    st.upload_device("Q", q32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    del q32
+    with ClockSampler(local) as clk:
+        ms, kern = timed_steps(st, a, world, a.steps, a.warmup, stream)
+    clocks = clk.summary()
+    value = world * units * a.steps / (ms / 1e3)
+    ab = alg_bytes(a, 4, 4)
+    sub_ms, sub_n = kern.get("substep", (0.0, 0))
+    sub_avg = sub_ms / max(sub_n, 1)
+    achieved = ab["substep"] / (sub_avg / 1e3) / 1e9 if sub_avg > 0 else None
+    step_gbs = ab["step"] * a.steps / (ms / 1e3) / 1e9
+    launches = sum(v[1] for v in kern.values())
+
+    # --------------------------------------------------------------- e2e leg
+    e2e = None
+    if not a.no_e2e:
+        fields_in = ["Q", "DELP", "CX", "CY", "MFX", "MFY"]
+        host = {}
+        src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
+        for name in fields_in:
+            h = torch.empty(st.field_shape(name), dtype=torch.float32, pin_memory=True)
+            h.copy_(src[name].to(torch.float32).cpu())
+            host[name] = h
+        hout = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, pin_memory=True)
+        h2d = sum(h.numel() * 4 for h in host.values())
+        d2h = hout.numel() * 4
+        s = stream.cuda_stream
+
+        def e2e_step():
+            for name in fields_in:
+                st.upload_async(name, host[name].data_ptr(), True, s)
+            st.step(a.q_split, use_graph=True, stream=s)
+            st.download_async("Q_REMAPPED", hout.data_ptr(), True, s)
+
+        st.set_timing(False)
+        for _ in range(max(1, min(a.warmup, 2))):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(a.steps):
+                e2e_step()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
+        e2e = {"value": world * units * a.steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": ems / a.steps,
+               "host_dtype": "f32 (as a 32BIT build of the model holds its tracers)",
+               "path": "fv3g_upload_async x6 -> fv3g_step (graph) -> fv3g_download_async"}
+        del host, hout
+    st.close()
+
+    # ---------------------------------------------------------- CPU oracle
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        rate, info = cpu_oracle_rate(a.n, 4, 2, a.q_split, a.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+               "sample": info["sample"] + f", {info['seconds']:.1f} s (C++ FP64 oracle, OpenMP)"}
+
+    if rank != 0:
+        return
+    traffic = committed_traffic("mixed")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 stencils; f64 pe/overlap schedule/mass sums", "data": "synthetic (seeded; no public dataset)",
+        "config": {**workload(a), "precision": "mixed", "replicas": world},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_substep<float,8> (fused fv_tp_2d + flux-form update)",
+                     "alg_bytes_per_launch": ab["substep"], "avg_launch_ms": sub_avg, "peak_kind": peak_kind},
+        "step_hbm": {"alg_bytes_per_update": ab["per_update"], "achieved_gbs": step_gbs, "frac": step_gbs / peak},
+        "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern.items()},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "fp64": out.get("fp64"),
+        "mixed_over_fp64": (value / out["fp64"]["value"]) if "fp64" in out else None,
+        "mixed_rel_l2_vs_fp64_per_tracer": err,
+        "mixed_mass_rel_change_one_step": [float(abs(x - y) / abs(y)) for x, y in zip(m1, m0)],
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "setup_s": {"generate": t_gen},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -167,6 +167,30 @@ class CubeState:
         _lib.call("fv3g_mass_sum", self._h, _lib.FIELDS[field], _p(out), C.c_void_p(stream or 0))
         return out
 
+    # ------------------------------------------------ host copies / timing
+    def upload_async(self, field: str, host_ptr: int, host_f32: bool, stream=None) -> None:
+        _lib.call("fv3g_upload_async", self._h, _lib.FIELDS[field], C.c_void_p(host_ptr), int(host_f32),
+                  C.c_void_p(stream or 0))
+
+    def download_async(self, field: str, host_ptr: int, host_f32: bool, stream=None) -> None:
+        _lib.call("fv3g_download_async", self._h, _lib.FIELDS[field], C.c_void_p(host_ptr), int(host_f32),
+                  C.c_void_p(stream or 0))
+
+    def sync(self, stream=None) -> None:
+        _lib.call("fv3g_stream_sync", self._h, C.c_void_p(stream or 0))
+
+    def set_timing(self, enable: bool) -> None:
+        _lib.call("fv3g_set_timing", self._h, int(enable))
+
+    KERNEL_KINDS = ("prologue", "substep", "edge_fix", "remap")
+
+    def kernel_times(self) -> dict:
+        """{kind: (total ms, launches)} of the last completed step."""
+        ms = (C.c_double * 4)()
+        cnt = (C.c_int * 4)()
+        _lib.call("fv3g_kernel_times", self._h, ms, cnt)
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(self.KERNEL_KINDS)}
+
     def error_code(self) -> int:
         code = C.c_int(0)
         _lib.call("fv3g_state_error", self._h, C.byref(code))

@@ -138,11 +138,40 @@ struct fv3g_state {
   bool levels_set = false;
   cudaGraphExec_t gexec = nullptr;
   int g_qsplit = -1;
+  // optional per-kernel timing: an event is recorded before the step and after
+  // every kernel of it (also inside the captured graph)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ev_kind;  // kernel kind ending at event i (i >= 1)
+  int nev = 0;
   Topo topo{};
   std::vector<void*> allocs;
 };
 
 namespace {
+
+enum { K_PROLOGUE = 0, K_SUBSTEP = 1, K_EDGEFIX = 2, K_REMAP = 3, K_NKINDS = 4 };
+
+// Record a timing event (when enabled) marking the end of a kernel of `kind`.
+int mark(fv3g_state* st, int kind, cudaStream_t s) {
+  if (!st->timing) return 0;
+  if (st->nev >= (int)st->ev.size()) {
+    cudaEvent_t e;
+    FV3G_CUDA(cudaEventCreate(&e));
+    st->ev.push_back(e);
+    st->ev_kind.push_back(kind);
+  }
+  st->ev_kind[st->nev] = kind;
+  // inside stream capture the record must become an event node of the graph
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  FV3G_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap == cudaStreamCaptureStatusActive)
+    FV3G_CUDA(cudaEventRecordWithFlags(st->ev[st->nev], s, cudaEventRecordExternal));
+  else
+    FV3G_CUDA(cudaEventRecord(st->ev[st->nev], s));
+  ++st->nev;
+  return 0;
+}
 
 int dalloc(fv3g_state* st, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes);
@@ -299,6 +328,7 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
                             (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
                             st->n, 1, st->n, 6, st->npz, frac, s));
+  CHECK(mark(st, K_PROLOGUE, s));
   const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 4);
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
@@ -306,7 +336,9 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
     const int dpo = (dpi == 1) ? 2 : 1;
     AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
     CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
+    CHECK(mark(st, K_SUBSTEP, s));
     CHECK(launch_edge_fix<T>(a, st->n, s));
+    CHECK(mark(st, K_EDGEFIX, s));
     st->dp_start = dpi;
     src = dst;
     dpi = dpo;
@@ -343,6 +375,7 @@ int remap_t(fv3g_state* st, cudaStream_t s) {
   r.scratch = (T*)st->rscratch;
   r.sched = st->sched;
   CHECK(launch_remap<T>(r, st->d.kord, s));
+  CHECK(mark(st, K_REMAP, s));
   st->q_cur = 0;
   st->remapped = true;
   return 0;
@@ -446,6 +479,7 @@ int fv3g_state_destroy(fv3g_state* st) {
   if (!st) return 0;
   if (st->stream) cudaStreamSynchronize(st->stream);
   if (st->gexec) cudaGraphExecDestroy(st->gexec);
+  for (cudaEvent_t e : st->ev) cudaEventDestroy(e);
   for (void* p : st->allocs) cudaFree(p);
   if (st->stage) cudaFree(st->stage);
   if (st->stream) cudaStreamDestroy(st->stream);
@@ -581,6 +615,8 @@ int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if (!use_graph) {
+    st->nev = 0;
+    CHECK(mark(st, -1, s));
     CHECK(fv3g_tracer_2d_batched(st, q_split, s));
     return fv3g_remap_batched(st, s);
   }
@@ -594,7 +630,9 @@ int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
     FV3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t g;
     FV3G_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    int rc = fv3g_tracer_2d_batched(st, q_split, cs);
+    st->nev = 0;
+    int rc = mark(st, -1, cs);
+    if (!rc) rc = fv3g_tracer_2d_batched(st, q_split, cs);
     if (!rc) rc = fv3g_remap_batched(st, cs);
     cudaError_t e = cudaStreamEndCapture(cs, &g);
     cudaStreamDestroy(cs);
@@ -645,6 +683,96 @@ int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream) {
   if (rc) return rc;
   FV3G_CUDA(cudaMemcpyAsync(host_out, st->mass_out, sizeof(double) * st->nq, cudaMemcpyDeviceToHost, s));
   FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int fv3g_set_timing(fv3g_state* st, int enable) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (st->timing != (enable != 0) && st->gexec) {  // recapture with/without event nodes
+    cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+  }
+  st->timing = enable != 0;
+  if (st->timing) {
+    // events exist before any capture: a full step records 3 + 2*64 + 1 at most
+    while (st->ev.size() < 2 + 2 * 64 + 2) {
+      cudaEvent_t e;
+      FV3G_CUDA(cudaEventCreate(&e));
+      st->ev.push_back(e);
+      st->ev_kind.push_back(0);
+    }
+  }
+  return 0;
+}
+
+int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind) {
+  if (!st || !ms_by_kind) return set_error(FV3G_E_ARG, "null argument");
+  for (int k = 0; k < K_NKINDS; ++k) {
+    ms_by_kind[k] = 0.0;
+    if (launches_by_kind) launches_by_kind[k] = 0;
+  }
+  if (!st->timing || st->nev < 2) return set_error(FV3G_E_ARG, "no timed step recorded (fv3g_set_timing)");
+  FV3G_CUDA(cudaEventSynchronize(st->ev[st->nev - 1]));
+  for (int i = 1; i < st->nev; ++i) {
+    float ms = 0.f;
+    FV3G_CUDA(cudaEventElapsedTime(&ms, st->ev[i - 1], st->ev[i]));
+    const int kind = st->ev_kind[i];
+    if (kind >= 0 && kind < K_NKINDS) {
+      ms_by_kind[kind] += ms;
+      if (launches_by_kind) launches_by_kind[kind] += 1;
+    }
+  }
+  return 0;
+}
+
+int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32, void* stream) {
+  if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
+  if (field == FV3G_FIELD_Q_REMAPPED || field == FV3G_FIELD_DELP_OUT)
+    return set_error(FV3G_E_ARG, "field %d is an output", field);
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, true));
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  if ((host_f32 != 0) == !st->fp64) {  // same element type: one pitched copy
+    const size_t es = st->esz;
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)host, fs.ni * es, fs.ni, fs.nj);
+    p.dstPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
+                                   st->pg.pitch, st->pg.rows);
+    p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
+    p.kind = cudaMemcpyHostToDevice;
+    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  } else if (!host_f32) {
+    CHECK(upload_t<float>(st, fs, (const double*)host, s));
+  } else {
+    return set_error(FV3G_E_UNSUPPORTED, "FP32 host data into an FP64 state");
+  }
+  if (field == FV3G_FIELD_Q) {
+    st->q_cur = 0;
+    st->remapped = false;
+  }
+  return 0;
+}
+
+int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream) {
+  if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, false));
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
+  const size_t es = st->esz;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
+                                 st->pg.pitch, st->pg.rows);
+  p.dstPtr = make_cudaPitchedPtr(host, fs.ni * es, fs.ni, fs.nj);
+  p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
+  p.kind = cudaMemcpyDeviceToHost;
+  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  return 0;
+}
+
+int fv3g_stream_sync(fv3g_state* st, void* stream) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  FV3G_CUDA(cudaStreamSynchronize(stream ? (cudaStream_t)stream : st->stream));
   return 0;
 }
 

@@ -198,6 +198,20 @@ int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream);
  * tracer, of the field (FV3G_FIELD_Q with DELP, or Q_REMAPPED with the
  * remapped thickness).  Writes nq doubles to host_out. */
 int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream);
+/* Asynchronous copies with the host data type chosen by the caller
+ * (host_f32 = 1: float host arrays, as a 32BIT build of the model holds them;
+ * 0: double).  An FP64 state needs double host data.  Use pinned host memory
+ * for full bandwidth; fv3g_stream_sync waits for them. */
+int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32, void* stream);
+int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream);
+int fv3g_stream_sync(fv3g_state* st, void* stream);
+/* Per-kernel timing of fv3g_step: with timing enabled, CUDA events are
+ * recorded around every kernel of the step (also inside the graph);
+ * fv3g_kernel_times returns, for the last completed step, the summed ms and
+ * the launch count per kernel kind: [0] prologue (area fluxes), [1] advection
+ * substep, [2] tile-edge flux fix, [3] column remap. */
+int fv3g_set_timing(fv3g_state* st, int enable);
+int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind);
 /* Sticky device error word of the state (0 = none); cleared by reading. */
 int fv3g_state_error(fv3g_state* st, int* code);
 /* Device pointer and element strides of a field (for zero-copy harnesses). */
