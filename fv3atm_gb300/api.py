@@ -85,6 +85,15 @@ def map_scalar_3d(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j1, j2, ibeg, iend, jbeg
               jbeg, jend, nq, iv, kord, C.c_double(q_min))
 
 
+def _stream(stream):
+    """C-ABI stream argument: None -> the state's own stream; a CUDA stream
+    handle otherwise.  Handle 0 (torch's default, the legacy NULL stream) is
+    passed as cudaStreamLegacy so that work stays ordered with it."""
+    if stream is None:
+        return C.c_void_p(0)
+    return C.c_void_p(1 if int(stream) == 0 else int(stream))
+
+
 class CubeState:
     """Six tiles x npz levels x nq tracers resident in HBM (fv3g_state)."""
 
@@ -133,10 +142,10 @@ class CubeState:
         return out
 
     def upload_device(self, field: str, dptr: int, stream=None) -> None:
-        _lib.call("fv3g_upload_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), C.c_void_p(stream or 0))
+        _lib.call("fv3g_upload_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), _stream(stream))
 
     def download_device(self, field: str, dptr: int, stream=None) -> None:
-        _lib.call("fv3g_download_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), C.c_void_p(stream or 0))
+        _lib.call("fv3g_download_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), _stream(stream))
 
     def field_shape(self, field: str) -> tuple:
         n, nd, npz, nq = self.n, self.nd, self.npz, self.nq
@@ -154,30 +163,30 @@ class CubeState:
 
     # ------------------------------------------------------------ compute
     def tracer_2d(self, q_split: int, stream=None) -> None:
-        _lib.call("fv3g_tracer_2d_batched", self._h, q_split, C.c_void_p(stream or 0))
+        _lib.call("fv3g_tracer_2d_batched", self._h, q_split, _stream(stream))
 
     def remap(self, stream=None) -> None:
-        _lib.call("fv3g_remap_batched", self._h, C.c_void_p(stream or 0))
+        _lib.call("fv3g_remap_batched", self._h, _stream(stream))
 
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
-        _lib.call("fv3g_step", self._h, q_split, int(use_graph), C.c_void_p(stream or 0))
+        _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))
 
     def mass(self, field: str = "Q", stream=None) -> np.ndarray:
         out = np.zeros(self.nq, dtype=np.float64)
-        _lib.call("fv3g_mass_sum", self._h, _lib.FIELDS[field], _p(out), C.c_void_p(stream or 0))
+        _lib.call("fv3g_mass_sum", self._h, _lib.FIELDS[field], _p(out), _stream(stream))
         return out
 
     # ------------------------------------------------ host copies / timing
     def upload_async(self, field: str, host_ptr: int, host_f32: bool, stream=None) -> None:
         _lib.call("fv3g_upload_async", self._h, _lib.FIELDS[field], C.c_void_p(host_ptr), int(host_f32),
-                  C.c_void_p(stream or 0))
+                  _stream(stream))
 
     def download_async(self, field: str, host_ptr: int, host_f32: bool, stream=None) -> None:
         _lib.call("fv3g_download_async", self._h, _lib.FIELDS[field], C.c_void_p(host_ptr), int(host_f32),
-                  C.c_void_p(stream or 0))
+                  _stream(stream))
 
     def sync(self, stream=None) -> None:
-        _lib.call("fv3g_stream_sync", self._h, C.c_void_p(stream or 0))
+        _lib.call("fv3g_stream_sync", self._h, _stream(stream))
 
     def set_timing(self, enable: bool) -> None:
         _lib.call("fv3g_set_timing", self._h, int(enable))

@@ -279,6 +279,17 @@ int field_shape(fv3g_state* st, int field, FieldShape& fs, bool for_upload) {
   }
 }
 
+// Copy a field between its device planes and a contiguous (nplanes, nj, ni)
+// buffer of the state's element type; to_buf selects the direction.
+int plane_copy(fv3g_state* st, const FieldShape& fs, void* buf, bool to_buf, cudaMemcpyKind kind, cudaStream_t s) {
+  const size_t es = st->esz;
+  char* dev = (char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es;
+  const size_t dp = (size_t)st->pg.pitch * es, ds = (size_t)st->plane * es;
+  const size_t bp = (size_t)fs.ni * es, bs = (size_t)fs.ni * fs.nj * es;
+  if (to_buf) return copy_planes(buf, bp, bs, dev, dp, ds, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s);
+  return copy_planes(dev, dp, ds, buf, bp, bs, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s);
+}
+
 int ensure_stage(fv3g_state* st, size_t bytes) {
   if (st->stage_bytes >= bytes) return 0;
   if (st->stage) cudaFree(st->stage);
@@ -550,16 +561,7 @@ int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream
   FieldShape fs;
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
-  const size_t es = st->esz;
-  {
-    cudaMemcpy3DParms p{};
-    p.srcPtr = make_cudaPitchedPtr((void*)dptr, fs.ni * es, fs.ni, fs.nj);
-    p.dstPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
-                                   st->pg.pitch, st->pg.rows);
-    p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
-    p.kind = cudaMemcpyDeviceToDevice;
-    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
-  }
+  CHECK(plane_copy(st, fs, const_cast<void*>(dptr), false, cudaMemcpyDeviceToDevice, s));
   if (field == FV3G_FIELD_Q) {
     st->q_cur = 0;
     st->remapped = false;
@@ -572,14 +574,7 @@ int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream) {
   FieldShape fs;
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
-  const size_t es = st->esz;
-  cudaMemcpy3DParms p{};
-  p.srcPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
-                                 st->pg.pitch, st->pg.rows);
-  p.dstPtr = make_cudaPitchedPtr(dptr, fs.ni * es, fs.ni, fs.nj);
-  p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
-  p.kind = cudaMemcpyDeviceToDevice;
-  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  CHECK(plane_copy(st, fs, dptr, true, cudaMemcpyDeviceToDevice, s));
   return 0;
 }
 
@@ -733,14 +728,7 @@ int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32,
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) == !st->fp64) {  // same element type: one pitched copy
-    const size_t es = st->esz;
-    cudaMemcpy3DParms p{};
-    p.srcPtr = make_cudaPitchedPtr((void*)host, fs.ni * es, fs.ni, fs.nj);
-    p.dstPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
-                                   st->pg.pitch, st->pg.rows);
-    p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
-    p.kind = cudaMemcpyHostToDevice;
-    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+    CHECK(plane_copy(st, fs, (void*)host, false, cudaMemcpyHostToDevice, s));
   } else if (!host_f32) {
     CHECK(upload_t<float>(st, fs, (const double*)host, s));
   } else {
@@ -759,14 +747,7 @@ int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, voi
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
-  const size_t es = st->esz;
-  cudaMemcpy3DParms p{};
-  p.srcPtr = make_cudaPitchedPtr((char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es, st->pg.pitch * es,
-                                 st->pg.pitch, st->pg.rows);
-  p.dstPtr = make_cudaPitchedPtr(host, fs.ni * es, fs.ni, fs.nj);
-  p.extent = make_cudaExtent(fs.ni * es, fs.nj, fs.nplanes);
-  p.kind = cudaMemcpyDeviceToHost;
-  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+  CHECK(plane_copy(st, fs, host, true, cudaMemcpyDeviceToHost, s));
   return 0;
 }
 

@@ -66,37 +66,23 @@ size_t padded(size_t count, size_t es) { return ((count * es + 255) / 256) * 256
 int h2d_planes(double* dev, const PlaneGeom& pg, const double* host, int ilo, int ihi, int jlo, int jhi,
                long long nplanes, cudaStream_t s) {
   const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
-  cudaMemcpy3DParms p{};
-  p.srcPtr = make_cudaPitchedPtr((void*)host, (size_t)ni * 8, ni, nj);
-  p.dstPtr = make_cudaPitchedPtr(dev + pg.at(ilo, jlo), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
-  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
-  p.kind = cudaMemcpyHostToDevice;
-  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
-  return 0;
+  return copy_planes(dev + pg.at(ilo, jlo), (size_t)pg.pitch * 8, (size_t)pg.plane() * 8, host, (size_t)ni * 8,
+                     (size_t)ni * nj * 8, (size_t)ni * 8, nj, nplanes, cudaMemcpyHostToDevice, s);
 }
 
 int d2h_planes(double* host, const double* dev, const PlaneGeom& pg, int ilo, int ihi, int jlo, int jhi,
                long long nplanes, cudaStream_t s) {
   const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
-  cudaMemcpy3DParms p{};
-  p.srcPtr = make_cudaPitchedPtr((void*)(dev + pg.at(ilo, jlo)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
-  p.dstPtr = make_cudaPitchedPtr(host, (size_t)ni * 8, ni, nj);
-  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
-  p.kind = cudaMemcpyDeviceToHost;
-  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
-  return 0;
+  return copy_planes(host, (size_t)ni * 8, (size_t)ni * nj * 8, dev + pg.at(ilo, jlo), (size_t)pg.pitch * 8,
+                     (size_t)pg.plane() * 8, (size_t)ni * 8, nj, nplanes, cudaMemcpyDeviceToHost, s);
 }
 
 int d2d_planes(double* dst, const double* src, const PlaneGeom& pg, int ilo, int ihi, int jlo, int jhi,
                long long nplanes, cudaStream_t s) {
   const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
-  cudaMemcpy3DParms p{};
-  p.srcPtr = make_cudaPitchedPtr((void*)(src + pg.at(ilo, jlo)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
-  p.dstPtr = make_cudaPitchedPtr(dst + pg.at(ilo, jlo), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
-  p.extent = make_cudaExtent((size_t)ni * 8, nj, nplanes);
-  p.kind = cudaMemcpyDeviceToDevice;
-  FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
-  return 0;
+  return copy_planes(dst + pg.at(ilo, jlo), (size_t)pg.pitch * 8, (size_t)pg.plane() * 8, src + pg.at(ilo, jlo),
+                     (size_t)pg.pitch * 8, (size_t)pg.plane() * 8, (size_t)ni * 8, nj, nplanes,
+                     cudaMemcpyDeviceToDevice, s);
 }
 
 __global__ void k_corners(double* q, PlaneGeom pg, int npx, int npy, int corners, int dir, long long nplanes) {
@@ -329,12 +315,9 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   {
     // dp1 compute domain of every level (halo of dp1 is left untouched)
     const int ni = ie - is + 1, nj = je - js + 1, nid = ied - isd + 1, njd = jed - jsd + 1;
-    cudaMemcpy3DParms p{};
-    p.srcPtr = make_cudaPitchedPtr((void*)(dpb[dp_start] + pg.at(is, js)), (size_t)pg.pitch * 8, pg.pitch, pg.rows);
-    p.dstPtr = make_cudaPitchedPtr(dp1 + (is - isd) + (size_t)(js - jsd) * nid, (size_t)nid * 8, nid, njd);
-    p.extent = make_cudaExtent((size_t)ni * 8, nj, npz);
-    p.kind = cudaMemcpyDeviceToHost;
-    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+    CHECK(copy_planes(dp1 + (is - isd) + (size_t)(js - jsd) * nid, (size_t)nid * 8, (size_t)nid * njd * 8,
+                      dpb[dp_start] + pg.at(is, js), (size_t)pg.pitch * 8, (size_t)pg.plane() * 8, (size_t)ni * 8,
+                      nj, npz, cudaMemcpyDeviceToHost, s));
   }
   CHECK(d2h_planes(cx, dcx, pg, is, ie + 1, jsd, jed, npz, s));
   CHECK(d2h_planes(cy, dcy, pg, isd, ied, js, je + 1, npz, s));
@@ -376,12 +359,9 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   const int nib = iend - ibeg + 1, njb = jend - jbeg + 1;
   // q1(ibeg:iend, jbeg:jend, km*nq): the (i1:i2, j1:j2) block of every plane
   {
-    cudaMemcpy3DParms p{};
-    p.srcPtr = make_cudaPitchedPtr((void*)(q1 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib), (size_t)nib * 8, nib, njb);
-    p.dstPtr = make_cudaPitchedPtr(d1, (size_t)ni * 8, ni, nj);
-    p.extent = make_cudaExtent((size_t)ni * 8, nj, (size_t)km * nq);
-    p.kind = cudaMemcpyHostToDevice;
-    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+    CHECK(copy_planes(d1, (size_t)ni * 8, (size_t)ni * nj * 8, q1 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib,
+                      (size_t)nib * 8, (size_t)nib * njb * 8, (size_t)ni * 8, nj, (long long)km * nq,
+                      cudaMemcpyHostToDevice, s));
   }
   FV3G_CUDA(cudaMemcpyAsync(dpe1, pe1, sizeof(double) * P * (km + 1), cudaMemcpyHostToDevice, s));
   FV3G_CUDA(cudaMemcpyAsync(dpe2, pe2, sizeof(double) * P * (kn + 1), cudaMemcpyHostToDevice, s));
@@ -407,12 +387,9 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   r.sched = sch;
   CHECK(launch_remap<double>(r, kord, s));
   {
-    cudaMemcpy3DParms p{};
-    p.srcPtr = make_cudaPitchedPtr(d2, (size_t)ni * 8, ni, nj);
-    p.dstPtr = make_cudaPitchedPtr(q2 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib, (size_t)nib * 8, nib, njb);
-    p.extent = make_cudaExtent((size_t)ni * 8, nj, (size_t)kn * nq);
-    p.kind = cudaMemcpyDeviceToHost;
-    FV3G_CUDA(cudaMemcpy3DAsync(&p, s));
+    CHECK(copy_planes(q2 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib, (size_t)nib * 8, (size_t)nib * njb * 8, d2,
+                      (size_t)ni * 8, (size_t)ni * nj * 8, (size_t)ni * 8, nj, (long long)kn * nq,
+                      cudaMemcpyDeviceToHost, s));
   }
   FV3G_CUDA(cudaStreamSynchronize(s));
   return 0;

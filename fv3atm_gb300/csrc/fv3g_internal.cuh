@@ -148,6 +148,12 @@ template <typename T>
 int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is,
                        int ie, int js, int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s);
 
+// Copy nplanes planes of width_bytes x height between pitched buffers
+// (slice = bytes from one plane to the next); device-to-device by a kernel,
+// host copies in chunks of cudaMemcpy3DAsync.
+int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
+                size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s);
+
 size_t substep_smem_bytes(bool fp64, int warps);
 int prepare_kernels();
 

@@ -180,7 +180,9 @@ int fv3g_state_destroy(fv3g_state* st);
 int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* grid);
 int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk); /* npz+1 each */
 /* Host <-> device copies (FP64 host data; converted to FP32 in MIXED mode).
- * stream may be NULL (the state's stream). */
+ * Every `stream` argument of this header: NULL selects the state's own
+ * (non-blocking) stream; any other handle is used as given, including
+ * cudaStreamLegacy ((void*)1) for the legacy default stream. */
 int fv3g_upload(fv3g_state* st, int field, const double* host);
 int fv3g_download(fv3g_state* st, int field, double* host);
 /* Raw device copies with the state's storage type (float in MIXED). */

@@ -248,3 +248,67 @@ def test_errors_are_reported_not_fatal(cuda, cube_prob):
                      1.0, None, None, 1)
     with pytest.raises(Fv3gError, match="kord 7"):
         api.CubeState(P.n, P.npz, P.nq, kord=7)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_field_copies_roundtrip_many_planes(cuda, precision):
+    """6 x 9 x 127 planes through the device, pinned-host and FP64-host copy paths."""
+    import torch
+    n, npz, nq = 96, 127, 9
+    st = api.CubeState(n, npz, nq, precision=precision)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    shape = st.field_shape("Q")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    src = torch.rand(shape, dtype=dt, device="cuda", generator=g)
+    cur = torch.cuda.current_stream().cuda_stream
+    st.upload_device("Q", src.data_ptr(), stream=cur)
+    back = torch.zeros_like(src)
+    st.download_device("Q", back.data_ptr(), stream=cur)
+    torch.cuda.synchronize()
+    assert torch.equal(back, src)
+    host = src.cpu().pin_memory()
+    st.upload_device("Q", torch.zeros_like(src).data_ptr(), stream=cur)
+    torch.cuda.synchronize()
+    st.upload_async("Q", host.data_ptr(), precision == "mixed", stream=cur)
+    hout = torch.zeros_like(host).pin_memory()
+    st.download_async("Q", hout.data_ptr(), precision == "mixed", stream=cur)
+    torch.cuda.synchronize()
+    assert torch.equal(hout, host)
+    h64 = src.double().cpu().numpy()
+    st.upload("Q", h64)
+    assert np.array_equal(st.download("Q"), h64 if precision == "fp64" else src.cpu().numpy().astype(np.float64))
+
+
+def test_mixed_matches_fp64_many_tracers(cuda):
+    """Every tracer of the multi-tracer CTA loop (nq > warps per CTA) within 1e-5 of FP64."""
+    P = S.make_problem(48, 16, 20, seed=21, cmax=0.8)
+    a = _run_cube(P, "fp64", remap=True).download("Q_REMAPPED")
+    b = _run_cube(P, "mixed", remap=True).download("Q_REMAPPED")
+    for iq in range(P.nq):
+        assert rel_l2(interior(b[:, iq], P.n), interior(a[:, iq], P.n)) <= MIXED_TOL, iq
+
+
+def test_device_upload_after_conversion_on_default_stream(cuda):
+    """Uploads issued on torch's default (legacy) stream stay ordered after the
+    dtype conversion that produced them (127-level fields, FP32 state)."""
+    import torch
+    P = S.make_problem(96, 127, 4, seed=2000, cmax=0.8, device="cuda")
+    out = {}
+    for prec, dt in (("fp64", torch.float64), ("mixed", torch.float32)):
+        st = api.CubeState(P.n, P.npz, P.nq, precision=prec)
+        st.set_grid(P.geoms)
+        st.set_levels(P.ak, P.bk)
+        for name, val in (("Q", P.q), ("DELP", P.dp), ("CX", P.cx), ("CY", P.cy), ("MFX", P.mfx),
+                          ("MFY", P.mfy)):
+            v = val.to(dt).contiguous()
+            st.upload_device(name, v.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+            del v
+        st.tracer_2d(1)
+        q = torch.empty(st.field_shape("Q"), dtype=dt, device="cuda")
+        st.download_device("Q", q.data_ptr())
+        st.sync()
+        out[prec] = q[..., 3:3 + P.n, 3:3 + P.n].double()
+    for iq in range(P.nq):
+        a, b = out["fp64"][:, iq], out["mixed"][:, iq]
+        assert float(torch.linalg.vector_norm(b - a) / torch.linalg.vector_norm(a)) <= MIXED_TOL, iq
