@@ -320,6 +320,7 @@ def main():
     if not a.no_fp64:
         st = build_state(P, "fp64", a.nq, a.npz, a.n)
         st.step(a.q_split, use_graph=False)
+        st.sync()  # the step ran on the state's stream; the copy below runs on torch's
         ref_q = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float64, device="cuda")
         st.download_device("Q_REMAPPED", ref_q.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
@@ -335,6 +336,7 @@ def main():
     st = build_state(P, "mixed", a.nq, a.npz, a.n)
     m0 = st.mass("Q")
     st.step(a.q_split, use_graph=False)
+    st.sync()
     m1 = st.mass("Q_REMAPPED")
     err = None
     if ref_q is not None:
