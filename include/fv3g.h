@@ -142,6 +142,25 @@ int fv3g_map_scalar_3d(int km, const double* pe1, const double* q1, const double
                        const double* pe2, double* q2, int i1, int i2, int j1, int j2, int ibeg,
                        int iend, int jbeg, int jend, int nq, int iv, int kord, double q_min);
 
+/* Column remap on caller-owned DEVICE arrays that allocates no device memory.
+ * No counterpart in the reference: it serves callers that cannot let a
+ * library call cudaMalloc/cudaFree -- a model that owns all of its device
+ * memory (e.g. Fortran ported with OpenACC, passing device pointers through
+ * host_data use_device) or code that must not take the implicit device
+ * synchronisation of an allocation inside its time loop.
+ *   pe1 [km+1][ncol], pe2 [kn+1][ncol], q1 [nfield][km][ncol],
+ *   q2 [nfield][kn][ncol], qs [ncol] or NULL; FP64, device pointers.
+ *   iv, kord, q_min as fv3g_map_scalar; stream: CUDA stream, NULL = default.
+ * Limits: ncol <= 1024 and km, kn <= 128 per call; larger requests return
+ * FV3G_E_ARG.  The scratch is one fixed device array (6.5 MB, kept by every
+ * GPU that loads the library until exit) shared by all calls, so calls that
+ * overlap on the GPU (on different streams or host threads) race; serialise
+ * them.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. */
+int fv3g_remap_columns_noalloc(int ncol, int km, const double* pe1, const double* q1, const double* qs,
+                               int kn, const double* pe2, double* q2, int nfield, int iv, int kord,
+                               double q_min, void* stream);
+
 /* ======================================================================== */
 /* Batched, device-resident entries (all six tiles, all tracers).           */
 /* ======================================================================== */
