@@ -42,6 +42,10 @@ __device__ __forceinline__ Profile<T> layer_profile(T q, T aL, T aR, int iv, T f
   }
   T bl = aL - q, br = aR - q;
   cw84(bl, br);
+  if (KORD != 9 && iv >= 0 && (q + bl < floor_v || q + br < floor_v)) {  // keep the floor: flatten
+    bl = T(0);
+    br = T(0);
+  }
   return Profile<T>{q, q + bl, q + br, T(-3) * (bl + br)};
 }
 

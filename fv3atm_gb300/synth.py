@@ -355,3 +355,50 @@ def pressure_edges(dp, ak: np.ndarray, bk: np.ndarray):
     b = torch.as_tensor(bk, device=dp.device, dtype=torch.float64).view(-1, 1, 1)
     pe2 = a + b * ps
     return pe1, pe2
+
+
+# ------------------------------------------------- single-tile C48 problem ---
+def c48_single_tile(n: int = 48, npz: int = 63, seed: int = 0, cmax: float = 0.4, u0: float = 40.0,
+                    ps_noise: float = 0.05, noise: float = 0.01):
+    """One C48 tile, one cosine-bell tracer, solid-body rotation tilted 45 deg,
+    hybrid delp with ps = 1e5 +- 5 % (the target thickness is unperturbed).
+
+    Returns (Problem, exact) where exact(t_seconds) gives the halo-ring values
+    of the analytic rotated bell on the neighbouring tiles' cell centres,
+    shape (npz, nd, nd) (interior and corner blocks left at zero)."""
+    import torch
+    P = make_problem(n, npz, 1, ntiles=1, seed=seed, cmax=cmax, u0=u0, pert_amp=0.0, dp_noise=0.0,
+                     ps_range=(1.0e5 * (1 - ps_noise), 1.0e5 * (1 + ps_noise)), tracer_kind="bell", noise=0.0)
+    ng = P.ng
+    nd = n + 2 * ng
+    g0 = P.geoms[0]
+    center = lonlat_vec(-35.0, 8.0)
+    vert = 0.6 + 0.4 * np.cos(np.linspace(0.0, math.pi, npz))
+    rng = np.random.default_rng(seed + 99)
+    base = bell(g0.centers, center)
+    q = base[None] * vert[:, None, None] + noise * rng.uniform(-1.0, 1.0, (npz, nd, nd))
+    P.q = torch.as_tensor(np.clip(q, 0.0, None)[None, None])  # (1, 1, npz, nd, nd)
+    P.meta["center"] = center
+    topo = G.cube_topology()
+    geoms = {t: G.tile_geometry(n, t, ng) for t in range(6)}
+    omega = u0 / G.RADIUS
+    halo_pts, halo_idx = [], []
+    for j in range(1 - ng, n + ng + 1):
+        for i in range(1 - ng, n + ng + 1):
+            if (1 <= i <= n) == (1 <= j <= n):
+                continue
+            t, si, sj = G.halo_source(topo, n, 0, i, j)
+            halo_pts.append(geoms[t].centers[sj - 1 + ng, si - 1 + ng])
+            halo_idx.append((j - 1 + ng, i - 1 + ng))
+    halo_pts = np.asarray(halo_pts)
+    jj, ii = np.asarray(halo_idx).T
+
+    def exact(t_seconds: float) -> np.ndarray:
+        # the stream function above turns the field by -omega*t about the
+        # tilted axis; sample the initial bell at the back-rotated positions
+        back = rotate(halo_pts, -omega * t_seconds)
+        out = np.zeros((npz, nd, nd))
+        out[:, jj, ii] = bell(back, center)[None] * vert[:, None]
+        return out
+
+    return P, exact

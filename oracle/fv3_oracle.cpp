@@ -401,7 +401,9 @@ void flux_update(double* qk, const double* dp1k, const Level& L, const double* f
 //   kord 9: every interface value is clamped to the range of its two adjacent
 //           layer means (boundary interfaces: the two outermost means), then
 //           the CW84 cell constraint -- monotone, no new extrema;
-//   kord 4: no clamp; edge values floored at the iv floor (iv >= 0), then CW84.
+//   kord 4: no clamp; edge values floored at the iv floor (iv >= 0), then CW84;
+//           a layer whose corrected edges still fall below the floor is
+//           flattened (its mean is kept).
 template <class T>
 void column_profile_t(const T* q, const double* dp, int km, int iv, int kord, double qs, double q_min,
                       T* aL, T* aR, T* a6) {
@@ -451,6 +453,11 @@ void column_profile_t(const T* q, const double* dp, int km, int iv, int kord, do
     }
     T bl = l - q[k], br = r - q[k];
     cw84(bl, br);
+    // the overshoot correction can move an edge below the floor: flatten
+    if (kord != 9 && iv >= 0 && (val(q[k] + bl) < floor_v || val(q[k] + br) < floor_v)) {
+      bl = T(0.0);
+      br = T(0.0);
+    }
     aL[k] = q[k] + bl;
     aR[k] = q[k] + br;
     a6[k] = T(-3.0) * (bl + br);

@@ -1,0 +1,63 @@
+"""Regenerate the golden fixtures of the tracer path.
+
+The reference tree holds no golden vectors for tracer_2d / fv_tp_2d /
+map_scalar (the dycore is an empty submodule and its only test parses a
+namelist), so these fixtures are produced by the FP64 CPU oracle (oracle/) on
+small seeded problems.  Every input the oracle consumes is stored with the
+outputs, so the fixtures do not depend on random-number streams or on the
+platform's math library.  Run from the repository root:
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from fv3atm_gb300 import synth as S  # noqa: E402
+
+GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg")
+
+
+def cube_fixture():
+    P = S.make_problem(12, 2, 2, seed=101, cmax=0.8)
+    d = {k: getattr(P, k).numpy() for k in ("q", "dp", "cx", "cy", "mfx", "mfy")}
+    for f in GEOM_FIELDS:
+        d["geom_" + f] = np.stack([getattr(g, f) for g in P.geoms])
+    d["ak"], d["bk"], d["topo"] = P.ak, P.bk, P.topo
+    out = {}
+    for hord, qs in ((8, 3), (5, 2)):
+        q1, dp_last, ns = O.tracer_2d_cube(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], P.geoms, P.topo,
+                                           hord=hord, q_split=qs)
+        out[f"q_h{hord}"] = q1[..., 3:15, 3:15]
+        out[f"dplast_h{hord}"] = dp_last[..., 3:15, 3:15]
+    return {**d, **out, "n": np.array(12)}
+
+
+def remap_fixture():
+    from fv3atm_gb300 import grid as G
+    rng = np.random.default_rng(202)
+    km, ncol = 63, 8
+    ak, bk = G.hybrid_levels(km)
+    ps = rng.uniform(95000, 103000, ncol)
+    dref = np.diff(ak)[:, None] + np.diff(bk)[:, None] * ps[None]
+    dp = dref * (1 + 0.1 * rng.uniform(-1, 1, dref.shape))
+    pe1 = np.concatenate([np.full((1, ncol), ak[0]), ak[0] + np.cumsum(dp, 0)])
+    pe2 = ak[:, None] + bk[:, None] * pe1[-1][None]
+    q1 = np.abs(rng.standard_normal((km, ncol))).cumsum(0) * 0.01 + rng.uniform(0, 0.1, (km, ncol))
+    qs = rng.uniform(0, 1, ncol)
+    d = {"pe1": pe1, "pe2": pe2, "q1": q1, "qs": qs}
+    for kord, iv, qmin in ((9, 0, 0.0), (9, 1, 0.05), (4, 0, 0.0), (4, -1, 0.0), (4, -2, 0.0), (4, 1, 0.05)):
+        d[f"q2_k{kord}_iv{iv}"] = O.remap_columns(pe1, q1, pe2, iv=iv, kord=kord, qs=qs, q_min=qmin)
+    return d
+
+
+if __name__ == "__main__":
+    np.savez_compressed(os.path.join(HERE, "cube_c12_l2.npz"), **cube_fixture())
+    np.savez_compressed(os.path.join(HERE, "remap_columns_l63.npz"), **remap_fixture())
+    print("written")

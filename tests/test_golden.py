@@ -1,0 +1,39 @@
+"""The oracle reproduces its committed golden fixtures (tests/golden/, made by
+tests/golden/make_golden.py).  The reference holds no fixtures for this path,
+so these pin the oracle against regressions; the GPU tests check the CUDA path
+against the same files."""
+import os
+import types
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg")
+
+
+def load_cube():
+    d = dict(np.load(os.path.join(HERE, "cube_c12_l2.npz")))
+    geoms = [types.SimpleNamespace(**{f: d["geom_" + f][t] for f in GEOM_FIELDS}, n=int(d["n"]), ng=3)
+             for t in range(6)]
+    return d, geoms
+
+
+@pytest.mark.parametrize("hord,q_split", [(8, 3), (5, 2)])
+def test_oracle_reproduces_cube_fixture(hord, q_split):
+    d, geoms = load_cube()
+    q1, dp_last, _ = O.tracer_2d_cube(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], geoms, d["topo"],
+                                      hord=hord, q_split=q_split)
+    n = int(d["n"])
+    assert np.array_equal(q1[..., 3:3 + n, 3:3 + n], d[f"q_h{hord}"])
+    assert np.array_equal(dp_last[..., 3:3 + n, 3:3 + n], d[f"dplast_h{hord}"])
+
+
+@pytest.mark.parametrize("kord,iv,qmin", [(9, 0, 0.0), (9, 1, 0.05), (4, 0, 0.0), (4, -1, 0.0), (4, -2, 0.0),
+                                          (4, 1, 0.05)])
+def test_oracle_reproduces_remap_fixture(kord, iv, qmin):
+    d = dict(np.load(os.path.join(HERE, "remap_columns_l63.npz")))
+    q2 = O.remap_columns(d["pe1"], d["q1"], d["pe2"], iv=iv, kord=kord, qs=d["qs"], q_min=qmin)
+    assert np.array_equal(q2, d[f"q2_k{kord}_iv{iv}"])

@@ -312,3 +312,31 @@ def test_device_upload_after_conversion_on_default_stream(cuda):
     for iq in range(P.nq):
         a, b = out["fp64"][:, iq], out["mixed"][:, iq]
         assert float(torch.linalg.vector_norm(b - a) / torch.linalg.vector_norm(a)) <= MIXED_TOL, iq
+
+
+# ------------------------------------------------------- committed fixtures
+def test_cube_matches_committed_golden_fixture(cuda):
+    from .test_golden import load_cube
+    d, geoms = load_cube()
+    n = int(d["n"])
+    for hord, q_split in ((8, 3), (5, 2)):
+        st = api.CubeState(n, d["q"].shape[2], d["q"].shape[1], precision="fp64", hord=hord)
+        st.set_grid(geoms)
+        st.set_levels(d["ak"], d["bk"])
+        for name, key in (("Q", "q"), ("DELP", "dp"), ("CX", "cx"), ("CY", "cy"), ("MFX", "mfx"), ("MFY", "mfy")):
+            st.upload(name, d[key])
+        st.tracer_2d(q_split)
+        q = st.download("Q")[..., 3:3 + n, 3:3 + n]
+        assert rel_l2(q, d[f"q_h{hord}"]) <= FP64_TOL, hord
+
+
+def test_remap_matches_committed_golden_fixture(cuda):
+    import os
+    d = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "remap_columns_l63.npz")))
+    km, ncol = d["q1"].shape
+    for kord, iv, qmin in ((9, 0, 0.0), (9, 1, 0.05), (4, 0, 0.0), (4, -1, 0.0), (4, -2, 0.0), (4, 1, 0.05)):
+        q1 = np.ascontiguousarray(d["q1"][None, :, None, :])
+        out = np.zeros_like(q1)
+        api.map_scalar_3d(km, np.ascontiguousarray(d["pe1"]), q1, np.ascontiguousarray(d["qs"]), km,
+                          np.ascontiguousarray(d["pe2"]), out, 1, ncol, 1, 1, 1, ncol, 1, 1, 1, iv, kord, qmin)
+        assert rel_l2(out[0, :, 0, :], d[f"q2_k{kord}_iv{iv}"]) <= FP64_TOL, (kord, iv)
