@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--warps", type=int, default=0, help="advection warps per CTA (0 = library default)")
     return ap.parse_args()
 
 
@@ -176,10 +177,10 @@ def max_over_ranks(x: float, world: int) -> float:
     return float(t.item())
 
 
-def build_state(P, precision, nq, npz, n):
+def build_state(P, precision, nq, npz, n, warps=0):
     import torch
     from fv3atm_gb300 import api
-    st = api.CubeState(n, npz, nq, precision=precision, hord=8, kord=9)
+    st = api.CubeState(n, npz, nq, precision=precision, hord=8, kord=9, warps_per_cta=warps)
     st.set_grid(P.geoms)
     st.set_levels(P.ak, P.bk)
     dt = torch.float64 if precision == "fp64" else torch.float32
@@ -318,7 +319,7 @@ def main():
     # ---------------------------------------------------- FP64 reference leg
     ref_q = None
     if not a.no_fp64:
-        st = build_state(P, "fp64", a.nq, a.npz, a.n)
+        st = build_state(P, "fp64", a.nq, a.npz, a.n, 0)
         st.step(a.q_split, use_graph=False)
         st.sync()  # the step ran on the state's stream; the copy below runs on torch's
         ref_q = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float64, device="cuda")
@@ -333,7 +334,7 @@ def main():
         torch.cuda.empty_cache()
 
     # --------------------------------------------------- mixed headline leg
-    st = build_state(P, "mixed", a.nq, a.npz, a.n)
+    st = build_state(P, "mixed", a.nq, a.npz, a.n, a.warps)
     m0 = st.mass("Q")
     st.step(a.q_split, use_graph=False)
     st.sync()

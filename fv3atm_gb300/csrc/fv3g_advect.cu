@@ -41,21 +41,26 @@ struct SmemLevel {
   T area[WIN][PQ];
   T rrx[WIN][PF];  // 1/ra_x [window row][interior col]
   T rry[TW][WIN];  // 1/ra_y [interior row][window col]
-  T ua[TW][TW];    // dp1/dp2
+  T dpa[TW][TW];   // dp1/rarea
   T ub[TW][TW];    // rarea/dp2
 };
 
 template <typename T>
 struct SmemWarp {
-  T q[WIN][PQ];   // tracer window
-  T qi[TW][PQ];   // q_i; later the x-flux divergence (or x fluxes)
-  T qj[WIN][PF];  // q_j [window row][interior col]
+  T q[WIN][PQ];   // tracer window; S2 overwrites each row with q_j (interior columns)
+  T qi[TW][PQ];   // q_i; then q dp1/rarea + x-flux divergence (or the x fluxes)
   T fy2[NF][TW];  // inner y flux [face][interior col]
 };
 
-size_t substep_smem_bytes(bool fp64, int warps) {
-  return fp64 ? sizeof(SmemLevel<double>) + warps * sizeof(SmemWarp<double>)
-              : sizeof(SmemLevel<float>) + warps * sizeof(SmemWarp<float>);
+// Per-warp shared memory; edge CTAs add the deviations of two lines at two
+// edges, [2][16][32] values.
+__host__ __device__ constexpr size_t warp_smem_bytes(bool fp64, bool edges) {
+  return fp64 ? sizeof(SmemWarp<double>) + (edges ? 2 * 16 * 32 * sizeof(double) : 0)
+              : sizeof(SmemWarp<float>) + (edges ? 2 * 16 * 32 * sizeof(float) : 0);
+}
+
+size_t substep_smem_bytes(bool fp64, int warps, bool edges) {
+  return (fp64 ? sizeof(SmemLevel<double>) : sizeof(SmemLevel<float>)) + warps * warp_smem_bytes(fp64, edges);
 }
 
 // ----------------------------------------------------------- halo source ---
@@ -116,16 +121,11 @@ __device__ __forceinline__ T ld_field(const T* base, const PlaneGeom& pg, int i,
 
 // ------------------------------------------------------- PPM line stream ---
 // Deviations (bl, br) of the four cells e-2..e+1 around a cube-face edge at
-// window face e, computed once per line from shared memory: the edge value is
+// window face e, computed once per line from shared memory and kept there
+// (o[c*32] = bl of cell e-2+c, o[(4+c)*32] = br; lane-strided): the edge value is
 // the mean of the two one-sided, dxa-weighted linear extrapolations; the two
 // neighbouring interfaces use one-sided third-order values (see the oracle's
 // xppm/yppm restatement).  Only cells 2..29 of a window feed its fluxes.
-template <typename T>
-struct EdgeDev {
-  int e;  // window face of the edge, NO_EDGE if none
-  T bl0, bl1, bl2, bl3, br0, br1, br2, br3;
-};
-
 template <typename T, int HORD, class EX>
 __device__ __forceinline__ T generic_bl(int c, EX&& x) {
   if (HORD == 8) {
@@ -149,8 +149,8 @@ __device__ __forceinline__ T generic_br(int c, EX&& x) {
 }
 
 template <typename T, int HORD, class EX, class ED>
-__device__ __noinline__ void edge_devs_impl(int e, EX x, ED ed, T* o) {
-  // o[0..3] = bl of cells e-2..e+1, o[4..7] = br
+__device__ __noinline__ void edge_devs(int e, EX x, ED ed, T* o) {
+  if (e == NO_EDGE) return;
   const bool need0 = (e - 2 >= 2 && e - 2 <= 29), need1 = (e - 1 >= 2 && e - 1 <= 29);
   const bool need2 = (e >= 2 && e <= 29), need3 = (e + 1 >= 2 && e + 1 <= 29);
   T aM = T(0), a0 = T(0), aP = T(0);
@@ -176,87 +176,298 @@ __device__ __noinline__ void edge_devs_impl(int e, EX x, ED ed, T* o) {
   if (need3) { b[3] = aP - x(e + 1); r[3] = generic_br<T, HORD>(e + 1, x); }
   if (HORD == 8)
     for (int c = 0; c < 4; ++c) cw84(b[c], r[c]);
-  for (int c = 0; c < 4; ++c) { o[c] = b[c]; o[4 + c] = r[c]; }
-}
-
-template <typename T, int HORD, class EX, class ED>
-__device__ __forceinline__ EdgeDev<T> edge_devs(int e, EX&& x, ED&& ed) {
-  EdgeDev<T> d;
-  d.e = e;
-  if (e == NO_EDGE) return d;
-  T o[8];
-  edge_devs_impl<T, HORD>(e, x, ed, o);
-  d.bl0 = o[0]; d.bl1 = o[1]; d.bl2 = o[2]; d.bl3 = o[3];
-  d.br0 = o[4]; d.br1 = o[5]; d.br2 = o[6]; d.br3 = o[7];
-  return d;
+  for (int c = 0; c < 4; ++c) { o[c * 32] = b[c]; o[(4 + c) * 32] = r[c]; }
 }
 
 // A line of 32 window cells x[0..31] marched with a rolling register window;
 // face f separates cells f-1 and f, and faces 3..29 are the CTA tile's.
-// Before step m the state holds x[m-3..m-1], dm[m-2], al[m-2] and the
-// deviations of cell m-3; step(x[m]) finalises cell m-2 and returns the flux
-// through face m-2 (meaningful for m >= 5).
+// Before step m the state holds x[m-3..m-1] (xa, xb, xc), dm[m-2] and al[m-2]
+// (hord 8) and the right deviation and b0 = bl + br of cell m-3; step(x[m])
+// finalises cell m-2 and returns the flux through face m-2 (valid for m >= 5).
+//   hord 8: dm = monotonized central slope (clamp form), al = interface value,
+//           |edge deviation| <= |2 dm| with the sign of dm (Lin 2004);
+//   flux  = x_up + w1 d_up - w2 b0_up with w1 = 1-|c|, w2 = |c| w1 and the
+//           upwind cell's deviation at the face (CW84 parabola integral).
+template <typename T>
+__device__ __forceinline__ T dm_clamp(T xm, T x0, T xp) {
+  const T xt = T(0.25) * (xp - xm);
+  const T mm = tmin(tmax(tmax(xm, x0), xp) - x0, x0 - tmin(tmin(xm, x0), xp));
+  return tmin(tmax(xt, -mm), mm);
+}
+
 template <typename T, int HORD>
 struct Line {
-  T xa = T(0), xb = T(0), xc = T(0), dmb = T(0), alb = T(0), pbl = T(0), pbr = T(0);
+  T xa, xb, xc, dmb, alb, pbr, pb0;
 
-  __device__ __forceinline__ static void splice(int c, const EdgeDev<T>& E, T& bl, T& br) {
-    const int d = c - (E.e - 2);
-    if (E.e != NO_EDGE && d >= 0 && d <= 3) {
-      bl = d == 0 ? E.bl0 : d == 1 ? E.bl1 : d == 2 ? E.bl2 : E.bl3;
-      br = d == 0 ? E.br0 : d == 1 ? E.br1 : d == 2 ? E.br2 : E.br3;
-    }
-  }
+  __device__ __forceinline__ void init() { xa = xb = xc = dmb = alb = pbr = pb0 = T(0); }
 
-  // consume x[m]; return the flux through face m-2 for Courant number c
-  __device__ __forceinline__ T step(int m, T x, T c, const EdgeDev<T>& E0, const EdgeDev<T>& E1) {
+  // ed: this lane's edge deviations (16 lane-strided slots: edge A bl0..3 br0..3, then edge B);
+  // eA/eB: window faces of the edges (warp-uniform), NO_EDGE if none
+  template <bool EDGES>
+  __device__ __forceinline__ T step(int m, T x, T c, const T* ed, int eA, int eB) {
     T alc, bl, br;
     if (HORD == 8) {
-      const T dmc = vl_slope(xb, xc, x);                      // dm[m-1]
+      const T dmc = dm_clamp(xb, xc, x);                      // dm[m-1]
       alc = T(0.5) * (xb + xc) + (dmb - dmc) * T(1.0 / 3.0);  // al[m-1]
-      const T xt = T(2) * dmb, axt = tabs(xt);                // cell m-2
-      bl = -tsign(tmin(axt, tabs(alb - xb)), xt);
-      br = tsign(tmin(axt, tabs(alc - xb)), xt);
+      const T xt = dmb + dmb;                                 // cell m-2
+      const T axt = tabs(xt);
+      bl = copysign_t(tmin(axt, tabs(alb - xb)), -xt);
+      br = copysign_t(tmin(axt, tabs(alc - xb)), xt);
       dmb = dmc;
     } else {
       alc = T(7.0 / 12.0) * (xb + xc) - T(1.0 / 12.0) * (xa + x);
       bl = alb - xb;
       br = alc - xb;
     }
-    splice(m - 2, E0, bl, br);
-    splice(m - 2, E1, bl, br);
-    const T fl = ppm_flux(c, xa, pbl, pbr, xb, bl, br);
+    if (EDGES) {  // cell m-2 is cell e-2+d of an edge
+      const int dA = m - eA, dB = m - eB;
+      if ((unsigned)dA < 4u) { bl = ed[dA * 32]; br = ed[(4 + dA) * 32]; }
+      if ((unsigned)dB < 4u) { bl = ed[(8 + dB) * 32]; br = ed[(12 + dB) * 32]; }
+    }
+    const T b0 = bl + br;
+    const bool pos = c > T(0);
+    const T a = tabs(c);
+    const T w1 = T(1) - a, w2 = a * w1;
+    const T xu = pos ? xa : xb, du = pos ? pbr : bl, bu = pos ? pb0 : b0;
+    const T fl = (xu + w1 * du) - w2 * bu;
     xa = xb;
     xb = xc;
     xc = x;
     alb = alc;
-    pbl = bl;
     pbr = br;
+    pb0 = b0;
     return fl;
   }
 };
 
 // ------------------------------------------------------------ the kernel ---
-template <typename T, int HORD, bool FLUXES>
-__global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a) {
+// One tracer of one CTA tile through the three stages (see file header).
+template <typename T, int HORD, bool FLUXES, bool EDGES>
+__device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>& L, SmemWarp<T>& S, int t, int k,
+                                               T* eds, int iq, int i0, int j0, int ni, int nj, int lane, int exA,
+                                               int exB, int eyA, int eyB, bool direct, bool corner_block,
+                                               long long efo, long long efe) {
+  const PlaneGeom& pg = a.pg;
+  const int n = a.npx - 1;
+  // ------------------------------------------ window load (y-sweep corners)
+  {
+    const int i = i0 - 3 + lane;
+    const T* qp = a.q_in + t * a.sQt + iq * a.sQq + k * a.sQk;
+    if (direct) {
+      const T* src = qp + pg.at(i, j0 - 3);
+#pragma unroll 8
+      for (int r = 0; r < WIN; ++r) S.q[r][lane] = src[(long long)r * pg.pitch];
+    } else {
+#pragma unroll 4
+      for (int r = 0; r < WIN; ++r) S.q[r][lane] = load_q(a, t, iq, k, i, j0 - 3 + r, 2);
+    }
+  }
+  __syncwarp();
+
+  // edge deviations of the lines in flight: eds[line][16][32], lines 0 (and 1 in S2)
+  T* const ed0 = eds + lane;
+  T* const ed1 = eds + 16 * 32 + lane;
+  // ------------------------------------------------ S1: inner y, q_i ------
+  {
+    const int w = lane;
+    const T* qcol = &S.q[0][w];
+    if (EDGES) {
+      auto ex = [qcol](int m) { return qcol[m * PQ]; };
+      const T* dya = a.dya + t * a.sMt;
+      const int ig = i0 - 3 + w;
+      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
+      edge_devs<T, HORD>(eyA, ex, ed, ed0);
+      edge_devs<T, HORD>(eyB, ex, ed, ed0 + 8 * 32);
+    }
+    const bool keep_fy2 = (w >= 3 && w < 29);
+    T* fy2 = &S.fy2[0][keep_fy2 ? w - 3 : 0];
+    Line<T, HORD> ln;
+    ln.init();
+#pragma unroll
+    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qcol[m * PQ], T(0), ed0, eyA, eyB);
+    T fy = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, eyA, eyB);
+    T fyy_prev = L.yf[0][w] * fy;
+    if (keep_fy2) fy2[0] = fy;
+#pragma unroll 2
+    for (int m = 6; m < WIN; ++m) {
+      const int f = m - 2;
+      const T xrow = ln.xa;  // cell row f-1 = m-3
+      fy = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, eyA, eyB);
+      const T fyy = L.yf[f - 3][w] * fy;
+      if (keep_fy2) fy2[(f - 3) * TW] = fy;
+      S.qi[f - 4][w] = (xrow * L.area[f - 1][w] + fyy_prev - fyy) * L.rry[f - 4][w];
+      fyy_prev = fyy;
+    }
+  }
+  __syncwarp();
+
+  // -------------------------------------- corner blocks for the x sweeps
+  if (corner_block) {
+    const int i = i0 - 3 + lane;
+#pragma unroll 1
+    for (int r = 0; r < WIN; ++r) {
+      const int j = j0 - 3 + r;
+      const bool oi = (i < 1) || (i > a.npx - 1), oj = (j < 1) || (j > a.npy - 1);
+      if (oi && oj) S.q[r][lane] = load_q(a, t, iq, k, i, j, 1);
+    }
+    __syncwarp();
+  }
+
+  // ---------- S2: inner x -> q_j (into the q row); outer x on q_i -> P -----
+  {
+    const int r = lane;
+    const bool outer = (r >= 3) && (r < 29);
+    const int ro = outer ? r - 3 : 0;
+    T* qrow = &S.q[r][0];
+    T* qirow = &S.qi[ro][0];
+    if (EDGES) {
+      auto exi = [qrow](int m) { return qrow[m]; };
+      auto exo = [qirow](int m) { return qirow[m]; };
+      const T* dxa = a.dxa + t * a.sMt;
+      const int jg = j0 - 3 + r;
+      auto ed = [dxa, pg, i0, jg](int m) { return ld_field(dxa, pg, i0 - 3 + m, jg); };
+      edge_devs<T, HORD>(exA, exi, ed, ed0);
+      edge_devs<T, HORD>(exB, exi, ed, ed0 + 8 * 32);
+      if (outer) {
+        edge_devs<T, HORD>(exA, exo, ed, ed1);
+        edge_devs<T, HORD>(exB, exo, ed, ed1 + 8 * 32);
+      }
+    }
+    const bool efw = EDGES && a.cube && a.eflux != nullptr && outer && ro < nj;
+    Line<T, HORD> li, lo;
+    li.init();
+    lo.init();
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      li.template step<EDGES>(m, qrow[m], T(0), ed0, exA, exB);
+      lo.template step<EDGES>(m, qirow[m], T(0), ed1, exA, exB);
+    }
+    // face 3
+    T c = L.cx[r][0];
+    T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, exA, exB);
+    T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, exA, exB);
+    T fxx_prev = L.xf[r][0] * fx2;
+    T F_prev = (fo + fx2) * L.mx[ro][0];
+    if (FLUXES && outer) qirow[0] = F_prev;
+    if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
+#pragma unroll 2
+    for (int m = 6; m < WIN; ++m) {
+      const int f = m - 2;
+      const T xcol = li.xa;  // q at window column f-1 of this row
+      c = L.cx[r][f - 3];
+      fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, exA, exB);
+      fo = lo.template step<EDGES>(m, qirow[m], c, ed1, exA, exB);
+      const T fxx = L.xf[r][f - 3] * fx2;
+      // q_j of window column f-1 (interior column f-4); column m-6 of this row is consumed
+      qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
+      fxx_prev = fxx;
+      const T F = (fo + fx2) * L.mx[ro][f - 3];
+      if (outer) {
+        if (FLUXES) qirow[f - 3] = F;  // column f-3 was consumed at step f-3
+        else qirow[f - 4] = xcol * L.dpa[ro][f - 4] + (F_prev - F);  // q dp1/rarea + x divergence
+      }
+      if (efw && i0 + f - 3 == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
+      F_prev = F;
+    }
+  }
+  __syncwarp();
+
+  // ---------------------------- S3: outer y on q_j, update / write -------
+  if (lane < TW) {
+    const int c = lane;
+    const T* qjcol = &S.q[0][c];
+    if (EDGES) {
+      auto ex = [qjcol](int m) { return qjcol[m * PQ]; };
+      const T* dya = a.dya + t * a.sMt;
+      const int ig = i0 + c;
+      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
+      edge_devs<T, HORD>(eyA, ex, ed, ed0);
+      edge_devs<T, HORD>(eyB, ex, ed, ed0 + 8 * 32);
+    }
+    const int ig = i0 + c;
+    const bool valid_c = c < ni;
+    const bool efw = EDGES && a.cube && a.eflux != nullptr && valid_c;
+    T* qo = a.q_out + t * a.sQt + iq * a.sQq + k * a.sQk + pg.at(ig, j0);
+    T* fyo = FLUXES ? a.fy_out + (long long)(k * a.nq + iq) * a.sFlux + pg.at(ig, j0) : nullptr;
+    Line<T, HORD> ln;
+    ln.init();
+#pragma unroll
+    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qjcol[m * PQ], T(0), ed0, eyA, eyB);
+    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, eyA, eyB) + S.fy2[0][c]) * L.my[0][c];
+    if (FLUXES && valid_c) fyo[0] = Fprev;
+    if (efw && j0 == 1) a.eflux[efo + 2 * efe + iq * (long long)n + (ig - 1)] = -Fprev;
+#pragma unroll 2
+    for (int m = 6; m < WIN; ++m) {
+      const int f = m - 2;
+      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, eyA, eyB) + S.fy2[f - 3][c]) *
+                  L.my[f - 3][c];
+      const int ir = f - 4;  // interior row between faces f-1 and f
+      if (FLUXES) {
+        if (valid_c && f - 3 <= nj) fyo[(long long)(f - 3) * pg.pitch] = F;
+      } else if (ir < nj && valid_c) {
+        qo[(long long)ir * pg.pitch] = (S.qi[ir][c] + Fprev - F) * L.ub[ir][c];
+      }
+      if (efw && j0 + f - 3 == a.npy) a.eflux[efo + 3 * efe + iq * (long long)n + (ig - 1)] = F;
+      Fprev = F;
+    }
+  }
+  if (FLUXES) {  // x fluxes staged in qi by S2
+    __syncwarp();
+    T* fxo = a.fx_out + (long long)(k * a.nq + iq) * a.sFlux;
+    for (int e = lane; e < TW * NF; e += 32) {
+      const int ir = e / NF, f = e % NF;
+      if (ir < nj && f <= ni) fxo[pg.at(i0 + f, j0 + ir)] = S.qi[ir][f];
+    }
+  }
+  __syncwarp();
+}
+
+// Interior CTAs (no cube-face edge in their window) and edge CTAs run as two
+// instantiations: the edge code path costs registers the interior one does
+// not need.  Interior CTAs cover the rectangle [bx0, bx0+nbxi) x [by0,
+// by0+nbyi) of CTA tiles; edge CTAs enumerate the ring around it row by row.
+template <typename T, int HORD, bool FLUXES, bool EDGES>
+__global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a, const BlockMap bm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  SmemWarp<T>& S = reinterpret_cast<SmemWarp<T>*>(smem_raw + sizeof(SmemLevel<T>))[warp];
+  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes(sizeof(T) == 8, EDGES);
+  SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
+  T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
 
   const int t = blockIdx.z, k = blockIdx.y;
-  const int nbx = (a.ie - a.is + TW) / TW;
-  const int i0 = a.is + (blockIdx.x % nbx) * TW, j0 = a.js + (blockIdx.x / nbx) * TW;
+  int bx, by;
+  {
+    const int e = blockIdx.x;
+    if (!EDGES) {
+      bx = bm.bx0 + e % bm.nbxi;
+      by = bm.by0 + e / bm.nbxi;
+    } else {
+      const int top = bm.by0 * bm.nbx, nside = bm.nbx - bm.nbxi, mid = nside * bm.nbyi;
+      if (e < top) {
+        by = e / bm.nbx;
+        bx = e % bm.nbx;
+      } else if (e < top + mid) {
+        const int r = e - top, sx = r % nside;
+        by = bm.by0 + r / nside;
+        bx = sx < bm.bx0 ? sx : sx + bm.nbxi;
+      } else {
+        const int r = e - top - mid;
+        by = bm.by0 + bm.nbyi + r / bm.nbx;
+        bx = r % bm.nbx;
+      }
+    }
+  }
+  const int i0 = a.is + bx * TW, j0 = a.js + by * TW;
   const int ni = min(TW, a.ie - i0 + 1), nj = min(TW, a.je - j0 + 1);
   const PlaneGeom& pg = a.pg;
   const int n = a.npx - 1;
 
   // window faces of cube-face edges (x: west/east, y: south/north)
-  auto inwin = [](int e) { return (e >= 1 && e <= 31) ? e : NO_EDGE; };
-  const int exA = (!a.nested && a.is == 1) ? inwin(1 - i0 + 3) : NO_EDGE;
-  const int exB = (!a.nested && a.ie + 1 == a.npx) ? inwin(a.npx - i0 + 3) : NO_EDGE;
-  const int eyA = (!a.nested && a.js == 1) ? inwin(1 - j0 + 3) : NO_EDGE;
-  const int eyB = (!a.nested && a.je + 1 == a.npy) ? inwin(a.npy - j0 + 3) : NO_EDGE;
+  const int exA = EDGES ? window_edge_lo(a.is, i0, a.nested) : NO_EDGE;
+  const int exB = EDGES ? window_edge_hi(a.ie, a.npx, i0, a.nested) : NO_EDGE;
+  const int eyA = EDGES ? window_edge_lo(a.js, j0, a.nested) : NO_EDGE;
+  const int eyB = EDGES ? window_edge_hi(a.je, a.npy, j0, a.nested) : NO_EDGE;
 
   // ---------------------------------------------- per-level staging -------
   {
@@ -308,7 +519,7 @@ __global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a) {
       const T d1 = ld_field(dp1, pg, i, j);
       const T d2 = d1 + (ld_field(mx, pg, i, j) - ld_field(mx, pg, i + 1, j) + ld_field(my, pg, i, j) -
                          ld_field(my, pg, i, j + 1)) * ra;
-      L.ua[r][c] = d1 / d2;
+      L.dpa[r][c] = d1 / ra;
       L.ub[r][c] = ra / d2;
       if (r < nj && c < ni && dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
     }
@@ -318,173 +529,16 @@ __global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a) {
   const bool corner_block = !a.nested && a.corners != 0 &&
                             ((i0 - 3 < 1) || (i0 + 28 > a.npx - 1)) && ((j0 - 3 < 1) || (j0 + 28 > a.npy - 1));
   const bool inside = i0 - 3 >= 1 && i0 + 28 <= n && j0 - 3 >= 1 && j0 + 28 <= n;
-  const bool fast = (!a.cube || inside) && !corner_block;
+  const bool in_plane = i0 - 3 >= pg.isd && i0 + 28 <= pg.isd + pg.pitch - 1 && j0 - 3 >= pg.jsd &&
+                        j0 + 28 <= pg.jsd + pg.rows - 1;
+  const bool direct = in_plane && (a.cube ? inside : true) && !corner_block;
   // edge-flux index (((t*4 + e)*npz + k)*nq + iq)*n + s = efo + e*efe + iq*n + s
   const long long efe = (long long)a.npz * a.nq * n;
   const long long efo = (((long long)t * 4) * a.npz + k) * a.nq * n;
 
-  for (int iq = warp; iq < a.nq; iq += W) {
-    // ------------------------------------------ window load (y-sweep corners)
-    {
-      const int i = i0 - 3 + lane;
-      const T* qp = a.q_in + t * a.sQt + iq * a.sQq + k * a.sQk;
-#pragma unroll 4
-      for (int r = 0; r < WIN; ++r) {
-        const int j = j0 - 3 + r;
-        S.q[r][lane] = fast ? ld_field(qp, pg, i, j) : load_q(a, t, iq, k, i, j, 2);
-      }
-    }
-    __syncwarp();
-
-    // ------------------------------------------------ S1: inner y, q_i ------
-    {
-      const int w = lane;
-      const T* qcol = &S.q[0][w];
-      auto ex = [qcol](int m) { return qcol[m * PQ]; };
-      const int ig = i0 - 3 + w;
-      const T* dya = a.dya + t * a.sMt;
-      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
-      const EdgeDev<T> EA = edge_devs<T, HORD>(eyA, ex, ed), EB = edge_devs<T, HORD>(eyB, ex, ed);
-      Line<T, HORD> ln;
-      T fyy_prev = T(0);
-#pragma unroll 1
-      for (int m = 0; m < WIN; ++m) {
-        const int f = m - 2;  // window face of the flux produced now
-        const T c = (m >= 5) ? L.cy[f - 3][w] : T(0);
-        const T xm1 = ln.xb;  // x[m-2] before the step: the cell below face m-2... (row f-1 = m-3 after)
-        (void)xm1;
-        const T xrow = ln.xa;  // x[m-3]: row f-1, whose faces are f-1 and f
-        const T fy = ln.step(m, qcol[m * PQ], c, EA, EB);
-        if (m >= 5) {
-          const T fyy = L.yf[f - 3][w] * fy;
-          if (w >= 3 && w < 29) S.fy2[f - 3][w - 3] = fy;
-          if (m >= 6) {
-            const int r = f - 1;
-            S.qi[r - 3][w] = (xrow * L.area[r][w] + fyy_prev - fyy) * L.rry[r - 3][w];
-          }
-          fyy_prev = fyy;
-        }
-      }
-    }
-    __syncwarp();
-
-    // -------------------------------------- corner blocks for the x sweeps
-    if (corner_block) {
-      const int i = i0 - 3 + lane;
-#pragma unroll 1
-      for (int r = 0; r < WIN; ++r) {
-        const int j = j0 - 3 + r;
-        const bool oi = (i < 1) || (i > a.npx - 1), oj = (j < 1) || (j > a.npy - 1);
-        if (oi && oj) S.q[r][lane] = load_q(a, t, iq, k, i, j, 1);
-      }
-      __syncwarp();
-    }
-
-    // ------------------------------ S2: inner x -> q_j; outer x on q_i -------
-    {
-      const int r = lane;
-      const bool outer = (r >= 3) && (r < 29);
-      const int ro = outer ? r - 3 : 0;
-      const T* qrow = &S.q[r][0];
-      T* qirow = &S.qi[ro][0];
-      auto exi = [qrow](int m) { return qrow[m]; };
-      auto exo = [qirow](int m) { return qirow[m]; };
-      const T* dxa = a.dxa + t * a.sMt;
-      const int jg = j0 - 3 + r;
-      auto ed = [dxa, pg, i0, jg](int m) { return ld_field(dxa, pg, i0 - 3 + m, jg); };
-      const EdgeDev<T> IA = edge_devs<T, HORD>(exA, exi, ed), IB = edge_devs<T, HORD>(exB, exi, ed);
-      EdgeDev<T> OA, OB;
-      OA.e = NO_EDGE;
-      OB.e = NO_EDGE;
-      if (outer) {
-        OA = edge_devs<T, HORD>(exA, exo, ed);
-        OB = edge_devs<T, HORD>(exB, exo, ed);
-      }
-      Line<T, HORD> li, lo;
-      T fxx_prev = T(0), F_prev = T(0);
-      const bool efw = a.cube && a.eflux != nullptr && outer && ro < nj;
-#pragma unroll 1
-      for (int m = 0; m < WIN; ++m) {
-        const int f = m - 2;
-        const T c = (m >= 5) ? L.cx[r][f - 3] : T(0);
-        const T xcol = li.xa;  // x[m-3]: column f-1
-        const T fx2 = li.step(m, qrow[m], c, IA, IB);
-        const T fo = lo.step(m, qirow[m], c, OA, OB);
-        if (m >= 5) {
-          const T fxx = L.xf[r][f - 3] * fx2;
-          if (m >= 6) {
-            const int cc = f - 1;  // window column with both faces
-            if (cc >= 3 && cc < 29) S.qj[r][cc - 3] = (xcol * L.area[r][cc] + fxx_prev - fxx) * L.rrx[r][cc - 3];
-          }
-          fxx_prev = fxx;
-          if (outer) {
-            const T F = (fo + fx2) * L.mx[ro][f - 3];
-            if (FLUXES) {
-              qirow[f - 3] = F;  // column f-3 was consumed at step f-3
-            } else if (m >= 6) {
-              qirow[f - 4] = F_prev - F;  // divergence of interior column f-4
-            }
-            if (efw) {
-              const int fi = i0 + f - 3;  // tile face index
-              if (fi == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F;
-              else if (fi == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
-            }
-            F_prev = F;
-          }
-        }
-      }
-    }
-    __syncwarp();
-
-    // ---------------------------- S3: outer y on q_j, update / write -------
-    if (lane < TW) {
-      const int c = lane;
-      const T* qjcol = &S.qj[0][c];
-      auto ex = [qjcol](int m) { return qjcol[m * PF]; };
-      const T* dya = a.dya + t * a.sMt;
-      const int ig = i0 + c;
-      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
-      const EdgeDev<T> EA = edge_devs<T, HORD>(eyA, ex, ed), EB = edge_devs<T, HORD>(eyB, ex, ed);
-      Line<T, HORD> ln;
-      T* qo = a.q_out + t * a.sQt + iq * a.sQq + k * a.sQk;
-      T* fyo = FLUXES ? a.fy_out + (long long)(k * a.nq + iq) * a.sFlux : nullptr;
-      T Fprev = T(0);
-      const bool efw = a.cube && a.eflux != nullptr && c < ni;
-#pragma unroll 1
-      for (int m = 0; m < WIN; ++m) {
-        const int f = m - 2;
-        const T cc = (m >= 5) ? L.cy[f - 3][c + 3] : T(0);
-        const T fo = ln.step(m, qjcol[m * PF], cc, EA, EB);
-        if (m >= 5) {
-          const T F = (fo + S.fy2[f - 3][c]) * L.my[f - 3][c];
-          const int fj = j0 + f - 3;  // tile face index
-          if (FLUXES) {
-            if (c < ni && f - 3 <= nj) fyo[pg.at(ig, fj)] = F;
-          } else if (m >= 6) {
-            const int ir = f - 4;  // interior row with faces f-1, f
-            if (ir < nj && c < ni) {
-              const T qn = S.q[ir + 3][c + 3] * L.ua[ir][c] + (S.qi[ir][c] + Fprev - F) * L.ub[ir][c];
-              qo[pg.at(ig, j0 + ir)] = qn;
-            }
-          }
-          if (efw) {
-            if (fj == 1) a.eflux[efo + 2 * efe + iq * (long long)n + (ig - 1)] = -F;
-            else if (fj == a.npy) a.eflux[efo + 3 * efe + iq * (long long)n + (ig - 1)] = F;
-          }
-          Fprev = F;
-        }
-      }
-    }
-    if (FLUXES) {  // x fluxes staged in qi by S2
-      __syncwarp();
-      T* fxo = a.fx_out + (long long)(k * a.nq + iq) * a.sFlux;
-      for (int e = lane; e < TW * NF; e += 32) {
-        const int ir = e / NF, f = e % NF;
-        if (ir < nj && f <= ni) fxo[pg.at(i0 + f, j0 + ir)] = S.qi[ir][f];
-      }
-    }
-    __syncwarp();
-  }
+  for (int iq = warp; iq < a.nq; iq += W)
+    advance_tracer<T, HORD, FLUXES, EDGES>(a, L, S, t, k, eds, iq, i0, j0, ni, nj, lane, exA, exB, eyA, eyB, direct,
+                                           corner_block, efo, efe);
 }
 
 // ------------------------------------------------ tile-edge reconciliation ---
@@ -601,20 +655,73 @@ __global__ void k_max_courant(const T* cx, const T* cy, long long sFt, long long
 }
 
 // ------------------------------------------------------------ launchers ---
-template <typename T, int HORD, bool FLUXES>
-static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
-  const size_t smem = substep_smem_bytes(sizeof(T) == 8, warps);
-  const int nbx = (a.ie - a.is + TW) / TW, nby = (a.je - a.js + TW) / TW;
-  dim3 grid(nbx * nby, a.npz, a.cube ? 6 : 1);
-  k_substep<T, HORD, FLUXES><<<grid, 32 * warps, smem, s>>>(a);
-  FV3G_CUDA(cudaGetLastError());
-  return 0;
+// Contiguous range [lo, lo+cnt) of CTA tiles along one axis whose windows see
+// no cube-face edge (edges sit only near the two ends of the axis).
+static void edge_free_range(int is, int ie, int np, int nested, int nb, int& lo, int& cnt) {
+  lo = nb;
+  int hi = -1;
+  for (int b = 0; b < nb; ++b) {
+    const int i0 = is + b * TW;
+    if (window_edge_lo(is, i0, nested) == NO_EDGE && window_edge_hi(ie, np, i0, nested) == NO_EDGE) {
+      lo = std::min(lo, b);
+      hi = b;
+    }
+  }
+  cnt = hi >= lo ? hi - lo + 1 : 0;
+}
+
+BlockMap block_map(int is, int ie, int js, int je, int npx, int npy, int nested) {
+  BlockMap m;
+  m.nbx = (ie - is + TW) / TW;
+  m.nby = (je - js + TW) / TW;
+  edge_free_range(is, ie, npx, nested, m.nbx, m.bx0, m.nbxi);
+  edge_free_range(js, je, npy, nested, m.nby, m.by0, m.nbyi);
+  if (m.nbxi == 0 || m.nbyi == 0) {  // no interior: the ring is every tile
+    m.bx0 = 0;
+    m.nbxi = 0;
+    m.by0 = m.nby;
+    m.nbyi = 0;
+  }
+  return m;
 }
 
 template <typename T, int HORD, bool FLUXES>
+static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
+  const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
+  const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
+  const int nt = a.cube ? 6 : 1;
+  if (nint > 0) {
+    dim3 grid(nint, a.npz, nt);
+    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes(sizeof(T) == 8, warps, false), s>>>(a, bm);
+    FV3G_CUDA(cudaGetLastError());
+  }
+  if (nring > 0) {
+    dim3 grid(nring, a.npz, nt);
+    k_substep<T, HORD, FLUXES, true><<<grid, 32 * warps, substep_smem_bytes(sizeof(T) == 8, warps, true), s>>>(a, bm);
+    FV3G_CUDA(cudaGetLastError());
+  }
+  return 0;
+}
+
+// Largest warps per CTA whose shared memory fits in 227 KB (at most 8).
+static int max_warps(bool fp64) {
+  int w = 8;
+  while (w > 1 && substep_smem_bytes(fp64, w, true) > 227 * 1024) --w;
+  return w;
+}
+
+template <typename T, int HORD, bool FLUXES, bool EDGES>
 static cudaError_t set_smem_attr() {
-  const int mx = (int)std::min<size_t>(substep_smem_bytes(sizeof(T) == 8, sizeof(T) == 8 ? 5 : 8), 227 * 1024);
-  return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  const int mx = (int)substep_smem_bytes(sizeof(T) == 8, max_warps(sizeof(T) == 8), EDGES);
+  return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+template <typename T, int HORD>
+static void set_attrs(cudaError_t& err) {
+  cudaError_t es[] = {set_smem_attr<T, HORD, false, false>(), set_smem_attr<T, HORD, false, true>(),
+                      set_smem_attr<T, HORD, true, false>(), set_smem_attr<T, HORD, true, true>()};
+  for (cudaError_t e : es)
+    if (e != cudaSuccess && err == cudaSuccess) err = e;
 }
 
 // Raise the dynamic shared-memory limit of every advection kernel once per
@@ -623,15 +730,15 @@ int prepare_kernels() {
   static std::once_flag once;
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
-    cudaError_t es[] = {set_smem_attr<float, 5, false>(),  set_smem_attr<float, 5, true>(),
-                        set_smem_attr<float, 8, false>(),  set_smem_attr<float, 8, true>(),
-                        set_smem_attr<double, 5, false>(), set_smem_attr<double, 5, true>(),
-                        set_smem_attr<double, 8, false>(), set_smem_attr<double, 8, true>()};
-    for (cudaError_t e : es)
-      if (e != cudaSuccess && err == cudaSuccess) err = e;
+    set_attrs<float, 5>(err);
+    set_attrs<float, 8>(err);
+    set_attrs<double, 5>(err);
+    set_attrs<double, 8>(err);
   });
   return err == cudaSuccess ? 0 : cuda_error(err, "cudaFuncSetAttribute(k_substep)");
 }
+
+int substep_max_warps(bool fp64) { return max_warps(fp64); }
 
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s) {
@@ -639,9 +746,10 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
     int prc = prepare_kernels();
     if (prc) return prc;
   }
-  if (warps < 1 || warps > 8) return set_error(FV3G_E_ARG, "warps per CTA must be 1..8 (got %d)", warps);
-  if (sizeof(T) == 8 && substep_smem_bytes(true, warps) > 227 * 1024)
-    return set_error(FV3G_E_ARG, "FP64 advection supports at most %d warps per CTA", 5);
+  const int mw = max_warps(sizeof(T) == 8);
+  if (warps < 1 || warps > mw)
+    return set_error(FV3G_E_ARG, "%s advection supports 1..%d warps per CTA (got %d)", sizeof(T) == 8 ? "FP64" : "FP32",
+                     mw, warps);
   if (hord == 8) return flux_mode ? launch_one<T, 8, true>(a, warps, s) : launch_one<T, 8, false>(a, warps, s);
   if (hord == 5) return flux_mode ? launch_one<T, 5, true>(a, warps, s) : launch_one<T, 5, false>(a, warps, s);
   return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);

@@ -83,6 +83,24 @@ struct AdvArgs {
   long long sFlux;
 };
 
+// CTA tiles of a substep launch: the interior rectangle [bx0, bx0+nbxi) x
+// [by0, by0+nbyi) of the nbx x nby tiles holds those whose 32-cell window
+// contains no cube-face edge.
+struct BlockMap {
+  int nbx, nby, bx0, nbxi, by0, nbyi;
+};
+
+// Window face (1..31) of the low / high cube-face edge seen by a CTA tile
+// starting at i0, NO_EDGE if its window has none.
+__host__ __device__ __forceinline__ int window_edge_lo(int is, int i0, int nested) {
+  const int e = 1 - i0 + NG;
+  return (!nested && is == 1 && e >= 1 && e <= WIN - 1) ? e : NO_EDGE;
+}
+__host__ __device__ __forceinline__ int window_edge_hi(int ie, int npx, int i0, int nested) {
+  const int e = npx - i0 + NG;
+  return (!nested && ie + 1 == npx && e >= 1 && e <= WIN - 1) ? e : NO_EDGE;
+}
+
 // ------------------------------------------------------------- helpers ----
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
@@ -92,6 +110,8 @@ template <typename T> __device__ __forceinline__ T tsign(T a, T b) {
   T m = tabs(a);
   return b < T(0) ? -m : m;
 }
+__device__ __forceinline__ float copysign_t(float a, float b) { return copysignf(a, b); }
+__device__ __forceinline__ double copysign_t(double a, double b) { return copysign(a, b); }
 template <typename T> __device__ __forceinline__ T clamp2(T a, T x0, T x1) {
   return tmin(tmax(a, tmin(x0, x1)), tmax(x0, x1));
 }
@@ -154,7 +174,9 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
 int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
                 size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s);
 
-size_t substep_smem_bytes(bool fp64, int warps);
+size_t substep_smem_bytes(bool fp64, int warps, bool edges);
 int prepare_kernels();
+int substep_max_warps(bool fp64);
+BlockMap block_map(int is, int ie, int js, int je, int npx, int npy, int nested);
 
 }  // namespace fv3g
