@@ -125,7 +125,6 @@ struct fv3g_state {
   void* dx = nullptr; void* dy = nullptr; void* sin4 = nullptr;
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
-  void* rscratch = nullptr; unsigned char* sched = nullptr;
   double* partials = nullptr; double* mass_out = nullptr;
   unsigned int* cmax = nullptr;
   int* err = nullptr;
@@ -340,7 +339,7 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
                             st->n, 1, st->n, 6, st->npz, frac, s));
   CHECK(mark(st, K_PROLOGUE, s));
-  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 7);
+  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 5);
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
     const int dst = (src == 1) ? 2 : 1;
@@ -383,8 +382,6 @@ int remap_t(fv3g_state* st, cudaStream_t s) {
   r.km = st->npz; r.kn = st->npz;
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
-  r.scratch = (T*)st->rscratch;
-  r.sched = st->sched;
   CHECK(launch_remap<T>(r, st->d.kord, s));
   CHECK(mark(st, K_REMAP, s));
   st->q_cur = 0;
@@ -441,6 +438,7 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   build_topo(st->topo);
   {
     int prc = prepare_kernels();
+    if (!prc) prc = prepare_remap_kernels();
     if (prc) {
       delete st;
       return prc;
@@ -467,9 +465,6 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (!rc) rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
   if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
-  const long long ncol = 6LL * d.n * d.n;
-  if (!rc) rc = dalloc(st, &st->rscratch, (size_t)ncol * (KMAX + 1) * 6 * st->esz);
-  if (!rc) rc = dalloc(st, (void**)&st->sched, (size_t)ncol * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);
   if (!rc) rc = dalloc(st, (void**)&st->mass_out, sizeof(double) * d.nq);
   if (!rc) rc = dalloc(st, (void**)&st->cmax, sizeof(unsigned));

@@ -347,15 +347,13 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   pg.rows = nj;
   const size_t P = (size_t)ni * nj;
   CHECK(g_ctx.begin(padded(P * km * nq, 8) + padded(P * kn * nq, 8) + padded(P * (km + 1), 8) +
-                    padded(P * (kn + 1), 8) + padded(P, 8) + remap_scratch_bytes(ncol, true) + 1024));
+                    padded(P * (kn + 1), 8) + padded(P, 8) + 1024));
   cudaStream_t s = g_ctx.stream;
   double* d1 = g_ctx.take<double>(P * km * nq);
   double* d2 = g_ctx.take<double>(P * kn * nq);
   double* dpe1 = g_ctx.take<double>(P * (km + 1));
   double* dpe2 = g_ctx.take<double>(P * (kn + 1));
   double* dqs = g_ctx.take<double>(P);
-  double* scr = g_ctx.take<double>((size_t)ncol * (KMAX + 1) * 6);
-  unsigned char* sch = g_ctx.take<unsigned char>((size_t)ncol * (KMAX + 1));
   const int nib = iend - ibeg + 1, njb = jend - jbeg + 1;
   // q1(ibeg:iend, jbeg:jend, km*nq): the (i1:i2, j1:j2) block of every plane
   {
@@ -383,8 +381,6 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   r.i1 = i1; r.j1 = j1; r.ni = ni; r.nj = nj;
   r.ncol = ncol;
   r.km = km; r.kn = kn; r.iv = iv; r.q_min = q_min;
-  r.scratch = scr;
-  r.sched = sch;
   CHECK(launch_remap<double>(r, kord, s));
   {
     CHECK(copy_planes(q2 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib, (size_t)nib * 8, (size_t)nib * njb * 8, d2,

@@ -15,7 +15,9 @@
 // constraints, and the integration of the sub-grid parabolas over the
 // overlaps.  Column-constant arrays and the interface values live in a
 // scratch buffer laid out [level][column] (coalesced, L2-resident).
+#include <algorithm>
 #include <cfloat>
+#include <mutex>
 
 #include "fv3g_internal.cuh"
 #include "fv3g_remap.cuh"
@@ -34,6 +36,35 @@ struct Profile {  // sub-grid parabola of one source layer
   T q, l, r, s6;
 };
 
+// cw84 with selects in place of branches (the same values): no divergence
+// when the lanes of a warp take different cases.
+template <typename T> __device__ __forceinline__ void cw84_sel(T& bl, T& br) {
+  const bool flat = bl * br >= T(0);
+  const T d = br - bl;
+  const T t = T(3) * d * (bl + br);
+  const T d2 = d * d;
+  const bool lo = -t > d2, hi = !lo && t > d2;
+  const T nbl = lo ? T(-2) * br : bl, nbr = hi ? T(-2) * bl : br;
+  bl = flat ? T(0) : nbl;
+  br = flat ? T(0) : nbr;
+}
+
+template <typename T, int KORD>
+__device__ __forceinline__ Profile<T> layer_profile_sel(T q, T aL, T aR, int iv, T floor_v) {
+  if (KORD != 9 && iv >= 0) {
+    aL = tmax(aL, floor_v);
+    aR = tmax(aR, floor_v);
+  }
+  T bl = aL - q, br = aR - q;
+  cw84_sel(bl, br);
+  if (KORD != 9 && iv >= 0) {
+    const bool flat = (q + bl < floor_v) || (q + br < floor_v);
+    bl = flat ? T(0) : bl;
+    br = flat ? T(0) : br;
+  }
+  return Profile<T>{q, q + bl, q + br, T(-3) * (bl + br)};
+}
+
 template <typename T, int KORD>
 __device__ __forceinline__ Profile<T> layer_profile(T q, T aL, T aR, int iv, T floor_v) {
   if (KORD != 9 && iv >= 0) {
@@ -49,8 +80,10 @@ __device__ __forceinline__ Profile<T> layer_profile(T q, T aL, T aR, int iv, T f
   return Profile<T>{q, q + bl, q + br, T(-3) * (bl + br)};
 }
 
+// Thread-per-column form with a global scratch (the caller's fixed buffer);
+// used where the library may not allocate (fv3g_remap_columns_noalloc).
 template <typename T, int KORD>
-__global__ void __launch_bounds__(128) k_remap(const RemapArgs<T> a) {
+__global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= a.ncol) return;
   const int km = a.km, kn = a.kn;
@@ -234,14 +267,436 @@ __global__ void __launch_bounds__(128) k_remap(const RemapArgs<T> a) {
 #undef SC
 }
 
+// ------------------------------------------------ warp-per-column form ---
+// One warp per column; lane l owns interfaces / layers u = l*NPL .. l*NPL+NPL-1,
+// so the column's constants stay in registers for all fields.  The three
+// first-order recurrences of the column are evaluated as warp scans and then
+// re-run locally with the sequential formulas from the scanned start value:
+//   * the FP64 running sum of delp (interface pressures pe1);
+//   * the LU pivots of the interface system, cp_u = d_u / (2(1+d_u) - cp_{u-1}),
+//     a Moebius map composed as 2x2 matrices (scaled by powers of two, exact);
+//   * per field, forward substitution y_u = (rhs_u - y_{u-1}) rd_u and back
+//     substitution a_u = y_u - cp_u a_{u+1}, affine maps composed in the scan.
+// The overlap schedule (source layer and fractional position of every target
+// interface) is a binary search in the warp's copy of pe1.
+// Shared arrays indexed by level take one pad element per 32 floats (16
+// doubles), so that lane l reading level 4l+j (the blocked ownership) hits
+// distinct banks.
+template <typename T>
+__host__ __device__ constexpr int pk(int k) { return k + (k >> (sizeof(T) == 8 ? 4 : 5)); }
+
+template <typename T, int NPL>
+struct ColSmem {
+  double pe1[pk<double>(32 * NPL) + 1];
+  T dp[pk<T>(32 * NPL)];
+  T pl[pk<T>(32 * NPL)];  // sub-grid parabola of every source layer: left, right edge and curvature
+  T pr[pk<T>(32 * NPL)];
+  T p6[pk<T>(32 * NPL)];
+};
+
+// Fields reach shared memory through a ring of RING slots, filled by
+// cp.async RING-1 fields ahead.  Each slot holds the CTA's 8 columns,
+// [column][padded level].  The CTA's threads copy it together:
+// thread t moves levels t/8 + 32r of column t%8, so 8 consecutive threads read
+// one 32-byte sector (consecutive columns are consecutive i).
+template <typename T>
+__host__ __device__ constexpr int ring_slots() { return sizeof(T) == 8 ? 3 : 4; }
+
+// Slot pitch per column: room for the padded levels, and a residue (4 mod 32
+// floats, 2 mod 16 doubles) that spreads the 8 columns of one copy
+// instruction over distinct banks.
+template <typename T, int NPL>
+__host__ __device__ constexpr int ring_pitch() {
+  int p = pk<T>(32 * NPL) + 1;
+  while (sizeof(T) == 8 ? (p % 16 != 2) : (p % 32 != 4)) ++p;
+  return p;
+}
+
+template <typename T, int NPL>
+__host__ __device__ constexpr size_t remap_warp_smem() {
+  return 8 * sizeof(ColSmem<T, NPL>) + (size_t)ring_slots<T>() * 8 * ring_pitch<T, NPL>() * sizeof(T);
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if (sizeof(T) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// 2^-e with e the binary exponent of m > 0: m * pow2_recip(m) lies in [1, 2)
+__device__ __forceinline__ float pow2_recip(float m) {
+  const int e = (__float_as_int(m) >> 23) & 0xff;
+  return __int_as_float((254 - e) << 23);
+}
+__device__ __forceinline__ double pow2_recip(double m) {
+  const long long e = (__double_as_longlong(m) >> 52) & 0x7ff;
+  return __longlong_as_double((2046 - e) << 52);
+}
+
+template <typename T>
+struct Mat2 {  // [[a, b], [c, d]]
+  T a, b, c, d;
+};
+
+// m2 * m1 (m1 applied first), rescaled by a power of two
+template <typename T>
+__device__ __forceinline__ Mat2<T> mat_after(const Mat2<T>& m2, const Mat2<T>& m1) {
+  Mat2<T> r{m2.a * m1.a + m2.b * m1.c, m2.a * m1.b + m2.b * m1.d, m2.c * m1.a + m2.d * m1.c,
+            m2.c * m1.b + m2.d * m1.d};
+  const T s = pow2_recip(tmax(tmax(tabs(r.a), tabs(r.b)), tmax(tabs(r.c), tabs(r.d))));
+  r.a *= s; r.b *= s; r.c *= s; r.d *= s;
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ Mat2<T> shfl_up_mat(const Mat2<T>& m, int o) {
+  return Mat2<T>{__shfl_up_sync(0xffffffffu, m.a, o), __shfl_up_sync(0xffffffffu, m.b, o),
+                 __shfl_up_sync(0xffffffffu, m.c, o), __shfl_up_sync(0xffffffffu, m.d, o)};
+}
+
+// Affine map x -> al * x + be.  Inclusive scans: forward (lane-o first) and
+// backward (lane+o first); both return the exclusive prefix's offset, i.e.
+// the recurrence value entering this lane's first (forward) or last
+// (backward) element, given that the chain starts with a constant map.
+template <typename T>
+__device__ __forceinline__ T affine_enter_fwd(T al, T be, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T pa = __shfl_up_sync(0xffffffffu, al, o), pb = __shfl_up_sync(0xffffffffu, be, o);
+    if (lane >= o) {
+      be = al * pb + be;
+      al = al * pa;
+    }
+  }
+  return __shfl_up_sync(0xffffffffu, be, 1);
+}
+template <typename T>
+__device__ __forceinline__ T affine_enter_bwd(T al, T be, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T pa = __shfl_down_sync(0xffffffffu, al, o), pb = __shfl_down_sync(0xffffffffu, be, o);
+    if (lane + o < 32) {
+      be = al * pb + be;
+      al = al * pa;
+    }
+  }
+  return __shfl_down_sync(0xffffffffu, be, 1);
+}
+
+template <typename T, int KORD, int NPL>
+__global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
+  constexpr int RING = ring_slots<T>(), RP = ring_pitch<T, NPL>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  ColSmem<T, NPL>& S = reinterpret_cast<ColSmem<T, NPL>*>(smem_raw)[warp];
+  T* const ring = reinterpret_cast<T*>(smem_raw + 8 * sizeof(ColSmem<T, NPL>));
+  const int nc = (int)a.ncol;  // launch_remap checks that it fits in an int
+  const int col0 = blockIdx.x * 8;
+  // the last CTA's surplus warps repeat the last column and store nothing
+  const bool real = col0 + warp < nc;
+  const int col = real ? col0 + warp : nc - 1;
+  auto offsets = [&a](int c, long long& fo_, long long& qo_) {
+    const unsigned ni = (unsigned)a.ni, nj = (unsigned)a.nj;
+    const unsigned rest = (unsigned)c / ni, ci = (unsigned)c - rest * ni;
+    const unsigned ct = rest / nj, cj = rest - ct * nj;
+    fo_ = ct * a.sFt + a.pg.at(a.i1 + ci, a.j1 + cj);
+    qo_ = ct * a.sQt + a.pg.at(a.i1 + ci, a.j1 + cj);
+  };
+  long long fo, qo;
+  offsets(col, fo, qo);
+  const int km = a.km, kn = a.kn;
+  const int u0 = lane * NPL;  // first interface / layer of this lane
+
+  // cooperative field copy: this thread's column and levels
+  const int cc = threadIdx.x & 7, kk = threadIdx.x >> 3;
+  long long fo_c, qo_c;
+  offsets(min(col0 + cc, nc - 1), fo_c, qo_c);
+  auto issue = [&](int f) {
+    if (f < a.nfield) {
+      const T* src = a.q_in + qo_c + f * a.sQq;
+      T* dst = ring + ((f % RING) * 8 + cc) * RP;
+#pragma unroll
+      for (int r = 0; r < NPL; ++r) {
+        const int k = kk + 32 * r;
+        if (k < km) cp_async_elem(dst + pk<T>(k), src + (long long)k * a.sQk);
+      }
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int f = 0; f < RING - 1; ++f) issue(f);
+
+  // ------------------------------------------------ interface pressures pe1
+  if (a.pe1 != nullptr) {
+#pragma unroll
+    for (int j = 0; j < NPL; ++j)
+      if (u0 + j <= km) S.pe1[pk<double>(u0 + j)] = a.pe1[(long long)(u0 + j) * nc + col];
+  } else {
+    const double ptop = a.ak[0];
+    double dl[NPL], tot = 0.0;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      dl[j] = (u0 + j < km) ? (double)a.dp[fo + (long long)(u0 + j) * a.sFk] : 0.0;
+      tot += dl[j];
+    }
+    double excl = affine_enter_fwd<double>(1.0, tot, lane);  // sum over lower lanes
+    double s = lane == 0 ? ptop : ptop + excl;
+    if (lane == 0) S.pe1[pk<double>(0)] = ptop;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      s += dl[j];
+      if (u0 + j < km) S.pe1[pk<double>(u0 + j + 1)] = s;
+    }
+  }
+  __syncwarp();
+  const double ps = S.pe1[pk<double>(km)];
+  auto pe2_at = [&](int k) -> double {
+    if (a.pe2 != nullptr) return a.pe2[(long long)k * nc + col];
+    return a.ak[k] + a.bk[k] * ps;
+  };
+#pragma unroll
+  for (int j = 0; j < NPL; ++j)
+    if (u0 + j < km) S.dp[pk<T>(u0 + j)] = T(S.pe1[pk<double>(u0 + j + 1)] - S.pe1[pk<double>(u0 + j)]);
+  __syncwarp();
+
+  // ----------------------------------------- overlap schedule, target dp
+  // Source layer k1 holding target interface p: the number of interior source
+  // interfaces at or above p (a short walk from the target's own index).
+  int Ls[NPL + 1];
+  T Xs[NPL + 1], dpk[NPL];
+  double p2v[NPL + 1];
+#pragma unroll
+  for (int j = 0; j <= NPL; ++j) {
+    const int k2 = min(u0 + j, kn);
+    const double p = pe2_at(k2);
+    p2v[j] = p;
+    int k1 = min(k2, km - 1);
+    while (k1 > 0 && S.pe1[pk<double>(k1)] > p) --k1;
+    while (k1 < km - 1 && S.pe1[pk<double>(k1 + 1)] <= p) ++k1;
+    const double pl = S.pe1[pk<double>(k1)], ph = S.pe1[pk<double>(k1 + 1)];
+    Ls[j] = k1;
+    Xs[j] = (sizeof(T) == 8) ? T((p - pl) / (ph - pl)) : T(float(p - pl) / float(ph - pl));
+  }
+#pragma unroll
+  for (int j = 0; j < NPL; ++j) {
+    const int t = u0 + j;
+    dpk[j] = (t < kn) ? T(p2v[j + 1] - p2v[j]) : T(1);
+    if (real && t < kn && a.dp_out != nullptr) a.dp_out[fo + (long long)t * a.sFk] = dpk[j];
+  }
+
+  // ------------------------------------------- LU of the interface system
+  // Row u of the system: rhs_u = wa q[ia] + wb q[ib] + wc qs, forward step
+  // y_u = (rhs_u - mco_u y_{u-1}) rd_u, back step a_u = y_u - cpb_u a_{u+1};
+  // rows above km have rd = 0.  The clamp of kord 9 uses the same two layers.
+  T wa[NPL], wb[NPL], wc[NPL], mco[NPL], rdv[NPL], cpb[NPL];
+  int ia[NPL], ib[NPL];
+#pragma unroll
+  for (int j = 0; j < NPL; ++j) {
+    const int u = u0 + j;
+    ia[j] = min(u == 0 ? 0 : u - 1, km - 1);
+    ib[j] = max(min(u == 0 ? 1 : (u == km ? km - 2 : u), km - 1), 0);
+    wa[j] = wb[j] = wc[j] = mco[j] = rdv[j] = cpb[j] = T(0);
+  }
+  if (km > 1) {
+    const T g = S.dp[pk<T>(1)] / S.dp[pk<T>(0)];
+    T dd[NPL];
+    Mat2<T> m{T(1), T(0), T(0), T(1)};
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      const int u = u0 + j;
+      dd[j] = (u >= 1 && u < km) ? S.dp[pk<T>(u - 1)] / S.dp[pk<T>(u)] : T(0);
+      if (u >= 1 && u < km) m = mat_after(Mat2<T>{T(0), dd[j], T(-1), T(2) * (T(1) + dd[j])}, m);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const Mat2<T> p = shfl_up_mat(m, o);
+      if (lane >= o) m = mat_after(m, p);
+    }
+    const Mat2<T> e = shfl_up_mat(m, 1);
+    const T cp0 = (g + T(1)) / g;
+    T cprev = (e.a * cp0 + e.b) / (e.c * cp0 + e.d);  // cp of interface u0-1 (lanes >= 1)
+    const T gb = S.dp[pk<T>(km - 2)] / S.dp[pk<T>(km - 1)];
+    const T lo_b = a.iv == -2 ? T(0) : gb + T(1);
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      const int u = u0 + j;
+      if (u == 0) {
+        rdv[j] = T(1) / g;
+        cpb[j] = cp0;
+        wa[j] = (g * (T(2) * g + T(3))) / (g + T(1));
+        wb[j] = T(1) / (g + T(1));
+      } else if (u < km) {
+        rdv[j] = T(1) / (T(2) * (T(1) + dd[j]) - cprev);
+        cpb[j] = dd[j] * rdv[j];
+        mco[j] = T(1);
+        wa[j] = T(3);
+        wb[j] = T(3) * dd[j];
+      } else if (u == km) {
+        rdv[j] = T(1) / ((a.iv == -2 ? T(1) : gb) - lo_b * cprev);
+        mco[j] = lo_b;
+        if (a.iv == -2) {
+          wc[j] = T(1);
+        } else {
+          wa[j] = (gb * (T(2) * gb + T(3))) / (gb + T(1));
+          wb[j] = T(1) / (gb + T(1));
+        }
+      }
+      cprev = cpb[j];
+    }
+  }
+
+  const T floor_v = (a.iv == 1) ? T(a.q_min) : T(0);
+  const T qsv = a.qs ? T(a.qs[col]) : T(0);
+  T rdpk[NPL];
+#pragma unroll
+  for (int j = 0; j < NPL; ++j) rdpk[j] = T(1) / dpk[j];
+  for (int f = 0; f < a.nfield; ++f) {
+    __syncthreads();  // every warp is done with field f-1, whose slot is refilled now
+    issue(f + RING - 1);
+    cp_async_wait<RING - 1>();
+    __syncthreads();  // field f is in its slot
+    const T* Q = ring + ((f % RING) * 8 + warp) * RP;
+    T* q2 = a.q_out + qo + f * a.sQqo;
+    T qv[NPL], st[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) qv[j] = (u0 + j < km) ? Q[pk<T>(u0 + j)] : T(0);
+    // -------------------------------------------- interface values a[0..km]
+    if (km == 1) {
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) st[j] = qv[0];
+    } else {
+      T rhs[NPL], qa[NPL], qb[NPL];
+      T al = T(1), be = T(0);
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        qa[j] = Q[pk<T>(ia[j])];
+        qb[j] = Q[pk<T>(ib[j])];
+        rhs[j] = wa[j] * qa[j] + wb[j] * qb[j] + wc[j] * qsv;
+        const T aj = -mco[j] * rdv[j];
+        be = aj * be + rhs[j] * rdv[j];
+        al = aj * al;
+      }
+      T y[NPL];
+      {
+        T yp = affine_enter_fwd<T>(al, be, lane);
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+          yp = (rhs[j] - mco[j] * yp) * rdv[j];
+          y[j] = yp;
+        }
+      }
+      al = T(1);
+      be = T(0);
+#pragma unroll
+      for (int j = NPL - 1; j >= 0; --j) {
+        be = -cpb[j] * be + y[j];
+        al = -cpb[j] * al;
+      }
+      T av = affine_enter_bwd<T>(al, be, lane);
+#pragma unroll
+      for (int j = NPL - 1; j >= 0; --j) {
+        const int u = u0 + j;
+        av = y[j] - cpb[j] * av;
+        const bool clampit = KORD == 9 && u <= km && !(u == km && a.iv == -2);
+        st[j] = clampit ? clamp2(av, qa[j], qb[j]) : av;
+      }
+    }
+    // ------------------------------------------ sub-grid parabolas of layers
+    {
+      const T st_next = __shfl_down_sync(0xffffffffu, st[0], 1);
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        const int u = u0 + j;
+        const Profile<T> p = layer_profile_sel<T, KORD>(qv[j], st[j], j + 1 < NPL ? st[j + 1] : st_next, a.iv,
+                                                        floor_v);
+        if (u < km) {
+          S.pl[pk<T>(u)] = p.l;
+          S.pr[pk<T>(u)] = p.r;
+          S.p6[pk<T>(u)] = p.s6;
+        }
+      }
+    }
+    __syncwarp();
+    // ------------------------------------------------------- integration
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      const int t = u0 + j;
+      const int Lt = Ls[j], Lb = Ls[j + 1];
+      const T Xt = Xs[j], Xb = Xs[j + 1];
+      const bool inside = (Lb == Lt) || (Lb == Lt + 1 && Xb == T(0));
+      const int it = pk<T>(Lt), ib_ = pk<T>(Lb);
+      const T qt = Q[it], dpt = S.dp[it];
+      const T pm1 = pmean(S.pl[it], S.pr[it], S.p6[it], Xt, (inside && Lb == Lt) ? Xb : T(1));
+      const T vin = (Xt == T(0) && (Lb == Lt + 1 || Xb == T(1))) ? qt : pm1;
+      T mass = Xt == T(0) ? qt * dpt : (dpt * (T(1) - Xt)) * pm1;
+      for (int m = Lt + 1; m < Lb; ++m) mass = mass + Q[pk<T>(m)] * S.dp[pk<T>(m)];
+      const T qb_ = Q[ib_], dpb = S.dp[ib_];
+      const T pm2 = pmean(S.pl[ib_], S.pr[ib_], S.p6[ib_], T(0), Xb);
+      const T bot = Xb >= T(1) ? qb_ * (dpb * Xb) : (Xb > T(0) ? (dpb * Xb) * pm2 : T(0));
+      mass = mass + bot;
+      const T out = inside ? vin : mass * rdpk[j];
+      if (real && t < kn) q2[(long long)t * a.sQk] = out;
+    }
+  }
+}
+
+template <typename T, int KORD, int NPL>
+static cudaError_t set_remap_attr() {
+  return cudaFuncSetAttribute(k_remap_warp<T, KORD, NPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)remap_warp_smem<T, NPL>());
+}
+
+// Raise the dynamic shared-memory limit of the remap kernels once per process
+// (before any stream capture).
+int prepare_remap_kernels() {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    cudaError_t es[] = {set_remap_attr<float, 9, 4>(),  set_remap_attr<float, 9, 5>(),  set_remap_attr<float, 4, 4>(),
+                        set_remap_attr<float, 4, 5>(),  set_remap_attr<double, 9, 4>(), set_remap_attr<double, 9, 5>(),
+                        set_remap_attr<double, 4, 4>(), set_remap_attr<double, 4, 5>()};
+    for (cudaError_t e : es)
+      if (e != cudaSuccess && err == cudaSuccess) err = e;
+  });
+  return err == cudaSuccess ? 0 : cuda_error(err, "cudaFuncSetAttribute(k_remap_warp)");
+}
+
+template <typename T, int KORD, int NPL>
+static cudaError_t launch_warp_npl(const RemapArgs<T>& a, cudaStream_t s) {
+  constexpr size_t smem = remap_warp_smem<T, NPL>();
+  const unsigned nb = (unsigned)((a.ncol + 7) / 8);
+  k_remap_warp<T, KORD, NPL><<<nb, 256, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int KORD>
+static cudaError_t launch_warp_form(const RemapArgs<T>& a, cudaStream_t s) {
+  if (std::max(a.km, a.kn) < 32 * 4) return launch_warp_npl<T, KORD, 4>(a, s);
+  return launch_warp_npl<T, KORD, 5>(a, s);
+}
+
 template <typename T>
 int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s) {
   if (a.km < 1 || a.km > KMAX || a.kn < 1 || a.kn > KMAX)
     return set_error(FV3G_E_ARG, "remap supports 1..%d layers (km=%d, kn=%d)", KMAX, a.km, a.kn);
-  const unsigned nb = (unsigned)((a.ncol + 127) / 128);
-  if (kord == 9) k_remap<T, 9><<<nb, 128, 0, s>>>(a);
-  else if (kord == 4) k_remap<T, 4><<<nb, 128, 0, s>>>(a);
-  else return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
+  if (kord != 9 && kord != 4) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
+  if (a.ncol > (1LL << 30)) return set_error(FV3G_E_ARG, "remap supports at most 2^30 columns per call");
+  {
+    const int prc = prepare_remap_kernels();
+    if (prc) return prc;
+  }
+  if (a.scratch != nullptr) {
+    const unsigned nb = (unsigned)((a.ncol + 127) / 128);
+    if (kord == 9) k_remap_scratch<T, 9><<<nb, 128, 0, s>>>(a);
+    else k_remap_scratch<T, 4><<<nb, 128, 0, s>>>(a);
+  } else {
+    const cudaError_t e = kord == 9 ? launch_warp_form<T, 9>(a, s) : launch_warp_form<T, 4>(a, s);
+    FV3G_CUDA(e);
+  }
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }

@@ -27,12 +27,16 @@ struct RemapArgs {
   long long ncol;      // ntiles * ni * nj
   int km, kn, iv;
   double q_min;
-  T* scratch;             // 6 * (KMAX+1) * ncol elements
-  unsigned char* sched;   // (KMAX+1) * ncol bytes
+  // Null: the warp-per-column kernel (no scratch).  Set: the thread-per-column
+  // kernel with this caller-owned scratch, 6 * (KMAX+1) * ncol elements and
+  // (KMAX+1) * ncol schedule bytes.
+  T* scratch;
+  unsigned char* sched;
 };
 
 template <typename T>
 int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s);
 size_t remap_scratch_bytes(long long ncol, bool fp64);
+int prepare_remap_kernels();
 
 }  // namespace fv3g
