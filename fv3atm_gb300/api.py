@@ -191,12 +191,12 @@ class CubeState:
     def set_timing(self, enable: bool) -> None:
         _lib.call("fv3g_set_timing", self._h, int(enable))
 
-    KERNEL_KINDS = ("prologue", "substep", "edge_fix", "remap")
+    KERNEL_KINDS = ("prologue", "substep", "edge_fix", "remap", "halo")
 
     def kernel_times(self) -> dict:
-        """{kind: (total ms, launches)} of the last completed step."""
-        ms = (C.c_double * 4)()
-        cnt = (C.c_int * 4)()
+        """{kind: (total ms, kernel launches)} of the last completed step."""
+        ms = (C.c_double * len(self.KERNEL_KINDS))()
+        cnt = (C.c_int * len(self.KERNEL_KINDS))()
         _lib.call("fv3g_kernel_times", self._h, ms, cnt)
         return {k: (ms[i], cnt[i]) for i, k in enumerate(self.KERNEL_KINDS)}
 

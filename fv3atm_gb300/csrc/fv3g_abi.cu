@@ -142,6 +142,7 @@ struct fv3g_state {
   bool timing = false;
   std::vector<cudaEvent_t> ev;
   std::vector<int> ev_kind;  // kernel kind ending at event i (i >= 1)
+  std::vector<int> ev_nk;    // kernels launched since event i-1
   int nev = 0;
   Topo topo{};
   std::vector<void*> allocs;
@@ -149,18 +150,21 @@ struct fv3g_state {
 
 namespace {
 
-enum { K_PROLOGUE = 0, K_SUBSTEP = 1, K_EDGEFIX = 2, K_REMAP = 3, K_NKINDS = 4 };
+enum { K_PROLOGUE = 0, K_SUBSTEP = 1, K_EDGEFIX = 2, K_REMAP = 3, K_HALO = 4, K_NKINDS = 5 };
 
-// Record a timing event (when enabled) marking the end of a kernel of `kind`.
-int mark(fv3g_state* st, int kind, cudaStream_t s) {
+// Record a timing event (when enabled) marking the end of the work of `kind`
+// since the previous mark: nkern kernel launches.
+int mark(fv3g_state* st, int kind, cudaStream_t s, int nkern = 1) {
   if (!st->timing) return 0;
   if (st->nev >= (int)st->ev.size()) {
     cudaEvent_t e;
     FV3G_CUDA(cudaEventCreate(&e));
     st->ev.push_back(e);
     st->ev_kind.push_back(kind);
+    st->ev_nk.push_back(nkern);
   }
   st->ev_kind[st->nev] = kind;
+  st->ev_nk[st->nev] = nkern;
   // inside stream capture the record must become an event node of the graph
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   FV3G_CUDA(cudaStreamIsCapturing(s, &cap));
@@ -338,15 +342,21 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
                             (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
                             st->n, 1, st->n, 6, st->npz, frac, s));
-  CHECK(mark(st, K_PROLOGUE, s));
+  CHECK(mark(st, K_PROLOGUE, s, 1));
   const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 5);
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
     const int dst = (src == 1) ? 2 : 1;
     const int dpo = (dpi == 1) ? 2 : 1;
     AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
+    CHECK(launch_cube_halo<T>((T*)st->q[src], a.sQt, st->plane, st->nq * st->npz, st->pg, st->n, st->topo, s));
+    CHECK(mark(st, K_HALO, s));
     CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
-    CHECK(mark(st, K_SUBSTEP, s));
+    {
+      const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
+      const int nint = bm.nbxi * bm.nbyi;
+      CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint)));
+    }
     CHECK(launch_edge_fix<T>(a, st->n, s));
     CHECK(mark(st, K_EDGEFIX, s));
     st->dp_start = dpi;
@@ -690,6 +700,7 @@ int fv3g_set_timing(fv3g_state* st, int enable) {
       FV3G_CUDA(cudaEventCreate(&e));
       st->ev.push_back(e);
       st->ev_kind.push_back(0);
+      st->ev_nk.push_back(0);
     }
   }
   return 0;
@@ -709,7 +720,7 @@ int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind)
     const int kind = st->ev_kind[i];
     if (kind >= 0 && kind < K_NKINDS) {
       ms_by_kind[kind] += ms;
-      if (launches_by_kind) launches_by_kind[kind] += 1;
+      if (launches_by_kind) launches_by_kind[kind] += st->ev_nk[i];
     }
   }
   return 0;

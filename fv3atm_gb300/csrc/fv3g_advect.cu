@@ -43,6 +43,8 @@ struct SmemLevel {
   T rry[TW][WIN];  // 1/ra_y [interior row][window col]
   T dpa[TW][TW];   // dp1/rarea
   T ub[TW][TW];    // rarea/dp2
+  T edx[2][4][WIN];  // edge CTAs: dxa at window columns e-2..e+1 of x edge A/B, per window row
+  T edy[2][4][WIN];  // dya at window rows e-2..e+1 of y edge A/B, per window column
 };
 
 template <typename T>
@@ -245,22 +247,34 @@ struct Line {
 template <typename T, int HORD, bool FLUXES, bool EDGES>
 __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>& L, SmemWarp<T>& S, int t, int k,
                                                T* eds, int iq, int i0, int j0, int ni, int nj, int lane, int exA,
-                                               int exB, int eyA, int eyB, bool direct, bool corner_block,
+                                               int exB, int eyA, int eyB, bool corner_block,
                                                long long efo, long long efe) {
   const PlaneGeom& pg = a.pg;
   const int n = a.npx - 1;
-  // ------------------------------------------ window load (y-sweep corners)
-  {
+  // Cube-corner halo blocks of the window, which copy_corners fills by a
+  // rotation that depends on the sweep direction (1 = x, 2 = y).
+  auto corner_cells = [&](int dir) {
     const int i = i0 - 3 + lane;
-    const T* qp = a.q_in + t * a.sQt + iq * a.sQq + k * a.sQk;
-    if (direct) {
-      const T* src = qp + pg.at(i, j0 - 3);
-#pragma unroll 8
-      for (int r = 0; r < WIN; ++r) S.q[r][lane] = src[(long long)r * pg.pitch];
-    } else {
-#pragma unroll 4
-      for (int r = 0; r < WIN; ++r) S.q[r][lane] = load_q(a, t, iq, k, i, j0 - 3 + r, 2);
+#pragma unroll 1
+    for (int r = 0; r < WIN; ++r) {
+      const int j = j0 - 3 + r;
+      const bool oi = (i < 1) || (i > a.npx - 1), oj = (j < 1) || (j > a.npy - 1);
+      if (oi && oj) S.q[r][lane] = load_q(a, t, iq, k, i, j, dir);
     }
+  };
+  // ------------------------------------------ window load (y-sweep corners)
+  // The planes hold their halo strips (caller-filled, or k_cube_halo); cells
+  // beyond the plane are clamped and feed only discarded outputs.
+  {
+    const int ic = min(max(i0 - 3 + lane, pg.isd), pg.isd + pg.pitch - 1);
+    const T* src = a.q_in + t * a.sQt + iq * a.sQq + k * a.sQk + (ic - pg.isd);
+    const int jhi = pg.jsd + pg.rows - 1;
+#pragma unroll 8
+    for (int r = 0; r < WIN; ++r) {
+      const int jr = min(max(j0 - 3 + r, pg.jsd), jhi);
+      S.q[r][lane] = src[(long long)(jr - pg.jsd) * pg.pitch];
+    }
+    if (corner_block) corner_cells(2);
   }
   __syncwarp();
 
@@ -273,11 +287,10 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     const T* qcol = &S.q[0][w];
     if (EDGES) {
       auto ex = [qcol](int m) { return qcol[m * PQ]; };
-      const T* dya = a.dya + t * a.sMt;
-      const int ig = i0 - 3 + w;
-      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
-      edge_devs<T, HORD>(eyA, ex, ed, ed0);
-      edge_devs<T, HORD>(eyB, ex, ed, ed0 + 8 * 32);
+      auto edA = [&L, w, eyA](int m) { return L.edy[0][m - eyA + 2][w]; };
+      auto edB = [&L, w, eyB](int m) { return L.edy[1][m - eyB + 2][w]; };
+      edge_devs<T, HORD>(eyA, ex, edA, ed0);
+      edge_devs<T, HORD>(eyB, ex, edB, ed0 + 8 * 32);
     }
     const bool keep_fy2 = (w >= 3 && w < 29);
     T* fy2 = &S.fy2[0][keep_fy2 ? w - 3 : 0];
@@ -303,13 +316,7 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
 
   // -------------------------------------- corner blocks for the x sweeps
   if (corner_block) {
-    const int i = i0 - 3 + lane;
-#pragma unroll 1
-    for (int r = 0; r < WIN; ++r) {
-      const int j = j0 - 3 + r;
-      const bool oi = (i < 1) || (i > a.npx - 1), oj = (j < 1) || (j > a.npy - 1);
-      if (oi && oj) S.q[r][lane] = load_q(a, t, iq, k, i, j, 1);
-    }
+    corner_cells(1);
     __syncwarp();
   }
 
@@ -323,14 +330,13 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     if (EDGES) {
       auto exi = [qrow](int m) { return qrow[m]; };
       auto exo = [qirow](int m) { return qirow[m]; };
-      const T* dxa = a.dxa + t * a.sMt;
-      const int jg = j0 - 3 + r;
-      auto ed = [dxa, pg, i0, jg](int m) { return ld_field(dxa, pg, i0 - 3 + m, jg); };
-      edge_devs<T, HORD>(exA, exi, ed, ed0);
-      edge_devs<T, HORD>(exB, exi, ed, ed0 + 8 * 32);
+      auto edA = [&L, r, exA](int m) { return L.edx[0][m - exA + 2][r]; };
+      auto edB = [&L, r, exB](int m) { return L.edx[1][m - exB + 2][r]; };
+      edge_devs<T, HORD>(exA, exi, edA, ed0);
+      edge_devs<T, HORD>(exB, exi, edB, ed0 + 8 * 32);
       if (outer) {
-        edge_devs<T, HORD>(exA, exo, ed, ed1);
-        edge_devs<T, HORD>(exB, exo, ed, ed1 + 8 * 32);
+        edge_devs<T, HORD>(exA, exo, edA, ed1);
+        edge_devs<T, HORD>(exB, exo, edB, ed1 + 8 * 32);
       }
     }
     const bool efw = EDGES && a.cube && a.eflux != nullptr && outer && ro < nj;
@@ -378,11 +384,10 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     const T* qjcol = &S.q[0][c];
     if (EDGES) {
       auto ex = [qjcol](int m) { return qjcol[m * PQ]; };
-      const T* dya = a.dya + t * a.sMt;
-      const int ig = i0 + c;
-      auto ed = [dya, pg, ig, j0](int m) { return ld_field(dya, pg, ig, j0 - 3 + m); };
-      edge_devs<T, HORD>(eyA, ex, ed, ed0);
-      edge_devs<T, HORD>(eyB, ex, ed, ed0 + 8 * 32);
+      auto edA = [&L, c, eyA](int m) { return L.edy[0][m - eyA + 2][c + 3]; };
+      auto edB = [&L, c, eyB](int m) { return L.edy[1][m - eyB + 2][c + 3]; };
+      edge_devs<T, HORD>(eyA, ex, edA, ed0);
+      edge_devs<T, HORD>(eyB, ex, edB, ed0 + 8 * 32);
     }
     const int ig = i0 + c;
     const bool valid_c = c < ni;
@@ -523,21 +528,27 @@ __global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a, const Block
       L.ub[r][c] = ra / d2;
       if (r < nj && c < ni && dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
     }
+    if (EDGES) {  // metrics of the one-sided edge values: dxa across x edges, dya across y edges
+      const T* dxa = a.dxa + t * a.sMt;
+      const T* dya = a.dya + t * a.sMt;
+      for (int e = threadIdx.x; e < 2 * 4 * WIN; e += blockDim.x) {
+        const int side = e / (4 * WIN), m = (e / WIN) % 4, w = e % WIN;
+        const int ex = side ? exB : exA, ey = side ? eyB : eyA;
+        L.edx[side][m][w] = ex == NO_EDGE ? T(1) : ld_field(dxa, pg, i0 - 3 + ex - 2 + m, j0 - 3 + w);
+        L.edy[side][m][w] = ey == NO_EDGE ? T(1) : ld_field(dya, pg, i0 - 3 + w, j0 - 3 + ey - 2 + m);
+      }
+    }
   }
   __syncthreads();
 
   const bool corner_block = !a.nested && a.corners != 0 &&
                             ((i0 - 3 < 1) || (i0 + 28 > a.npx - 1)) && ((j0 - 3 < 1) || (j0 + 28 > a.npy - 1));
-  const bool inside = i0 - 3 >= 1 && i0 + 28 <= n && j0 - 3 >= 1 && j0 + 28 <= n;
-  const bool in_plane = i0 - 3 >= pg.isd && i0 + 28 <= pg.isd + pg.pitch - 1 && j0 - 3 >= pg.jsd &&
-                        j0 + 28 <= pg.jsd + pg.rows - 1;
-  const bool direct = in_plane && (a.cube ? inside : true) && !corner_block;
   // edge-flux index (((t*4 + e)*npz + k)*nq + iq)*n + s = efo + e*efe + iq*n + s
   const long long efe = (long long)a.npz * a.nq * n;
   const long long efo = (((long long)t * 4) * a.npz + k) * a.nq * n;
 
   for (int iq = warp; iq < a.nq; iq += W)
-    advance_tracer<T, HORD, FLUXES, EDGES>(a, L, S, t, k, eds, iq, i0, j0, ni, nj, lane, exA, exB, eyA, eyB, direct,
+    advance_tracer<T, HORD, FLUXES, EDGES>(a, L, S, t, k, eds, iq, i0, j0, ni, nj, lane, exA, exB, eyA, eyB,
                                            corner_block, efo, efe);
 }
 
@@ -565,6 +576,34 @@ __device__ __forceinline__ T edge_correction(const AdvArgs<T>& a, int n, int t, 
   const T own = a.eflux[((((long long)nt * 4 + ne) * a.npz + k) * a.nq + iq) * n + sb];
   const T mine = a.eflux[((((long long)t * 4 + e) * a.npz + k) * a.nq + iq) * n + s];
   return own + mine;
+}
+
+// Halo strips (NG cells deep along the four tile edges) of every plane of
+// the six tiles, copied from the neighbouring tiles through the cube-edge
+// mapping of cube_source.  The corner blocks are left to the sweeps: their
+// copy_corners rotation depends on the sweep direction.  Reads touch only
+// interior cells and writes only halo cells, so one buffer serves as both.
+template <typename T>
+__global__ void k_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, Topo topo) {
+  const int t = blockIdx.z;
+  const int cells = 4 * NG * n;
+  for (int pl = blockIdx.y; pl < nplanes; pl += gridDim.y) {
+    T* qp = q + pl * splane;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
+      const int e = c / (NG * n), r = c - e * (NG * n);
+      const int d = r / n + 1, sv = r - (d - 1) * n;
+      int i, j;
+      switch (e) {
+        case EW: i = 1 - d; j = sv + 1; break;
+        case EE: i = n + d; j = sv + 1; break;
+        case ES: i = sv + 1; j = 1 - d; break;
+        default: i = sv + 1; j = n + d; break;
+      }
+      int ts = t, is = i, js = j;
+      cube_source(topo, n, ts, is, js);
+      qp[t * sQt + pg.at(i, j)] = qp[ts * sQt + pg.at(is, js)];
+    }
+  }
 }
 
 template <typename T>
@@ -756,6 +795,16 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
 }
 
 template <typename T>
+int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
+                     cudaStream_t s) {
+  const int cells = 4 * NG * n;
+  dim3 grid((unsigned)std::min((cells + 255) / 256, 64), (unsigned)std::min(nplanes, 65535), 6);
+  k_cube_halo<T><<<grid, 256, 0, s>>>(q, sQt, splane, nplanes, pg, n, topo);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <typename T>
 int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s) {
   const long long tot = (long long)6 * 4 * n;
   dim3 grid((unsigned)((tot + 127) / 128), a.npz * a.nq);
@@ -789,6 +838,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
 #define FV3G_INST(T)                                                                                          \
   template int launch_substep<T>(const AdvArgs<T>&, int, bool, int, cudaStream_t);                          \
   template int launch_edge_fix<T>(const AdvArgs<T>&, int, cudaStream_t);                                     \
+  template int launch_cube_halo<T>(T*, long long, long long, int, PlaneGeom, int, const Topo&, cudaStream_t);   \
   template int launch_area_flux<T>(T*, T*, T*, T*, T*, T*, const T*, const T*, const T*, const T*, const T*, \
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \
                                    int, T, cudaStream_t);                                                    \

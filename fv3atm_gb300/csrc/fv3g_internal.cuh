@@ -72,7 +72,7 @@ struct AdvArgs {
   int nq;
   int corners;  // bit 0 sw, 1 se, 2 nw, 3 ne: tile corner is a cube corner
   int nested;
-  int cube;     // 1: halo gathered from neighbour tiles through topo
+  int cube;     // 1: six tiles; halo strips of q_in already filled (k_cube_halo), eflux written
   Topo topo;
   T* eflux;     // cube: outward tile-edge fluxes [tile][edge][level][tracer][n]
   int npz;
@@ -155,6 +155,9 @@ int cuda_error(cudaError_t e, const char* what);
   } while (0)
 
 // Host launchers (fv3g_advect.cu)
+template <typename T>
+int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
+                     cudaStream_t s);
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s);
 template <typename T>

@@ -229,8 +229,10 @@ int fv3g_stream_sync(fv3g_state* st, void* stream);
 /* Per-kernel timing of fv3g_step: with timing enabled, CUDA events are
  * recorded around every kernel of the step (also inside the graph);
  * fv3g_kernel_times returns, for the last completed step, the summed ms and
- * the launch count per kernel kind: [0] prologue (area fluxes), [1] advection
- * substep, [2] tile-edge flux fix, [3] column remap. */
+ * the kernel launch count per kind (arrays of FV3G_KERNEL_KINDS entries):
+ * [0] prologue (area fluxes), [1] advection substep, [2] tile-edge flux fix,
+ * [3] column remap, [4] halo strips of the six tiles. */
+#define FV3G_KERNEL_KINDS 5
 int fv3g_set_timing(fv3g_state* st, int enable);
 int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind);
 /* Sticky device error word of the state (0 = none); cleared by reading. */
