@@ -343,7 +343,7 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
                             st->n, 1, st->n, 6, st->npz, frac, s));
   CHECK(mark(st, K_PROLOGUE, s, 1));
-  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 4 : 5);
+  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
     const int dst = (src == 1) ? 2 : 1;

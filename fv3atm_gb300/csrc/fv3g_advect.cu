@@ -14,8 +14,9 @@
 //   S2  lane = window row: inner x-PPM on q (corners re-filled for an x sweep)
 //       -> q_j, and on the 26 interior rows the outer x-PPM on q_i, combined
 //       into the final x flux and its divergence;
-//   S3  lane = interior column: outer y-PPM on q_j, final y flux, and the
-//       flux-form update q <- (q dp1 + div F * rarea) / dp2 written to HBM.
+//   S3  lane = window column (interior ones): outer y-PPM on q_j, final y
+//       flux, and the flux-form update q <- (q dp1 + div F * rarea) / dp2
+//       written to HBM.  The inner y flux of S1 stays in the lane's registers.
 // Each lane marches its line with a register pipeline (slope -> interface ->
 // edge deviations -> flux), so intermediate fluxes never leave the SM and q
 // is read once and written once per substep.  Halo cells are gathered from
@@ -51,7 +52,6 @@ template <typename T>
 struct SmemWarp {
   T q[WIN][PQ];   // tracer window; S2 overwrites each row with q_j (interior columns)
   T qi[TW][PQ];   // q_i; then q dp1/rarea + x-flux divergence (or the x fluxes)
-  T fy2[NF][TW];  // inner y flux [face][interior col]
 };
 
 // Per-warp shared memory; edge CTAs add the deviations of two lines at two
@@ -193,8 +193,7 @@ __device__ __noinline__ void edge_devs(int e, EX x, ED ed, T* o) {
 template <typename T>
 __device__ __forceinline__ T dm_clamp(T xm, T x0, T xp) {
   const T xt = T(0.25) * (xp - xm);
-  const T mm = tmin(tmax(tmax(xm, x0), xp) - x0, x0 - tmin(tmin(xm, x0), xp));
-  return tmin(tmax(xt, -mm), mm);
+  return copysign_t(tmin3(tabs(xt), tmax3(xm, x0, xp) - x0, x0 - tmin3(xm, x0, xp)), xt);
 }
 
 template <typename T, int HORD>
@@ -227,11 +226,11 @@ struct Line {
       if ((unsigned)dB < 4u) { bl = ed[(8 + dB) * 32]; br = ed[(12 + dB) * 32]; }
     }
     const T b0 = bl + br;
-    const bool pos = c > T(0);
     const T a = tabs(c);
     const T w1 = T(1) - a, w2 = a * w1;
-    const T xu = pos ? xa : xb, du = pos ? pbr : bl, bu = pos ? pb0 : b0;
-    const T fl = (xu + w1 * du) - w2 * bu;
+    const T fl_l = (xa + w1 * pbr) - w2 * pb0;  // upwind cell on the left (c > 0)
+    const T fl_r = (xb + w1 * bl) - w2 * b0;
+    const T fl = c > T(0) ? fl_l : fl_r;
     xa = xb;
     xb = xc;
     xc = x;
@@ -278,6 +277,7 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
   }
   __syncwarp();
 
+  T fyr[NF];  // inner y flux of this lane's column at faces 3..29 (S1 -> S3)
   // edge deviations of the lines in flight: eds[line][16][32], lines 0 (and 1 in S2)
   T* const ed0 = eds + lane;
   T* const ed1 = eds + 16 * 32 + lane;
@@ -292,22 +292,18 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       edge_devs<T, HORD>(eyA, ex, edA, ed0);
       edge_devs<T, HORD>(eyB, ex, edB, ed0 + 8 * 32);
     }
-    const bool keep_fy2 = (w >= 3 && w < 29);
-    T* fy2 = &S.fy2[0][keep_fy2 ? w - 3 : 0];
     Line<T, HORD> ln;
     ln.init();
 #pragma unroll
     for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qcol[m * PQ], T(0), ed0, eyA, eyB);
-    T fy = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, eyA, eyB);
-    T fyy_prev = L.yf[0][w] * fy;
-    if (keep_fy2) fy2[0] = fy;
-#pragma unroll 2
+    fyr[0] = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, eyA, eyB);
+    T fyy_prev = L.yf[0][w] * fyr[0];
+#pragma unroll
     for (int m = 6; m < WIN; ++m) {
       const int f = m - 2;
       const T xrow = ln.xa;  // cell row f-1 = m-3
-      fy = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, eyA, eyB);
-      const T fyy = L.yf[f - 3][w] * fy;
-      if (keep_fy2) fy2[(f - 3) * TW] = fy;
+      fyr[f - 3] = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, eyA, eyB);
+      const T fyy = L.yf[f - 3][w] * fyr[f - 3];
       S.qi[f - 4][w] = (xrow * L.area[f - 1][w] + fyy_prev - fyy) * L.rry[f - 4][w];
       fyy_prev = fyy;
     }
@@ -379,8 +375,8 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
   __syncwarp();
 
   // ---------------------------- S3: outer y on q_j, update / write -------
-  if (lane < TW) {
-    const int c = lane;
+  if (lane >= 3 && lane < 3 + TW) {
+    const int c = lane - 3;  // interior column
     const T* qjcol = &S.q[0][c];
     if (EDGES) {
       auto ex = [qjcol](int m) { return qjcol[m * PQ]; };
@@ -398,13 +394,13 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     ln.init();
 #pragma unroll
     for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qjcol[m * PQ], T(0), ed0, eyA, eyB);
-    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, eyA, eyB) + S.fy2[0][c]) * L.my[0][c];
+    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, eyA, eyB) + fyr[0]) * L.my[0][c];
     if (FLUXES && valid_c) fyo[0] = Fprev;
     if (efw && j0 == 1) a.eflux[efo + 2 * efe + iq * (long long)n + (ig - 1)] = -Fprev;
-#pragma unroll 2
+#pragma unroll
     for (int m = 6; m < WIN; ++m) {
       const int f = m - 2;
-      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, eyA, eyB) + S.fy2[f - 3][c]) *
+      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, eyA, eyB) + fyr[f - 3]) *
                   L.my[f - 3][c];
       const int ir = f - 4;  // interior row between faces f-1 and f
       if (FLUXES) {
@@ -432,7 +428,7 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
 // not need.  Interior CTAs cover the rectangle [bx0, bx0+nbxi) x [by0,
 // by0+nbyi) of CTA tiles; edge CTAs enumerate the ring around it row by row.
 template <typename T, int HORD, bool FLUXES, bool EDGES>
-__global__ void __launch_bounds__(256) k_substep(const AdvArgs<T> a, const BlockMap bm) {
+__global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const BlockMap bm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
@@ -742,9 +738,9 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   return 0;
 }
 
-// Largest warps per CTA whose shared memory fits in 227 KB (at most 8).
+// Largest warps per CTA whose shared memory fits in 227 KB (at most 10).
 static int max_warps(bool fp64) {
-  int w = 8;
+  int w = 10;
   while (w > 1 && substep_smem_bytes(fp64, w, true) > 227 * 1024) --w;
   return w;
 }

@@ -112,6 +112,19 @@ template <typename T> __device__ __forceinline__ T tsign(T a, T b) {
 }
 __device__ __forceinline__ float copysign_t(float a, float b) { return copysignf(a, b); }
 __device__ __forceinline__ double copysign_t(double a, double b) { return copysign(a, b); }
+// three-input min / max (one instruction for f32 on sm_100 and later)
+__device__ __forceinline__ float tmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float tmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ double tmax3(double a, double b, double c) { return fmax(fmax(a, b), c); }
+__device__ __forceinline__ double tmin3(double a, double b, double c) { return fmin(fmin(a, b), c); }
 template <typename T> __device__ __forceinline__ T clamp2(T a, T x0, T x1) {
   return tmin(tmax(a, tmin(x0, x1)), tmax(x0, x1));
 }
