@@ -80,6 +80,32 @@ def map1_ppm(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv
               iv, kord)
 
 
+def fv_tp_2d_tl(q, q_tl, crx, cry, npx, npy, hord, fx, fx_tl, fy, fy_tl, xfx, yfx, gridstruct: GridStruct,
+                bd: Bounds, ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+    """Tangent-linear fv_tp_2d (Courant numbers and mass fluxes frozen); fx / fy may be None."""
+    _lib.call("fv3g_fv_tp_2d_tl", _p(q), _p(q_tl), _p(crx), _p(cry), npx, npy, hord, _p(fx), _p(fx_tl), _p(fy),
+              _p(fy_tl), _p(xfx), _p(yfx), C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y),
+              C.c_double(lim_fac), _p(mfx), _p(mfy), nord, C.c_double(damp_c))
+
+
+def fv_tp_2d_ad(q, q_ad, crx, cry, npx, npy, hord, fx_ad, fy_ad, xfx, yfx, gridstruct: GridStruct, bd: Bounds,
+                ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+    """Adjoint fv_tp_2d at trajectory q: q_ad += J^T (fx_ad, fy_ad); fx_ad, fy_ad are zeroed."""
+    _lib.call("fv3g_fv_tp_2d_ad", _p(q), _p(q_ad), _p(crx), _p(cry), npx, npy, hord, _p(fx_ad), _p(fy_ad), _p(xfx),
+              _p(yfx), C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y), C.c_double(lim_fac), _p(mfx),
+              _p(mfy), nord, C.c_double(damp_c))
+
+
+def map1_ppm_tl(km, pe1, q1, q1_tl, qs, kn, pe2, q2, q2_tl, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord) -> None:
+    _lib.call("fv3g_map1_ppm_tl", km, _p(pe1), _p(q1), _p(q1_tl), _p(qs), kn, _p(pe2), _p(q2), _p(q2_tl), i1, i2, j,
+              ibeg, iend, jbeg, jend, iv, kord)
+
+
+def map1_ppm_ad(km, pe1, q1, q1_ad, qs, kn, pe2, q2_ad, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord) -> None:
+    _lib.call("fv3g_map1_ppm_ad", km, _p(pe1), _p(q1), _p(q1_ad), _p(qs), kn, _p(pe2), _p(q2_ad), i1, i2, j, ibeg,
+              iend, jbeg, jend, iv, kord)
+
+
 def map_scalar_3d(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j1, j2, ibeg, iend, jbeg, jend, nq, iv, kord, q_min) -> None:
     _lib.call("fv3g_map_scalar_3d", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j1, j2, ibeg, iend,
               jbeg, jend, nq, iv, kord, C.c_double(q_min))

@@ -56,13 +56,14 @@ struct SmemWarp {
 
 // Per-warp shared memory; edge CTAs add the deviations of two lines at two
 // edges, [2][16][32] values.
-__host__ __device__ constexpr size_t warp_smem_bytes(bool fp64, bool edges) {
-  return fp64 ? sizeof(SmemWarp<double>) + (edges ? 2 * 16 * 32 * sizeof(double) : 0)
-              : sizeof(SmemWarp<float>) + (edges ? 2 * 16 * 32 * sizeof(float) : 0);
+template <typename T>
+__host__ __device__ constexpr size_t warp_smem_bytes(bool edges) {
+  return sizeof(SmemWarp<T>) + (edges ? 2 * 16 * 32 * sizeof(T) : 0);
 }
 
-size_t substep_smem_bytes(bool fp64, int warps, bool edges) {
-  return (fp64 ? sizeof(SmemLevel<double>) : sizeof(SmemLevel<float>)) + warps * warp_smem_bytes(fp64, edges);
+template <typename T>
+size_t substep_smem_bytes(int warps, bool edges) {
+  return sizeof(SmemLevel<T>) + warps * warp_smem_bytes<T>(edges);
 }
 
 // ----------------------------------------------------------- halo source ---
@@ -196,16 +197,26 @@ __device__ __forceinline__ T dm_clamp(T xm, T x0, T xp) {
   return copysign_t(tmin3(tabs(xt), tmax3(xm, x0, xp) - x0, x0 - tmin3(xm, x0, xp)), xt);
 }
 
+// Steps of a line whose cell m-2 lies next to a cube-face edge: bit m of
+// mask, for the two edges at window faces eA and eB (warp-uniform).
+struct EdgeSel {
+  unsigned mask;
+  int eA, eB;
+};
+__device__ __forceinline__ EdgeSel edge_sel(int eA, int eB) {
+  auto bits = [](int e) { return (e >= 0 && e < 32) ? (0xFu << e) : 0u; };
+  return EdgeSel{bits(eA) | bits(eB), eA, eB};
+}
+
 template <typename T, int HORD>
 struct Line {
   T xa, xb, xc, dmb, alb, pbr, pb0;
 
   __device__ __forceinline__ void init() { xa = xb = xc = dmb = alb = pbr = pb0 = T(0); }
 
-  // ed: this lane's edge deviations (16 lane-strided slots: edge A bl0..3 br0..3, then edge B);
-  // eA/eB: window faces of the edges (warp-uniform), NO_EDGE if none
+  // ed: this lane's edge deviations (16 lane-strided slots: edge A bl0..3 br0..3, then edge B)
   template <bool EDGES>
-  __device__ __forceinline__ T step(int m, T x, T c, const T* ed, int eA, int eB) {
+  __device__ __forceinline__ T step(int m, T x, T c, const T* ed, const EdgeSel& es) {
     T alc, bl, br;
     if (HORD == 8) {
       const T dmc = dm_clamp(xb, xc, x);                      // dm[m-1]
@@ -220,10 +231,11 @@ struct Line {
       bl = alb - xb;
       br = alc - xb;
     }
-    if (EDGES) {  // cell m-2 is cell e-2+d of an edge
-      const int dA = m - eA, dB = m - eB;
-      if ((unsigned)dA < 4u) { bl = ed[dA * 32]; br = ed[(4 + dA) * 32]; }
-      if ((unsigned)dB < 4u) { bl = ed[(8 + dB) * 32]; br = ed[(12 + dB) * 32]; }
+    if (EDGES && ((es.mask >> m) & 1u)) {  // cell m-2 is cell e-2+d of an edge
+      const int dA = m - es.eA;
+      const int slot = (unsigned)dA < 4u ? dA : 8 + (m - es.eB);
+      bl = ed[slot * 32];
+      br = ed[(slot + 4) * 32];
     }
     const T b0 = bl + br;
     const T a = tabs(c);
@@ -264,20 +276,22 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
   // ------------------------------------------ window load (y-sweep corners)
   // The planes hold their halo strips (caller-filled, or k_cube_halo); cells
   // beyond the plane are clamped and feed only discarded outputs.
-  {
+  auto load_window = [&](const T* base) {
     const int ic = min(max(i0 - 3 + lane, pg.isd), pg.isd + pg.pitch - 1);
-    const T* src = a.q_in + t * a.sQt + iq * a.sQq + k * a.sQk + (ic - pg.isd);
+    const T* src = base + t * a.sQt + iq * a.sQq + k * a.sQk + (ic - pg.isd);
     const int jhi = pg.jsd + pg.rows - 1;
 #pragma unroll 8
     for (int r = 0; r < WIN; ++r) {
       const int jr = min(max(j0 - 3 + r, pg.jsd), jhi);
       S.q[r][lane] = src[(long long)(jr - pg.jsd) * pg.pitch];
     }
-    if (corner_block) corner_cells(2);
-  }
+  };
+  load_window(a.q_in);
+  if (corner_block) corner_cells(2);
   __syncwarp();
 
   T fyr[NF];  // inner y flux of this lane's column at faces 3..29 (S1 -> S3)
+  const EdgeSel esx = edge_sel(exA, exB), esy = edge_sel(eyA, eyB);
   // edge deviations of the lines in flight: eds[line][16][32], lines 0 (and 1 in S2)
   T* const ed0 = eds + lane;
   T* const ed1 = eds + 16 * 32 + lane;
@@ -295,14 +309,14 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     Line<T, HORD> ln;
     ln.init();
 #pragma unroll
-    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qcol[m * PQ], T(0), ed0, eyA, eyB);
-    fyr[0] = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, eyA, eyB);
+    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qcol[m * PQ], T(0), ed0, esy);
+    fyr[0] = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, esy);
     T fyy_prev = L.yf[0][w] * fyr[0];
 #pragma unroll
     for (int m = 6; m < WIN; ++m) {
       const int f = m - 2;
       const T xrow = ln.xa;  // cell row f-1 = m-3
-      fyr[f - 3] = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, eyA, eyB);
+      fyr[f - 3] = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, esy);
       const T fyy = L.yf[f - 3][w] * fyr[f - 3];
       S.qi[f - 4][w] = (xrow * L.area[f - 1][w] + fyy_prev - fyy) * L.rry[f - 4][w];
       fyy_prev = fyy;
@@ -311,7 +325,10 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
   __syncwarp();
 
   // -------------------------------------- corner blocks for the x sweeps
-  if (corner_block) {
+  if (a.q_in_x != nullptr) {  // separate input of the x sweeps (adjoint assembly)
+    load_window(a.q_in_x);
+    __syncwarp();
+  } else if (corner_block) {
     corner_cells(1);
     __syncwarp();
   }
@@ -341,13 +358,13 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     lo.init();
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      li.template step<EDGES>(m, qrow[m], T(0), ed0, exA, exB);
-      lo.template step<EDGES>(m, qirow[m], T(0), ed1, exA, exB);
+      li.template step<EDGES>(m, qrow[m], T(0), ed0, esx);
+      lo.template step<EDGES>(m, qirow[m], T(0), ed1, esx);
     }
     // face 3
     T c = L.cx[r][0];
-    T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, exA, exB);
-    T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, exA, exB);
+    T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, esx);
+    T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, esx);
     T fxx_prev = L.xf[r][0] * fx2;
     T F_prev = (fo + fx2) * L.mx[ro][0];
     if (FLUXES && outer) qirow[0] = F_prev;
@@ -357,8 +374,8 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       const int f = m - 2;
       const T xcol = li.xa;  // q at window column f-1 of this row
       c = L.cx[r][f - 3];
-      fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, exA, exB);
-      fo = lo.template step<EDGES>(m, qirow[m], c, ed1, exA, exB);
+      fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, esx);
+      fo = lo.template step<EDGES>(m, qirow[m], c, ed1, esx);
       const T fxx = L.xf[r][f - 3] * fx2;
       // q_j of window column f-1 (interior column f-4); column m-6 of this row is consumed
       qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
@@ -393,14 +410,14 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     Line<T, HORD> ln;
     ln.init();
 #pragma unroll
-    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qjcol[m * PQ], T(0), ed0, eyA, eyB);
-    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, eyA, eyB) + fyr[0]) * L.my[0][c];
+    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qjcol[m * PQ], T(0), ed0, esy);
+    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, esy) + fyr[0]) * L.my[0][c];
     if (FLUXES && valid_c) fyo[0] = Fprev;
     if (efw && j0 == 1) a.eflux[efo + 2 * efe + iq * (long long)n + (ig - 1)] = -Fprev;
 #pragma unroll
     for (int m = 6; m < WIN; ++m) {
       const int f = m - 2;
-      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, eyA, eyB) + fyr[f - 3]) *
+      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, esy) + fyr[f - 3]) *
                   L.my[f - 3][c];
       const int ir = f - 4;  // interior row between faces f-1 and f
       if (FLUXES) {
@@ -432,7 +449,7 @@ __global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const Block
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes(sizeof(T) == 8, EDGES);
+  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES);
   SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
   T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
 
@@ -727,28 +744,36 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const int nt = a.cube ? 6 : 1;
   if (nint > 0) {
     dim3 grid(nint, a.npz, nt);
-    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes(sizeof(T) == 8, warps, false), s>>>(a, bm);
+    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false), s>>>(a, bm);
     FV3G_CUDA(cudaGetLastError());
   }
   if (nring > 0) {
     dim3 grid(nring, a.npz, nt);
-    k_substep<T, HORD, FLUXES, true><<<grid, 32 * warps, substep_smem_bytes(sizeof(T) == 8, warps, true), s>>>(a, bm);
+    k_substep<T, HORD, FLUXES, true><<<grid, 32 * warps, substep_smem_bytes<T>(warps, true), s>>>(a, bm);
     FV3G_CUDA(cudaGetLastError());
   }
   return 0;
 }
 
 // Largest warps per CTA whose shared memory fits in 227 KB (at most 10).
-static int max_warps(bool fp64) {
+template <typename T>
+static int max_warps() {
   int w = 10;
-  while (w > 1 && substep_smem_bytes(fp64, w, true) > 227 * 1024) --w;
+  while (w > 1 && substep_smem_bytes<T>(w, true) > 227 * 1024) --w;
   return w;
 }
 
 template <typename T, int HORD, bool FLUXES, bool EDGES>
 static cudaError_t set_smem_attr() {
-  const int mx = (int)substep_smem_bytes(sizeof(T) == 8, max_warps(sizeof(T) == 8), EDGES);
+  const int mx = (int)substep_smem_bytes<T>(max_warps<T>(), EDGES);
   return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+template <typename T, int HORD>
+static void set_attrs_tl(cudaError_t& err) {
+  cudaError_t es[] = {set_smem_attr<T, HORD, true, false>(), set_smem_attr<T, HORD, true, true>()};
+  for (cudaError_t e : es)
+    if (e != cudaSuccess && err == cudaSuccess) err = e;
 }
 
 template <typename T, int HORD>
@@ -769,11 +794,12 @@ int prepare_kernels() {
     set_attrs<float, 8>(err);
     set_attrs<double, 5>(err);
     set_attrs<double, 8>(err);
+    set_attrs_tl<Dual<double>, 5>(err);
+    set_attrs_tl<Dual<double>, 8>(err);
   });
   return err == cudaSuccess ? 0 : cuda_error(err, "cudaFuncSetAttribute(k_substep)");
 }
 
-int substep_max_warps(bool fp64) { return max_warps(fp64); }
 
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s) {
@@ -781,10 +807,9 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
     int prc = prepare_kernels();
     if (prc) return prc;
   }
-  const int mw = max_warps(sizeof(T) == 8);
+  const int mw = max_warps<T>();
   if (warps < 1 || warps > mw)
-    return set_error(FV3G_E_ARG, "%s advection supports 1..%d warps per CTA (got %d)", sizeof(T) == 8 ? "FP64" : "FP32",
-                     mw, warps);
+    return set_error(FV3G_E_ARG, "this precision supports 1..%d advection warps per CTA (got %d)", mw, warps);
   if (hord == 8) return flux_mode ? launch_one<T, 8, true>(a, warps, s) : launch_one<T, 8, false>(a, warps, s);
   if (hord == 5) return flux_mode ? launch_one<T, 5, true>(a, warps, s) : launch_one<T, 5, false>(a, warps, s);
   return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
@@ -798,6 +823,17 @@ int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGe
   k_cube_halo<T><<<grid, 256, 0, s>>>(q, sQt, splane, nplanes, pg, n, topo);
   FV3G_CUDA(cudaGetLastError());
   return 0;
+}
+
+// Tangent-linear fluxes (fv_tp_2d flux mode on value/tangent pairs), one warp.
+int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s) {
+  {
+    int prc = prepare_kernels();
+    if (prc) return prc;
+  }
+  if (hord == 8) return launch_one<Dual<double>, 8, true>(a, 1, s);
+  if (hord == 5) return launch_one<Dual<double>, 5, true>(a, 1, s);
+  return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
 }
 
 template <typename T>

@@ -15,6 +15,8 @@
 
 #include "../../include/fv3g.h"
 
+#include "fv3g_dual.cuh"
+
 namespace fv3g {
 
 constexpr int NG = 3;    // halo width
@@ -78,6 +80,7 @@ struct AdvArgs {
   int npz;
   const T* ra_x;  // optional caller-supplied ra_x / ra_y planes (single level)
   const T* ra_y;
+  const T* q_in_x;  // optional separate input of the x sweeps, no corner fill (adjoint assembly)
   T* fx_out;    // flux mode: planes [level*nq + tracer] of the tile
   T* fy_out;
   long long sFlux;
@@ -168,6 +171,7 @@ int cuda_error(cudaError_t e, const char* what);
   } while (0)
 
 // Host launchers (fv3g_advect.cu)
+int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s);
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
                      cudaStream_t s);
@@ -190,9 +194,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
 int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
                 size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s);
 
-size_t substep_smem_bytes(bool fp64, int warps, bool edges);
 int prepare_kernels();
-int substep_max_warps(bool fp64);
 BlockMap block_map(int is, int ie, int js, int je, int npx, int npy, int nested);
 
 }  // namespace fv3g

@@ -114,14 +114,14 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
   } else {
     ptop = a.ak[0];
     double s = ptop;
-    for (int k = 0; k < km; ++k) s += (double)a.dp[fo + k * a.sFk];
+    for (int k = 0; k < km; ++k) s += value_of(a.dp[fo + k * a.sFk]);
     ps = s;
   }
   auto pe2_at = [&](int k) -> double {
     if (a.pe2 != nullptr) return a.pe2[(long long)k * nc + col];
     return a.ak[k] + a.bk[k] * ps;
   };
-  auto dp_src = [&](int k) -> double { return (double)a.dp[fo + k * a.sFk]; };
+  auto dp_src = [&](int k) -> double { return value_of(a.dp[fo + k * a.sFk]); };
   // source thickness (from pe differences, as the oracle) and schedule
   {
     double p1 = ptop;
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
         hi = (a.pe1 != nullptr) ? a.pe1[(long long)(k1 + 1) * nc + col] : hi + dp_src(k1);
       }
       s_L[(long long)k2 * nc + col] = (unsigned char)k1;
-      SC(s_x, k2) = (sizeof(T) == 8) ? T((p - lo) / (hi - lo)) : T(float(p - lo) / float(hi - lo));
+      SC(s_x, k2) = Single<T>::value ? T(float(p - lo) / float(hi - lo)) : T((p - lo) / (hi - lo));
     }
   }
   // LU factors of the interface system (rows 0..km), see the oracle restatement
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
     while (k1 < km - 1 && S.pe1[pk<double>(k1 + 1)] <= p) ++k1;
     const double pl = S.pe1[pk<double>(k1)], ph = S.pe1[pk<double>(k1 + 1)];
     Ls[j] = k1;
-    Xs[j] = (sizeof(T) == 8) ? T((p - pl) / (ph - pl)) : T(float(p - pl) / float(ph - pl));
+    Xs[j] = Single<T>::value ? T(float(p - pl) / float(ph - pl)) : T((p - pl) / (ph - pl));
   }
 #pragma unroll
   for (int j = 0; j < NPL; ++j) {
@@ -701,8 +701,22 @@ int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s) {
   return 0;
 }
 
-size_t remap_scratch_bytes(long long ncol, bool fp64) {
-  return (size_t)ncol * (KMAX + 1) * (6 * (fp64 ? 8 : 4) + 1) + 256;
+// Tangent-linear remap: the thread-per-column kernel on value/tangent pairs
+// (scratch supplied by the caller, remap_scratch_bytes(ncol, 16)).
+int launch_remap_tl(const RemapArgs<Dual<double>>& a, int kord, cudaStream_t s) {
+  if (a.km < 1 || a.km > KMAX || a.kn < 1 || a.kn > KMAX)
+    return set_error(FV3G_E_ARG, "remap supports 1..%d layers (km=%d, kn=%d)", KMAX, a.km, a.kn);
+  if (a.scratch == nullptr || a.sched == nullptr) return set_error(FV3G_E_ARG, "tangent-linear remap needs scratch");
+  const unsigned nb = (unsigned)((a.ncol + 127) / 128);
+  if (kord == 9) k_remap_scratch<Dual<double>, 9><<<nb, 128, 0, s>>>(a);
+  else if (kord == 4) k_remap_scratch<Dual<double>, 4><<<nb, 128, 0, s>>>(a);
+  else return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+size_t remap_scratch_bytes(long long ncol, size_t elem_bytes) {
+  return (size_t)ncol * (KMAX + 1) * (6 * elem_bytes + 1) + 256;
 }
 
 template int launch_remap<float>(const RemapArgs<float>&, int, cudaStream_t);

@@ -36,7 +36,8 @@ struct RemapArgs {
 
 template <typename T>
 int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s);
-size_t remap_scratch_bytes(long long ncol, bool fp64);
+size_t remap_scratch_bytes(long long ncol, size_t elem_bytes);  // scratch + schedule of the scratch kernel
 int prepare_remap_kernels();
+int launch_remap_tl(const RemapArgs<Dual<double>>& a, int kord, cudaStream_t s);
 
 }  // namespace fv3g

@@ -142,6 +142,40 @@ int fv3g_map_scalar_3d(int km, const double* pe1, const double* q1, const double
                        const double* pe2, double* q2, int i1, int i2, int j1, int j2, int ibeg,
                        int iend, int jbeg, int jend, int nq, int iv, int kord, double q_min);
 
+/* ------------------------------------------------------------------------ */
+/* Tangent-linear and adjoint models (tp_core / fv_mapz TL-AD pairs): the    */
+/* derivative with respect to the tracer only -- Courant numbers, mass       */
+/* fluxes and pressures frozen -- with every limiter branch frozen at the    */
+/* trajectory q.  Adjoints follow the generated-code convention: input       */
+/* adjoints are incremented, output adjoints are consumed (set to zero).     */
+/* ------------------------------------------------------------------------ */
+
+/* fv_tp_2d tangent-linear: (q, q_tl) -> (fx, fx_tl, fy, fy_tl); q and q_tl
+ * are read only (the copy_corners side effect on q is not reproduced);
+ * fx / fy may be NULL.  Other arguments as fv3g_fv_tp_2d. */
+int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, const double* cry, int npx,
+                     int npy, int hord, double* fx, double* fx_tl, double* fy, double* fy_tl,
+                     const double* xfx, const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd,
+                     const double* ra_x, const double* ra_y, double lim_fac, const double* mfx,
+                     const double* mfy, int nord, double damp_c);
+
+/* fv_tp_2d adjoint at trajectory q: q_ad (isd:ied, jsd:jed) += J^T (fx_ad, fy_ad);
+ * fx_ad (is:ie+1, js:je) and fy_ad (is:ie, js:je+1) are set to zero. */
+int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const double* cry, int npx, int npy,
+                     int hord, double* fx_ad, double* fy_ad, const double* xfx, const double* yfx,
+                     const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x, const double* ra_y,
+                     double lim_fac, const double* mfx, const double* mfy, int nord, double damp_c);
+
+/* map1_ppm tangent-linear on row j: (q1, q1_tl) -> (q2, q2_tl); q2 may be NULL. */
+int fv3g_map1_ppm_tl(int km, const double* pe1, const double* q1, const double* q1_tl, const double* qs,
+                     int kn, const double* pe2, double* q2, double* q2_tl, int i1, int i2, int j, int ibeg,
+                     int iend, int jbeg, int jend, int iv, int kord);
+
+/* map1_ppm adjoint on row j at trajectory q1: q1_ad += J^T q2_ad; q2_ad = 0. */
+int fv3g_map1_ppm_ad(int km, const double* pe1, const double* q1, double* q1_ad, const double* qs, int kn,
+                     const double* pe2, double* q2_ad, int i1, int i2, int j, int ibeg, int iend, int jbeg,
+                     int jend, int iv, int kord);
+
 /* Column remap on caller-owned DEVICE arrays that allocates no device memory.
  * No counterpart in the reference: it serves callers that cannot let a
  * library call cudaMalloc/cudaFree -- a model that owns all of its device

@@ -784,6 +784,22 @@ void orc_remap_columns(int ncol, int km, const double* pe1, const double* q1, co
   }
 }
 
+void orc_remap_columns_tl(int ncol, int km, const double* pe1, const double* q1, const double* dq1, const double* qs,
+                          int kn, const double* pe2, double* q2, double* dq2, int iv, int kord, double q_min) {
+  std::vector<double> p1(km + 1), p2(kn + 1);
+  std::vector<Dual> c1(km), c2(kn);
+  for (int c = 0; c < ncol; ++c) {
+    for (int k = 0; k <= km; ++k) p1[k] = pe1[c + (size_t)k * ncol];
+    for (int k = 0; k <= kn; ++k) p2[k] = pe2[c + (size_t)k * ncol];
+    for (int k = 0; k < km; ++k) c1[k] = Dual(q1[c + (size_t)k * ncol], dq1[c + (size_t)k * ncol]);
+    remap_column_t<Dual>(km, p1.data(), c1.data(), qs ? qs[c] : 0.0, kn, p2.data(), c2.data(), iv, kord, q_min);
+    for (int k = 0; k < kn; ++k) {
+      q2[c + (size_t)k * ncol] = c2[k].v;
+      dq2[c + (size_t)k * ncol] = c2[k].d;
+    }
+  }
+}
+
 double orc_mass_sum(const double* q, const double* dp, const double* area, long n, long narea) {
   double s = 0.0, comp = 0.0;  // Neumaier
   for (long i = 0; i < n; ++i) {

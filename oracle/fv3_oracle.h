@@ -110,6 +110,10 @@ void orc_map1_ppm(int km, const double* pe1, const double* q1, const double* qs,
 void orc_remap_columns(int ncol, int km, const double* pe1, const double* q1, const double* qs,
                        int kn, const double* pe2, double* q2, int iv, int kord, double q_min);
 
+/* Tangent-linear of orc_remap_columns (limiter branches frozen at q1). */
+void orc_remap_columns_tl(int ncol, int km, const double* pe1, const double* q1, const double* dq1, const double* qs,
+                          int kn, const double* pe2, double* q2, double* dq2, int iv, int kord, double q_min);
+
 /* Neumaier-compensated sum of a[i]*b[i]*c[i % nc] over n items. */
 double orc_mass_sum(const double* q, const double* dp, const double* area, long n, long narea);
 

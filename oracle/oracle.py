@@ -179,6 +179,18 @@ def remap_columns(pe1, q1, pe2, iv=0, kord=9, qs=None, q_min=0.0) -> np.ndarray:
     return q2
 
 
+def remap_columns_tl(pe1, q1, dq1, pe2, iv=0, kord=9, qs=None, q_min=0.0):
+    """Tangent-linear of remap_columns (limiter branches frozen at q1) -> (q2, dq2)."""
+    pe1, q1, dq1, pe2 = _f64(pe1), _f64(q1), _f64(dq1), _f64(pe2)
+    km, ncol = q1.shape
+    kn = pe2.shape[0] - 1
+    q2, dq2 = np.zeros((kn, ncol)), np.zeros((kn, ncol))
+    qsa = _f64(qs) if qs is not None else None
+    lib().orc_remap_columns_tl(ncol, km, _p(pe1), _p(q1), _p(dq1), _p(qsa) if qsa is not None else None, kn,
+                               _p(pe2), _p(q2), _p(dq2), iv, kord, C.c_double(q_min))
+    return q2, dq2
+
+
 def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min):
     """Row-wise map_scalar on Fortran-shaped arrays (q1 (km, jdim, idim) C-order == (i,j,k) Fortran)."""
     pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
