@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--warps", type=int, default=0, help="advection warps per CTA (0 = library default)")
+    ap.add_argument("--warps", type=int, default=0,
+                    help="advection warps per CTA (0 = chosen by fv3g_state_autotune)")
     return ap.parse_args()
 
 
@@ -308,6 +309,16 @@ def main():
     from fv3atm_gb300 import synth as S
 
     units = 6 * a.n * a.n * a.npz * a.nq  # tracer-cell-levels per step
+    # Pinned host arrays of the end-to-end leg, allocated first, as a model
+    # allocates its state at start-up: on this host, pinned blocks taken after
+    # the process has churned through tens of GB read back at a fraction of the
+    # link bandwidth.
+    nd = a.n + 6
+    e2e_shapes = {"Q": (6, a.nq, a.npz, nd, nd), "DELP": (6, a.npz, nd, nd), "CX": (6, a.npz, nd, a.n + 1),
+                  "CY": (6, a.npz, a.n + 1, nd), "MFX": (6, a.npz, a.n, a.n + 1), "MFY": (6, a.npz, a.n + 1, a.n),
+                  "Q_REMAPPED": (6, a.nq, a.npz, nd, nd)}
+    pinned = {} if a.no_e2e else {k: torch.empty(v, dtype=torch.float32, pin_memory=True)
+                                  for k, v in e2e_shapes.items()}
     t_gen = time.perf_counter()
     P = S.make_problem(a.n, a.npz, a.nq, seed=2000 + rank, cmax=0.8, pert_amp=10.0, dp_noise=0.10, device="cuda")
     torch.cuda.synchronize()
@@ -316,37 +327,18 @@ def main():
     peak, peak_kind = measured_peak()
     out = {}
 
-    # ---------------------------------------------------- FP64 reference leg
-    ref_q = None
-    if not a.no_fp64:
-        st = build_state(P, "fp64", a.nq, a.npz, a.n, 0)
-        st.step(a.q_split, use_graph=False)
-        st.sync()  # the step ran on the state's stream; the copy below runs on torch's
-        ref_q = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float64, device="cuda")
-        st.download_device("Q_REMAPPED", ref_q.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
-        torch.cuda.synchronize()
-        torch.cuda.synchronize()
-        ms, kern = timed_steps(st, a, world, max(1, a.steps), max(1, min(a.warmup, 3)), stream)
-        out["fp64"] = {"value": world * units * a.steps / (ms / 1e3), "ms_per_step": ms / a.steps,
-                       "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern.items()}}
-        st.close()
-        del st
-        torch.cuda.empty_cache()
-
     # --------------------------------------------------- mixed headline leg
     st = build_state(P, "mixed", a.nq, a.npz, a.n, a.warps)
+    warps = a.warps if a.warps > 0 else st.autotune()
     m0 = st.mass("Q")
     st.step(a.q_split, use_graph=False)
     st.sync()
     m1 = st.mass("Q_REMAPPED")
-    err = None
-    if ref_q is not None:
+    mq = None
+    if not a.no_fp64:  # kept for the comparison with the FP64 leg, which runs last
         mq = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, device="cuda")
         st.download_device("Q_REMAPPED", mq.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
-        err = rel_err_per_tracer(mq, ref_q, a.n)
-        del mq, ref_q
-        torch.cuda.empty_cache()
     q32 = P.q.to(torch.float32).contiguous()
     st.upload_device("Q", q32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
@@ -370,23 +362,44 @@ def main():
         host = {}
         src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
         for name in fields_in:
-            h = torch.empty(st.field_shape(name), dtype=torch.float32, pin_memory=True)
+            h = pinned[name]
+            assert tuple(h.shape) == tuple(st.field_shape(name)), name
             h.copy_(src[name].to(torch.float32).cpu())
             host[name] = h
-        hout = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, pin_memory=True)
+        hout = pinned["Q_REMAPPED"]
+        assert tuple(hout.shape) == tuple(st.field_shape("Q_REMAPPED"))
         h2d = sum(h.numel() * 4 for h in host.values())
         d2h = hout.numel() * 4
         s = stream.cuda_stream
 
+        marks = []
+
         def e2e_step():
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
             for name in fields_in:
                 st.upload_async(name, host[name].data_ptr(), True, s)
+            ev[1].record(stream)
             st.step(a.q_split, use_graph=True, stream=s)
+            ev[2].record(stream)
             st.download_async("Q_REMAPPED", hout.data_ptr(), True, s)
+            ev[3].record(stream)
+            marks.append(ev)
 
         st.set_timing(False)
         for _ in range(max(1, min(a.warmup, 2))):
             e2e_step()
+        torch.cuda.synchronize()
+        # link check in this process: one plain pinned copy of the largest input
+        probe = torch.empty(host["Q"].numel(), dtype=torch.float32, device="cuda")
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        with torch.cuda.stream(stream):
+            probe.copy_(host["Q"].view(-1), non_blocking=True)
+        l1.record(stream)
+        torch.cuda.synchronize()
+        link_h2d = host["Q"].numel() * 4 / (l0.elapsed_time(l1) / 1e3) / 1e9
+        del probe
         torch.cuda.synchronize()
         barrier(world)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -399,12 +412,38 @@ def main():
         torch.cuda.synchronize()
         barrier(world)
         ems = max_over_ranks(e0.elapsed_time(e1), world)
+        timed = marks[-a.steps:]
+        phase = {k: sum(ev[i].elapsed_time(ev[i + 1]) for ev in timed) / a.steps
+                 for i, k in enumerate(("h2d_ms", "step_ms", "d2h_ms"))}
         e2e = {"value": world * units * a.steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": ems / a.steps,
+               "d2h_bytes_per_step": d2h, "ms_per_step": ems / a.steps, "phases": phase,
+               "link_h2d_gbs_plain_copy": link_h2d,
                "host_dtype": "f32 (as a 32BIT build of the model holds its tracers)",
                "path": "fv3g_upload_async x6 -> fv3g_step (graph) -> fv3g_download_async"}
         del host, hout
     st.close()
+
+    # ---------------------------------------------------- FP64 reference leg
+    # Runs after the FP32 legs: its ~80 GB of device allocations and frees
+    # leave host-to-device copies from pinned memory several times slower for
+    # the rest of the process on this host, which would distort the e2e leg.
+    err = None
+    if not a.no_fp64:
+        st = build_state(P, "fp64", a.nq, a.npz, a.n, 0)
+        st.step(a.q_split, use_graph=False)
+        st.sync()  # the step ran on the state's stream; the copy below runs on torch's
+        ref_q = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float64, device="cuda")
+        st.download_device("Q_REMAPPED", ref_q.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        err = rel_err_per_tracer(mq, ref_q, a.n)
+        del mq, ref_q
+        torch.cuda.empty_cache()
+        ms64, kern64 = timed_steps(st, a, world, max(1, a.steps), max(1, min(a.warmup, 3)), stream)
+        out["fp64"] = {"value": world * units * a.steps / (ms64 / 1e3), "ms_per_step": ms64 / a.steps,
+                       "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern64.items()}}
+        st.close()
+        del st
+        torch.cuda.empty_cache()
 
     # ---------------------------------------------------------- CPU oracle
     cpu = None
@@ -420,7 +459,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 stencils; f64 pe/overlap schedule/mass sums", "data": "synthetic (seeded; no public dataset)",
-        "config": {**workload(a), "precision": "mixed", "replicas": world},
+        "config": {**workload(a), "precision": "mixed", "replicas": world, "warps_per_cta": warps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "k_substep<float,8> (fused fv_tp_2d + flux-form update), interior + edge-ring launch "

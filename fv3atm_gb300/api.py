@@ -194,6 +194,12 @@ class CubeState:
     def remap(self, stream=None) -> None:
         _lib.call("fv3g_remap_batched", self._h, _stream(stream))
 
+    def autotune(self) -> int:
+        """Pick the advection CTA width by timing a substep; returns it."""
+        w = C.c_int(0)
+        _lib.call("fv3g_state_autotune", self._h, C.byref(w))
+        return w.value
+
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
         _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))
 

@@ -605,6 +605,63 @@ int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
   return st->fp64 ? tracer_2d_t<double>(st, q_split, s) : tracer_2d_t<float>(st, q_split, s);
 }
 
+// Time one substep (interior + edge-ring launches, halo fill and prologue)
+// for each candidate CTA width and keep the fastest.  Reads the home tracer
+// buffer and writes only scratch buffers; the logical state is unchanged.
+int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  const int cand[] = {4, 5, 6, 8, 10};
+  const int saved_w = st->d.warps_per_cta, q_cur = st->q_cur, dp_start = st->dp_start, dp_end = st->dp_end;
+  const bool remapped = st->remapped, timing = st->timing;
+  st->timing = false;
+  cudaEvent_t e0, e1;
+  FV3G_CUDA(cudaEventCreate(&e0));
+  FV3G_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 0.f;
+  int rc = 0;
+  for (int w : cand) {
+    st->d.warps_per_cta = w;
+    int r = fv3g_tracer_2d_batched(st, 1, st->stream);  // warm-up; rejects widths that do not fit
+    if (r == FV3G_E_ARG) continue;
+    if (r) { rc = r; break; }
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2 && !rc; ++rep) {
+      cudaEventRecord(e0, st->stream);
+      rc = fv3g_tracer_2d_batched(st, 1, st->stream);
+      cudaEventRecord(e1, st->stream);
+      if (!rc && cudaEventSynchronize(e1) == cudaSuccess) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        ms = std::min(ms, t);
+      }
+    }
+    if (rc) break;
+    if (best == 0 || ms < best_ms) {
+      best = w;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  st->timing = timing;
+  st->q_cur = q_cur;
+  st->dp_start = dp_start;
+  st->dp_end = dp_end;
+  st->remapped = remapped;
+  if (rc || best == 0) {
+    st->d.warps_per_cta = saved_w;
+    return rc ? rc : set_error(FV3G_E_ARG, "no advection CTA width fits this precision");
+  }
+  st->d.warps_per_cta = best;
+  if (st->gexec) {  // the captured step was built for the old width
+    cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+  }
+  if (warps_out) *warps_out = best;
+  return 0;
+}
+
 int fv3g_remap_batched(fv3g_state* st, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;

@@ -593,29 +593,55 @@ __device__ __forceinline__ T edge_correction(const AdvArgs<T>& a, int n, int t, 
 
 // Halo strips (NG cells deep along the four tile edges) of every plane of
 // the six tiles, copied from the neighbouring tiles through the cube-edge
-// mapping of cube_source.  The corner blocks are left to the sweeps: their
-// copy_corners rotation depends on the sweep direction.  Reads touch only
-// interior cells and writes only halo cells, so one buffer serves as both.
+// mapping (the strip of edge e of tile t is the NG-deep interior strip along
+// edge nedge of tile nbr, position reversed when rev).  The corner blocks are
+// left to the sweeps: their copy_corners rotation depends on the sweep
+// direction.  One CTA per (plane, edge, tile): the source strip is read in
+// its own storage order into shared memory and the halo strip written in
+// its own, so rows are coalesced and column strips move NG cells per row.
 template <typename T>
-__global__ void k_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, Topo topo) {
-  const int t = blockIdx.z;
-  const int cells = 4 * NG * n;
-  for (int pl = blockIdx.y; pl < nplanes; pl += gridDim.y) {
-    T* qp = q + pl * splane;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
-      const int e = c / (NG * n), r = c - e * (NG * n);
-      const int d = r / n + 1, sv = r - (d - 1) * n;
-      int i, j;
-      switch (e) {
-        case EW: i = 1 - d; j = sv + 1; break;
-        case EE: i = n + d; j = sv + 1; break;
-        case ES: i = sv + 1; j = 1 - d; break;
-        default: i = sv + 1; j = n + d; break;
+__global__ void __launch_bounds__(256) k_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg,
+                                                   int n, Topo topo) {
+  extern __shared__ __align__(16) unsigned char halo_raw[];
+  T* strip = reinterpret_cast<T*>(halo_raw);  // [depth][position along the source edge]
+  const int e = blockIdx.y, t = blockIdx.z;
+  const int nt = topo.nbr[t][e], ne = topo.nedge[t][e], rev = topo.rev[t][e];
+  const int cells = NG * n;
+  for (int pl = blockIdx.x; pl < nplanes; pl += gridDim.x) {
+    const T* src = q + nt * sQt + pl * splane;
+    T* dst = q + t * sQt + pl * splane;
+    for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+      int d, sp, i, j;
+      if (ne == ES || ne == EN) {  // source rows: positions along i are contiguous
+        d = c / n + 1;
+        sp = c - (d - 1) * n;
+        i = sp + 1;
+        j = ne == ES ? d : n + 1 - d;
+      } else {  // source columns: the NG depths of a row are contiguous
+        sp = c / NG;
+        d = c - sp * NG + 1;
+        i = ne == EW ? d : n + 1 - d;
+        j = sp + 1;
       }
-      int ts = t, is = i, js = j;
-      cube_source(topo, n, ts, is, js);
-      qp[t * sQt + pg.at(i, j)] = qp[ts * sQt + pg.at(is, js)];
+      strip[(d - 1) * n + sp] = src[pg.at(i, j)];
     }
+    __syncthreads();
+    for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+      int d, sv, i, j;
+      if (e == ES || e == EN) {
+        d = c / n + 1;
+        sv = c - (d - 1) * n;
+        i = sv + 1;
+        j = e == ES ? 1 - d : n + d;
+      } else {
+        sv = c / NG;
+        d = c - sv * NG + 1;
+        i = e == EW ? 1 - d : n + d;
+        j = sv + 1;
+      }
+      dst[pg.at(i, j)] = strip[(d - 1) * n + (rev ? n - 1 - sv : sv)];
+    }
+    __syncthreads();
   }
 }
 
@@ -818,9 +844,10 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
                      cudaStream_t s) {
-  const int cells = 4 * NG * n;
-  dim3 grid((unsigned)std::min((cells + 255) / 256, 64), (unsigned)std::min(nplanes, 65535), 6);
-  k_cube_halo<T><<<grid, 256, 0, s>>>(q, sQt, splane, nplanes, pg, n, topo);
+  const size_t smem = (size_t)NG * n * sizeof(T);
+  if (smem > 48 * 1024) return set_error(FV3G_E_ARG, "tile size %d too large for the halo kernel", n);
+  dim3 grid((unsigned)std::min(nplanes, 65535), 4, 6);
+  k_cube_halo<T><<<grid, 256, smem, s>>>(q, sQt, splane, nplanes, pg, n, topo);
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }

@@ -1,9 +1,11 @@
 // fv3g_copy.cu -- pitched copies of stacks of planes.
 //
 // Device-to-device stacks are moved by a kernel (4-byte words, one grid-stride
-// loop); host<->device stacks are issued as cudaMemcpy3DAsync calls of at most
-// kChunk planes each, with every pitched pointer's logical width given in
-// bytes.
+// loop).  A host<->device stack whose host side is dense (the usual Fortran
+// array) goes through a per-thread device staging buffer: one large
+// cudaMemcpyAsync per 256 MB chunk at full link bandwidth, and the pitch
+// change done by the kernel in device memory.  Other host stacks are issued as
+// cudaMemcpy3DAsync calls of at most kChunk planes each.
 #include <algorithm>
 
 #include "fv3g_internal.cuh"
@@ -11,18 +13,92 @@
 namespace fv3g {
 
 namespace {
+#define CHECK_RC(expr)          \
+  do {                          \
+    int rc__ = (expr);          \
+    if (rc__ != 0) return rc__; \
+  } while (0)
+
 constexpr long long kChunk = 256;
 
+// One warp per row of one plane (rows in a grid-stride loop, one integer
+// division per row), the row's words across the lanes: coalesced rows.
 __global__ void k_copy_planes(unsigned* dst, long long dpitch, long long dslice, const unsigned* src, long long spitch,
                               long long sslice, int width, int height, long long nplanes) {
-  const long long tot = (long long)width * height * nplanes;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(e % width);
-    const long long r = e / width;
-    const int y = (int)(r % height);
+  const long long rows = (long long)height * nplanes;
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = w0; r < rows; r += nw) {
     const long long p = r / height;
-    dst[p * dslice + (long long)y * dpitch + x] = src[p * sslice + (long long)y * spitch + x];
+    const long long y = r - p * height;
+    unsigned* d = dst + p * dslice + y * dpitch;
+    const unsigned* sp = src + p * sslice + y * spitch;
+    for (int x = lane; x < width; x += 32) d[x] = sp[x];
   }
+}
+}  // namespace
+
+namespace {
+// Per-thread staging buffer; `done` marks the end of its last use, which a
+// copy on any stream waits for before reusing the buffer.
+struct Staging {
+  void* buf = nullptr;
+  size_t cap = 0;
+  cudaEvent_t done = nullptr;
+  ~Staging() {
+    if (buf) cudaFree(buf);
+    if (done) cudaEventDestroy(done);
+  }
+};
+thread_local Staging g_staging;
+constexpr size_t kStageBytes = size_t(256) << 20;
+
+int device_words(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
+                 size_t width_bytes, size_t height, long long nplanes, cudaStream_t s) {
+  const int width = (int)(width_bytes / 4);
+  const long long rows = (long long)height * nplanes;
+  const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((rows + 7) / 8, 152LL * 16));
+  k_copy_planes<<<grid, 256, 0, s>>>((unsigned*)dst, (long long)(dpitch / 4), (long long)(dslice / 4),
+                                     (const unsigned*)src, (long long)(spitch / 4), (long long)(sslice / 4),
+                                     (int)(width_bytes / 4), (int)height, nplanes);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// dense host stack <-> pitched device stack through the staging buffer
+int staged_copy(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
+                size_t width_bytes, size_t height, long long nplanes, bool h2d, cudaStream_t s) {
+  Staging& g = g_staging;
+  const size_t plane = width_bytes * height;
+  const long long per = std::max<long long>(1, (long long)(kStageBytes / plane));
+  const size_t need = (size_t)std::min<long long>(per, nplanes) * plane;
+  if (g.cap < need) {
+    if (g.buf) {
+      FV3G_CUDA(cudaEventSynchronize(g.done));
+      cudaFree(g.buf);
+      g.buf = nullptr;
+      g.cap = 0;
+    }
+    FV3G_CUDA(cudaMalloc(&g.buf, std::max(need, size_t(1) << 20)));
+    g.cap = std::max(need, size_t(1) << 20);
+  }
+  if (!g.done) FV3G_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+  FV3G_CUDA(cudaStreamWaitEvent(s, g.done, 0));
+  for (long long p0 = 0; p0 < nplanes; p0 += per) {
+    const long long np = std::min(per, nplanes - p0);
+    if (h2d) {
+      FV3G_CUDA(cudaMemcpyAsync(g.buf, (const char*)src + p0 * sslice, np * plane, cudaMemcpyHostToDevice, s));
+      CHECK_RC(device_words((char*)dst + p0 * dslice, dpitch, dslice, g.buf, width_bytes, plane, width_bytes, height,
+                            np, s));
+    } else {
+      CHECK_RC(device_words(g.buf, width_bytes, plane, (const char*)src + p0 * sslice, spitch, sslice, width_bytes,
+                            height, np, s));
+      FV3G_CUDA(cudaMemcpyAsync((char*)dst + p0 * dslice, g.buf, np * plane, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  FV3G_CUDA(cudaEventRecord(g.done, s));
+  return 0;
 }
 }  // namespace
 
@@ -32,13 +108,16 @@ int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t
   if (kind == cudaMemcpyDeviceToDevice) {
     if ((dpitch | dslice | spitch | sslice | width_bytes | (size_t)dst | (size_t)src) & 3)
       return set_error(FV3G_E_ARG, "device plane copy needs 4-byte aligned pitches and pointers");
-    const long long words = (long long)(width_bytes / 4) * (long long)height * nplanes;
-    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((words + 255) / 256, 152LL * 32));
-    k_copy_planes<<<grid, 256, 0, s>>>((unsigned*)dst, (long long)(dpitch / 4), (long long)(dslice / 4),
-                                       (const unsigned*)src, (long long)(spitch / 4), (long long)(sslice / 4),
-                                       (int)(width_bytes / 4), (int)height, nplanes);
-    FV3G_CUDA(cudaGetLastError());
-    return 0;
+    return device_words(dst, dpitch, dslice, src, spitch, sslice, width_bytes, height, nplanes, s);
+  }
+  {  // dense host side: staged
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    const size_t hp = h2d ? spitch : dpitch, hs = h2d ? sslice : dslice;
+    const size_t dp = h2d ? dpitch : spitch, ds = h2d ? dslice : sslice;
+    const void* dev = h2d ? dst : src;
+    const bool aligned = !((dp | ds | width_bytes | (size_t)dev) & 3);
+    if (hp == width_bytes && hs == width_bytes * height && aligned)
+      return staged_copy(dst, dpitch, dslice, src, spitch, sslice, width_bytes, height, nplanes, h2d, s);
   }
   for (long long p0 = 0; p0 < nplanes; p0 += kChunk) {
     const long long np = std::min(kChunk, nplanes - p0);

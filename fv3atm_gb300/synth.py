@@ -379,6 +379,8 @@ def c48_single_tile(n: int = 48, npz: int = 63, seed: int = 0, cmax: float = 0.4
     q = base[None] * vert[:, None, None] + noise * rng.uniform(-1.0, 1.0, (npz, nd, nd))
     P.q = torch.as_tensor(np.clip(q, 0.0, None)[None, None])  # (1, 1, npz, nd, nd)
     P.meta["center"] = center
+    P.meta["omega"] = u0 / G.RADIUS
+    P.meta["vert"] = vert
     topo = G.cube_topology()
     geoms = {t: G.tile_geometry(n, t, ng) for t in range(6)}
     omega = u0 / G.RADIUS

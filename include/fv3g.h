@@ -260,6 +260,11 @@ int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream);
 int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32, void* stream);
 int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream);
 int fv3g_stream_sync(fv3g_state* st, void* stream);
+/* Choose the advection CTA width (warps per CTA) by timing one substep of
+ * the loaded fields at each candidate width; the fastest is kept for the
+ * state (warps_out may be NULL).  Side-effect free on the state's fields.
+ * Call it outside stream capture, after the inputs are uploaded. */
+int fv3g_state_autotune(fv3g_state* st, int* warps_out);
 /* Per-kernel timing of fv3g_step: with timing enabled, CUDA events are
  * recorded around every kernel of the step (also inside the graph);
  * fv3g_kernel_times returns, for the last completed step, the summed ms and

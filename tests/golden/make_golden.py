@@ -57,7 +57,20 @@ def remap_fixture():
     return d
 
 
+def c48_bell_norms():
+    """Relative L1 / L2 / Linf errors of the single-tile C48 L63 cosine bell after
+    10 steps (tests/_c48.py), as the oracle computes them."""
+    import json
+    from tests import _c48
+    P, exact_halo = _c48.problem()
+    q, t = _c48.oracle_run(P, exact_halo)
+    return json.dumps({"config": "C48 L63 1 tracer, n_split 1, hord 8, kord 9", "steps": _c48.NSTEPS, "t": t,
+                       "norms_l1_l2_linf": list(_c48.norms(P, q, t))}, indent=1)
+
+
 if __name__ == "__main__":
     np.savez_compressed(os.path.join(HERE, "cube_c12_l2.npz"), **cube_fixture())
     np.savez_compressed(os.path.join(HERE, "remap_columns_l63.npz"), **remap_fixture())
+    with open(os.path.join(HERE, "c48_bell_norms.json"), "w") as f:
+        f.write(c48_bell_norms() + "\n")
     print("written")

@@ -37,3 +37,17 @@ def test_oracle_reproduces_remap_fixture(kord, iv, qmin):
     d = dict(np.load(os.path.join(HERE, "remap_columns_l63.npz")))
     q2 = O.remap_columns(d["pe1"], d["q1"], d["pe2"], iv=iv, kord=kord, qs=d["qs"], q_min=qmin)
     assert np.array_equal(q2, d[f"q2_k{kord}_iv{iv}"])
+
+
+def test_oracle_c48_bell_norms_match_golden():
+    """The single-tile C48 L63 cosine bell, 10 steps (tests/_c48.py): the oracle's
+    error norms against the analytic rotated bell are the recorded golden numbers."""
+    import json
+    import os
+    from . import _c48
+    with open(os.path.join(os.path.dirname(__file__), "golden", "c48_bell_norms.json")) as f:
+        gold = json.load(f)
+    P, exact_halo = _c48.problem()
+    q, t = _c48.oracle_run(P, exact_halo)
+    assert abs(t - gold["t"]) <= 1e-9 * gold["t"]
+    assert np.allclose(_c48.norms(P, q, t), gold["norms_l1_l2_linf"], rtol=1e-9, atol=0)

@@ -340,3 +340,30 @@ def test_remap_matches_committed_golden_fixture(cuda):
         api.map_scalar_3d(km, np.ascontiguousarray(d["pe1"]), q1, np.ascontiguousarray(d["qs"]), km,
                           np.ascontiguousarray(d["pe2"]), out, 1, ncol, 1, 1, 1, ncol, 1, 1, 1, iv, kord, qmin)
         assert rel_l2(out[0, :, 0, :], d[f"q2_k{kord}_iv{iv}"]) <= FP64_TOL, (kord, iv)
+
+
+def test_c48_bell_ten_steps_matches_oracle_and_golden_norms(cuda):
+    """C48 L63 cosine bell, n_split 1, hord 8, kord 9, 10 steps through the drop-in
+    tracer_2d (halo callback) and map_scalar_3d entries."""
+    import json
+    import os
+    from . import _c48
+    P, exact_halo = _c48.problem()
+    qg, t = _c48.device_run(P, exact_halo)
+    qo, _ = _c48.oracle_run(P, exact_halo)
+    assert rel_l2(interior(qg, P.n), interior(qo, P.n)) <= FP64_TOL
+    with open(os.path.join(os.path.dirname(__file__), "golden", "c48_bell_norms.json")) as f:
+        gold = json.load(f)
+    assert np.allclose(_c48.norms(P, qg, t), gold["norms_l1_l2_linf"], rtol=1e-9, atol=0)
+
+
+def test_autotune_picks_a_width_and_leaves_results_unchanged(cuda, cube_prob):
+    P = cube_prob
+    st = api.CubeState(P.n, P.npz, P.nq, precision="mixed")
+    st.load_problem(P)
+    w = st.autotune()
+    assert w in (4, 5, 6, 8, 10)
+    st.step(3)
+    got = st.download("Q_REMAPPED")
+    want = _run_cube(P, "mixed", remap=True, graph=True, warps=4).download("Q_REMAPPED")
+    assert np.array_equal(got, want)  # every tracer's arithmetic is independent of the CTA width
