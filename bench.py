@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--warps", type=int, default=0,
                     help="advection warps per CTA (0 = chosen by fv3g_state_autotune)")
     return ap.parse_args()
@@ -176,6 +177,44 @@ def max_over_ranks(x: float, world: int) -> float:
     t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+# Ensemble configuration: 32 single-tile members (16 x C48 L32, 10 x C96 L64,
+# 6 x C192 L127), 4 tracers each, Courant <= 0.7, n_split 2, hord 8, kord 9.
+ENSEMBLE = [(48, 32)] * 16 + [(96, 64)] * 10 + [(192, 127)] * 6
+
+
+def ensemble_leg(a, stream):
+    """All members advanced by one CUDA graph per step (fv3g_ensemble_step), mixed precision."""
+    import torch
+    from fv3atm_gb300 import api
+    from fv3atm_gb300 import synth as S
+    states = []
+    units = 0
+    for k, (n, npz) in enumerate(ENSEMBLE):
+        P = S.make_problem(n, npz, 4, ntiles=1, seed=5000 + k, cmax=0.7)
+        st = api.CubeState(n, npz, 4, precision="mixed", ntiles=1)
+        st.load_problem(P)
+        states.append(st)
+        units += n * n * npz * 4
+    ens = api.Ensemble(states)
+    s = stream.cuda_stream
+    for _ in range(max(1, min(a.warmup, 3))):
+        ens.step(2, stream=s)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        ens.step(2, stream=s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    ens.close()
+    for st in states:
+        st.close()
+    return {"value": units / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "members": len(ENSEMBLE),
+            "config": "16 x C48 L32 + 10 x C96 L64 + 6 x C192 L127 single tiles (prescribed halo ring), 4 tracers, "
+                      "n_split 2, hord 8, kord 9, mixed precision, one graph per ensemble step"}
 
 
 def build_state(P, precision, nq, npz, n, warps=0):
@@ -423,6 +462,11 @@ def main():
         del host, hout
     st.close()
 
+    # ------------------------------------------------------- ensemble leg
+    ens = None
+    if not a.no_ensemble and world == 1:
+        ens = ensemble_leg(a, stream)
+
     # ---------------------------------------------------- FP64 reference leg
     # Runs after the FP32 legs: its ~80 GB of device allocations and frees
     # leave host-to-device copies from pinned memory several times slower for
@@ -477,6 +521,7 @@ def main():
         "mixed_rel_l2_vs_fp64_per_tracer": err,
         "mixed_mass_rel_change_one_step": [float(abs(x - y) / abs(y)) for x, y in zip(m1, m0)],
         "e2e": e2e,
+        "ensemble": ens,
         "cpu_baseline": cpu,
         "setup_s": {"generate": t_gen},
     }

@@ -121,16 +121,17 @@ def _stream(stream):
 
 
 class CubeState:
-    """Six tiles x npz levels x nq tracers resident in HBM (fv3g_state)."""
+    """ntiles (6: the cube; 1: one face with a prescribed halo ring) x npz levels x nq tracers
+    resident in HBM (fv3g_state)."""
 
     def __init__(self, n: int, npz: int, nq: int, *, precision: str = "fp64", hord: int = 8, kord: int = 9,
-                 iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0):
+                 iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0, ntiles: int = 6):
         L = _lib.load()
-        self.n, self.npz, self.nq = n, npz, nq
+        self.n, self.npz, self.nq, self.ntiles = n, npz, nq, ntiles
         self.nd = n + 6
         self.precision = precision
         prec = _lib.FV3G_FP64 if precision == "fp64" else _lib.FV3G_MIXED
-        desc = StateDesc(n, 6, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta)
+        desc = StateDesc(n, ntiles, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta)
         self._h = C.c_void_p()
         _lib.check(L.fv3g_state_create(C.byref(desc), C.byref(self._h)), "fv3g_state_create")
         self._grids = []
@@ -174,10 +175,10 @@ class CubeState:
         _lib.call("fv3g_download_device", self._h, _lib.FIELDS[field], C.c_void_p(dptr), _stream(stream))
 
     def field_shape(self, field: str) -> tuple:
-        n, nd, npz, nq = self.n, self.nd, self.npz, self.nq
-        return {"Q": (6, nq, npz, nd, nd), "Q_REMAPPED": (6, nq, npz, nd, nd), "DELP": (6, npz, nd, nd),
-                "DELP_OUT": (6, npz, nd, nd), "CX": (6, npz, nd, n + 1), "CY": (6, npz, n + 1, nd),
-                "MFX": (6, npz, n, n + 1), "MFY": (6, npz, n + 1, n)}[field]
+        n, nd, npz, nq, t = self.n, self.nd, self.npz, self.nq, self.ntiles
+        return {"Q": (t, nq, npz, nd, nd), "Q_REMAPPED": (t, nq, npz, nd, nd), "DELP": (t, npz, nd, nd),
+                "DELP_OUT": (t, npz, nd, nd), "CX": (t, npz, nd, n + 1), "CY": (t, npz, n + 1, nd),
+                "MFX": (t, npz, n, n + 1), "MFY": (t, npz, n + 1, n)}[field]
 
     def load_problem(self, prob) -> None:
         """Upload a synth.Problem (grid, levels and every input field)."""
@@ -202,6 +203,9 @@ class CubeState:
 
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
         _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))
+
+    def handle(self):
+        return self._h
 
     def mass(self, field: str = "Q", stream=None) -> np.ndarray:
         out = np.zeros(self.nq, dtype=np.float64)
@@ -236,3 +240,28 @@ class CubeState:
         code = C.c_int(0)
         _lib.call("fv3g_state_error", self._h, C.byref(code))
         return code.value
+
+
+class Ensemble:
+    """Independent states advanced together by one graph per step (fv3g_ensemble)."""
+
+    def __init__(self, members):
+        L = _lib.load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.handle() for m in self.members])
+        self._h = C.c_void_p()
+        _lib.check(L.fv3g_ensemble_create(arr, len(self.members), C.byref(self._h)), "fv3g_ensemble_create")
+
+    def step(self, q_split: int, stream=None) -> None:
+        _lib.call("fv3g_ensemble_step", self._h, q_split, _stream(stream))
+
+    def close(self):
+        if self._h:
+            _lib.load().fv3g_ensemble_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -112,6 +112,7 @@ struct fv3g_state {
   fv3g_state_desc d{};
   bool fp64 = true;
   int n = 0, nd = 0, npz = 0, nq = 0;
+  int nt = 6;  // tiles: 6 (cube, halos from the neighbours) or 1 (one face, halo ring prescribed by the caller)
   PlaneGeom pg{};
   long long plane = 0;
   size_t esz = 8;
@@ -248,7 +249,7 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.npz = st->npz;
   a.corners = 15;
   a.nested = 0;
-  a.cube = 1;
+  a.cube = st->nt == 6 ? 1 : 0;
   a.topo = st->topo;
   a.eflux = (T*)st->eflux;
   return a;
@@ -264,7 +265,7 @@ struct FieldShape {
 
 int field_shape(fv3g_state* st, int field, FieldShape& fs, bool for_upload) {
   const int n = st->n, nd = st->nd;
-  const long long t = 6;
+  const long long t = st->nt;
   switch (field) {
     case FV3G_FIELD_Q:
       fs = {t * st->nq * st->npz, nd, nd, 0, 0, for_upload ? st->q[0] : st->q[st->q_cur]};
@@ -330,7 +331,7 @@ int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t 
 
 template <typename T>
 int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
-  const long long fsz = st->plane * st->npz * 6;
+  const long long fsz = st->plane * st->npz * st->nt;
   const size_t fb = (size_t)fsz * sizeof(T);
   // scaled work copies and area fluxes
   FV3G_CUDA(cudaMemcpyAsync(st->cxs, st->cx, fb, cudaMemcpyDeviceToDevice, s));
@@ -341,7 +342,7 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   CHECK(launch_area_flux<T>((T*)st->cxs, (T*)st->cys, (T*)st->xfx, (T*)st->yfx, (T*)st->mfxs, (T*)st->mfys,
                             (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
-                            st->n, 1, st->n, 6, st->npz, frac, s));
+                            st->n, 1, st->n, st->nt, st->npz, frac, s));
   CHECK(mark(st, K_PROLOGUE, s, 1));
   const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
   int src = 0, dpi = 0;
@@ -349,16 +350,24 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
     const int dst = (src == 1) ? 2 : 1;
     const int dpo = (dpi == 1) ? 2 : 1;
     AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
-    CHECK(launch_cube_halo<T>((T*)st->q[src], a.sQt, st->plane, st->nq * st->npz, st->pg, st->n, st->topo, s));
-    CHECK(mark(st, K_HALO, s));
+    if (st->nt == 6) {
+      CHECK(launch_cube_halo<T>((T*)st->q[src], a.sQt, st->plane, st->nq * st->npz, st->pg, st->n, st->topo, s));
+      CHECK(mark(st, K_HALO, s));
+    } else if (src != 0) {  // the prescribed ring of the home buffer, held over the step
+      CHECK(launch_copy_halo_ring<T>((T*)st->q[src], (const T*)st->q[0], st->plane, st->nq * st->npz, st->pg,
+                                     st->n, s));
+      CHECK(mark(st, K_HALO, s));
+    }
     CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
     {
       const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
       const int nint = bm.nbxi * bm.nbyi;
       CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint)));
     }
-    CHECK(launch_edge_fix<T>(a, st->n, s));
-    CHECK(mark(st, K_EDGEFIX, s));
+    if (st->nt == 6) {
+      CHECK(launch_edge_fix<T>(a, st->n, s));
+      CHECK(mark(st, K_EDGEFIX, s));
+    }
     st->dp_start = dpi;
     src = dst;
     dpi = dpo;
@@ -388,7 +397,7 @@ int remap_t(fv3g_state* st, cudaStream_t s) {
   r.bk = st->bk;
   r.pg = st->pg;
   r.i1 = 1; r.j1 = 1; r.ni = st->n; r.nj = st->n;
-  r.ncol = 6LL * st->n * st->n;
+  r.ncol = (long long)st->nt * st->n * st->n;
   r.km = st->npz; r.kn = st->npz;
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
@@ -424,7 +433,8 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (!desc || !out) return set_error(FV3G_E_ARG, "null argument");
   *out = nullptr;
   const fv3g_state_desc& d = *desc;
-  if (d.ntiles != 6) return set_error(FV3G_E_UNSUPPORTED, "batched state supports the six-tile cube (ntiles=6)");
+  if (d.ntiles != 6 && d.ntiles != 1)
+    return set_error(FV3G_E_UNSUPPORTED, "batched state supports ntiles 6 (cube) or 1 (one face, prescribed halo)");
   if (d.n < 12 || d.npz < 2 || d.npz > KMAX || d.nq < 1)
     return set_error(FV3G_E_ARG, "bad sizes n=%d npz=%d nq=%d (n>=12, 2<=npz<=%d, nq>=1)", d.n, d.npz, d.nq, KMAX);
   if (d.precision != FV3G_FP64 && d.precision != FV3G_MIXED) return set_error(FV3G_E_ARG, "bad precision %d", d.precision);
@@ -440,6 +450,7 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   st->nd = d.n + 2 * NG;
   st->npz = d.npz;
   st->nq = d.nq;
+  st->nt = d.ntiles;
   st->pg.pitch = ((st->nd + 1 + 7) / 8) * 8;
   st->pg.rows = st->nd + 1;
   st->pg.isd = 1 - NG;
@@ -460,7 +471,8 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
     return cuda_error(e, "cudaStreamCreate");
   }
   const size_t P = (size_t)st->plane * st->esz;
-  const size_t qb = P * 6 * d.nq * d.npz, fb = P * 6 * d.npz;
+  const size_t nt = (size_t)d.ntiles;
+  const size_t qb = P * nt * d.nq * d.npz, fb = P * nt * d.npz;
   int rc = 0;
   for (int b = 0; b < 3 && !rc; ++b) rc = dalloc(st, &st->q[b], qb);
   for (int b = 0; b < 3 && !rc; ++b) rc = dalloc(st, &st->dp[b], fb);
@@ -470,9 +482,9 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
     if (!rc) rc = dalloc(st, f, fb);
   void** metrics[] = {&st->area, &st->rarea, &st->dxa, &st->dya, &st->dx, &st->dy};
   for (void** m : metrics)
-    if (!rc) rc = dalloc(st, m, P * 6);
-  if (!rc) rc = dalloc(st, &st->sin4, P * 6 * 4);
-  if (!rc) rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
+    if (!rc) rc = dalloc(st, m, P * nt);
+  if (!rc) rc = dalloc(st, &st->sin4, P * nt * 4);
+  if (!rc && nt == 6) rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
   if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);
@@ -504,7 +516,7 @@ int fv3g_state_destroy(fv3g_state* st) {
 }
 
 int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* g) {
-  if (!st || !g || tile < 0 || tile > 5) return set_error(FV3G_E_ARG, "bad state/grid/tile");
+  if (!st || !g || tile < 0 || tile >= st->nt) return set_error(FV3G_E_ARG, "bad state/grid/tile");
   const int nd = st->nd;
   struct M { const double* src; void* dst; int ni, nj; long long off; };
   const size_t P = (size_t)st->plane;
@@ -662,6 +674,106 @@ int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
   return 0;
 }
 
+// ============================================================= ensemble ====
+// Independent states (members of an ensemble, any sizes) advanced together:
+// one captured graph forks to a stream per member, runs each member's
+// tracer_2d + remap there, and joins, so small members overlap on the GPU.
+}  // extern "C"
+
+struct fv3g_ensemble {
+  std::vector<fv3g_state*> m;
+  std::vector<cudaStream_t> ms;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int g_qsplit = -1;
+};
+
+extern "C" {
+
+int fv3g_ensemble_destroy(fv3g_ensemble* e) {
+  if (!e) return 0;
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  for (cudaStream_t s : e->ms) cudaStreamDestroy(s);
+  for (cudaEvent_t v : e->join) cudaEventDestroy(v);
+  if (e->fork) cudaEventDestroy(e->fork);
+  delete e;
+  return 0;
+}
+
+int fv3g_ensemble_create(fv3g_state* const* members, int n, fv3g_ensemble** out) {
+  if (!members || !out || n < 1) return set_error(FV3G_E_ARG, "ensemble needs at least one member");
+  *out = nullptr;
+  fv3g_ensemble* e = new (std::nothrow) fv3g_ensemble();
+  if (!e) return set_error(FV3G_E_NOMEM, "host allocation failed");
+  cudaError_t err = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  for (int i = 0; i < n && err == cudaSuccess; ++i) {
+    if (!members[i]) {
+      fv3g_ensemble_destroy(e);
+      return set_error(FV3G_E_ARG, "null member %d", i);
+    }
+    e->m.push_back(members[i]);
+    cudaStream_t s;
+    cudaEvent_t v;
+    err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (err == cudaSuccess) {
+      e->ms.push_back(s);
+      err = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
+      if (err == cudaSuccess) e->join.push_back(v);
+    }
+  }
+  if (err != cudaSuccess) {
+    fv3g_ensemble_destroy(e);
+    return cuda_error(err, "ensemble streams");
+  }
+  *out = e;
+  return 0;
+}
+
+int fv3g_ensemble_step(fv3g_ensemble* e, int q_split, void* stream) {
+  if (!e) return set_error(FV3G_E_ARG, "null ensemble");
+  for (fv3g_state* st : e->m) {
+    if (!st->levels_set) return set_error(FV3G_E_ARG, "a member has no levels (fv3g_state_set_levels)");
+    if (st->timing) return set_error(FV3G_E_ARG, "per-kernel timing is not available inside an ensemble step");
+  }
+  if (e->gexec == nullptr || e->g_qsplit != q_split) {
+    if (e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+    cudaStream_t cs;
+    FV3G_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    FV3G_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    cudaError_t ce = cudaEventRecord(e->fork, cs);
+    for (size_t i = 0; i < e->m.size() && !rc && ce == cudaSuccess; ++i) {
+      ce = cudaStreamWaitEvent(e->ms[i], e->fork, 0);
+      if (ce != cudaSuccess) break;
+      rc = fv3g_tracer_2d_batched(e->m[i], q_split, e->ms[i]);
+      if (!rc) rc = fv3g_remap_batched(e->m[i], e->ms[i]);
+      if (!rc) ce = cudaEventRecord(e->join[i], e->ms[i]);
+      if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, e->join[i], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_error(ce, "ensemble capture");
+    if (ee != cudaSuccess) return cuda_error(ee, "cudaStreamEndCapture");
+    ee = cudaGraphInstantiate(&e->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ee != cudaSuccess) return cuda_error(ee, "cudaGraphInstantiate");
+    e->g_qsplit = q_split;
+  }
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->ms[0];
+  FV3G_CUDA(cudaGraphLaunch(e->gexec, s));
+  for (fv3g_state* st : e->m) {
+    st->q_cur = 0;
+    st->remapped = true;
+  }
+  return 0;
+}
+
 int fv3g_remap_batched(fv3g_state* st, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
@@ -732,7 +844,7 @@ int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream) {
     m.pg = st->pg;
     m.i1 = 1; m.j1 = 1; m.ni = st->n; m.nj = st->n;
     m.npz = st->npz;
-    m.ntiles = 6;
+    m.ntiles = st->nt;
     m.partials = st->partials;
     return launch_mass<T>(m, st->nq, st->mass_out, s);
   };

@@ -863,6 +863,42 @@ int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s) 
   return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
 }
 
+// Halo ring (the NG-deep strips and the corner blocks) of every plane copied
+// from src to dst: the prescribed halo of a single-tile state, held over the
+// substeps of a step.
+template <typename T>
+__global__ void k_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n) {
+  const int nd = n + 2 * NG, ring = nd * nd - n * n;
+  for (int pl = blockIdx.y; pl < nplanes; pl += gridDim.y)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ring; c += gridDim.x * blockDim.x) {
+      int i, j;
+      if (c < NG * nd) {  // rows below the tile
+        j = 1 - NG + c / nd;
+        i = 1 - NG + c % nd;
+      } else if (c < 2 * NG * nd) {  // rows above
+        const int r = c - NG * nd;
+        j = n + 1 + r / nd;
+        i = 1 - NG + r % nd;
+      } else {  // the two side strips of the tile's rows
+        const int r = c - 2 * NG * nd;
+        j = 1 + r / (2 * NG);
+        const int k = r % (2 * NG);
+        i = k < NG ? 1 - NG + k : n + 1 + (k - NG);
+      }
+      const long long p = pl * splane + pg.at(i, j);
+      dst[p] = src[p];
+    }
+}
+
+template <typename T>
+int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n, cudaStream_t s) {
+  const int nd = n + 2 * NG, ring = nd * nd - n * n;
+  dim3 grid((unsigned)std::min((ring + 255) / 256, 16), (unsigned)std::min(nplanes, 65535));
+  k_copy_halo_ring<T><<<grid, 256, 0, s>>>(dst, src, splane, nplanes, pg, n);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
 template <typename T>
 int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s) {
   const long long tot = (long long)6 * 4 * n;
@@ -898,6 +934,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
   template int launch_substep<T>(const AdvArgs<T>&, int, bool, int, cudaStream_t);                          \
   template int launch_edge_fix<T>(const AdvArgs<T>&, int, cudaStream_t);                                     \
   template int launch_cube_halo<T>(T*, long long, long long, int, PlaneGeom, int, const Topo&, cudaStream_t);   \
+  template int launch_copy_halo_ring<T>(T*, const T*, long long, int, PlaneGeom, int, cudaStream_t);             \
   template int launch_area_flux<T>(T*, T*, T*, T*, T*, T*, const T*, const T*, const T*, const T*, const T*, \
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \
                                    int, T, cudaStream_t);                                                    \

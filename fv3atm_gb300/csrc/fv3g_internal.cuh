@@ -171,6 +171,8 @@ int cuda_error(cudaError_t e, const char* what);
   } while (0)
 
 // Host launchers (fv3g_advect.cu)
+template <typename T>
+int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n, cudaStream_t s);
 int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s);
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,

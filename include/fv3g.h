@@ -203,7 +203,8 @@ typedef struct fv3g_state fv3g_state;
 
 typedef struct {
   int n;          /* cells per tile edge (C_n) */
-  int ntiles;     /* 6 (cube) */
+  int ntiles;     /* 6: the cube, halos from the neighbouring tiles; 1: one cube face whose halo ring
+                     (strips and corner blocks of Q) is uploaded by the caller and held over the step */
   int npz;        /* Lagrangian levels */
   int nq;         /* tracers */
   int precision;  /* FV3G_FP64 or FV3G_MIXED */
@@ -265,6 +266,16 @@ int fv3g_stream_sync(fv3g_state* st, void* stream);
  * state (warps_out may be NULL).  Side-effect free on the state's fields.
  * Call it outside stream capture, after the inputs are uploaded. */
 int fv3g_state_autotune(fv3g_state* st, int* warps_out);
+/* Ensembles: independent states of any sizes advanced together.  One step
+ * runs tracer_2d (q_split substeps) and the remap of every member, as one
+ * CUDA graph that forks to a stream per member and joins; members must have
+ * their levels set and timing off.  The ensemble does not own its members.
+ * The graph runs on `stream` (NULL: the ensemble's own first stream);
+ * synchronise that stream, or the device, before reading the members. */
+typedef struct fv3g_ensemble fv3g_ensemble;
+int fv3g_ensemble_create(fv3g_state* const* members, int n, fv3g_ensemble** out);
+int fv3g_ensemble_step(fv3g_ensemble* ens, int q_split, void* stream);
+int fv3g_ensemble_destroy(fv3g_ensemble* ens);
 /* Per-kernel timing of fv3g_step: with timing enabled, CUDA events are
  * recorded around every kernel of the step (also inside the graph);
  * fv3g_kernel_times returns, for the last completed step, the summed ms and
