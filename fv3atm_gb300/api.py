@@ -106,6 +106,16 @@ def map1_ppm_ad(km, pe1, q1, q1_ad, qs, kn, pe2, q2_ad, i1, i2, j, ibeg, iend, j
               iend, jbeg, jend, iv, kord)
 
 
+def fillz(im, km, nq, q, dp) -> None:
+    """q (nq, km, im) (Fortran q(im, km, nq)) filled in place; dp (km, im)."""
+    _lib.call("fv3g_fillz", im, km, nq, _p(q), _p(dp))
+
+
+def pressure_vars(im, km, ptop, akap, delp, pe, peln, pk, pkz) -> None:
+    _lib.call("fv3g_pressure_vars", im, km, C.c_double(ptop), C.c_double(akap), _p(delp), _p(pe), _p(peln), _p(pk),
+              _p(pkz))
+
+
 def map_scalar_3d(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j1, j2, ibeg, iend, jbeg, jend, nq, iv, kord, q_min) -> None:
     _lib.call("fv3g_map_scalar_3d", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j1, j2, ibeg, iend,
               jbeg, jend, nq, iv, kord, C.c_double(q_min))
@@ -194,6 +204,10 @@ class CubeState:
 
     def remap(self, stream=None) -> None:
         _lib.call("fv3g_remap_batched", self._h, _stream(stream))
+
+    def fillz(self, stream=None) -> None:
+        """fillz on the remapped tracers."""
+        _lib.call("fv3g_fillz_batched", self._h, _stream(stream))
 
     def autotune(self) -> int:
         """Pick the advection CTA width by timing a substep; returns it."""

@@ -774,6 +774,21 @@ int fv3g_ensemble_step(fv3g_ensemble* e, int q_split, void* stream) {
   return 0;
 }
 
+// fillz on the remapped tracers of every column (the `fill` option applied
+// after the tracer remap in Lagrangian_to_Eulerian).
+int fv3g_fillz_batched(fv3g_state* st, void* stream) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (!st->remapped) return set_error(FV3G_E_ARG, "fillz acts on the remapped tracers (run the remap first)");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  const long long sQk = st->plane, sQq = st->plane * st->npz, sQt = sQq * st->nq;
+  const long long sFk = st->plane, sFt = st->plane * st->npz;
+  if (st->fp64)
+    return launch_fillz_planes<double>((double*)st->q[0], (const double*)st->dp_eul, st->n, st->nt, st->npz, st->nq,
+                                       sQt, sQq, sQk, sFt, sFk, st->pg, s);
+  return launch_fillz_planes<float>((float*)st->q[0], (const float*)st->dp_eul, st->n, st->nt, st->npz, st->nq, sQt,
+                                    sQq, sQk, sFt, sFk, st->pg, s);
+}
+
 int fv3g_remap_batched(fv3g_state* st, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;

@@ -170,6 +170,11 @@ int cuda_error(cudaError_t e, const char* what);
     if (e__ != cudaSuccess) return ::fv3g::cuda_error(e__, #call); \
   } while (0)
 
+// fillz over the interior columns of a state's planes (fv3g_l2e.cu)
+template <typename T>
+int launch_fillz_planes(T* q, const T* dp, int n, int ntiles, int km, int nq, long long sQt, long long sQq,
+                        long long sQk, long long sFt, long long sFk, PlaneGeom pg, cudaStream_t s);
+
 // Host launchers (fv3g_advect.cu)
 template <typename T>
 int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n, cudaStream_t s);

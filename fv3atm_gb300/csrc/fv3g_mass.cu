@@ -18,24 +18,33 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
   s = t;
 }
 
+// One warp per row (tile, level, j) in a grid-stride loop, lanes along i.
+// FP64 fields: every term q*dp*area goes through Neumaier's sum.  FP32 fields:
+// the term is formed in FP32 and added to a plain FP64 running sum (its
+// rounding is random, ~1e-12 of the total over 1e9 terms), which keeps the
+// FP64 pipe -- 1/64 of the FP32 rate on this GPU -- out of the inner loop; the
+// per-thread partials are then combined with Neumaier's sum.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mass_partial(const MassArgs<T> a) {
   const int iq = blockIdx.y;
-  const long long per_tile = (long long)a.npz * a.ni * a.nj;
-  const long long tot = per_tile * a.ntiles;
+  const int lane = threadIdx.x & 31;
+  const int rows = a.ntiles * a.npz * a.nj;
   double s = 0.0, c = 0.0;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % a.ni);
-    long long r = e / a.ni;
-    const int j = (int)(r % a.nj);
-    r /= a.nj;
-    const int k = (int)(r % a.npz);
-    const int t = (int)(r / a.npz);
-    const long long p = a.pg.at(a.i1 + i, a.j1 + j);
-    const double q = (double)a.q[t * a.sQt + iq * a.sQq + k * a.sQk + p];
-    const double dp = (double)a.dp[t * a.sFt + k * a.sFk + p];
-    const double ar = (double)a.area[t * a.sMt + p];
-    neumaier(s, c, q * dp * ar);
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += gridDim.x * (blockDim.x >> 5)) {
+    const int j = r % a.nj;
+    const int tk = r / a.nj;
+    const int k = tk % a.npz, t = tk / a.npz;
+    const long long p0 = a.pg.at(a.i1, a.j1 + j);
+    const T* qr = a.q + t * a.sQt + iq * a.sQq + k * a.sQk + p0;
+    const T* dr = a.dp + t * a.sFt + k * a.sFk + p0;
+    const T* ar = a.area + t * a.sMt + p0;
+    if (Single<T>::value) {
+      double acc = 0.0;
+      for (int i = lane; i < a.ni; i += 32) acc += (double)(qr[i] * dr[i] * ar[i]);
+      neumaier(s, c, acc);
+    } else {
+      for (int i = lane; i < a.ni; i += 32) neumaier(s, c, (double)qr[i] * (double)dr[i] * (double)ar[i]);
+    }
   }
   __shared__ double ss[256], sc[256];
   ss[threadIdx.x] = s;

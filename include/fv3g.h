@@ -176,6 +176,18 @@ int fv3g_map1_ppm_ad(int km, const double* pe1, const double* q1, double* q1_ad,
                      const double* pe2, double* q2_ad, int i1, int i2, int j, int ibeg, int iend, int jbeg,
                      int jend, int iv, int kord);
 
+/* fillz (fv_fill.F90): negative tracer values filled column by column,
+ * conserving each column's mass.  q (im, km, nq) inout, dp (im, km) in.
+ * Replaces: fillz(im, km, nq, q, dp). */
+int fv3g_fillz(int im, int km, int nq, double* q, const double* dp);
+
+/* Pressure variables after the remap (the pe/peln/pk/pkz recompute of
+ * Lagrangian_to_Eulerian): pe = ptop + running sum of delp, peln = ln pe,
+ * pk = pe^akap, pkz = (pk(k+1) - pk(k)) / (akap (peln(k+1) - peln(k))).
+ * delp (im, km) in; pe, peln, pk (im, km+1) and pkz (im, km) out. */
+int fv3g_pressure_vars(int im, int km, double ptop, double akap, const double* delp, double* pe, double* peln,
+                       double* pk, double* pkz);
+
 /* Column remap on caller-owned DEVICE arrays that allocates no device memory.
  * No counterpart in the reference: it serves callers that cannot let a
  * library call cudaMalloc/cudaFree -- a model that owns all of its device
@@ -266,6 +278,9 @@ int fv3g_stream_sync(fv3g_state* st, void* stream);
  * state (warps_out may be NULL).  Side-effect free on the state's fields.
  * Call it outside stream capture, after the inputs are uploaded. */
 int fv3g_state_autotune(fv3g_state* st, int* warps_out);
+/* fillz on the state's remapped tracers (every interior column and tracer). */
+int fv3g_fillz_batched(fv3g_state* st, void* stream);
+
 /* Ensembles: independent states of any sizes advanced together.  One step
  * runs tracer_2d (q_split substeps) and the remap of every member, as one
  * CUDA graph that forks to a stream per member and joins; members must have

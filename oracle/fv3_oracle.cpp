@@ -800,6 +800,79 @@ void orc_remap_columns_tl(int ncol, int km, const double* pe1, const double* q1,
   }
 }
 
+// fillz (fv_fill.F90), restated: per column and tracer, a negative top layer
+// is pushed into the layer below; an interior negative borrows first from the
+// layer above, then from the layer below, as much as they hold; a negative
+// bottom layer borrows from above; if negatives remain, the column's positive
+// layer masses are scaled by (total mass)/(positive mass) and the negatives
+// zeroed (no change when the total is not positive).  q (im, km, nq),
+// dp (im, km), i fastest.
+void orc_fillz(int im, int km, int nq, double* q, const double* dp) {
+  for (int iq = 0; iq < nq; ++iq)
+    for (int i = 0; i < im; ++i) {
+      auto Q = [&](int k) -> double& { return q[i + (size_t)im * (k + (size_t)km * iq)]; };
+      auto D = [&](int k) { return dp[i + (size_t)im * k]; };
+      if (km < 2) continue;
+      if (Q(0) < 0.0) {
+        Q(1) += Q(0) * D(0) / D(1);
+        Q(0) = 0.0;
+      }
+      bool fix = false;
+      for (int k = 1; k < km - 1; ++k) {
+        if (Q(k) >= 0.0) continue;
+        fix = true;
+        if (Q(k - 1) > 0.0) {
+          const double dq = std::min(Q(k - 1) * D(k - 1), -Q(k) * D(k));
+          Q(k - 1) -= dq / D(k - 1);
+          Q(k) += dq / D(k);
+        }
+        if (Q(k) < 0.0 && Q(k + 1) > 0.0) {
+          const double dq = std::min(Q(k + 1) * D(k + 1), -Q(k) * D(k));
+          Q(k + 1) -= dq / D(k + 1);
+          Q(k) += dq / D(k);
+        }
+      }
+      const int kb = km - 1;
+      if (Q(kb) < 0.0 && Q(kb - 1) > 0.0) {
+        fix = true;
+        const double dq = std::min(Q(kb - 1) * D(kb - 1), -Q(kb) * D(kb));
+        Q(kb - 1) -= dq / D(kb - 1);
+        Q(kb) += dq / D(kb);
+      }
+      if (!fix) continue;
+      double tot = 0.0, pos = 0.0;
+      for (int k = 0; k < km; ++k) {
+        const double m = Q(k) * D(k);
+        tot += m;
+        pos += std::max(m, 0.0);
+      }
+      if (tot > 0.0 && pos > 0.0 && tot < pos) {
+        const double f = tot / pos;
+        for (int k = 0; k < km; ++k) Q(k) = std::max(Q(k), 0.0) * f;
+      }
+    }
+}
+
+// Pressure variables of the columns after the remap: interface pressure pe,
+// its logarithm peln, pk = pe^akap and the layer mean pkz of p^akap over
+// ln p, (pk(k+1) - pk(k)) / (akap (peln(k+1) - peln(k))).  delp (im, km);
+// pe, peln, pk (im, km+1); pkz (im, km).
+void orc_pressure_vars(int im, int km, double ptop, double akap, const double* delp, double* pe, double* peln,
+                       double* pk, double* pkz) {
+  for (int i = 0; i < im; ++i) {
+    double p = ptop;
+    for (int k = 0; k <= km; ++k) {
+      if (k > 0) p += delp[i + (size_t)im * (k - 1)];
+      pe[i + (size_t)im * k] = p;
+      peln[i + (size_t)im * k] = std::log(p);
+      pk[i + (size_t)im * k] = std::exp(akap * peln[i + (size_t)im * k]);
+    }
+    for (int k = 0; k < km; ++k)
+      pkz[i + (size_t)im * k] = (pk[i + (size_t)im * (k + 1)] - pk[i + (size_t)im * k]) /
+                                (akap * (peln[i + (size_t)im * (k + 1)] - peln[i + (size_t)im * k]));
+  }
+}
+
 double orc_mass_sum(const double* q, const double* dp, const double* area, long n, long narea) {
   double s = 0.0, comp = 0.0;  // Neumaier
   for (long i = 0; i < n; ++i) {

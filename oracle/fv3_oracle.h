@@ -114,6 +114,13 @@ void orc_remap_columns(int ncol, int km, const double* pe1, const double* q1, co
 void orc_remap_columns_tl(int ncol, int km, const double* pe1, const double* q1, const double* dq1, const double* qs,
                           int kn, const double* pe2, double* q2, double* dq2, int iv, int kord, double q_min);
 
+/* fillz negative filler, column-mass conserving: q (im, km, nq) inout, dp (im, km). */
+void orc_fillz(int im, int km, int nq, double* q, const double* dp);
+
+/* pe, peln, pk (im, km+1) and pkz (im, km) of columns with thickness delp (im, km). */
+void orc_pressure_vars(int im, int km, double ptop, double akap, const double* delp, double* pe, double* peln,
+                       double* pk, double* pkz);
+
 /* Neumaier-compensated sum of a[i]*b[i]*c[i % nc] over n items. */
 double orc_mass_sum(const double* q, const double* dp, const double* area, long n, long narea);
 

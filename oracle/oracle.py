@@ -201,6 +201,25 @@ def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, 
     return q2
 
 
+def fillz(q, dp) -> np.ndarray:
+    """q (nq, km, im), dp (km, im) (C order of Fortran q(im, km, nq)) -> filled copy of q."""
+    q = _f64(q).copy()
+    dp = _f64(dp)
+    nq, km, im = q.shape
+    lib().orc_fillz(im, km, nq, _p(q), _p(dp))
+    return q
+
+
+def pressure_vars(delp, ptop, akap):
+    """delp (km, im) -> pe, peln, pk (km+1, im), pkz (km, im)."""
+    delp = _f64(delp)
+    km, im = delp.shape
+    pe, peln, pk = (np.zeros((km + 1, im)) for _ in range(3))
+    pkz = np.zeros((km, im))
+    lib().orc_pressure_vars(im, km, C.c_double(ptop), C.c_double(akap), _p(delp), _p(pe), _p(peln), _p(pk), _p(pkz))
+    return pe, peln, pk, pkz
+
+
 def mass_sum(q, dp, area) -> float:
     """Neumaier-compensated sum of q*dp*area; q, dp (..., ncell) broadcast area (ncell)."""
     q, dp, area = _f64(q), _f64(dp), _f64(area)

@@ -367,3 +367,53 @@ def test_autotune_picks_a_width_and_leaves_results_unchanged(cuda, cube_prob):
     got = st.download("Q_REMAPPED")
     want = _run_cube(P, "mixed", remap=True, graph=True, warps=4).download("Q_REMAPPED")
     assert np.array_equal(got, want)  # every tracer's arithmetic is independent of the CTA width
+
+
+# ---------------------------------------------------- Lagrangian_to_Eulerian
+def test_fillz_dropin_matches_oracle(cuda):
+    rng = np.random.default_rng(9)
+    km, im, nq = 32, 50, 3
+    dp = rng.uniform(50.0, 900.0, (km, im))
+    q = rng.uniform(0.0, 1.0, (nq, km, im))
+    q[rng.uniform(size=q.shape) < 0.3] *= -0.4
+    want = O.fillz(q, dp)
+    got = q.copy()
+    api.fillz(im, km, nq, got, dp)
+    assert np.allclose(got, want, rtol=1e-13, atol=1e-15)
+
+
+def test_pressure_vars_dropin_matches_oracle(cuda):
+    rng = np.random.default_rng(10)
+    km, im = 64, 40
+    dp = rng.uniform(50.0, 900.0, (km, im))
+    pe, peln, pk = (np.zeros((km + 1, im)) for _ in range(3))
+    pkz = np.zeros((km, im))
+    api.pressure_vars(im, km, 100.0, 0.2857, dp, pe, peln, pk, pkz)
+    # log / exp of the device and host math libraries differ in the last bit; pkz divides a difference of
+    # neighbouring pk values by a difference of neighbouring logs, which magnifies that by pk / dpk ~ 1e2
+    for got, want, tol in zip((pe, peln, pk, pkz), O.pressure_vars(dp, 100.0, 0.2857), (1e-15, 1e-14, 1e-14, 1e-12)):
+        assert np.allclose(got, want, rtol=tol, atol=0)
+
+
+def test_state_fillz_conserves_column_mass(cuda):
+    P = S.make_problem(16, 6, 2, seed=12, cmax=0.7)
+    q = P.q.numpy().copy()
+    q[:, :, 2] -= 0.3  # a level with negative values everywhere
+    st = api.CubeState(P.n, P.npz, P.nq, precision="fp64")
+    st.load_problem(P)
+    st.upload("Q", q)
+    st.step(2)
+    before = st.download("Q_REMAPPED")
+    st.fillz()
+    after = st.download("Q_REMAPPED")
+    dpo = st.download("DELP_OUT")
+    n = P.n
+    ps = P.ak[0] + interior(dpo, n).sum(1)                       # (6, n, n)
+    pe2 = P.ak[:, None, None, None] + P.bk[:, None, None, None] * ps[None]
+    dpe = np.diff(pe2, axis=0).transpose(1, 0, 2, 3)              # (6, npz, n, n)
+    for iq in range(P.nq):
+        m0 = (interior(before[:, iq], n) * dpe).sum(1)
+        m1 = (interior(after[:, iq], n) * dpe).sum(1)
+        assert np.all(np.abs(m1 - m0) <= 1e-12 * np.abs(interior(before[:, iq], n) * dpe).sum(1))
+        pos = m0 > 0
+        assert np.all(interior(after[:, iq], n).transpose(0, 2, 3, 1)[pos] >= 0.0)
