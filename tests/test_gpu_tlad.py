@@ -197,3 +197,110 @@ def test_gradcheck_map1_ppm_kord4_slice(cuda):
     args = dict(pe1=pe1, pe2=pe2, iv=-1, kord=4)
     q = torch.tensor(q1, dtype=torch.float64, requires_grad=True)
     assert torch.autograd.gradcheck(lambda x: Map1Ppm.apply(x, args), (q,), eps=1e-6, atol=1e-8, rtol=1e-6)
+
+
+# ------------------------------------------- C96 tracer substeps (TL / AD)
+def _c96_substeps(nsub=6, hord=5):
+    """One C96 tile, one level, nsub tracer_2d substeps with the Courant numbers and
+    mass fluxes scaled by 1/nsub; the halo ring is prescribed (no perturbation)."""
+    P = S.make_problem(96, 1, 1, ntiles=1, seed=96, cmax=0.8)
+    g = P.geoms[0]
+    n, ng = P.n, 3
+    cx, cy = P.cx[0, 0].numpy() / nsub, P.cy[0, 0].numpy() / nsub
+    mfx, mfy = P.mfx[0, 0].numpy() / nsub, P.mfy[0, 0].numpy() / nsub
+    xfx, yfx = area_fluxes(cx, cy, g)
+    rax, ray = ra_xy(xfx, yfx, g)
+    s = slice(ng, ng + n)
+    rarea = g.rarea[s, s]
+    dps = [P.dp[0, 0].numpy()[s, s]]
+    for _ in range(nsub):
+        dps.append(dps[-1] + (mfx[:, :-1] - mfx[:, 1:] + mfy[:-1, :] - mfy[1:, :]) * rarea)
+    d = dict(n=n, g=g, cx=cx, cy=cy, xfx=xfx, yfx=yfx, rax=rax, ray=ray, mfx=mfx, mfy=mfy)
+    return P, d, dps, rarea, s, hord
+
+
+def _div(fx, fy):
+    return fx[:, :-1] - fx[:, 1:] + fy[:-1, :] - fy[1:, :]
+
+
+def _forward(P, d, dps, rarea, s, hord, q):
+    traj = [q]
+    n = d["n"]
+    for k in range(len(dps) - 1):
+        fx, fy = np.zeros((n, n + 1)), np.zeros((n + 1, n))
+        api.fv_tp_2d(q.copy(), d["cx"], d["cy"], n + 1, n + 1, hord, fx, fy, d["xfx"], d["yfx"], api.GridStruct(d["g"]),
+                     api.bounds_for(n), d["rax"], d["ray"], 1.0, d["mfx"], d["mfy"])
+        q = q.copy()
+        q[s, s] = (q[s, s] * dps[k] + _div(fx, fy) * rarea) / dps[k + 1]
+        traj.append(q)
+    return traj
+
+
+def _tl_substeps(d, dps, rarea, s, hord, traj, dq):
+    for k in range(len(dps) - 1):
+        d["q"] = traj[k]
+        _, fxt, _, fyt = _tl(d, dq, hord)
+        out = np.zeros_like(dq)  # the prescribed halo carries no perturbation
+        out[s, s] = (dq[s, s] * dps[k] + _div(fxt, fyt) * rarea) / dps[k + 1]
+        dq = out
+    return dq
+
+
+def _ad_substeps(d, dps, rarea, s, hord, traj, a):
+    n = d["n"]
+    for k in reversed(range(len(dps) - 1)):
+        ai = a[s, s]
+        prev = np.zeros_like(a)
+        prev[s, s] = ai * dps[k] / dps[k + 1]
+        gq = ai * rarea / dps[k + 1]
+        fx_ad, fy_ad = np.zeros((n, n + 1)), np.zeros((n + 1, n))
+        fx_ad[:, :-1] += gq
+        fx_ad[:, 1:] -= gq
+        fy_ad[:-1, :] += gq
+        fy_ad[1:, :] -= gq
+        d["q"] = traj[k]
+        _ad(d, prev, fx_ad, fy_ad, hord)
+        halo = np.ones_like(prev, bool)
+        halo[s, s] = False
+        prev[halo] = 0.0  # adjoints of the prescribed halo are not state
+        a = prev
+    return a
+
+
+def test_c96_six_substeps_tl_ad_dot_product_and_finite_differences(cuda):
+    P, d, dps, rarea, s, hord = _c96_substeps()
+    q = np.ascontiguousarray(P.q[0, 0, 0].numpy())
+    rng = np.random.default_rng(960)
+    rms = float(np.sqrt(np.mean(q[s, s] ** 2)))
+    x = np.zeros_like(q)
+    x[s, s] = 1e-3 * rms * rng.standard_normal(x[s, s].shape)
+    y = np.zeros_like(q)
+    y[s, s] = 1e-3 * rms * rng.standard_normal(y[s, s].shape)
+    traj = _forward(P, d, dps, rarea, s, hord, q)
+    tlx = _tl_substeps(d, dps, rarea, s, hord, traj, x)
+    ady = _ad_substeps(d, dps, rarea, s, hord, traj, y)
+    lhs, rhs = float((tlx * y).sum()), float((x * ady).sum())
+    assert abs(lhs - rhs) <= DOT_TOL * abs(lhs), (lhs, rhs)
+    # finite differences of the (linear) hord-5 substeps at steps 1e-4 .. 1e-8 of the perturbation
+    errs = []
+    base = traj[-1][s, s]
+    for eps in (1e-4, 1e-5, 1e-6, 1e-7, 1e-8):
+        fd = (_forward(P, d, dps, rarea, s, hord, q + eps * x / (1e-3 * rms))[-1][s, s] - base) / eps
+        errs.append(rel_l2(fd, tlx[s, s] / (1e-3 * rms)))
+    assert min(errs) <= 1e-9, errs
+
+
+def test_c96_map1_ppm_kord4_adjoint_dot_product(cuda):
+    pe1, pe2, q1, rng = _row(km=64, ni=96, seed=96)
+    km, ni = q1.shape
+    rms = float(np.sqrt(np.mean(q1 ** 2)))
+    dq = 1e-3 * rms * rng.standard_normal(q1.shape)
+    w = 1e-3 * rms * rng.standard_normal((km, ni))
+    q2t = np.zeros((km, 1, ni))
+    api.map1_ppm_tl(km, pe1, q1[:, None, :].copy(), dq[:, None, :].copy(), None, km, pe2, None, q2t, 1, ni, 1, 1, ni,
+                    1, 1, -1, 4)
+    q1_ad = np.zeros((km, 1, ni))
+    api.map1_ppm_ad(km, pe1, q1[:, None, :].copy(), q1_ad, None, km, pe2, w[:, None, :].copy(), 1, ni, 1, 1, ni, 1, 1,
+                    -1, 4)
+    lhs, rhs = float((q2t[:, 0] * w).sum()), float((q1_ad[:, 0] * dq).sum())
+    assert abs(lhs - rhs) <= DOT_TOL * abs(lhs), (lhs, rhs)
