@@ -292,7 +292,29 @@ struct ColSmem {
   T pl[pk<T>(32 * NPL)];  // sub-grid parabola of every source layer: left, right edge and curvature
   T pr[pk<T>(32 * NPL)];
   T p6[pk<T>(32 * NPL)];
+  float mh[pk<float>(32 * NPL) + 1];  // FP32 fields: cumulative layer mass at every source interface,
+  float ml[pk<float>(32 * NPL) + 1];  // as an unevaluated sum hi + lo (float-float)
 };
+
+// Float-float arithmetic (an unevaluated sum of two floats, ~48-bit
+// significand): the error-free transformations TwoSum (Knuth) and TwoProd
+// (with fma), then one renormalisation.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  const float h = s + e;
+  return FF{h, e - (h - s)};
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = a * b;
+  return FF{p, fmaf(a, b, -p)};
+}
 
 // Fields reach shared memory through a ring of RING slots, filled by
 // cp.async RING-1 fields ahead.  Each slot holds the CTA's 8 columns,
@@ -620,26 +642,79 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
         }
       }
     }
+    if (Single<T>::value) {
+      // FP32 fields: cumulative source mass in float-float at every source
+      // interface (layer masses q*dp are exact as float-float products), so a
+      // target layer's mass is a difference of two cumulative values and the
+      // column mass telescopes; only the final division rounds per value.
+      FF m[NPL], tot{0.f, 0.f};
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        m[j] = (u0 + j < km) ? ff_prod((float)qv[j], (float)S.dp[pk<T>(u0 + j)]) : FF{0.f, 0.f};
+        tot = ff_add(tot, m[j]);
+      }
+      FF ex = tot;  // inclusive scan of the lane totals, then shifted by one lane
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const FF p{__shfl_up_sync(0xffffffffu, ex.hi, o), __shfl_up_sync(0xffffffffu, ex.lo, o)};
+        if (lane >= o) ex = ff_add(p, ex);
+      }
+      FF run{__shfl_up_sync(0xffffffffu, ex.hi, 1), __shfl_up_sync(0xffffffffu, ex.lo, 1)};
+      if (lane == 0) run = FF{0.f, 0.f};
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        if (u0 + j <= km) {
+          S.mh[pk<float>(u0 + j)] = run.hi;
+          S.ml[pk<float>(u0 + j)] = run.lo;
+        }
+        run = ff_add(run, m[j]);
+      }
+    }
     __syncwarp();
     // ------------------------------------------------------- integration
+    if (Single<T>::value) {
+      FF cm[NPL + 1];  // cumulative mass at this lane's target interfaces
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-      const int t = u0 + j;
-      const int Lt = Ls[j], Lb = Ls[j + 1];
-      const T Xt = Xs[j], Xb = Xs[j + 1];
-      const bool inside = (Lb == Lt) || (Lb == Lt + 1 && Xb == T(0));
-      const int it = pk<T>(Lt), ib_ = pk<T>(Lb);
-      const T qt = Q[it], dpt = S.dp[it];
-      const T pm1 = pmean(S.pl[it], S.pr[it], S.p6[it], Xt, (inside && Lb == Lt) ? Xb : T(1));
-      const T vin = (Xt == T(0) && (Lb == Lt + 1 || Xb == T(1))) ? qt : pm1;
-      T mass = Xt == T(0) ? qt * dpt : (dpt * (T(1) - Xt)) * pm1;
-      for (int m = Lt + 1; m < Lb; ++m) mass = mass + Q[pk<T>(m)] * S.dp[pk<T>(m)];
-      const T qb_ = Q[ib_], dpb = S.dp[ib_];
-      const T pm2 = pmean(S.pl[ib_], S.pr[ib_], S.p6[ib_], T(0), Xb);
-      const T bot = Xb >= T(1) ? qb_ * (dpb * Xb) : (Xb > T(0) ? (dpb * Xb) * pm2 : T(0));
-      mass = mass + bot;
-      const T out = inside ? vin : mass * rdpk[j];
-      if (real && t < kn) q2[(long long)t * a.sQk] = out;
+      for (int j = 0; j <= NPL; ++j) {
+        const int L = Ls[j];
+        const float X = (float)Xs[j];
+        const int il = pk<float>(L), iu = pk<float>(L + 1);
+        FF c{S.mh[il], S.ml[il]};
+        if (X >= 1.f) {
+          c = FF{S.mh[iu], S.ml[iu]};
+        } else if (X > 0.f) {
+          const int it = pk<T>(L);
+          const float part = (float)S.dp[it] * X * (float)pmean(S.pl[it], S.pr[it], S.p6[it], T(0), T(X));
+          c = ff_add(c, FF{part, 0.f});
+        }
+        cm[j] = c;
+      }
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        const int t = u0 + j;
+        const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
+        if (real && t < kn) q2[(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) {
+        const int t = u0 + j;
+        const int Lt = Ls[j], Lb = Ls[j + 1];
+        const T Xt = Xs[j], Xb = Xs[j + 1];
+        const bool inside = (Lb == Lt) || (Lb == Lt + 1 && Xb == T(0));
+        const int it = pk<T>(Lt), ib_ = pk<T>(Lb);
+        const T qt = Q[it], dpt = S.dp[it];
+        const T pm1 = pmean(S.pl[it], S.pr[it], S.p6[it], Xt, (inside && Lb == Lt) ? Xb : T(1));
+        const T vin = (Xt == T(0) && (Lb == Lt + 1 || Xb == T(1))) ? qt : pm1;
+        T mass = Xt == T(0) ? qt * dpt : (dpt * (T(1) - Xt)) * pm1;
+        for (int mm = Lt + 1; mm < Lb; ++mm) mass = mass + Q[pk<T>(mm)] * S.dp[pk<T>(mm)];
+        const T qb_ = Q[ib_], dpb = S.dp[ib_];
+        const T pm2 = pmean(S.pl[ib_], S.pr[ib_], S.p6[ib_], T(0), Xb);
+        const T bot = Xb >= T(1) ? qb_ * (dpb * Xb) : (Xb > T(0) ? (dpb * Xb) * pm2 : T(0));
+        mass = mass + bot;
+        const T out = inside ? vin : mass * rdpk[j];
+        if (real && t < kn) q2[(long long)t * a.sQk] = out;
+      }
     }
   }
 }
