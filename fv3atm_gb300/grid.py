@@ -1,7 +1,8 @@
 """Equiangular gnomonic cubed-sphere geometry, tile topology and hybrid levels.
 
 This module generates the grid metrics that FV3's ``fv_grid_type`` carries into
-the tracer path (dx, dy, dxa, dya, area, rarea, sin_sg, corner flags; upstream
+the tracer path (dx, dy, dxa, dya, area, rarea, sin_sg, the damping metrics
+del6_u/del6_v and da_min, corner flags; upstream
 ``fv_grid_tools`` / ``fv_grid_utils``, absent from the reference tree, whose only
 in-tree users are ``atmos_model.F90:578-614``) and the six-tile connectivity that
 the on-device halo gather and the tile-edge flux reconciliation use.
@@ -125,6 +126,8 @@ class TileGeom:
     sin_sg: np.ndarray  # (9, n+2ng, n+2ng); slots 0..3 = W, S, E, N edges
     corners: np.ndarray  # (n+2ng+1, n+2ng+1, 3) unit vectors of cell corners
     centers: np.ndarray  # (n+2ng, n+2ng, 3)
+    del6_u: np.ndarray   # (n+2ng+1, n+2ng)   y faces: sina_v dx / dyc
+    del6_v: np.ndarray   # (n+2ng, n+2ng+1)   x faces: sina_u dy / dxc
     sw_corner: int = 1
     se_corner: int = 1
     nw_corner: int = 1
@@ -160,8 +163,25 @@ def tile_geometry(n: int, tile: int, ng: int = 3, radius: float = RADIUS) -> Til
     sin_sg[2] = _sin_angle(Aw[:, 1:], Bw[:, 1:])     # east edge
     sin_sg[3] = _sin_angle(As[1:, :], Bs[1:, :])     # north edge
     sin_sg[4:] = _sin_angle(Am, Bm)[None]
+    # Damping metrics of the del-n tracer diffusion: face length times the sine
+    # of the grid angle at the face over the distance between the two cell
+    # centres across it (dxc, dyc), on the extended grid of the face.
+    ae = np.concatenate([[ac[0] - 0.5 * h], am, [ac[-1] + 0.5 * h]])  # centres, one extra each side
+    Bx, Ax = np.meshgrid(am, ae, indexing="ij")                          # (nd, nd+2)
+    cx_ext = _gnomonic(tile, Ax, Bx)
+    dxc = radius * _arc(cx_ext[:, :-1], cx_ext[:, 1:])                   # (nd, nd+1) x faces
+    By, Ay = np.meshgrid(ae, am, indexing="ij")                          # (nd+2, nd)
+    cy_ext = _gnomonic(tile, Ay, By)
+    dyc = radius * _arc(cy_ext[:-1, :], cy_ext[1:, :])                   # (nd+1, nd) y faces
+    del6_v = _sin_angle(Aw, Bw) * dy / dxc
+    del6_u = _sin_angle(As, Bs) * dx / dyc
     return TileGeom(n=n, ng=ng, tile=tile, dx=dx, dy=dy, dxa=dxa, dya=dya, area=area, rarea=1.0 / area,
-                    sin_sg=sin_sg, corners=corners, centers=centers)
+                    sin_sg=sin_sg, corners=corners, centers=centers, del6_u=del6_u, del6_v=del6_v)
+
+
+def da_min(geoms) -> float:
+    """Smallest interior cell area over the tiles given (gridstruct%da_min)."""
+    return float(min(g.area[g.ng:g.ng + g.n, g.ng:g.ng + g.n].min() for g in geoms))
 
 
 def cube_geometry(n: int, ng: int = 3, radius: float = RADIUS) -> list:

@@ -76,25 +76,45 @@ template <class T> inline T clamp2(T a, T x0, T x1) {  // a into [min(x0,x1), ma
 
 // Fluxes at faces f in [flo, fhi] (face f separates cells f-1 and f).
 // x(m) for m in [flo-3, fhi+2] via xs(m) = x[m - (flo-3)]; c[f - flo];
-// dxa(m) in the same indexing as x.  eW / eE: tile-edge faces in range, or
-// INT_MIN when the line has none.
+// dxa(m) in the same indexing as x.  eW / eE: the tile-edge face at the low
+// end (tile interior above it) / high end (interior below), or kNoEdge.
+//   hord 8: monotonized central slope dm, interface al, Lin (2004) limit of
+//           the edge deviations to |2 dm|;
+//   hord 5: fourth-order interfaces (7/12, -1/12), no limiter, and a 2-dx
+//           filter: the parabola's correction is dropped (first-order upwind
+//           flux) when both cells beside the face are extrema (bl br >= 0);
+//   hord 1: hord 5 with the filter test |lim_fac b0| < |bl - br| (lim_fac 1
+//           is hord 5's test, lim_fac 3 the stricter hord-6 one).
 constexpr int kNoEdge = -1000000;
+constexpr double kS11 = 11.0 / 14.0, kS14 = 4.0 / 7.0, kS15 = 3.0 / 14.0;    // hord 8 edge values
+constexpr double kC1 = -2.0 / 14.0, kC2 = 11.0 / 14.0, kC3 = 5.0 / 14.0;    // hord < 8 edge values
 
 template <class T>
-void ppm_line(int hord, const T* x, const double* c, const double* dxa, int flo, int fhi, int eW,
+void ppm_line(int hord, double lim_fac, const T* x, const double* c, const double* dxa, int flo, int fhi, int eW,
               int eE, T* flux) {
   const int m0 = flo - 3;  // first cell index held in x
   const int ncell = fhi - flo + 6;
   auto X = [&](int m) -> const T& { return x[m - m0]; };
   auto DX = [&](int m) -> double { return dxa[m - m0]; };
-  std::vector<T> bl(ncell), br(ncell);
+  std::vector<T> bl(ncell), br(ncell), al(ncell + 1);
+  std::vector<char> smt(ncell, 1);
   auto BL = [&](int m) -> T& { return bl[m - m0]; };
   auto BR = [&](int m) -> T& { return br[m - m0]; };
+  auto AL = [&](int f) -> T& { return al[f - m0]; };
+  const int lo = flo - 1, hi = fhi;  // cells whose bl/br feed a flux
+  auto in_cells = [&](int m) { return m >= lo && m <= hi; };
+  auto in_faces = [&](int f) { return f >= lo && f <= hi + 1; };
+  // Edge value at a cube-face edge e (Putman & Lin 2007): the mean of the two
+  // one-sided, dxa-weighted linear extrapolations from either face.
+  auto edge_mean = [&](int e) -> T {
+    T extL = ((2.0 * DX(e - 1) + DX(e - 2)) * X(e - 1) - DX(e - 1) * X(e - 2)) / (DX(e - 2) + DX(e - 1));
+    T extR = ((2.0 * DX(e) + DX(e + 1)) * X(e) - DX(e) * X(e + 1)) / (DX(e) + DX(e + 1));
+    return T(0.5) * (extL + extR);
+  };
 
   if (hord == 8) {
-    std::vector<T> dm(ncell), al(ncell + 1);
+    std::vector<T> dm(ncell);
     auto DM = [&](int m) -> T& { return dm[m - m0]; };
-    auto AL = [&](int f) -> T& { return al[f - m0]; };
     for (int m = flo - 2; m <= fhi + 1; ++m) {
       // monotonized central slope in half-increment form (Lin et al. 1994)
       T xt = T(0.25) * (X(m + 1) - X(m - 1));
@@ -104,57 +124,76 @@ void ppm_line(int hord, const T* x, const double* c, const double* dxa, int flo,
     }
     for (int f = flo - 1; f <= fhi + 1; ++f)
       AL(f) = T(0.5) * (X(f - 1) + X(f)) + (DM(f - 1) - DM(f)) * T(1.0 / 3.0);
-    for (int m = flo - 1; m <= fhi; ++m) {
+    for (int m = lo; m <= hi; ++m) {
       // Lin (2004) constraint: |edge deviation| <= |2 dm|, same sign as dm
       T xt = T(2.0) * DM(m);
       BL(m) = -tsign(tmin(tabs(xt), tabs(AL(m) - X(m))), xt);
       BR(m) = tsign(tmin(tabs(xt), tabs(AL(m + 1) - X(m))), xt);
     }
-  } else {  // hord 5: unlimited fourth-order PPM (linear in x)
-    for (int m = flo - 1; m <= fhi; ++m) {
-      T aL = T(7.0 / 12.0) * (X(m - 1) + X(m)) - T(1.0 / 12.0) * (X(m - 2) + X(m + 1));
-      T aR = T(7.0 / 12.0) * (X(m) + X(m + 1)) - T(1.0 / 12.0) * (X(m - 1) + X(m + 2));
-      BL(m) = aL - X(m);
-      BR(m) = aR - X(m);
+    // Cube-face edges: the edge value clamped to the two cells beside it; the
+    // next interfaces inward take a one-sided value from two cells and the
+    // slope of the second (s15 q + s11 q' -+ s14 dm'); the interface beyond
+    // is left unlimited; then the CW84 constraint on the three edge cells.
+    // The same one-sided value serves a halo cell's outer edge, so the two
+    // tiles sharing an edge compute the same face values.
+    auto set = [&](int m, bool left, T v) {
+      if (in_cells(m)) (left ? BL(m) : BR(m)) = v;
+    };
+    if (eW != kNoEdge) {
+      const int e = eW;
+      T a0 = clamp2(edge_mean(e), X(e - 1), X(e));
+      set(e - 1, true, T(kS14) * DM(e - 2) + T(kS11) * (X(e - 2) - X(e - 1)));
+      set(e - 1, false, a0 - X(e - 1));
+      set(e, true, a0 - X(e));
+      T ap = T(kS15) * X(e) + T(kS11) * X(e + 1) - T(kS14) * DM(e + 1);
+      set(e, false, ap - X(e));
+      set(e + 1, true, ap - X(e + 1));
+      if (in_cells(e + 1)) BR(e + 1) = AL(e + 2) - X(e + 1);
+      for (int m = e - 1; m <= e + 1; ++m)
+        if (in_cells(m)) cw84(BL(m), BR(m));
+    }
+    if (eE != kNoEdge) {
+      const int e = eE;
+      if (in_cells(e - 2)) BL(e - 2) = AL(e - 2) - X(e - 2);
+      T am = T(kS15) * X(e - 1) + T(kS11) * X(e - 2) + T(kS14) * DM(e - 2);
+      set(e - 2, false, am - X(e - 2));
+      set(e - 1, true, am - X(e - 1));
+      T a0 = clamp2(edge_mean(e), X(e - 1), X(e));
+      set(e - 1, false, a0 - X(e - 1));
+      set(e, true, a0 - X(e));
+      set(e, false, T(kS11) * (X(e + 1) - X(e)) - T(kS14) * DM(e + 1));
+      for (int m = e - 2; m <= e; ++m)
+        if (in_cells(m)) cw84(BL(m), BR(m));
+    }
+  } else {
+    for (int f = lo; f <= hi + 1; ++f)
+      AL(f) = T(7.0 / 12.0) * (X(f - 1) + X(f)) - T(1.0 / 12.0) * (X(f - 2) + X(f + 1));
+    // Cube-face edges: one-sided three-cell interfaces next to the edge
+    // (c1, c2, c3) and the edge value itself, unlimited.
+    for (int e : {eW, eE}) {
+      if (e == kNoEdge) continue;
+      if (in_faces(e - 1)) AL(e - 1) = T(kC1) * X(e - 3) + T(kC2) * X(e - 2) + T(kC3) * X(e - 1);
+      if (in_faces(e)) AL(e) = edge_mean(e);
+      if (in_faces(e + 1)) AL(e + 1) = T(kC3) * X(e) + T(kC2) * X(e + 1) + T(kC1) * X(e + 2);
+    }
+    for (int m = lo; m <= hi; ++m) {
+      BL(m) = AL(m) - X(m);
+      BR(m) = AL(m + 1) - X(m);
+      if (hord == 5) smt[m - m0] = val(BL(m)) * val(BR(m)) < 0.0;
+      else smt[m - m0] = std::fabs(lim_fac * val(BL(m) + BR(m))) < std::fabs(val(BL(m) - BR(m)));
     }
   }
 
-  // Cube-face edge at face e (Putman & Lin 2007): the edge value is the mean of
-  // the two one-sided linear extrapolations (dxa-weighted) from either face;
-  // the two neighbouring interfaces use one-sided third-order values that do
-  // not reach across the edge.
-  auto edge = [&](int e) {
-    T extL = ((2.0 * DX(e - 1) + DX(e - 2)) * X(e - 1) - DX(e - 1) * X(e - 2)) / (DX(e - 2) + DX(e - 1));
-    T extR = ((2.0 * DX(e) + DX(e + 1)) * X(e) - DX(e) * X(e + 1)) / (DX(e) + DX(e + 1));
-    T a0 = T(0.5) * (extL + extR);
-    T aM = T(-1.0 / 6.0) * X(e - 3) + T(5.0 / 6.0) * X(e - 2) + T(1.0 / 3.0) * X(e - 1);
-    T aP = T(1.0 / 3.0) * X(e) + T(5.0 / 6.0) * X(e + 1) - T(1.0 / 6.0) * X(e + 2);
-    if (hord == 8) {
-      aM = clamp2(aM, X(e - 2), X(e - 1));
-      a0 = clamp2(a0, X(e - 1), X(e));
-      aP = clamp2(aP, X(e), X(e + 1));
-    }
-    int lo = flo - 1, hi = fhi;  // cells whose bl/br feed a flux
-    if (e - 2 >= lo && e - 2 <= hi) BR(e - 2) = aM - X(e - 2);
-    if (e - 1 >= lo && e - 1 <= hi) { BL(e - 1) = aM - X(e - 1); BR(e - 1) = a0 - X(e - 1); }
-    if (e >= lo && e <= hi) { BL(e) = a0 - X(e); BR(e) = aP - X(e); }
-    if (e + 1 >= lo && e + 1 <= hi) BL(e + 1) = aP - X(e + 1);
-    if (hord == 8)
-      for (int m = e - 2; m <= e + 1; ++m)
-        if (m >= lo && m <= hi) cw84(BL(m), BR(m));
-  };
-  if (eW != kNoEdge) edge(eW);
-  if (eE != kNoEdge) edge(eE);
-
-  // upwind integral of the sub-grid parabola over the swept fraction |c|
+  // upwind integral of the sub-grid parabola over the swept fraction
   for (int f = flo; f <= fhi; ++f) {
     double cf = c[f - flo];
+    const bool high = hord == 8 || smt[f - 1 - m0] || smt[f - m0];
     if (cf > 0.0) {
       T b0 = BL(f - 1) + BR(f - 1);
-      flux[f - flo] = X(f - 1) + T(1.0 - cf) * (BR(f - 1) - T(cf) * b0);
+      flux[f - flo] = high ? X(f - 1) + T(1.0 - cf) * (BR(f - 1) - T(cf) * b0) : X(f - 1);
     } else {
       T b0 = BL(f) + BR(f);
-      flux[f - flo] = X(f) + T(1.0 + cf) * (BL(f) + T(cf) * b0);
+      flux[f - flo] = high ? X(f) + T(1.0 + cf) * (BL(f) + T(cf) * b0) : X(f);
     }
   }
 }
@@ -201,7 +240,7 @@ void copy_corners_t(T* q, int npx, int npy, int dir, const orc_grid* g, const or
 // x sweep: fluxes at faces [bd->is, bd->ie+1] for rows [j1, j2].
 template <class T>
 void xppm_t(T* flux /*(is:ie+1, j1:j2)*/, const T* q /*(isd:ied,jsd:jed)*/, const double* c /*(is:ie+1, clo..)*/,
-            int cjlo, int hord, int j1, int j2, int npx, const orc_grid* g, const orc_bounds* bd) {
+            int cjlo, int hord, double lim_fac, int j1, int j2, int npx, const orc_grid* g, const orc_bounds* bd) {
   const int is = bd->is, ie = bd->ie;
   View2<const T> Q{q, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
   View2<const double> C{c, is, cjlo, ie - is + 2};
@@ -214,7 +253,7 @@ void xppm_t(T* flux /*(is:ie+1, j1:j2)*/, const T* q /*(isd:ied,jsd:jed)*/, cons
   for (int j = j1; j <= j2; ++j) {
     for (int m = is - 3; m <= ie + 3; ++m) { line[m - is + 3] = Q(m, j); dl[m - is + 3] = DXA(m, j); }
     for (int f = is; f <= ie + 1; ++f) cl[f - is] = C(f, j);
-    ppm_line<T>(hord, line.data(), cl.data(), dl.data(), is, ie + 1, eW, eE, out.data());
+    ppm_line<T>(hord, lim_fac, line.data(), cl.data(), dl.data(), is, ie + 1, eW, eE, out.data());
     for (int f = is; f <= ie + 1; ++f) F(f, j) = out[f - is];
   }
 }
@@ -222,7 +261,7 @@ void xppm_t(T* flux /*(is:ie+1, j1:j2)*/, const T* q /*(isd:ied,jsd:jed)*/, cons
 // y sweep: fluxes at faces [bd->js, bd->je+1] for columns [i1, i2].
 template <class T>
 void yppm_t(T* flux /*(i1:i2, js:je+1)*/, const T* q, const double* c /*(cilo.., js:je+1)*/, int cilo,
-            int cni, int hord, int i1, int i2, int npy, const orc_grid* g, const orc_bounds* bd) {
+            int cni, int hord, double lim_fac, int i1, int i2, int npy, const orc_grid* g, const orc_bounds* bd) {
   const int js = bd->js, je = bd->je;
   View2<const T> Q{q, bd->isd, bd->jsd, bd->ied - bd->isd + 1};
   View2<const double> C{c, cilo, js, cni};
@@ -235,16 +274,100 @@ void yppm_t(T* flux /*(i1:i2, js:je+1)*/, const T* q, const double* c /*(cilo..,
   for (int i = i1; i <= i2; ++i) {
     for (int m = js - 3; m <= je + 3; ++m) { line[m - js + 3] = Q(i, m); dl[m - js + 3] = DYA(i, m); }
     for (int f = js; f <= je + 1; ++f) cl[f - js] = C(i, f);
-    ppm_line<T>(hord, line.data(), cl.data(), dl.data(), js, je + 1, eS, eN, out.data());
+    ppm_line<T>(hord, lim_fac, line.data(), cl.data(), dl.data(), js, je + 1, eS, eN, out.data());
     for (int f = js; f <= je + 1; ++f) F(i, f) = out[f - js];
   }
 }
 
+struct Dom {  // convenience sizes of one domain
+  int is, ie, js, je, isd, ied, jsd, jed, nid, njd;
+  size_t plane, nxf, nyf, nmx, nmy;
+  explicit Dom(const orc_bounds* b)
+      : is(b->is), ie(b->ie), js(b->js), je(b->je), isd(b->isd), ied(b->ied), jsd(b->jsd), jed(b->jed) {
+    nid = ied - isd + 1;
+    njd = jed - jsd + 1;
+    plane = (size_t)nid * njd;
+    nxf = (size_t)(ie - is + 2) * njd;           // cx, xfx
+    nyf = (size_t)nid * (je - js + 2);           // cy, yfx
+    nmx = (size_t)(ie - is + 2) * (je - js + 1); // mfx, fx
+    nmy = (size_t)(ie - is + 1) * (je - js + 2); // mfy, fy
+  }
+};
+
+// ---------------------------------------------------------- tracer damping ---
+// deln_flux: del-2(nord+1) damping fluxes added to fx, fy.  nord = 0 is a del-2
+// flux of the field (del6_v / del6_u times the difference across the face);
+// every further order takes the flux divergence times rarea as the new field
+// and differences it again with the opposite sign, so the added flux always
+// damps.  copy_corners fills the field's cube-corner blocks before each
+// direction when nord > 0.  With mass, the field is q and the face flux is
+// scaled by damp times the face mean of mass; without, the field is damp q.
+template <class T>
+void deln_flux_t(int nord, int npx, int npy, double damp, const T* q, T* fx, T* fy, const orc_grid* g,
+                 const orc_bounds* bd, const double* mass) {
+  Dom d(bd);
+  const int is = d.is, ie = d.ie, js = d.js, je = d.je, isd = d.isd, jsd = d.jsd, nid = d.nid;
+  View2<const T> Q{q, isd, jsd, nid};
+  View2<const double> RAREA{g->rarea, isd, jsd, nid};
+  View2<const double> D6U{g->del6_u, isd, jsd, nid};      // (isd:ied, jsd:jed+1)
+  View2<const double> D6V{g->del6_v, isd, jsd, nid + 1};  // (isd:ied+1, jsd:jed)
+  std::vector<T> d2v(d.plane), fx2v((size_t)(nid + 1) * d.njd), fy2v((size_t)nid * (d.njd + 1));
+  View2<T> D2{d2v.data(), isd, jsd, nid};
+  View2<T> FX2{fx2v.data(), isd, jsd, nid + 1};
+  View2<T> FY2{fy2v.data(), isd, jsd, nid};
+  for (int j = js - 1 - nord; j <= je + 1 + nord; ++j)
+    for (int i = is - 1 - nord; i <= ie + 1 + nord; ++i) D2(i, j) = mass ? Q(i, j) : T(damp) * Q(i, j);
+  if (nord > 0) copy_corners_t<T>(d2v.data(), npx, npy, 1, g, bd);
+  for (int j = js - nord; j <= je + nord; ++j)
+    for (int i = is - nord; i <= ie + nord + 1; ++i) FX2(i, j) = T(D6V(i, j)) * (D2(i - 1, j) - D2(i, j));
+  if (nord > 0) copy_corners_t<T>(d2v.data(), npx, npy, 2, g, bd);
+  for (int j = js - nord; j <= je + nord + 1; ++j)
+    for (int i = is - nord; i <= ie + nord; ++i) FY2(i, j) = T(D6U(i, j)) * (D2(i, j - 1) - D2(i, j));
+  for (int n = 1; n <= nord; ++n) {
+    const int nt = nord - n;
+    for (int j = js - nt - 1; j <= je + nt + 1; ++j)
+      for (int i = is - nt - 1; i <= ie + nt + 1; ++i)
+        D2(i, j) = (FX2(i, j) - FX2(i + 1, j) + FY2(i, j) - FY2(i, j + 1)) * T(RAREA(i, j));
+    copy_corners_t<T>(d2v.data(), npx, npy, 1, g, bd);
+    for (int j = js - nt; j <= je + nt; ++j)
+      for (int i = is - nt; i <= ie + nt + 1; ++i) FX2(i, j) = T(D6V(i, j)) * (D2(i, j) - D2(i - 1, j));
+    copy_corners_t<T>(d2v.data(), npx, npy, 2, g, bd);
+    for (int j = js - nt; j <= je + nt + 1; ++j)
+      for (int i = is - nt; i <= ie + nt; ++i) FY2(i, j) = T(D6U(i, j)) * (D2(i, j) - D2(i, j - 1));
+  }
+  View2<T> FX{fx, is, js, ie - is + 2};
+  View2<T> FY{fy, is, js, ie - is + 1};
+  if (mass) {
+    View2<const double> M{mass, isd, jsd, nid};
+    const double damp2 = 0.5 * damp;
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie + 1; ++i) FX(i, j) = FX(i, j) + T(damp2 * (M(i - 1, j) + M(i, j))) * FX2(i, j);
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie; ++i) FY(i, j) = FY(i, j) + T(damp2 * (M(i, j - 1) + M(i, j))) * FY2(i, j);
+  } else {
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie + 1; ++i) FX(i, j) = FX(i, j) + FX2(i, j);
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie; ++i) FY(i, j) = FY(i, j) + FY2(i, j);
+  }
+}
+
+// damp = (damp_c da_min)^(nord+1), as a product
+inline double damp_coefficient(double damp_c, double da_min, int nord) {
+  const double b = damp_c * da_min;
+  double r = b;
+  for (int n = 0; n < nord; ++n) r *= b;
+  return r;
+}
+
 // fv_tp_2d: Lin & Rood inner/outer operators.  q's corner halo is modified.
+// Damping (deln_flux) is added when damp_c > 1e-4: with mass fluxes only if
+// mass is given (mass-weighted), without them unweighted.
 template <class T>
 void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, int hord, T* fx, T* fy,
                 const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
-                const double* ra_x, const double* ra_y, const double* mfx, const double* mfy) {
+                const double* ra_x, const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
+                const double* mass, int nord, double damp_c) {
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je;
   const int isd = bd->isd, ied = bd->ied, jsd = bd->jsd, jed = bd->jed;
   const int nid = ied - isd + 1;
@@ -258,7 +381,7 @@ void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, in
   // inner y operator on every column of the data domain, then outer x
   copy_corners_t<T>(q, npx, npy, 2, g, bd);
   std::vector<T> fy2((size_t)nid * (je - js + 2));
-  yppm_t<T>(fy2.data(), q, cry, isd, nid, hord, isd, ied, npy, g, bd);
+  yppm_t<T>(fy2.data(), q, cry, isd, nid, hord, lim_fac, isd, ied, npy, g, bd);
   View2<T> FY2{fy2.data(), isd, js, nid};
   std::vector<T> qi((size_t)nid * (jed - jsd + 1));
   View2<T> QI{qi.data(), isd, jsd, nid};
@@ -266,12 +389,12 @@ void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, in
     for (int i = isd; i <= ied; ++i)
       QI(i, j) = (Q(i, j) * T(AREA(i, j)) + T(YFX(i, j)) * FY2(i, j) - T(YFX(i, j + 1)) * FY2(i, j + 1)) /
                  T(RAY(i, j));
-  xppm_t<T>(fx, qi.data(), crx, jsd, hord, js, je, npx, g, bd);
+  xppm_t<T>(fx, qi.data(), crx, jsd, hord, lim_fac, js, je, npx, g, bd);
 
   // inner x operator on every row of the data domain, then outer y
   copy_corners_t<T>(q, npx, npy, 1, g, bd);
   std::vector<T> fx2((size_t)(ie - is + 2) * (jed - jsd + 1));
-  xppm_t<T>(fx2.data(), q, crx, jsd, hord, jsd, jed, npx, g, bd);
+  xppm_t<T>(fx2.data(), q, crx, jsd, hord, lim_fac, jsd, jed, npx, g, bd);
   View2<T> FX2{fx2.data(), is, jsd, ie - is + 2};
   std::vector<T> qj((size_t)nid * (jed - jsd + 1));
   View2<T> QJ{qj.data(), isd, jsd, nid};
@@ -279,7 +402,7 @@ void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, in
     for (int i = is; i <= ie; ++i)
       QJ(i, j) = (Q(i, j) * T(AREA(i, j)) + T(XFX(i, j)) * FX2(i, j) - T(XFX(i + 1, j)) * FX2(i + 1, j)) /
                  T(RAX(i, j));
-  yppm_t<T>(fy, qj.data(), cry, isd, nid, hord, is, ie, npy, g, bd);
+  yppm_t<T>(fy, qj.data(), cry, isd, nid, hord, lim_fac, is, ie, npy, g, bd);
 
   View2<T> FX{fx, is, js, ie - is + 2};
   View2<T> FY{fy, is, js, ie - is + 1};
@@ -293,6 +416,9 @@ void fv_tp_2d_t(T* q, const double* crx, const double* cry, int npx, int npy, in
       double w = mfy ? View2<const double>{mfy, is, js, ie - is + 1}(i, j) : YFX(i, j);
       FY(i, j) = T(0.5) * (FY(i, j) + FY2(i, j)) * T(w);
     }
+  if (damp_c > 1e-4 && (mfx == nullptr || mass != nullptr))
+    deln_flux_t<T>(nord, npx, npy, damp_coefficient(damp_c, g->da_min, nord), q, fx, fy, g, bd,
+                   mfx ? mass : nullptr);
 }
 
 // --------------------------------------------------------- tracer_2d parts ---
@@ -324,20 +450,6 @@ void area_fluxes(const double* cx, const double* cy, double* xfx, double* yfx, c
     }
 }
 
-struct Dom {  // convenience sizes of one domain
-  int is, ie, js, je, isd, ied, jsd, jed, nid, njd;
-  size_t plane, nxf, nyf, nmx, nmy;
-  explicit Dom(const orc_bounds* b)
-      : is(b->is), ie(b->ie), js(b->js), je(b->je), isd(b->isd), ied(b->ied), jsd(b->jsd), jed(b->jed) {
-    nid = ied - isd + 1;
-    njd = jed - jsd + 1;
-    plane = (size_t)nid * njd;
-    nxf = (size_t)(ie - is + 2) * njd;           // cx, xfx
-    nyf = (size_t)nid * (je - js + 2);           // cy, yfx
-    nmx = (size_t)(ie - is + 2) * (je - js + 1); // mfx, fx
-    nmy = (size_t)(ie - is + 1) * (je - js + 2); // mfy, fy
-  }
-};
 
 double max_courant(const double* cx, const double* cy, const Dom& d, int npz) {
   double cmax = 0.0;
@@ -526,26 +638,29 @@ void orc_copy_corners(double* q, int npx, int npy, int dir, const orc_grid* g, c
 
 void orc_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord, double* fx,
                   double* fy, const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
-                  const double* ra_x, const double* ra_y, const double* mfx, const double* mfy) {
-  fv_tp_2d_t<double>(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, g, bd, ra_x, ra_y, mfx, mfy);
+                  const double* ra_x, const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
+                  const double* mass, int nord, double damp_c) {
+  fv_tp_2d_t<double>(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, g, bd, ra_x, ra_y, lim_fac, mfx, mfy, mass, nord,
+                     damp_c);
 }
 
 void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const double* cry, int npx,
                      int npy, int hord, double* dfx, double* dfy, const double* xfx, const double* yfx,
                      const orc_grid* g, const orc_bounds* bd, const double* ra_x, const double* ra_y,
-                     const double* mfx, const double* mfy) {
+                     double lim_fac, const double* mfx, const double* mfy, const double* mass, int nord,
+                     double damp_c) {
   Dom d(bd);
   std::vector<Dual> qq(d.plane), fx(d.nmx), fy(d.nmy);
   for (size_t n = 0; n < d.plane; ++n) qq[n] = Dual(q[n], dq[n]);
-  fv_tp_2d_t<Dual>(qq.data(), crx, cry, npx, npy, hord, fx.data(), fy.data(), xfx, yfx, g, bd, ra_x, ra_y, mfx,
-                   mfy);
+  fv_tp_2d_t<Dual>(qq.data(), crx, cry, npx, npy, hord, fx.data(), fy.data(), xfx, yfx, g, bd, ra_x, ra_y, lim_fac,
+                   mfx, mfy, mass, nord, damp_c);
   for (size_t n = 0; n < d.nmx; ++n) dfx[n] = fx[n].d;
   for (size_t n = 0; n < d.nmy; ++n) dfy[n] = fy[n].d;
 }
 
 int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
                   const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
-                  orc_halo_fn halo_fn, void* halo_ctx) {
+                  int nord_tr, double trdm, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx) {
   (void)dt;
   Dom d(bd);
   std::vector<double> xfx(d.nxf * npz), yfx(d.nyf * npz);
@@ -569,8 +684,10 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
       level_setup(L, dp1 + k * d.plane, mfx + k * d.nmx, mfy + k * d.nmy, g, d);
       for (int iq = 0; iq < nq; ++iq) {
         double* qk = q + ((size_t)iq * npz + k) * d.plane;
+        // damping on the first substep only, weighted by the thickness at its start
         fv_tp_2d_t<double>(qk, cx + k * d.nxf, cy + k * d.nyf, npx, npy, hord, fx.data(), fy.data(), L.xfx.data(),
-                           L.yfx.data(), g, bd, L.rax.data(), L.ray.data(), mfx + k * d.nmx, mfy + k * d.nmy);
+                           L.yfx.data(), g, bd, L.rax.data(), L.ray.data(), lim_fac, mfx + k * d.nmx,
+                           mfy + k * d.nmy, dp1 + k * d.plane, nord_tr, it == 0 ? trdm : 0.0);
         flux_update(qk, dp1 + k * d.plane, L, fx.data(), fy.data(), g, d);
       }
       if (it < nsplt - 1) {
@@ -619,7 +736,7 @@ void orc_cube_halo_fill(double* q, int n, int ng, int nplanes, const int* topo) 
 
 int orc_tracer_2d_cube(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
                        const orc_grid* g6, int n, int npz, int nq, int hord, int q_split, const int* topo,
-                       int sync_edges) {
+                       int sync_edges, int nord_tr, double trdm, double lim_fac) {
   const int ng = 3;
   orc_bounds bd{1, n, 1, n, 1 - ng, n + ng, 1 - ng, n + ng, ng};
   Dom d(&bd);
@@ -659,8 +776,9 @@ int orc_tracer_2d_cube(double* q, double* dp1, double* mfx, double* mfy, double*
           double* qk = q + (((size_t)t * nq + iq) * npz + k) * d.plane;
           fv_tp_2d_t<double>(qk, cx + (t * npz + k) * d.nxf, cy + (t * npz + k) * d.nyf, npx, npy, hord,
                              fx.data() + t * d.nmx, fy.data() + t * d.nmy, L[t].xfx.data(), L[t].yfx.data(),
-                             &g6[t], &bd, L[t].rax.data(), L[t].ray.data(), mfx + (t * npz + k) * d.nmx,
-                             mfy + (t * npz + k) * d.nmy);
+                             &g6[t], &bd, L[t].rax.data(), L[t].ray.data(), lim_fac, mfx + (t * npz + k) * d.nmx,
+                             mfy + (t * npz + k) * d.nmy, dp1 + (t * npz + k) * d.plane, nord_tr,
+                             it == 0 ? trdm : 0.0);
         }
         if (sync_edges) {
           // outward flux of every tile-edge face, then adopt the owner's value

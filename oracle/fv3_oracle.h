@@ -46,6 +46,9 @@ typedef struct {
   const double* sin_sg;  /* (isd:ied,   jsd:jed, 9) slots 1..4 = W,S,E,N edge */
   int sw_corner, se_corner, nw_corner, ne_corner;  /* tile corner is a cube corner */
   int nested;            /* 1: no cube-edge treatment, no corner fill */
+  const double* del6_u;  /* (isd:ied,   jsd:jed+1) damping metric of y faces: sina_v dx / dyc */
+  const double* del6_v;  /* (isd:ied+1, jsd:jed)   damping metric of x faces: sina_u dy / dxc */
+  double da_min;         /* smallest cell area of the cube */
 } orc_grid;
 
 /* Cube topology: for tile t and edge e (0=W,1=E,2=S,3=N):
@@ -58,11 +61,14 @@ void orc_copy_corners(double* q, int npx, int npy, int dir, const orc_grid* g, c
 
 /* fv_tp_2d: fluxes fx (is:ie+1, js:je), fy (is:ie, js:je+1) of one level of
  * one tracer.  q's cube-corner halo blocks are overwritten (copy_corners).
- * mfx/mfy may be NULL (then xfx/yfx weight the fluxes). */
+ * hord 1 (with lim_fac), 5 or 8.  mfx/mfy may be NULL (then xfx/yfx weight the
+ * fluxes).  damp_c > 1e-4 adds del-2(nord+1) damping fluxes (nord 0..2),
+ * weighted by mass (isd:ied, jsd:jed) when mfx is given (mass NULL: none). */
 void orc_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord,
                   double* fx, double* fy, const double* xfx, const double* yfx,
                   const orc_grid* g, const orc_bounds* bd, const double* ra_x, const double* ra_y,
-                  const double* mfx, const double* mfy);
+                  double lim_fac, const double* mfx, const double* mfy, const double* mass, int nord,
+                  double damp_c);
 
 /* Halo refresh callback used by tracer_2d between substeps (single domain). */
 typedef void (*orc_halo_fn)(double* q, int nq, int npz, void* ctx);
@@ -74,7 +80,8 @@ typedef void (*orc_halo_fn)(double* q, int nq, int npz, void* ctx);
  * scaled in place by 1/nsplt and dp1 is advanced, as upstream.  Returns nsplt. */
 int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
                   const orc_grid* g, const orc_bounds* bd, int npx, int npy, int npz, int nq,
-                  int hord, int q_split, double dt, orc_halo_fn halo_fn, void* halo_ctx);
+                  int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
+                  orc_halo_fn halo_fn, void* halo_ctx);
 
 /* Fill the edge halo strips of six tiles (all levels/tracers stacked in nplanes
  * planes of (isd:ied, jsd:jed) per tile; tile stride = nplanes planes). */
@@ -86,7 +93,7 @@ void orc_cube_halo_fill(double* q, int n, int ng, int nplanes, const int* topo);
  * lower-numbered tile so global tracer mass is conserved exactly. */
 int orc_tracer_2d_cube(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
                        const orc_grid* g6, int n, int npz, int nq, int hord, int q_split,
-                       const int* topo, int sync_edges);
+                       const int* topo, int sync_edges, int nord_tr, double trdm, double lim_fac);
 
 /* cs_profile / ppm_profile of one column: a4 = (mean, left, right, a6) per
  * layer, a4[4*k + 0..3].  delp > 0 for km layers. */
@@ -129,7 +136,8 @@ double orc_mass_sum(const double* q, const double* dp, const double* area, long 
 void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const double* cry,
                      int npx, int npy, int hord, double* dfx, double* dfy, const double* xfx,
                      const double* yfx, const orc_grid* g, const orc_bounds* bd,
-                     const double* ra_x, const double* ra_y, const double* mfx, const double* mfy);
+                     const double* ra_x, const double* ra_y, double lim_fac, const double* mfx,
+                     const double* mfy, const double* mass, int nord, double damp_c);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ class Bounds(C.Structure):
 class Grid(C.Structure):
     _fields_ = [("dx", DP), ("dy", DP), ("dxa", DP), ("dya", DP), ("area", DP), ("rarea", DP), ("sin_sg", DP),
                 ("sw_corner", C.c_int), ("se_corner", C.c_int), ("nw_corner", C.c_int), ("ne_corner", C.c_int),
-                ("nested", C.c_int)]
+                ("nested", C.c_int), ("del6_u", DP), ("del6_v", DP), ("da_min", C.c_double)]
 
 
 HALO_FN = C.CFUNCTYPE(None, DP, C.c_int, C.c_int, C.c_void_p)
@@ -70,10 +70,15 @@ def bounds_for(n: int, ng: int = 3) -> Bounds:
 class GridRef:
     """An orc_grid plus the arrays it points to (kept alive)."""
 
-    def __init__(self, geom, corners=(1, 1, 1, 1), nested=0):
+    def __init__(self, geom, corners=(1, 1, 1, 1), nested=0, da_min=None):
         self.arrays = [_f64(geom.dx), _f64(geom.dy), _f64(geom.dxa), _f64(geom.dya), _f64(geom.area),
                        _f64(geom.rarea), _f64(geom.sin_sg)]
-        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested)
+        self.damp = [_f64(geom.del6_u), _f64(geom.del6_v)]
+        if da_min is None:
+            ng, n = geom.ng, geom.n
+            da_min = float(np.min(geom.area[ng:ng + n, ng:ng + n]))
+        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested, *[_p(a) for a in self.damp],
+                           C.c_double(da_min))
 
 
 def copy_corners(q: np.ndarray, n: int, direction: int, geom, ng: int = 3) -> np.ndarray:
@@ -83,23 +88,30 @@ def copy_corners(q: np.ndarray, n: int, direction: int, geom, ng: int = 3) -> np
     return q
 
 
-def fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3):
+def _opt(a):
+    return _p(a) if a is not None else None
+
+
+def fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3, lim_fac=1.0,
+             mass=None, nord=0, damp_c=0.0, nested=0, da_min=None):
     """Returns (fx, fy, q_with_corners)."""
     q = _f64(q).copy()
     n = q.shape[-1] - 2 * ng
     fx = np.zeros((n, n + 1))
     fy = np.zeros((n + 1, n))
-    g = GridRef(geom)
+    g = GridRef(geom, nested=nested, da_min=da_min)
     arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y)]
     mx = _f64(mfx) if mfx is not None else None
     my = _f64(mfy) if mfy is not None else None
+    ms = _f64(mass) if mass is not None else None
     lib().orc_fv_tp_2d(_p(q), _p(arrs[0]), _p(arrs[1]), n + 1, n + 1, hord, _p(fx), _p(fy), _p(arrs[2]),
                        _p(arrs[3]), C.byref(g.struct), C.byref(bounds_for(n, ng)), _p(arrs[4]), _p(arrs[5]),
-                       _p(mx) if mx is not None else None, _p(my) if my is not None else None)
+                       C.c_double(lim_fac), _opt(mx), _opt(my), _opt(ms), nord, C.c_double(damp_c))
     return fx, fy, q
 
 
-def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3):
+def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3, lim_fac=1.0,
+                mass=None, nord=0, damp_c=0.0):
     q = _f64(q)
     dq = _f64(dq)
     n = q.shape[-1] - 2 * ng
@@ -111,11 +123,13 @@ def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy
     my = _f64(mfy) if mfy is not None else None
     lib().orc_fv_tp_2d_tl(_p(q), _p(dq), _p(arrs[0]), _p(arrs[1]), n + 1, n + 1, hord, _p(dfx), _p(dfy),
                           _p(arrs[2]), _p(arrs[3]), C.byref(g.struct), C.byref(bounds_for(n, ng)), _p(arrs[4]),
-                          _p(arrs[5]), _p(mx) if mx is not None else None, _p(my) if my is not None else None)
+                          _p(arrs[5]), C.c_double(lim_fac), _opt(mx), _opt(my),
+                          _opt(_f64(mass) if mass is not None else None), nord, C.c_double(damp_c))
     return dfx, dfy
 
 
-def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3):
+def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3, nord_tr=0, trdm=0.0,
+              lim_fac=1.0):
     """Single-domain tracer_2d.  q (nq, npz, nd, nd).  Returns (q, dp1, mfx, mfy, cx, cy, nsplt)."""
     q = _f64(q).copy()
     dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
@@ -125,21 +139,25 @@ def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, n
     cb = HALO_FN(halo_fn) if halo_fn is not None else HALO_FN()
     nsplt = lib().orc_tracer_2d(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(g.struct),
                                 C.byref(bounds_for(n, ng)), n + 1, n + 1, npz, nq, hord, q_split, C.c_double(0.0),
-                                cb, None)
+                                nord_tr, C.c_double(trdm), C.c_double(lim_fac), cb, None)
     return q, dp1, mfx, mfy, cx, cy, nsplt
 
 
-def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=True, ng: int = 3):
+def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=True, ng: int = 3,
+                   nord_tr=0, trdm=0.0, lim_fac=1.0):
     """Six-tile tracer_2d.  q (6, nq, npz, nd, nd).  Returns (q, dp1, nsplt)."""
     q = _f64(q).copy()
     dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
     nq, npz = q.shape[1], q.shape[2]
     n = q.shape[-1] - 2 * ng
-    refs = [GridRef(g) for g in geoms]
+    ng_, n_ = geoms[0].ng, geoms[0].n
+    da = float(min(np.min(g.area[ng_:ng_ + n_, ng_:ng_ + n_]) for g in geoms))
+    refs = [GridRef(g, da_min=da) for g in geoms]
     arr = (Grid * 6)(*[r.struct for r in refs])
     topo = np.ascontiguousarray(topo, dtype=np.int32)
     nsplt = lib().orc_tracer_2d_cube(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), arr, n, npz, nq, hord,
-                                     q_split, topo.ctypes.data_as(C.POINTER(C.c_int)), int(sync_edges))
+                                     q_split, topo.ctypes.data_as(C.POINTER(C.c_int)), int(sync_edges), nord_tr,
+                                     C.c_double(trdm), C.c_double(lim_fac))
     return q, dp1, nsplt
 
 

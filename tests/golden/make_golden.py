@@ -21,7 +21,18 @@ sys.path.insert(0, ROOT)
 import oracle as O  # noqa: E402
 from fv3atm_gb300 import synth as S  # noqa: E402
 
-GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg")
+GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg", "del6_u", "del6_v")
+
+
+# tracer_2d_cube cases of the cube fixture: name -> oracle keyword arguments
+CUBE_CASES = {
+    "h8": dict(hord=8, q_split=3),
+    "h5": dict(hord=5, q_split=2),
+    "h1_lim3": dict(hord=1, q_split=2, lim_fac=3.0),
+    "h8_nord0": dict(hord=8, q_split=3, nord_tr=0, trdm=0.12),
+    "h8_nord1": dict(hord=8, q_split=2, nord_tr=1, trdm=0.1),
+    "h5_nord2": dict(hord=5, q_split=2, nord_tr=2, trdm=0.1),
+}
 
 
 def cube_fixture():
@@ -31,11 +42,11 @@ def cube_fixture():
         d["geom_" + f] = np.stack([getattr(g, f) for g in P.geoms])
     d["ak"], d["bk"], d["topo"] = P.ak, P.bk, P.topo
     out = {}
-    for hord, qs in ((8, 3), (5, 2)):
+    for name, kw in CUBE_CASES.items():
         q1, dp_last, ns = O.tracer_2d_cube(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], P.geoms, P.topo,
-                                           hord=hord, q_split=qs)
-        out[f"q_h{hord}"] = q1[..., 3:15, 3:15]
-        out[f"dplast_h{hord}"] = dp_last[..., 3:15, 3:15]
+                                           **kw)
+        out[f"q_{name}"] = q1[..., 3:15, 3:15]
+        out[f"dplast_{name}"] = dp_last[..., 3:15, 3:15]
     return {**d, **out, "n": np.array(12)}
 
 

@@ -11,7 +11,7 @@ import pytest
 import oracle as O
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg")
+GEOM_FIELDS = ("dx", "dy", "dxa", "dya", "area", "rarea", "sin_sg", "del6_u", "del6_v")
 
 
 def load_cube():
@@ -21,14 +21,25 @@ def load_cube():
     return d, geoms
 
 
-@pytest.mark.parametrize("hord,q_split", [(8, 3), (5, 2)])
-def test_oracle_reproduces_cube_fixture(hord, q_split):
+# name -> oracle keyword arguments (the cases make_golden.py records)
+CUBE_CASES = {
+    "h8": dict(hord=8, q_split=3),
+    "h5": dict(hord=5, q_split=2),
+    "h1_lim3": dict(hord=1, q_split=2, lim_fac=3.0),
+    "h8_nord0": dict(hord=8, q_split=3, nord_tr=0, trdm=0.12),
+    "h8_nord1": dict(hord=8, q_split=2, nord_tr=1, trdm=0.1),
+    "h5_nord2": dict(hord=5, q_split=2, nord_tr=2, trdm=0.1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CUBE_CASES))
+def test_oracle_reproduces_cube_fixture(name):
     d, geoms = load_cube()
     q1, dp_last, _ = O.tracer_2d_cube(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], geoms, d["topo"],
-                                      hord=hord, q_split=q_split)
+                                      **CUBE_CASES[name])
     n = int(d["n"])
-    assert np.array_equal(q1[..., 3:3 + n, 3:3 + n], d[f"q_h{hord}"])
-    assert np.array_equal(dp_last[..., 3:3 + n, 3:3 + n], d[f"dplast_h{hord}"])
+    assert np.array_equal(q1[..., 3:3 + n, 3:3 + n], d[f"q_{name}"])
+    assert np.array_equal(dp_last[..., 3:3 + n, 3:3 + n], d[f"dplast_{name}"])
 
 
 @pytest.mark.parametrize("kord,iv,qmin", [(9, 0, 0.0), (9, 1, 0.05), (4, 0, 0.0), (4, -1, 0.0), (4, -2, 0.0),

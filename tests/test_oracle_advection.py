@@ -129,7 +129,8 @@ def _transpose_geom(g):
                    dya=g.dxa.T.copy(), area=g.area.T.copy(), rarea=g.rarea.T.copy(),
                    sin_sg=np.stack([g.sin_sg[1].T, g.sin_sg[0].T, g.sin_sg[3].T, g.sin_sg[2].T] +
                                    [s.T for s in g.sin_sg[4:]]).copy(),
-                   corners=g.corners.transpose(1, 0, 2).copy(), centers=g.centers.transpose(1, 0, 2).copy())
+                   corners=g.corners.transpose(1, 0, 2).copy(), centers=g.centers.transpose(1, 0, 2).copy(),
+                   del6_u=g.del6_v.T.copy(), del6_v=g.del6_u.T.copy())
     return t
 
 
@@ -151,20 +152,115 @@ def test_x_sweep_on_transposed_data_equals_y_sweep(hord):
     assert np.allclose(fyT, fx.T, rtol=1e-14, atol=1e-14 * np.abs(fx).max())
 
 
-def test_tangent_linear_hord5_is_the_scheme_itself():
-    """hord 5 is linear in q, so its tangent-linear model applied to dq equals fv_tp_2d(dq)."""
-    P = S.make_problem(16, 1, 1, seed=2, ntiles=1)
-    g = P.geoms[0]
-    q = np.ascontiguousarray(P.q[0, 0, 0].numpy())
-    dq = np.random.default_rng(3).standard_normal(q.shape)
-    cx, cy = P.cx[0, 0].numpy(), P.cy[0, 0].numpy()
+def _tile_args(P, t=0, k=0):
+    g = P.geoms[t]
+    cx, cy = P.cx[t, k].numpy(), P.cy[t, k].numpy()
     xfx, yfx = area_fluxes(cx, cy, g)
     rax, ray = ra_xy(xfx, yfx, g)
-    mfx, mfy = P.mfx[0, 0].numpy(), P.mfy[0, 0].numpy()
-    dfx, dfy = O.fv_tp_2d_tl(q, dq, cx, cy, 5, xfx, yfx, g, rax, ray, mfx, mfy)
-    fx, fy, _ = O.fv_tp_2d(dq, cx, cy, 5, xfx, yfx, g, rax, ray, mfx, mfy)
-    assert np.allclose(dfx, fx, rtol=1e-12, atol=1e-12 * np.abs(fx).max())
-    assert np.allclose(dfy, fy, rtol=1e-12, atol=1e-12 * np.abs(fy).max())
+    return g, cx, cy, xfx, yfx, rax, ray, P.mfx[t, k].numpy(), P.mfy[t, k].numpy()
+
+
+def test_tangent_linear_hord5_is_linear_in_the_perturbation():
+    """hord 5 is piecewise linear in q (its 2-dx filter switches); with the filter frozen at the
+    trajectory the tangent-linear model is a linear map of dq."""
+    P = S.make_problem(16, 1, 1, seed=2, ntiles=1)
+    g, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_args(P)
+    q = np.ascontiguousarray(P.q[0, 0, 0].numpy())
+    rng = np.random.default_rng(3)
+    x, y = rng.standard_normal(q.shape), rng.standard_normal(q.shape)
+    tl = [O.fv_tp_2d_tl(q, d, cx, cy, 5, xfx, yfx, g, rax, ray, mfx, mfy) for d in (x, y, 2.0 * x - 3.0 * y)]
+    for c in range(2):
+        want = 2.0 * tl[0][c] - 3.0 * tl[1][c]
+        assert np.allclose(tl[2][c], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("hord", [1, 5])
+def test_two_dx_filter_gives_first_order_fluxes_on_a_checkerboard(hord):
+    """On q = 1 + a (-1)^i (constant in j) every cell is an extremum (bl = br), so hord 5 and hord 1 drop
+    the parabola's correction: away from the cube edges the x flux is the upwind value times mfx."""
+    P = S.make_problem(16, 1, 1, seed=4, ntiles=1)
+    g, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_args(P)
+    nd, n, ng = P.nd, P.n, 3
+    i = np.arange(nd)[None, :] + np.zeros((nd, 1))
+    q = np.ascontiguousarray(1.0 + 0.1 * (-1.0) ** i)
+    fx, _, _ = O.fv_tp_2d(q, cx, cy, hord, xfx, yfx, g, rax, ray, mfx, mfy, lim_fac=2.0)
+    c = cx[ng:ng + n, :]                                  # (n rows, n+1 faces)
+    up = np.where(c > 0, q[ng:ng + n, ng - 1:ng + n], q[ng:ng + n, ng:ng + n + 1])
+    sl = slice(3, n - 2)                                  # faces 4 .. n-2
+    assert np.allclose(fx[:, sl], (up * mfx)[:, sl], rtol=1e-13, atol=0)
+    # hord 8 on the same field: the limiter flattens every cell as well
+    fx8, _, _ = O.fv_tp_2d(q, cx, cy, 8, xfx, yfx, g, rax, ray, mfx, mfy)
+    assert np.allclose(fx8[:, sl], (up * mfx)[:, sl], rtol=1e-13, atol=0)
+
+
+def test_hord1_with_lim_fac_1_is_hord5():
+    """|b0| < |bl - br| is bl br < 0: hord 1 with lim_fac 1 reproduces hord 5; lim_fac 3 filters more."""
+    P = S.make_problem(16, 1, 1, seed=6, ntiles=1)
+    g, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_args(P)
+    q = np.ascontiguousarray(P.q[0, 0, 0].numpy())
+    f5 = O.fv_tp_2d(q, cx, cy, 5, xfx, yfx, g, rax, ray, mfx, mfy)
+    f1 = O.fv_tp_2d(q, cx, cy, 1, xfx, yfx, g, rax, ray, mfx, mfy, lim_fac=1.0)
+    f3 = O.fv_tp_2d(q, cx, cy, 1, xfx, yfx, g, rax, ray, mfx, mfy, lim_fac=3.0)
+    assert np.array_equal(f5[0], f1[0]) and np.array_equal(f5[1], f1[1])
+    assert not np.array_equal(f5[0], f3[0])
+
+
+def _laplacian_fluxes(d2, g, ng=3):
+    """x and y fluxes del6 * (d2 upwind-side difference) on the whole data domain (NaN where undefined)."""
+    nd = d2.shape[0]
+    fx = np.full((nd, nd + 1), np.nan)
+    fy = np.full((nd + 1, nd), np.nan)
+    fx[:, 1:nd] = g.del6_v[:, 1:nd] * (d2[:, :-1] - d2[:, 1:])
+    fy[1:nd, :] = g.del6_u[1:nd, :] * (d2[:-1, :] - d2[1:, :])
+    return fx, fy
+
+
+@pytest.mark.parametrize("nord", [0, 1, 2])
+def test_damping_fluxes_are_powers_of_the_discrete_laplacian(nord):
+    """Without winds or mass, fv_tp_2d's fluxes are the del-2(nord+1) damping fluxes alone.  Restated here
+    with numpy: F0 = del6 * (d(i-1) - d(i)) on d = damp q; each order replaces d by div F * rarea and takes
+    the difference the other way.  (nested: no cube-edge or corner treatment.)"""
+    P = S.make_problem(16, 1, 1, seed=8, ntiles=1)
+    g = P.geoms[0]
+    nd, n, ng = P.nd, P.n, 3
+    q = np.ascontiguousarray(P.q[0, 0, 0].numpy())
+    z = lambda shp: np.zeros(shp)
+    cx, cy, xfx, yfx = z((nd, n + 1)), z((n + 1, nd)), z((nd, n + 1)), z((n + 1, nd))
+    rax, ray = ra_xy(xfx, yfx, g)
+    damp_c = 0.07
+    da = float(g.area[ng:ng + n, ng:ng + n].min())
+    damp = (damp_c * da) ** (nord + 1)
+    fx, fy, _ = O.fv_tp_2d(q, cx, cy, 8, xfx, yfx, g, rax, ray, nord=nord, damp_c=damp_c, nested=1, da_min=da)
+    d2 = damp * q
+    Fx, Fy = _laplacian_fluxes(d2, g)
+    for _ in range(nord):
+        d2 = (Fx[:, :-1] - Fx[:, 1:] + Fy[:-1, :] - Fy[1:, :]) * g.rarea
+        Fx, Fy = _laplacian_fluxes(d2, g)
+        Fx, Fy = -Fx, -Fy
+    s = slice(ng, ng + n)
+    wx, wy = Fx[s, ng:ng + n + 1], Fy[ng:ng + n + 1, s]
+    assert np.allclose(fx, wx, rtol=1e-12, atol=1e-12 * np.abs(wx).max())
+    assert np.allclose(fy, wy, rtol=1e-12, atol=1e-12 * np.abs(wy).max())
+    if nord == 0:  # a del-2 flux runs down the gradient
+        assert np.all(fx * (q[s, ng - 1:ng + n] - q[s, ng:ng + n + 1]) >= 0)
+
+
+@pytest.mark.parametrize("nord,trdm", [(0, 0.12), (1, 0.1), (2, 0.1)])
+def test_damped_transport_conserves_mass_and_smooths(prob, nord, trdm):
+    P = prob
+    q0, dp_last0, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=8, q_split=3)
+    q1, dp_last, ns1 = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=8, q_split=3,
+                                        nord_tr=nord, trdm=trdm)
+    assert ns1 == ns and np.array_equal(dp_last, dp_last0)  # damping moves tracer mass only
+    dpf = final_dp(dp_last, P.mfx.numpy(), P.mfy.numpy(), P.geoms, ns, P.n)
+    m0 = cube_mass(P.q.numpy(), P.dp.numpy(), P.geoms, P.n)
+    m1 = cube_mass(q1, dpf, P.geoms, P.n)
+    assert np.all(np.abs(m1 - m0) <= 1e-13 * np.abs(m0)), (m1 - m0) / m0
+    # the damped field has less grid-scale variance than the undamped one
+    def roughness(q):
+        qi = interior(q, P.n)
+        return float(np.sum(np.diff(qi, axis=-1) ** 2) + np.sum(np.diff(qi, axis=-2) ** 2))
+    assert roughness(q1) < roughness(q0)
 
 
 def test_tangent_linear_hord8_matches_finite_differences_on_a_monotone_field():
