@@ -42,13 +42,13 @@ class Bounds(C.Structure):
 class Grid(C.Structure):
     _fields_ = [("dx", DP), ("dy", DP), ("dxa", DP), ("dya", DP), ("area", DP), ("rarea", DP), ("sin_sg", DP),
                 ("sw_corner", C.c_int), ("se_corner", C.c_int), ("nw_corner", C.c_int), ("ne_corner", C.c_int),
-                ("nested", C.c_int)]
+                ("nested", C.c_int), ("del6_u", DP), ("del6_v", DP), ("da_min", C.c_double)]
 
 
 class StateDesc(C.Structure):
     _fields_ = [("n", C.c_int), ("ntiles", C.c_int), ("npz", C.c_int), ("nq", C.c_int), ("precision", C.c_int),
                 ("hord", C.c_int), ("kord", C.c_int), ("iv", C.c_int), ("q_min", C.c_double),
-                ("warps_per_cta", C.c_int)]
+                ("warps_per_cta", C.c_int), ("nord_tr", C.c_int), ("trdm", C.c_double), ("lim_fac", C.c_double)]
 
 
 HALO_FN = C.CFUNCTYPE(None, DP, C.c_int, C.c_int, VP)

@@ -40,17 +40,23 @@ def bounds_for(n: int, ng: int = 3, is_: int = 1, ie: int | None = None, js: int
 class GridStruct:
     """fv3g_grid built from a tile geometry (keeps its arrays alive)."""
 
-    def __init__(self, geom, corners=(1, 1, 1, 1), nested: int = 0):
+    def __init__(self, geom, corners=(1, 1, 1, 1), nested: int = 0, da_min: float | None = None):
         self.arrays = [np.ascontiguousarray(a, dtype=np.float64)
                        for a in (geom.dx, geom.dy, geom.dxa, geom.dya, geom.area, geom.rarea, geom.sin_sg)]
-        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested)
+        self.damp = [np.ascontiguousarray(getattr(geom, f), dtype=np.float64) if hasattr(geom, f) else None
+                     for f in ("del6_u", "del6_v")]
+        if da_min is None:
+            ng, n = geom.ng, geom.n
+            da_min = float(np.min(geom.area[ng:ng + n, ng:ng + n]))
+        self.struct = Grid(*[_p(a) for a in self.arrays], *corners, nested, _p(self.damp[0]), _p(self.damp[1]),
+                           C.c_double(da_min))
 
 
 def fv_tp_2d(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, gridstruct: GridStruct, bd: Bounds, ra_x, ra_y,
-             lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+             lim_fac=1.0, mfx=None, mfy=None, mass=None, nord=0, damp_c=0.0) -> None:
     _lib.call("fv3g_fv_tp_2d", _p(q), _p(crx), _p(cry), npx, npy, hord, _p(fx), _p(fy), _p(xfx), _p(yfx),
               C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y), C.c_double(lim_fac), _p(mfx), _p(mfy),
-              nord, C.c_double(damp_c))
+              _p(mass), nord, C.c_double(damp_c))
 
 
 def tracer_2d(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, npx, npy, npz, nq, hord, q_split, dt,
@@ -81,19 +87,19 @@ def map1_ppm(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv
 
 
 def fv_tp_2d_tl(q, q_tl, crx, cry, npx, npy, hord, fx, fx_tl, fy, fy_tl, xfx, yfx, gridstruct: GridStruct,
-                bd: Bounds, ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+                bd: Bounds, ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, mass=None, nord=0, damp_c=0.0) -> None:
     """Tangent-linear fv_tp_2d (Courant numbers and mass fluxes frozen); fx / fy may be None."""
     _lib.call("fv3g_fv_tp_2d_tl", _p(q), _p(q_tl), _p(crx), _p(cry), npx, npy, hord, _p(fx), _p(fx_tl), _p(fy),
               _p(fy_tl), _p(xfx), _p(yfx), C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y),
-              C.c_double(lim_fac), _p(mfx), _p(mfy), nord, C.c_double(damp_c))
+              C.c_double(lim_fac), _p(mfx), _p(mfy), _p(mass), nord, C.c_double(damp_c))
 
 
 def fv_tp_2d_ad(q, q_ad, crx, cry, npx, npy, hord, fx_ad, fy_ad, xfx, yfx, gridstruct: GridStruct, bd: Bounds,
-                ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, nord=0, damp_c=0.0) -> None:
+                ra_x, ra_y, lim_fac=1.0, mfx=None, mfy=None, mass=None, nord=0, damp_c=0.0) -> None:
     """Adjoint fv_tp_2d at trajectory q: q_ad += J^T (fx_ad, fy_ad); fx_ad, fy_ad are zeroed."""
     _lib.call("fv3g_fv_tp_2d_ad", _p(q), _p(q_ad), _p(crx), _p(cry), npx, npy, hord, _p(fx_ad), _p(fy_ad), _p(xfx),
               _p(yfx), C.byref(gridstruct.struct), C.byref(bd), _p(ra_x), _p(ra_y), C.c_double(lim_fac), _p(mfx),
-              _p(mfy), nord, C.c_double(damp_c))
+              _p(mfy), _p(mass), nord, C.c_double(damp_c))
 
 
 def map1_ppm_tl(km, pe1, q1, q1_tl, qs, kn, pe2, q2, q2_tl, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord) -> None:
@@ -135,13 +141,14 @@ class CubeState:
     resident in HBM (fv3g_state)."""
 
     def __init__(self, n: int, npz: int, nq: int, *, precision: str = "fp64", hord: int = 8, kord: int = 9,
-                 iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0, ntiles: int = 6):
+                 iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0, ntiles: int = 6, nord_tr: int = 0,
+                 trdm: float = 0.0, lim_fac: float = 1.0):
         L = _lib.load()
         self.n, self.npz, self.nq, self.ntiles = n, npz, nq, ntiles
         self.nd = n + 6
         self.precision = precision
         prec = _lib.FV3G_FP64 if precision == "fp64" else _lib.FV3G_MIXED
-        desc = StateDesc(n, ntiles, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta)
+        desc = StateDesc(n, ntiles, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta, nord_tr, trdm, lim_fac)
         self._h = C.c_void_p()
         _lib.check(L.fv3g_state_create(C.byref(desc), C.byref(self._h)), "fv3g_state_create")
         self._grids = []
@@ -159,8 +166,10 @@ class CubeState:
 
     # ------------------------------------------------------------- setup
     def set_grid(self, geoms) -> None:
+        ng, n = geoms[0].ng, geoms[0].n
+        da = float(min(np.min(g.area[ng:ng + n, ng:ng + n]) for g in geoms))  # over the cube
         for t, g in enumerate(geoms):
-            gs = GridStruct(g)
+            gs = GridStruct(g, da_min=da)
             self._grids.append(gs)
             _lib.call("fv3g_state_set_grid", self._h, t, C.byref(gs.struct))
 

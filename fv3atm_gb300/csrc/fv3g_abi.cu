@@ -124,6 +124,9 @@ struct fv3g_state {
   void* dp_eul = nullptr;
   void* area = nullptr; void* rarea = nullptr; void* dxa = nullptr; void* dya = nullptr;
   void* dx = nullptr; void* dy = nullptr; void* sin4 = nullptr;
+  void* del6u = nullptr; void* del6v = nullptr;  // tracer-damping metrics
+  int del6_tiles = 0;                            // tiles whose damping metrics were set
+  double da_min = 0.0;
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
   double* partials = nullptr; double* mass_out = nullptr;
@@ -252,6 +255,7 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.cube = st->nt == 6 ? 1 : 0;
   a.topo = st->topo;
   a.eflux = (T*)st->eflux;
+  a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
   return a;
 }
 
@@ -331,6 +335,8 @@ int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t 
 
 template <typename T>
 int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
+  if (st->d.trdm > 1e-4 && (st->del6_tiles != (1 << st->nt) - 1 || !(st->da_min > 0.0)))
+    return set_error(FV3G_E_ARG, "tracer damping (trdm > 1e-4) needs every tile's grid with del6_u, del6_v, da_min");
   const long long fsz = st->plane * st->npz * st->nt;
   const size_t fb = (size_t)fsz * sizeof(T);
   // scaled work copies and area fluxes
@@ -359,10 +365,19 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
       CHECK(mark(st, K_HALO, s));
     }
     CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
+    const bool damp = it == 0 && st->d.trdm > 1e-4;  // upstream damps the first substep only
+    if (damp) {
+      a.del6_u = (const T*)st->del6u;
+      a.del6_v = (const T*)st->del6v;
+      a.damp = T(damp_coefficient(st->d.trdm, st->da_min, st->d.nord_tr));
+      a.nord = st->d.nord_tr;
+      a.damp_mass = 1;
+      CHECK(launch_damp<T>(a, false, s));
+    }
     {
       const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
       const int nint = bm.nbxi * bm.nbyi;
-      CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint)));
+      CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint) + (damp ? 1 : 0)));
     }
     if (st->nt == 6) {
       CHECK(launch_edge_fix<T>(a, st->n, s));
@@ -438,7 +453,11 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (d.n < 12 || d.npz < 2 || d.npz > KMAX || d.nq < 1)
     return set_error(FV3G_E_ARG, "bad sizes n=%d npz=%d nq=%d (n>=12, 2<=npz<=%d, nq>=1)", d.n, d.npz, d.nq, KMAX);
   if (d.precision != FV3G_FP64 && d.precision != FV3G_MIXED) return set_error(FV3G_E_ARG, "bad precision %d", d.precision);
-  if (d.hord != 5 && d.hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented", d.hord);
+  if (d.hord != 1 && d.hord != 5 && d.hord != 8)
+    return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", d.hord);
+  if (d.lim_fac < 0.0) return set_error(FV3G_E_ARG, "lim_fac must be positive (0 selects 1), got %g", d.lim_fac);
+  if (d.trdm > 1e-4 && (d.nord_tr < 0 || d.nord_tr > 2))
+    return set_error(FV3G_E_UNSUPPORTED, "tracer damping supports nord_tr 0..2 (got %d)", d.nord_tr);
   if (d.kord != 4 && d.kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented", d.kord);
   if (d.iv < -2 || d.iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", d.iv);
   fv3g_state* st = new (std::nothrow) fv3g_state();
@@ -480,7 +499,7 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
                      &st->xfx, &st->yfx, &st->dp_eul};
   for (void** f : fields)
     if (!rc) rc = dalloc(st, f, fb);
-  void** metrics[] = {&st->area, &st->rarea, &st->dxa, &st->dya, &st->dx, &st->dy};
+  void** metrics[] = {&st->area, &st->rarea, &st->dxa, &st->dya, &st->dx, &st->dy, &st->del6u, &st->del6v};
   for (void** m : metrics)
     if (!rc) rc = dalloc(st, m, P * nt);
   if (!rc) rc = dalloc(st, &st->sin4, P * nt * 4);
@@ -530,6 +549,16 @@ int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* g) {
     int rc = st->fp64 ? upload_t<double>(st, fs, m.src, st->stream) : upload_t<float>(st, fs, m.src, st->stream);
     if (rc) return rc;
   }
+  if (g->del6_u && g->del6_v) {  // damping metrics (optional unless trdm > 1e-4)
+    M dm[] = {{g->del6_u, at(st->del6u, tile), nd, nd + 1, 0}, {g->del6_v, at(st->del6v, tile), nd + 1, nd, 0}};
+    for (const M& m : dm) {
+      FieldShape fs{1, m.ni, m.nj, 0, 0, m.dst};
+      int rc = st->fp64 ? upload_t<double>(st, fs, m.src, st->stream) : upload_t<float>(st, fs, m.src, st->stream);
+      if (rc) return rc;
+    }
+    st->del6_tiles |= 1 << tile;
+  }
+  if (g->da_min > 0.0) st->da_min = g->da_min;
   if (!g->sin_sg) return set_error(FV3G_E_ARG, "null sin_sg");
   for (int sl = 0; sl < 4; ++sl) {
     FieldShape fs{1, nd, nd, 0, 0, at(st->sin4, (long long)tile * 4 + sl)};

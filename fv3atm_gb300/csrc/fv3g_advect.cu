@@ -1,569 +1,17 @@
-// fv3g_advect.cu -- fused fv_tp_2d + flux-form update (one tracer_2d substep).
-//
-// Restates, GB300-first, the body of the substep loop of tracer_2d
-// (fv_tracer2d.F90) and fv_tp_2d / xppm / yppm / copy_corners (tp_core.F90) of
-// GFDL_atmos_cubed_sphere (absent submodule, .gitmodules:1-4).
-//
-// One CTA owns a 26 x 26 block of output cells of one (tile, level) and a
-// 32 x 32 window (3-cell halo) of every tracer.  Per-level fields (Courant
-// numbers, area and mass fluxes, 1/ra_x, 1/ra_y, dp ratios) are staged once
-// in shared memory and shared by the CTA's warps; each warp advances one
-// tracer at a time through three on-chip stages:
-//   S1  lane = window column: inner y-PPM on q (corner blocks filled for a y
-//       sweep) -> inner y flux and the advective update q_i;
-//   S2  lane = window row: inner x-PPM on q (corners re-filled for an x sweep)
-//       -> q_j, and on the 26 interior rows the outer x-PPM on q_i, combined
-//       into the final x flux and its divergence;
-//   S3  lane = window column (interior ones): outer y-PPM on q_j, final y
-//       flux, and the flux-form update q <- (q dp1 + div F * rarea) / dp2
-//       written to HBM.  The inner y flux of S1 stays in the lane's registers.
-// Each lane marches its line with a register pipeline (slope -> interface ->
-// edge deviations -> flux), so intermediate fluxes never leave the SM and q
-// is read once and written once per substep.  Halo cells are gathered from
-// the neighbouring tiles of the cube (or read from the caller's halo), and
-// the cube-corner blocks are filled by the rotation of copy_corners at load.
+// fv3g_advect.cu -- the kernels around the advection substep of tracer_2d
+// (tracer_2d / copy_corners of GFDL_atmos_cubed_sphere, fv_tracer2d.F90 and
+// tp_core.F90; absent submodule, .gitmodules:1-4): halo strips of the six
+// tiles, the tile-edge flux reconciliation, the area fluxes and Courant
+// maximum of the prologue, and the dispatch of the substep kernels
+// (fv3g_substep.cuh) by hord.
 #include <cstdio>
 #include <algorithm>
 #include <mutex>
 #include <type_traits>
 
-#include "fv3g_internal.cuh"
+#include "fv3g_stencil.cuh"
 
 namespace fv3g {
-
-template <typename T>
-struct SmemLevel {
-  T cy[NF][WIN];  // inner/outer y Courant [face j][window col]
-  T yf[NF][WIN];  // yfx
-  T cx[WIN][PF];  // [window row][face i]
-  T xf[WIN][PF];
-  T mx[TW][PF];   // 0.5*mfx [interior row][face i]
-  T my[NF][TW];   // 0.5*mfy [face j][interior col]
-  T area[WIN][PQ];
-  T rrx[WIN][PF];  // 1/ra_x [window row][interior col]
-  T rry[TW][WIN];  // 1/ra_y [interior row][window col]
-  T dpa[TW][TW];   // dp1/rarea
-  T ub[TW][TW];    // rarea/dp2
-  T edx[2][4][WIN];  // edge CTAs: dxa at window columns e-2..e+1 of x edge A/B, per window row
-  T edy[2][4][WIN];  // dya at window rows e-2..e+1 of y edge A/B, per window column
-};
-
-template <typename T>
-struct SmemWarp {
-  T q[WIN][PQ];   // tracer window; S2 overwrites each row with q_j (interior columns)
-  T qi[TW][PQ];   // q_i; then q dp1/rarea + x-flux divergence (or the x fluxes)
-};
-
-// Per-warp shared memory; edge CTAs add the deviations of two lines at two
-// edges, [2][16][32] values.
-template <typename T>
-__host__ __device__ constexpr size_t warp_smem_bytes(bool edges) {
-  return sizeof(SmemWarp<T>) + (edges ? 2 * 16 * 32 * sizeof(T) : 0);
-}
-
-template <typename T>
-size_t substep_smem_bytes(int warps, bool edges) {
-  return sizeof(SmemLevel<T>) + warps * warp_smem_bytes<T>(edges);
-}
-
-// ----------------------------------------------------------- halo source ---
-// Rotate a cube-corner halo cell (tile indices) into the halo strip that a
-// sweep in direction dir (1 = x, 2 = y) continues: about the corner point,
-// +90 deg maps (u,v) -> (-v,u) and -90 deg maps (u,v) -> (v,-u).
-__device__ __forceinline__ void corner_rotate(int& i, int& j, int npx, int npy, int dir) {
-  const int su = (i < 1) ? -1 : 1, sv = (j < 1) ? -1 : 1;
-  const int cx2 = (su < 0) ? 1 : 2 * npx - 1;  // doubled corner coordinates
-  const int cy2 = (sv < 0) ? 1 : 2 * npy - 1;
-  const int U = 2 * i - cx2, V = 2 * j - cy2;
-  const bool plus = (dir == 1) ? (su == -sv) : (su == sv);
-  const int U2 = plus ? -V : V, V2 = plus ? U : -U;
-  i = (U2 + cx2) / 2;
-  j = (V2 + cy2) / 2;
-}
-
-// Interior cell of the neighbouring tile that tile t's edge-halo cell (i, j) is.
-__device__ __forceinline__ void cube_source(const Topo& tp, int n, int& t, int& i, int& j) {
-  int e, d, s;
-  if (i < 1) { e = EW; d = 1 - i; s = j - 1; }
-  else if (i > n) { e = EE; d = i - n; s = j - 1; }
-  else if (j < 1) { e = ES; d = 1 - j; s = i - 1; }
-  else { e = EN; d = j - n; s = i - 1; }
-  const int nt = tp.nbr[t][e], ne = tp.nedge[t][e];
-  const int sb = tp.rev[t][e] ? n - 1 - s : s;
-  switch (ne) {
-    case EW: i = d; j = sb + 1; break;
-    case EE: i = n + 1 - d; j = sb + 1; break;
-    case ES: i = sb + 1; j = d; break;
-    default: i = sb + 1; j = n + 1 - d; break;
-  }
-  t = nt;
-}
-
-template <typename T>
-__device__ __forceinline__ T load_q(const AdvArgs<T>& a, int t, int iq, int k, int i, int j, int dir) {
-  const int n = a.npx - 1;
-  const bool out_i = (i < 1) || (i > a.npx - 1), out_j = (j < 1) || (j > a.npy - 1);
-  if (out_i && out_j && !a.nested) {
-    const int bit = (i < 1 ? 0 : 1) + (j < 1 ? 0 : 2);
-    if (a.corners & (1 << bit)) corner_rotate(i, j, a.npx, a.npy, dir);
-  }
-  if (a.cube && (i < 1 || i > n || j < 1 || j > n) && !(((i < 1) || (i > n)) && ((j < 1) || (j > n))))
-    cube_source(a.topo, n, t, i, j);
-  // stay inside the data domain; clamped cells feed only discarded outputs
-  i = min(max(i, a.pg.isd), a.pg.isd + a.pg.pitch - 1);
-  j = min(max(j, a.pg.jsd), a.pg.jsd + a.pg.rows - 1);
-  return a.q_in[t * a.sQt + iq * a.sQq + k * a.sQk + a.pg.at(i, j)];
-}
-
-template <typename T>
-__device__ __forceinline__ T ld_field(const T* base, const PlaneGeom& pg, int i, int j) {
-  i = min(max(i, pg.isd), pg.isd + pg.pitch - 1);
-  j = min(max(j, pg.jsd), pg.jsd + pg.rows - 1);
-  return base[pg.at(i, j)];
-}
-
-// ------------------------------------------------------- PPM line stream ---
-// Deviations (bl, br) of the four cells e-2..e+1 around a cube-face edge at
-// window face e, computed once per line from shared memory and kept there
-// (o[c*32] = bl of cell e-2+c, o[(4+c)*32] = br; lane-strided): the edge value is
-// the mean of the two one-sided, dxa-weighted linear extrapolations; the two
-// neighbouring interfaces use one-sided third-order values (see the oracle's
-// xppm/yppm restatement).  Only cells 2..29 of a window feed its fluxes.
-template <typename T, int HORD, class EX>
-__device__ __forceinline__ T generic_bl(int c, EX&& x) {
-  if (HORD == 8) {
-    T dm0 = vl_slope(x(c - 2), x(c - 1), x(c)), dm1 = vl_slope(x(c - 1), x(c), x(c + 1));
-    T al = T(0.5) * (x(c - 1) + x(c)) + (dm0 - dm1) * T(1.0 / 3.0);
-    T xt = T(2) * dm1;
-    return -tsign(tmin(tabs(xt), tabs(al - x(c))), xt);
-  }
-  return T(7.0 / 12.0) * (x(c - 1) + x(c)) - T(1.0 / 12.0) * (x(c - 2) + x(c + 1)) - x(c);
-}
-
-template <typename T, int HORD, class EX>
-__device__ __forceinline__ T generic_br(int c, EX&& x) {
-  if (HORD == 8) {
-    T dm0 = vl_slope(x(c - 1), x(c), x(c + 1)), dm1 = vl_slope(x(c), x(c + 1), x(c + 2));
-    T al = T(0.5) * (x(c) + x(c + 1)) + (dm0 - dm1) * T(1.0 / 3.0);
-    T xt = T(2) * dm0;
-    return tsign(tmin(tabs(xt), tabs(al - x(c))), xt);
-  }
-  return T(7.0 / 12.0) * (x(c) + x(c + 1)) - T(1.0 / 12.0) * (x(c - 1) + x(c + 2)) - x(c);
-}
-
-template <typename T, int HORD, class EX, class ED>
-__device__ __noinline__ void edge_devs(int e, EX x, ED ed, T* o) {
-  if (e == NO_EDGE) return;
-  const bool need0 = (e - 2 >= 2 && e - 2 <= 29), need1 = (e - 1 >= 2 && e - 1 <= 29);
-  const bool need2 = (e >= 2 && e <= 29), need3 = (e + 1 >= 2 && e + 1 <= 29);
-  T aM = T(0), a0 = T(0), aP = T(0);
-  if (need0 || need1) {
-    aM = T(-1.0 / 6.0) * x(e - 3) + T(5.0 / 6.0) * x(e - 2) + T(1.0 / 3.0) * x(e - 1);
-    if (HORD == 8) aM = clamp2(aM, x(e - 2), x(e - 1));
-  }
-  if (need1 || need2) {
-    T d2 = ed(e - 2), d1 = ed(e - 1), d0 = ed(e), d3 = ed(e + 1);
-    T xl = ((T(2) * d1 + d2) * x(e - 1) - d1 * x(e - 2)) / (d2 + d1);
-    T xr = ((T(2) * d0 + d3) * x(e) - d0 * x(e + 1)) / (d0 + d3);
-    a0 = T(0.5) * (xl + xr);
-    if (HORD == 8) a0 = clamp2(a0, x(e - 1), x(e));
-  }
-  if (need2 || need3) {
-    aP = T(1.0 / 3.0) * x(e) + T(5.0 / 6.0) * x(e + 1) - T(1.0 / 6.0) * x(e + 2);
-    if (HORD == 8) aP = clamp2(aP, x(e), x(e + 1));
-  }
-  T b[4] = {T(0), T(0), T(0), T(0)}, r[4] = {T(0), T(0), T(0), T(0)};
-  if (need0) { b[0] = generic_bl<T, HORD>(e - 2, x); r[0] = aM - x(e - 2); }
-  if (need1) { b[1] = aM - x(e - 1); r[1] = a0 - x(e - 1); }
-  if (need2) { b[2] = a0 - x(e); r[2] = aP - x(e); }
-  if (need3) { b[3] = aP - x(e + 1); r[3] = generic_br<T, HORD>(e + 1, x); }
-  if (HORD == 8)
-    for (int c = 0; c < 4; ++c) cw84(b[c], r[c]);
-  for (int c = 0; c < 4; ++c) { o[c * 32] = b[c]; o[(4 + c) * 32] = r[c]; }
-}
-
-// A line of 32 window cells x[0..31] marched with a rolling register window;
-// face f separates cells f-1 and f, and faces 3..29 are the CTA tile's.
-// Before step m the state holds x[m-3..m-1] (xa, xb, xc), dm[m-2] and al[m-2]
-// (hord 8) and the right deviation and b0 = bl + br of cell m-3; step(x[m])
-// finalises cell m-2 and returns the flux through face m-2 (valid for m >= 5).
-//   hord 8: dm = monotonized central slope (clamp form), al = interface value,
-//           |edge deviation| <= |2 dm| with the sign of dm (Lin 2004);
-//   flux  = x_up + w1 d_up - w2 b0_up with w1 = 1-|c|, w2 = |c| w1 and the
-//           upwind cell's deviation at the face (CW84 parabola integral).
-template <typename T>
-__device__ __forceinline__ T dm_clamp(T xm, T x0, T xp) {
-  const T xt = T(0.25) * (xp - xm);
-  return copysign_t(tmin3(tabs(xt), tmax3(xm, x0, xp) - x0, x0 - tmin3(xm, x0, xp)), xt);
-}
-
-// Steps of a line whose cell m-2 lies next to a cube-face edge: bit m of
-// mask, for the two edges at window faces eA and eB (warp-uniform).
-struct EdgeSel {
-  unsigned mask;
-  int eA, eB;
-};
-__device__ __forceinline__ EdgeSel edge_sel(int eA, int eB) {
-  auto bits = [](int e) { return (e >= 0 && e < 32) ? (0xFu << e) : 0u; };
-  return EdgeSel{bits(eA) | bits(eB), eA, eB};
-}
-
-template <typename T, int HORD>
-struct Line {
-  T xa, xb, xc, dmb, alb, pbr, pb0;
-
-  __device__ __forceinline__ void init() { xa = xb = xc = dmb = alb = pbr = pb0 = T(0); }
-
-  // ed: this lane's edge deviations (16 lane-strided slots: edge A bl0..3 br0..3, then edge B)
-  template <bool EDGES>
-  __device__ __forceinline__ T step(int m, T x, T c, const T* ed, const EdgeSel& es) {
-    T alc, bl, br;
-    if (HORD == 8) {
-      const T dmc = dm_clamp(xb, xc, x);                      // dm[m-1]
-      alc = T(0.5) * (xb + xc) + (dmb - dmc) * T(1.0 / 3.0);  // al[m-1]
-      const T xt = dmb + dmb;                                 // cell m-2
-      const T axt = tabs(xt);
-      bl = copysign_t(tmin(axt, tabs(alb - xb)), -xt);
-      br = copysign_t(tmin(axt, tabs(alc - xb)), xt);
-      dmb = dmc;
-    } else {
-      alc = T(7.0 / 12.0) * (xb + xc) - T(1.0 / 12.0) * (xa + x);
-      bl = alb - xb;
-      br = alc - xb;
-    }
-    if (EDGES && ((es.mask >> m) & 1u)) {  // cell m-2 is cell e-2+d of an edge
-      const int dA = m - es.eA;
-      const int slot = (unsigned)dA < 4u ? dA : 8 + (m - es.eB);
-      bl = ed[slot * 32];
-      br = ed[(slot + 4) * 32];
-    }
-    const T b0 = bl + br;
-    const T a = tabs(c);
-    const T w1 = T(1) - a, w2 = a * w1;
-    const T fl_l = (xa + w1 * pbr) - w2 * pb0;  // upwind cell on the left (c > 0)
-    const T fl_r = (xb + w1 * bl) - w2 * b0;
-    const T fl = c > T(0) ? fl_l : fl_r;
-    xa = xb;
-    xb = xc;
-    xc = x;
-    alb = alc;
-    pbr = br;
-    pb0 = b0;
-    return fl;
-  }
-};
-
-// ------------------------------------------------------------ the kernel ---
-// One tracer of one CTA tile through the three stages (see file header).
-template <typename T, int HORD, bool FLUXES, bool EDGES>
-__device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>& L, SmemWarp<T>& S, int t, int k,
-                                               T* eds, int iq, int i0, int j0, int ni, int nj, int lane, int exA,
-                                               int exB, int eyA, int eyB, bool corner_block,
-                                               long long efo, long long efe) {
-  const PlaneGeom& pg = a.pg;
-  const int n = a.npx - 1;
-  // Cube-corner halo blocks of the window, which copy_corners fills by a
-  // rotation that depends on the sweep direction (1 = x, 2 = y).
-  auto corner_cells = [&](int dir) {
-    const int i = i0 - 3 + lane;
-#pragma unroll 1
-    for (int r = 0; r < WIN; ++r) {
-      const int j = j0 - 3 + r;
-      const bool oi = (i < 1) || (i > a.npx - 1), oj = (j < 1) || (j > a.npy - 1);
-      if (oi && oj) S.q[r][lane] = load_q(a, t, iq, k, i, j, dir);
-    }
-  };
-  // ------------------------------------------ window load (y-sweep corners)
-  // The planes hold their halo strips (caller-filled, or k_cube_halo); cells
-  // beyond the plane are clamped and feed only discarded outputs.
-  auto load_window = [&](const T* base) {
-    const int ic = min(max(i0 - 3 + lane, pg.isd), pg.isd + pg.pitch - 1);
-    const T* src = base + t * a.sQt + iq * a.sQq + k * a.sQk + (ic - pg.isd);
-    const int jhi = pg.jsd + pg.rows - 1;
-#pragma unroll 8
-    for (int r = 0; r < WIN; ++r) {
-      const int jr = min(max(j0 - 3 + r, pg.jsd), jhi);
-      S.q[r][lane] = src[(long long)(jr - pg.jsd) * pg.pitch];
-    }
-  };
-  load_window(a.q_in);
-  if (corner_block) corner_cells(2);
-  __syncwarp();
-
-  T fyr[NF];  // inner y flux of this lane's column at faces 3..29 (S1 -> S3)
-  const EdgeSel esx = edge_sel(exA, exB), esy = edge_sel(eyA, eyB);
-  // edge deviations of the lines in flight: eds[line][16][32], lines 0 (and 1 in S2)
-  T* const ed0 = eds + lane;
-  T* const ed1 = eds + 16 * 32 + lane;
-  // ------------------------------------------------ S1: inner y, q_i ------
-  {
-    const int w = lane;
-    const T* qcol = &S.q[0][w];
-    if (EDGES) {
-      auto ex = [qcol](int m) { return qcol[m * PQ]; };
-      auto edA = [&L, w, eyA](int m) { return L.edy[0][m - eyA + 2][w]; };
-      auto edB = [&L, w, eyB](int m) { return L.edy[1][m - eyB + 2][w]; };
-      edge_devs<T, HORD>(eyA, ex, edA, ed0);
-      edge_devs<T, HORD>(eyB, ex, edB, ed0 + 8 * 32);
-    }
-    Line<T, HORD> ln;
-    ln.init();
-#pragma unroll
-    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qcol[m * PQ], T(0), ed0, esy);
-    fyr[0] = ln.template step<EDGES>(5, qcol[5 * PQ], L.cy[0][w], ed0, esy);
-    T fyy_prev = L.yf[0][w] * fyr[0];
-#pragma unroll
-    for (int m = 6; m < WIN; ++m) {
-      const int f = m - 2;
-      const T xrow = ln.xa;  // cell row f-1 = m-3
-      fyr[f - 3] = ln.template step<EDGES>(m, qcol[m * PQ], L.cy[f - 3][w], ed0, esy);
-      const T fyy = L.yf[f - 3][w] * fyr[f - 3];
-      S.qi[f - 4][w] = (xrow * L.area[f - 1][w] + fyy_prev - fyy) * L.rry[f - 4][w];
-      fyy_prev = fyy;
-    }
-  }
-  __syncwarp();
-
-  // -------------------------------------- corner blocks for the x sweeps
-  if (a.q_in_x != nullptr) {  // separate input of the x sweeps (adjoint assembly)
-    load_window(a.q_in_x);
-    __syncwarp();
-  } else if (corner_block) {
-    corner_cells(1);
-    __syncwarp();
-  }
-
-  // ---------- S2: inner x -> q_j (into the q row); outer x on q_i -> P -----
-  {
-    const int r = lane;
-    const bool outer = (r >= 3) && (r < 29);
-    const int ro = outer ? r - 3 : 0;
-    T* qrow = &S.q[r][0];
-    T* qirow = &S.qi[ro][0];
-    if (EDGES) {
-      auto exi = [qrow](int m) { return qrow[m]; };
-      auto exo = [qirow](int m) { return qirow[m]; };
-      auto edA = [&L, r, exA](int m) { return L.edx[0][m - exA + 2][r]; };
-      auto edB = [&L, r, exB](int m) { return L.edx[1][m - exB + 2][r]; };
-      edge_devs<T, HORD>(exA, exi, edA, ed0);
-      edge_devs<T, HORD>(exB, exi, edB, ed0 + 8 * 32);
-      if (outer) {
-        edge_devs<T, HORD>(exA, exo, edA, ed1);
-        edge_devs<T, HORD>(exB, exo, edB, ed1 + 8 * 32);
-      }
-    }
-    const bool efw = EDGES && a.cube && a.eflux != nullptr && outer && ro < nj;
-    Line<T, HORD> li, lo;
-    li.init();
-    lo.init();
-#pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      li.template step<EDGES>(m, qrow[m], T(0), ed0, esx);
-      lo.template step<EDGES>(m, qirow[m], T(0), ed1, esx);
-    }
-    // face 3
-    T c = L.cx[r][0];
-    T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, esx);
-    T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, esx);
-    T fxx_prev = L.xf[r][0] * fx2;
-    T F_prev = (fo + fx2) * L.mx[ro][0];
-    if (FLUXES && outer) qirow[0] = F_prev;
-    if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
-#pragma unroll 2
-    for (int m = 6; m < WIN; ++m) {
-      const int f = m - 2;
-      const T xcol = li.xa;  // q at window column f-1 of this row
-      c = L.cx[r][f - 3];
-      fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, esx);
-      fo = lo.template step<EDGES>(m, qirow[m], c, ed1, esx);
-      const T fxx = L.xf[r][f - 3] * fx2;
-      // q_j of window column f-1 (interior column f-4); column m-6 of this row is consumed
-      qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
-      fxx_prev = fxx;
-      const T F = (fo + fx2) * L.mx[ro][f - 3];
-      if (outer) {
-        if (FLUXES) qirow[f - 3] = F;  // column f-3 was consumed at step f-3
-        else qirow[f - 4] = xcol * L.dpa[ro][f - 4] + (F_prev - F);  // q dp1/rarea + x divergence
-      }
-      if (efw && i0 + f - 3 == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
-      F_prev = F;
-    }
-  }
-  __syncwarp();
-
-  // ---------------------------- S3: outer y on q_j, update / write -------
-  if (lane >= 3 && lane < 3 + TW) {
-    const int c = lane - 3;  // interior column
-    const T* qjcol = &S.q[0][c];
-    if (EDGES) {
-      auto ex = [qjcol](int m) { return qjcol[m * PQ]; };
-      auto edA = [&L, c, eyA](int m) { return L.edy[0][m - eyA + 2][c + 3]; };
-      auto edB = [&L, c, eyB](int m) { return L.edy[1][m - eyB + 2][c + 3]; };
-      edge_devs<T, HORD>(eyA, ex, edA, ed0);
-      edge_devs<T, HORD>(eyB, ex, edB, ed0 + 8 * 32);
-    }
-    const int ig = i0 + c;
-    const bool valid_c = c < ni;
-    const bool efw = EDGES && a.cube && a.eflux != nullptr && valid_c;
-    T* qo = a.q_out + t * a.sQt + iq * a.sQq + k * a.sQk + pg.at(ig, j0);
-    T* fyo = FLUXES ? a.fy_out + (long long)(k * a.nq + iq) * a.sFlux + pg.at(ig, j0) : nullptr;
-    Line<T, HORD> ln;
-    ln.init();
-#pragma unroll
-    for (int m = 0; m < 5; ++m) ln.template step<EDGES>(m, qjcol[m * PQ], T(0), ed0, esy);
-    T Fprev = (ln.template step<EDGES>(5, qjcol[5 * PQ], L.cy[0][c + 3], ed0, esy) + fyr[0]) * L.my[0][c];
-    if (FLUXES && valid_c) fyo[0] = Fprev;
-    if (efw && j0 == 1) a.eflux[efo + 2 * efe + iq * (long long)n + (ig - 1)] = -Fprev;
-#pragma unroll
-    for (int m = 6; m < WIN; ++m) {
-      const int f = m - 2;
-      const T F = (ln.template step<EDGES>(m, qjcol[m * PQ], L.cy[f - 3][c + 3], ed0, esy) + fyr[f - 3]) *
-                  L.my[f - 3][c];
-      const int ir = f - 4;  // interior row between faces f-1 and f
-      if (FLUXES) {
-        if (valid_c && f - 3 <= nj) fyo[(long long)(f - 3) * pg.pitch] = F;
-      } else if (ir < nj && valid_c) {
-        qo[(long long)ir * pg.pitch] = (S.qi[ir][c] + Fprev - F) * L.ub[ir][c];
-      }
-      if (efw && j0 + f - 3 == a.npy) a.eflux[efo + 3 * efe + iq * (long long)n + (ig - 1)] = F;
-      Fprev = F;
-    }
-  }
-  if (FLUXES) {  // x fluxes staged in qi by S2
-    __syncwarp();
-    T* fxo = a.fx_out + (long long)(k * a.nq + iq) * a.sFlux;
-    for (int e = lane; e < TW * NF; e += 32) {
-      const int ir = e / NF, f = e % NF;
-      if (ir < nj && f <= ni) fxo[pg.at(i0 + f, j0 + ir)] = S.qi[ir][f];
-    }
-  }
-  __syncwarp();
-}
-
-// Interior CTAs (no cube-face edge in their window) and edge CTAs run as two
-// instantiations: the edge code path costs registers the interior one does
-// not need.  Interior CTAs cover the rectangle [bx0, bx0+nbxi) x [by0,
-// by0+nbyi) of CTA tiles; edge CTAs enumerate the ring around it row by row.
-template <typename T, int HORD, bool FLUXES, bool EDGES>
-__global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const BlockMap bm) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES);
-  SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
-  T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
-
-  const int t = blockIdx.z, k = blockIdx.y;
-  int bx, by;
-  {
-    const int e = blockIdx.x;
-    if (!EDGES) {
-      bx = bm.bx0 + e % bm.nbxi;
-      by = bm.by0 + e / bm.nbxi;
-    } else {
-      const int top = bm.by0 * bm.nbx, nside = bm.nbx - bm.nbxi, mid = nside * bm.nbyi;
-      if (e < top) {
-        by = e / bm.nbx;
-        bx = e % bm.nbx;
-      } else if (e < top + mid) {
-        const int r = e - top, sx = r % nside;
-        by = bm.by0 + r / nside;
-        bx = sx < bm.bx0 ? sx : sx + bm.nbxi;
-      } else {
-        const int r = e - top - mid;
-        by = bm.by0 + bm.nbyi + r / bm.nbx;
-        bx = r % bm.nbx;
-      }
-    }
-  }
-  const int i0 = a.is + bx * TW, j0 = a.js + by * TW;
-  const int ni = min(TW, a.ie - i0 + 1), nj = min(TW, a.je - j0 + 1);
-  const PlaneGeom& pg = a.pg;
-  const int n = a.npx - 1;
-
-  // window faces of cube-face edges (x: west/east, y: south/north)
-  const int exA = EDGES ? window_edge_lo(a.is, i0, a.nested) : NO_EDGE;
-  const int exB = EDGES ? window_edge_hi(a.ie, a.npx, i0, a.nested) : NO_EDGE;
-  const int eyA = EDGES ? window_edge_lo(a.js, j0, a.nested) : NO_EDGE;
-  const int eyB = EDGES ? window_edge_hi(a.je, a.npy, j0, a.nested) : NO_EDGE;
-
-  // ---------------------------------------------- per-level staging -------
-  {
-    const long long fo = t * a.sFt + k * a.sFk;
-    const T* cx = a.cx + fo;
-    const T* cy = a.cy + fo;
-    const T* xf = a.xfx + fo;
-    const T* yf = a.yfx + fo;
-    const T* mx = a.mfx + fo;
-    const T* my = a.mfy + fo;
-    const T* area = a.area + t * a.sMt;
-    const T* rarea = a.rarea + t * a.sMt;
-    for (int e = threadIdx.x; e < NF * WIN; e += blockDim.x) {
-      const int f = e / WIN, w = e % WIN;
-      L.cy[f][w] = ld_field(cy, pg, i0 - 3 + w, j0 + f);
-      L.yf[f][w] = ld_field(yf, pg, i0 - 3 + w, j0 + f);
-    }
-    for (int e = threadIdx.x; e < WIN * NF; e += blockDim.x) {
-      const int r = e / NF, f = e % NF;
-      L.cx[r][f] = ld_field(cx, pg, i0 + f, j0 - 3 + r);
-      L.xf[r][f] = ld_field(xf, pg, i0 + f, j0 - 3 + r);
-    }
-    for (int e = threadIdx.x; e < TW * NF; e += blockDim.x) {
-      const int r = e / NF, f = e % NF;
-      L.mx[r][f] = T(0.5) * ld_field(mx, pg, i0 + f, j0 + r);
-      const int ff = e / TW, c = e % TW;
-      L.my[ff][c] = T(0.5) * ld_field(my, pg, i0 + c, j0 + ff);
-    }
-    for (int e = threadIdx.x; e < WIN * WIN; e += blockDim.x) {
-      const int r = e / WIN, w = e % WIN;
-      L.area[r][w] = ld_field(area, pg, i0 - 3 + w, j0 - 3 + r);
-    }
-    for (int e = threadIdx.x; e < WIN * TW; e += blockDim.x) {
-      const int r = e / TW, c = e % TW;
-      const int i = i0 + c, j = j0 - 3 + r;
-      L.rrx[r][c] = T(1) / (a.ra_x ? ld_field(a.ra_x, pg, i, j)
-                                   : ld_field(area, pg, i, j) + ld_field(xf, pg, i, j) - ld_field(xf, pg, i + 1, j));
-      const int r2 = e / WIN, w = e % WIN;
-      const int i2 = i0 - 3 + w, j2 = j0 + r2;
-      L.rry[r2][w] = T(1) / (a.ra_y ? ld_field(a.ra_y, pg, i2, j2)
-                                    : ld_field(area, pg, i2, j2) + ld_field(yf, pg, i2, j2) - ld_field(yf, pg, i2, j2 + 1));
-    }
-    const T* dp1 = a.dp1 ? a.dp1 + fo : nullptr;
-    T* dp2o = a.dp2 ? a.dp2 + fo : nullptr;
-    for (int e = threadIdx.x; dp1 != nullptr && e < TW * TW; e += blockDim.x) {
-      const int r = e / TW, c = e % TW;
-      const int i = i0 + c, j = j0 + r;
-      const T ra = ld_field(rarea, pg, i, j);
-      const T d1 = ld_field(dp1, pg, i, j);
-      const T d2 = d1 + (ld_field(mx, pg, i, j) - ld_field(mx, pg, i + 1, j) + ld_field(my, pg, i, j) -
-                         ld_field(my, pg, i, j + 1)) * ra;
-      L.dpa[r][c] = d1 / ra;
-      L.ub[r][c] = ra / d2;
-      if (r < nj && c < ni && dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
-    }
-    if (EDGES) {  // metrics of the one-sided edge values: dxa across x edges, dya across y edges
-      const T* dxa = a.dxa + t * a.sMt;
-      const T* dya = a.dya + t * a.sMt;
-      for (int e = threadIdx.x; e < 2 * 4 * WIN; e += blockDim.x) {
-        const int side = e / (4 * WIN), m = (e / WIN) % 4, w = e % WIN;
-        const int ex = side ? exB : exA, ey = side ? eyB : eyA;
-        L.edx[side][m][w] = ex == NO_EDGE ? T(1) : ld_field(dxa, pg, i0 - 3 + ex - 2 + m, j0 - 3 + w);
-        L.edy[side][m][w] = ey == NO_EDGE ? T(1) : ld_field(dya, pg, i0 - 3 + w, j0 - 3 + ey - 2 + m);
-      }
-    }
-  }
-  __syncthreads();
-
-  const bool corner_block = !a.nested && a.corners != 0 &&
-                            ((i0 - 3 < 1) || (i0 + 28 > a.npx - 1)) && ((j0 - 3 < 1) || (j0 + 28 > a.npy - 1));
-  // edge-flux index (((t*4 + e)*npz + k)*nq + iq)*n + s = efo + e*efe + iq*n + s
-  const long long efe = (long long)a.npz * a.nq * n;
-  const long long efo = (((long long)t * 4) * a.npz + k) * a.nq * n;
-
-  for (int iq = warp; iq < a.nq; iq += W)
-    advance_tracer<T, HORD, FLUXES, EDGES>(a, L, S, t, k, eds, iq, i0, j0, ni, nj, lane, exA, exB, eyA, eyB,
-                                           corner_block, efo, efe);
-}
 
 // ------------------------------------------------ tile-edge reconciliation ---
 // Every shared tile-edge face carries one flux: the one computed by the tile
@@ -763,69 +211,18 @@ BlockMap block_map(int is, int ie, int js, int je, int npx, int npy, int nested)
   return m;
 }
 
-template <typename T, int HORD, bool FLUXES>
-static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
-  const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
-  const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
-  const int nt = a.cube ? 6 : 1;
-  if (nint > 0) {
-    dim3 grid(nint, a.npz, nt);
-    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false), s>>>(a, bm);
-    FV3G_CUDA(cudaGetLastError());
-  }
-  if (nring > 0) {
-    dim3 grid(nring, a.npz, nt);
-    k_substep<T, HORD, FLUXES, true><<<grid, 32 * warps, substep_smem_bytes<T>(warps, true), s>>>(a, bm);
-    FV3G_CUDA(cudaGetLastError());
-  }
-  return 0;
-}
-
-// Largest warps per CTA whose shared memory fits in 227 KB (at most 10).
-template <typename T>
-static int max_warps() {
-  int w = 10;
-  while (w > 1 && substep_smem_bytes<T>(w, true) > 227 * 1024) --w;
-  return w;
-}
-
-template <typename T, int HORD, bool FLUXES, bool EDGES>
-static cudaError_t set_smem_attr() {
-  const int mx = (int)substep_smem_bytes<T>(max_warps<T>(), EDGES);
-  return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-}
-
-template <typename T, int HORD>
-static void set_attrs_tl(cudaError_t& err) {
-  cudaError_t es[] = {set_smem_attr<T, HORD, true, false>(), set_smem_attr<T, HORD, true, true>()};
-  for (cudaError_t e : es)
-    if (e != cudaSuccess && err == cudaSuccess) err = e;
-}
-
-template <typename T, int HORD>
-static void set_attrs(cudaError_t& err) {
-  cudaError_t es[] = {set_smem_attr<T, HORD, false, false>(), set_smem_attr<T, HORD, false, true>(),
-                      set_smem_attr<T, HORD, true, false>(), set_smem_attr<T, HORD, true, true>()};
-  for (cudaError_t e : es)
-    if (e != cudaSuccess && err == cudaSuccess) err = e;
-}
-
 // Raise the dynamic shared-memory limit of every advection kernel once per
 // process (before any stream capture).
 int prepare_kernels() {
   static std::once_flag once;
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
-    set_attrs<float, 5>(err);
-    set_attrs<float, 8>(err);
-    set_attrs<double, 5>(err);
-    set_attrs<double, 8>(err);
-    set_attrs_tl<Dual<double>, 5>(err);
-    set_attrs_tl<Dual<double>, 8>(err);
+    prepare_substep_hord<1>(err);
+    prepare_substep_hord<5>(err);
+    prepare_substep_hord<8>(err);
   });
-  return err == cudaSuccess ? 0 : cuda_error(err, "cudaFuncSetAttribute(k_substep)");
+  return err == cudaSuccess ? 0 : cuda_error(err, "cudaFuncSetAttribute(advection kernels)");
 }
-
 
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s) {
@@ -833,12 +230,13 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
     int prc = prepare_kernels();
     if (prc) return prc;
   }
-  const int mw = max_warps<T>();
-  if (warps < 1 || warps > mw)
-    return set_error(FV3G_E_ARG, "this precision supports 1..%d advection warps per CTA (got %d)", mw, warps);
-  if (hord == 8) return flux_mode ? launch_one<T, 8, true>(a, warps, s) : launch_one<T, 8, false>(a, warps, s);
-  if (hord == 5) return flux_mode ? launch_one<T, 5, true>(a, warps, s) : launch_one<T, 5, false>(a, warps, s);
-  return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
+  if (hord == 1 && !(a.lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", a.lim_fac);
+  switch (hord) {
+    case 8: return launch_substep_hord<T, 8>(a, flux_mode, warps, s);
+    case 5: return launch_substep_hord<T, 5>(a, flux_mode, warps, s);
+    case 1: return launch_substep_hord<T, 1>(a, flux_mode, warps, s);
+    default: return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", hord);
+  }
 }
 
 template <typename T>
@@ -858,9 +256,13 @@ int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s) 
     int prc = prepare_kernels();
     if (prc) return prc;
   }
-  if (hord == 8) return launch_one<Dual<double>, 8, true>(a, 1, s);
-  if (hord == 5) return launch_one<Dual<double>, 5, true>(a, 1, s);
-  return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
+  if (hord == 1 && !(a.lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", a.lim_fac);
+  switch (hord) {
+    case 8: return launch_substep_tl_hord<8>(a, s);
+    case 5: return launch_substep_tl_hord<5>(a, s);
+    case 1: return launch_substep_tl_hord<1>(a, s);
+    default: return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", hord);
+  }
 }
 
 // Halo ring (the NG-deep strips and the corner blocks) of every plane copied

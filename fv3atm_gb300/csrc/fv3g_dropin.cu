@@ -22,29 +22,57 @@ using namespace fv3g;
 
 #include "fv3g_hostio.cuh"
 
+namespace {
+
+int check_scheme(int hord, double lim_fac) {
+  if (hord != 1 && hord != 5 && hord != 8)
+    return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", hord);
+  if (hord == 1 && !(lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", lim_fac);
+  return 0;
+}
+
+int check_damping(const fv3g_grid* grid, int nord, bool need_rarea) {
+  if (nord < 0 || nord > 2)
+    return set_error(FV3G_E_UNSUPPORTED, "tracer damping supports nord 0..2 with a 3-cell halo (got %d)", nord);
+  if (!grid->del6_u || !grid->del6_v) return set_error(FV3G_E_ARG, "tracer damping needs grid del6_u and del6_v");
+  if (!(grid->da_min > 0.0)) return set_error(FV3G_E_ARG, "tracer damping needs grid da_min > 0");
+  if (need_rarea && !grid->rarea) return set_error(FV3G_E_ARG, "tracer damping needs grid rarea");
+  return 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord, double* fx, double* fy,
                   const double* xfx, const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd,
                   const double* ra_x, const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
-                  int nord, double damp_c) {
-  (void)damp_c;
+                  const double* mass, int nord, double damp_c) {
   CHECK(check_bounds(bd, npx, npy));
   if (!q || !crx || !cry || !fx || !fy || !xfx || !yfx || !grid || !ra_x || !ra_y)
     return set_error(FV3G_E_ARG, "null array argument");
   if (!grid->dxa || !grid->dya || !grid->area) return set_error(FV3G_E_ARG, "grid needs dxa, dya, area");
-  if (hord != 5 && hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
-  if (nord != 0) return set_error(FV3G_E_UNSUPPORTED, "tracer diffusion (nord=%d) is not implemented", nord);
-  if (lim_fac != 1.0) return set_error(FV3G_E_UNSUPPORTED, "lim_fac must be 1 (got %g)", lim_fac);
+  CHECK(check_scheme(hord, lim_fac));
+  // upstream damps when damp_c > 1e-4: mass-weighted with mass fluxes (and only
+  // if mass is present), unweighted without them
+  const bool damping = damp_c > 1e-4 && (mfx == nullptr || mass != nullptr);
+  if (damping) CHECK(check_damping(grid, nord, true));
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
-  CHECK(g_ctx.begin(14 * padded(P, 8)));
+  CHECK(g_ctx.begin((14 + (damping ? 4 : 0)) * padded(P, 8)));
   cudaStream_t s = g_ctx.stream;
   double *dq = g_ctx.take<double>(P), *dcx = g_ctx.take<double>(P), *dcy = g_ctx.take<double>(P);
   double *dxf = g_ctx.take<double>(P), *dyf = g_ctx.take<double>(P), *drx = g_ctx.take<double>(P);
   double *dry = g_ctx.take<double>(P), *dmx = g_ctx.take<double>(P), *dmy = g_ctx.take<double>(P);
   double *ddxa = g_ctx.take<double>(P), *ddya = g_ctx.take<double>(P), *dar = g_ctx.take<double>(P);
   double *dfx = g_ctx.take<double>(P), *dfy = g_ctx.take<double>(P);
+  double *d6u = nullptr, *d6v = nullptr, *dms = nullptr, *drar = nullptr;
+  if (damping) {
+    d6u = g_ctx.take<double>(P);
+    d6v = g_ctx.take<double>(P);
+    dms = g_ctx.take<double>(P);
+    drar = g_ctx.take<double>(P);
+  }
   FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
             jed = bd->jed;
@@ -60,6 +88,12 @@ int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int 
   CHECK(h2d_planes(ddxa, pg, grid->dxa, isd, ied, jsd, jed, 1, s));
   CHECK(h2d_planes(ddya, pg, grid->dya, isd, ied, jsd, jed, 1, s));
   CHECK(h2d_planes(dar, pg, grid->area, isd, ied, jsd, jed, 1, s));
+  if (damping) {
+    CHECK(h2d_planes(d6u, pg, grid->del6_u, isd, ied, jsd, jed + 1, 1, s));
+    CHECK(h2d_planes(d6v, pg, grid->del6_v, isd, ied + 1, jsd, jed, 1, s));
+    CHECK(h2d_planes(drar, pg, grid->rarea, isd, ied, jsd, jed, 1, s));
+    if (mfx) CHECK(h2d_planes(dms, pg, mass, isd, ied, jsd, jed, 1, s));
+  }
   AdvArgs<double> a{};
   a.q_in = dq;
   a.q_out = nullptr;
@@ -78,7 +112,19 @@ int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int 
   a.nested = grid->nested;
   a.cube = 0;
   a.fx_out = dfx; a.fy_out = dfy; a.sFlux = (long long)P;
+  a.lim_fac = lim_fac;
   CHECK(launch_substep<double>(a, hord, true, 1, s));
+  if (damping) {  // deln_flux on the same q, added to the fluxes
+    AdvArgs<double> ad = a;
+    ad.del6_u = d6u;
+    ad.del6_v = d6v;
+    ad.rarea = drar;
+    ad.damp = damp_coefficient(damp_c, grid->da_min, nord);
+    ad.nord = nord;
+    ad.damp_mass = mfx != nullptr;
+    ad.dp1 = mfx ? dms : nullptr;
+    CHECK(launch_damp<double>(ad, true, s));
+  }
   if (!grid->nested && a.corners) {
     k_corners<<<1, 64, 0, s>>>(dq, pg, npx, npy, a.corners, 1, 1);
     FV3G_CUDA(cudaGetLastError());
@@ -94,19 +140,19 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
                    const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
                    int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out) {
   (void)dt;
-  (void)trdm;
   CHECK(check_bounds(bd, npx, npy));
   if (!q || !dp1 || !mfx || !mfy || !cx || !cy || !grid) return set_error(FV3G_E_ARG, "null array argument");
   if (!grid->dx || !grid->dy || !grid->dxa || !grid->dya || !grid->area || !grid->rarea || !grid->sin_sg)
     return set_error(FV3G_E_ARG, "incomplete grid");
   if (npz < 1 || nq < 1) return set_error(FV3G_E_ARG, "npz and nq must be positive");
-  if (hord != 5 && hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
-  if (nord_tr != 0) return set_error(FV3G_E_UNSUPPORTED, "tracer diffusion (nord_tr=%d) is not implemented", nord_tr);
-  if (lim_fac != 1.0) return set_error(FV3G_E_UNSUPPORTED, "lim_fac must be 1 (got %g)", lim_fac);
+  CHECK(check_scheme(hord, lim_fac));
+  // damping of the first substep, weighted by its starting thickness
+  const bool damping = trdm > 1e-4;
+  if (damping) CHECK(check_damping(grid, nord_tr, false));
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
   const size_t nqp = (size_t)nq * npz;
-  CHECK(g_ctx.begin(padded(P * nqp, 8) * 2 + padded(P * npz, 8) * 9 + padded(P, 8) * 12 + 256));
+  CHECK(g_ctx.begin(padded(P * nqp, 8) * 2 + padded(P * npz, 8) * 9 + padded(P, 8) * 14 + 256));
   cudaStream_t s = g_ctx.stream;
   double* qa = g_ctx.take<double>(P * nqp);
   double* qb = g_ctx.take<double>(P * nqp);
@@ -117,6 +163,7 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   double *ddx = g_ctx.take<double>(P), *ddy = g_ctx.take<double>(P), *ddxa = g_ctx.take<double>(P);
   double *ddya = g_ctx.take<double>(P), *dar = g_ctx.take<double>(P), *drar = g_ctx.take<double>(P);
   double* dsin = g_ctx.take<double>(4 * P);
+  double *d6u = g_ctx.take<double>(P), *d6v = g_ctx.take<double>(P);
   unsigned long long* dmax = g_ctx.take<unsigned long long>(1);
   FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
@@ -134,6 +181,10 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   CHECK(h2d_planes(dar, pg, grid->area, isd, ied, jsd, jed, 1, s));
   CHECK(h2d_planes(drar, pg, grid->rarea, isd, ied, jsd, jed, 1, s));
   CHECK(h2d_planes(dsin, pg, grid->sin_sg, isd, ied, jsd, jed, 4, s));  // slots 1..4 of sin_sg(:,:,9)
+  if (damping) {
+    CHECK(h2d_planes(d6u, pg, grid->del6_u, isd, ied, jsd, jed + 1, 1, s));
+    CHECK(h2d_planes(d6v, pg, grid->del6_v, isd, ied + 1, jsd, jed, 1, s));
+  }
 
   int nsplt = q_split;
   if (q_split <= 0) {
@@ -177,7 +228,16 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
     a.corners = corner_mask(grid);
     a.nested = grid->nested;
     a.cube = 0;
+    a.lim_fac = lim_fac;
     CHECK(launch_substep<double>(a, hord, false, std::min(nq, 4), s));
+    if (damping && it == 0) {
+      a.del6_u = d6u;
+      a.del6_v = d6v;
+      a.damp = damp_coefficient(trdm, grid->da_min, nord_tr);
+      a.nord = nord_tr;
+      a.damp_mass = 1;
+      CHECK(launch_damp<double>(a, false, s));
+    }
     // the updated compute domain goes back into the halo-carrying buffer
     CHECK(d2d_planes(qa, qb, pg, is, ie, js, je, (long long)nqp, s));
     dp_start = dpi;

@@ -84,6 +84,13 @@ struct AdvArgs {
   T* fx_out;    // flux mode: planes [level*nq + tracer] of the tile
   T* fy_out;
   long long sFlux;
+  double lim_fac;  // hord 1: 2-dx filter factor (upstream default 1)
+  // del-2(nord+1) tracer damping (deln_flux), run after the substep kernel
+  const T* del6_u;  // [tile] planes: y-face metric (isd:ied, jsd:jed+1)
+  const T* del6_v;  // x-face metric (isd:ied+1, jsd:jed)
+  T damp;           // (damp_c da_min)^(nord+1)
+  int nord;
+  int damp_mass;    // 1: field q, flux weighted by damp times the face mean of dp1; 0: field damp q
 };
 
 // CTA tiles of a substep launch: the interior rectangle [bx0, bx0+nbxi) x
@@ -174,6 +181,22 @@ int cuda_error(cudaError_t e, const char* what);
 template <typename T>
 int launch_fillz_planes(T* q, const T* dp, int n, int ntiles, int km, int nq, long long sQt, long long sQq,
                         long long sQk, long long sFt, long long sFk, PlaneGeom pg, cudaStream_t s);
+
+// Advection substep kernels, one translation unit per hord (fv3g_substep_h*.cu)
+template <typename T, int HORD>
+int launch_substep_hord(const AdvArgs<T>& a, bool flux_mode, int warps, cudaStream_t s);
+template <int HORD>
+int launch_substep_tl_hord(const AdvArgs<Dual<double>>& a, cudaStream_t s);
+template <int HORD>
+void prepare_substep_hord(cudaError_t& err);
+
+// Tracer damping (fv3g_damp.cu): adds the deln_flux fluxes of a substep's
+// input q_in (a.damp, a.nord) to the fluxes (flux mode) or to q_out and the
+// tile-edge fluxes; runs after the substep kernel on the same stream.
+template <typename T>
+int launch_damp(const AdvArgs<T>& a, bool flux_mode, cudaStream_t s);
+// damp = (damp_c da_min)^(nord+1), as the product upstream's integer power is
+double damp_coefficient(double damp_c, double da_min, int nord);
 
 // Host launchers (fv3g_advect.cu)
 template <typename T>

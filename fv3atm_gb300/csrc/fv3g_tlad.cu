@@ -117,12 +117,15 @@ __global__ void k_corners_adjoint(double* g, PlaneGeom pg, int npx, int npy, int
 unsigned grid_1d(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 4096); }
 
 int check_tp_args(const fv3g_bounds* bd, int npx, int npy, int hord, const fv3g_grid* grid, double lim_fac,
-                  int nord) {
+                  const double* mfx, const double* mass, double damp_c) {
   CHECK(check_bounds(bd, npx, npy));
   if (!grid || !grid->dxa || !grid->dya || !grid->area) return set_error(FV3G_E_ARG, "grid needs dxa, dya, area");
-  if (hord != 5 && hord != 8) return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (5 and 8 are)", hord);
-  if (nord != 0) return set_error(FV3G_E_UNSUPPORTED, "tracer diffusion (nord=%d) is not implemented", nord);
-  if (lim_fac != 1.0) return set_error(FV3G_E_UNSUPPORTED, "lim_fac must be 1 (got %g)", lim_fac);
+  if (hord != 1 && hord != 5 && hord != 8)
+    return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", hord);
+  if (hord == 1 && !(lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", lim_fac);
+  if (damp_c > 1e-4 && (mfx == nullptr || mass != nullptr))
+    return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint fv_tp_2d has no tracer damping (damp_c=%g)",
+                     damp_c);
   return 0;
 }
 
@@ -304,10 +307,10 @@ int fv3g_map1_ppm_ad(int km, const double* pe1, const double* q1, double* q1_ad,
 int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, const double* cry, int npx, int npy,
                      int hord, double* fx, double* fx_tl, double* fy, double* fy_tl, const double* xfx,
                      const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x,
-                     const double* ra_y, double lim_fac, const double* mfx, const double* mfy, int nord,
-                     double damp_c) {
-  (void)damp_c;
-  CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, nord));
+                     const double* ra_y, double lim_fac, const double* mfx, const double* mfy, const double* mass,
+                     int nord, double damp_c) {
+  (void)nord;
+  CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, mfx, mass, damp_c));
   if (!q || !q_tl || !crx || !cry || !xfx || !yfx || !ra_x || !ra_y || !fx_tl || !fy_tl)
     return set_error(FV3G_E_ARG, "null array argument");
   const PlaneGeom pg = plane_for(bd);
@@ -329,6 +332,7 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
   a.q_in = dq;
   a.corners = corner_mask(grid);
   a.nested = grid->nested;
+  a.lim_fac = lim_fac;
   a.fx_out = dfx;
   a.fy_out = dfy;
   CHECK(launch_substep_tl(a, hord, s));
@@ -351,9 +355,9 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
 int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const double* cry, int npx, int npy, int hord,
                      double* fx_ad, double* fy_ad, const double* xfx, const double* yfx, const fv3g_grid* grid,
                      const fv3g_bounds* bd, const double* ra_x, const double* ra_y, double lim_fac,
-                     const double* mfx, const double* mfy, int nord, double damp_c) {
-  (void)damp_c;
-  CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, nord));
+                     const double* mfx, const double* mfy, const double* mass, int nord, double damp_c) {
+  (void)nord;
+  CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, mfx, mass, damp_c));
   if (!q || !q_ad || !crx || !cry || !xfx || !yfx || !ra_x || !ra_y || !fx_ad || !fy_ad)
     return set_error(FV3G_E_ARG, "null array argument");
   constexpr int NC = 42;  // colours per input: 7 x 6
@@ -388,6 +392,7 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
   a.q_in_x = in_x;
   a.corners = 0;  // fills are in the trajectories; their transposes follow
   a.nested = grid->nested;
+  a.lim_fac = lim_fac;
   a.fx_out = fl;
   a.fy_out = fl + P * NC;
   for (int pass = 0; pass < 2; ++pass) {  // 0: x-sweep input, 1: y-sweep input

@@ -64,6 +64,10 @@ typedef struct {
   const double* sin_sg; /* (isd:ied,   jsd:jed, 9) */
   int sw_corner, se_corner, nw_corner, ne_corner; /* tile corner is a cube corner */
   int nested;           /* 1: no cube-edge treatment and no corner fill */
+  const double* del6_u; /* (isd:ied,   jsd:jed+1) tracer-damping metric of y faces (sina_v dx / dyc);
+                           may be NULL when no damping is asked for */
+  const double* del6_v; /* (isd:ied+1, jsd:jed)   of x faces (sina_u dy / dxc) */
+  double da_min;        /* smallest cell area of the cube (gridstruct%da_min) */
 } fv3g_grid;
 
 /* Halo refresh called by fv3g_tracer_2d before every substep with the HOST
@@ -87,22 +91,28 @@ int fv3g_device_info(char* buf, int len);    /* GPU name and SM count */
  *   xfx (is:ie+1, jsd:jed)   yfx (isd:ied, js:je+1)
  *   ra_x (is:ie, jsd:jed)    ra_y (isd:ied, js:je)
  *   mfx (is:ie+1, js:je)     mfy (is:ie, js:je+1)   may be NULL (then xfx/yfx weight the fluxes)
- *   hord: 5 (unlimited PPM) or 8 (Lin 2004 monotone).  lim_fac must be 1.
- *   nord must be 0 (tracer diffusion is not implemented); damp_c ignored.
+ *   mass (isd:ied, jsd:jed)  may be NULL
+ *   hord: 8 (PPM, Lin 2004 monotone constraint), 5 (fourth-order PPM with the
+ *   2-dx filter) or 1 (as 5 with the filter test |lim_fac b0| < |bl - br|);
+ *   lim_fac is read by hord 1 only, as upstream.
+ *   damp_c > 1e-4 adds del-2(nord+1) damping fluxes (deln_flux; nord 0..2,
+ *   damp = (damp_c da_min)^(nord+1)): with mfx given only when mass is given,
+ *   mass-weighted; without mfx, unweighted.  Damping needs grid->del6_u/v.
  * Replaces: fv_tp_2d(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, gridstruct,
  *           bd, ra_x, ra_y, lim_fac, mfx, mfy, mass, nord, damp_c). */
 int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int npy, int hord,
                   double* fx, double* fy, const double* xfx, const double* yfx,
                   const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x,
                   const double* ra_y, double lim_fac, const double* mfx, const double* mfy,
-                  int nord, double damp_c);
+                  const double* mass, int nord, double damp_c);
 
 /* tracer_2d (fv_tracer2d.F90) on one domain, FP64.
  *   q   (isd:ied, jsd:jed, npz, nq) inout     dp1 (isd:ied, jsd:jed, npz) inout
  *   mfx (is:ie+1, js:je, npz)  mfy (is:ie, js:je+1, npz)                 inout (scaled by 1/nsplt)
  *   cx  (is:ie+1, jsd:jed, npz) cy (isd:ied, js:je+1, npz)               inout (scaled by 1/nsplt)
  *   q_split > 0 fixes the substep count, 0 derives it from the max Courant
- *   number.  nord_tr must be 0; lim_fac must be 1.
+ *   number.  hord and lim_fac as fv3g_fv_tp_2d.  trdm > 1e-4 damps the first
+ *   substep with del-2(nord_tr+1) fluxes weighted by dp1 (nord_tr 0..2).
  * On return dp1 holds the layer thickness at the start of the last substep,
  * as upstream.  nsplt_out (may be NULL) receives the substep count.
  * Replaces: tracer_2d(q, dp1, mfx, mfy, cx, cy, gridstruct, bd, domain, npx,
@@ -157,14 +167,17 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
                      int npy, int hord, double* fx, double* fx_tl, double* fy, double* fy_tl,
                      const double* xfx, const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd,
                      const double* ra_x, const double* ra_y, double lim_fac, const double* mfx,
-                     const double* mfy, int nord, double damp_c);
+                     const double* mfy, const double* mass, int nord, double damp_c);
 
 /* fv_tp_2d adjoint at trajectory q: q_ad (isd:ied, jsd:jed) += J^T (fx_ad, fy_ad);
- * fx_ad (is:ie+1, js:je) and fy_ad (is:ie, js:je+1) are set to zero. */
+ * fx_ad (is:ie+1, js:je) and fy_ad (is:ie, js:je+1) are set to zero.
+ * Damping (damp_c > 1e-4 where it applies) is not differentiated here:
+ * both entries return FV3G_E_UNSUPPORTED for it. */
 int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const double* cry, int npx, int npy,
                      int hord, double* fx_ad, double* fy_ad, const double* xfx, const double* yfx,
                      const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x, const double* ra_y,
-                     double lim_fac, const double* mfx, const double* mfy, int nord, double damp_c);
+                     double lim_fac, const double* mfx, const double* mfy, const double* mass, int nord,
+                     double damp_c);
 
 /* map1_ppm tangent-linear on row j: (q1, q1_tl) -> (q2, q2_tl); q2 may be NULL. */
 int fv3g_map1_ppm_tl(int km, const double* pe1, const double* q1, const double* q1_tl, const double* qs,
@@ -220,11 +233,14 @@ typedef struct {
   int npz;        /* Lagrangian levels */
   int nq;         /* tracers */
   int precision;  /* FV3G_FP64 or FV3G_MIXED */
-  int hord;       /* 5 or 8 */
+  int hord;       /* 1, 5 or 8 (see fv3g_fv_tp_2d) */
   int kord;       /* 4 or 9 */
   int iv;         /* remap iv (see fv3g_map_scalar) */
   double q_min;   /* remap floor for iv == 1 */
   int warps_per_cta; /* advection CTA width in warps (0 = default) */
+  int nord_tr;    /* tracer damping order 0..2 (del-2(nord_tr+1)) */
+  double trdm;    /* damping coefficient; > 1e-4 damps the first substep (needs the grid's del6_u/v) */
+  double lim_fac; /* hord 1 filter factor; 0 means 1 */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */

@@ -93,13 +93,13 @@ def _opt(a):
 
 
 def fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3, lim_fac=1.0,
-             mass=None, nord=0, damp_c=0.0, nested=0, da_min=None):
+             mass=None, nord=0, damp_c=0.0, nested=0, da_min=None, corners=(1, 1, 1, 1)):
     """Returns (fx, fy, q_with_corners)."""
     q = _f64(q).copy()
     n = q.shape[-1] - 2 * ng
     fx = np.zeros((n, n + 1))
     fy = np.zeros((n + 1, n))
-    g = GridRef(geom, nested=nested, da_min=da_min)
+    g = GridRef(geom, corners=corners, nested=nested, da_min=da_min)
     arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y)]
     mx = _f64(mfx) if mfx is not None else None
     my = _f64(mfy) if mfy is not None else None
@@ -111,13 +111,13 @@ def fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, 
 
 
 def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy=None, ng: int = 3, lim_fac=1.0,
-                mass=None, nord=0, damp_c=0.0):
+                mass=None, nord=0, damp_c=0.0, corners=(1, 1, 1, 1)):
     q = _f64(q)
     dq = _f64(dq)
     n = q.shape[-1] - 2 * ng
     dfx = np.zeros((n, n + 1))
     dfy = np.zeros((n + 1, n))
-    g = GridRef(geom)
+    g = GridRef(geom, corners=corners)
     arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y)]
     mx = _f64(mfx) if mfx is not None else None
     my = _f64(mfy) if mfy is not None else None

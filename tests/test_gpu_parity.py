@@ -74,6 +74,40 @@ def test_cube_hord5_matches_oracle(cuda, cube_prob):
     assert rel_l2(interior(q, P.n), interior(q_ref, P.n)) <= FP64_TOL
 
 
+# (hord, nord_tr, trdm, lim_fac): the hord-1 / hord-5 filters, and del-2 / del-4 / del-6 damping of
+# the first substep
+SCHEMES = [(1, 0, 0.0, 3.0), (5, 0, 0.0, 1.0), (8, 0, 0.12, 1.0), (8, 1, 0.1, 1.0), (8, 2, 0.1, 1.0),
+           (5, 2, 0.1, 1.0)]
+# The 2-dx filter of hord 1 / 5 is a switch: where bl br (or |lim_fac b0| - |bl - br|) is within FP32
+# rounding of zero the mixed path can take the other branch than the FP64 oracle, and each such face
+# moves by the parabola's correction, O(the local variation of q).  On these noisy tracers that leaves
+# the mixed path within 2e-4 of the oracle; hord 8's limiter is continuous and keeps 1e-5.
+FILTER_MIXED_TOL = 2e-4
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+@pytest.mark.parametrize("hord,nord,trdm,lim_fac", SCHEMES)
+def test_cube_schemes_and_damping_match_oracle(cuda, cube_prob, precision, tol, hord, nord, trdm, lim_fac):
+    P = cube_prob
+    if precision == "mixed" and hord != 8:
+        tol = FILTER_MIXED_TOL
+    q_ref, dp_last, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=hord,
+                                          q_split=3, nord_tr=nord, trdm=trdm, lim_fac=lim_fac)
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision, hord=hord, nord_tr=nord, trdm=trdm, lim_fac=lim_fac)
+    st.load_problem(P)
+    st.tracer_2d(3)
+    q = st.download("Q")
+    for iq in range(P.nq):
+        e = rel_l2(interior(q[:, iq], P.n), interior(q_ref[:, iq], P.n))
+        assert e <= tol, (iq, e)
+    if precision == "fp64":  # damping moves tracer mass between cells only
+        dpf = final_dp(dp_last, P.mfx.numpy(), P.mfy.numpy(), P.geoms, ns, P.n)
+        m0 = cube_mass(P.q.numpy(), P.dp.numpy(), P.geoms, P.n)
+        m1 = cube_mass(q, dpf, P.geoms, P.n)
+        assert np.all(np.abs(m1 - m0) <= 1e-13 * np.abs(m0)), (m1 - m0) / m0
+    st.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
 def test_cube_remap_matches_oracle(cuda, cube_prob, cube_oracle, precision, tol):
     P = cube_prob
@@ -132,25 +166,47 @@ def _tile_inputs(P, t=0, k=2, iq=1):
     return g, q, cx, cy, xfx, yfx, rax, ray, P.mfx[t, k].numpy(), P.mfy[t, k].numpy()
 
 
-@pytest.mark.parametrize("hord", [5, 8])
+@pytest.mark.parametrize("hord,lim_fac", [(1, 2.5), (5, 1.0), (8, 1.0)])
 @pytest.mark.parametrize("with_mass", [True, False])
-def test_fv_tp_2d_dropin_matches_oracle(cuda, cube_prob, hord, with_mass):
+def test_fv_tp_2d_dropin_matches_oracle(cuda, cube_prob, hord, lim_fac, with_mass):
     P = cube_prob
     g, q, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_inputs(P)
     mx, my = (mfx, mfy) if with_mass else (None, None)
-    fx_r, fy_r, q_r = O.fv_tp_2d(q, cx, cy, hord, xfx, yfx, g, rax, ray, mx, my)
+    fx_r, fy_r, q_r = O.fv_tp_2d(q, cx, cy, hord, xfx, yfx, g, rax, ray, mx, my, lim_fac=lim_fac)
     n = P.n
     fx = np.zeros((n, n + 1))
     fy = np.zeros((n + 1, n))
     qg = q.copy()
     api.fv_tp_2d(qg, cx, cy, n + 1, n + 1, hord, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray,
-                 1.0, mx, my)
+                 lim_fac, mx, my)
     assert rel_l2(fx, fx_r) <= FP64_TOL
     assert rel_l2(fy, fy_r) <= FP64_TOL
     assert np.array_equal(qg, q_r)  # corner blocks rewritten exactly as copy_corners does
 
 
-def test_tracer_2d_dropin_matches_oracle_with_halo_callback(cuda, cube_prob):
+@pytest.mark.parametrize("nord,damp_c", [(0, 0.12), (1, 0.1), (2, 0.1)])
+@pytest.mark.parametrize("with_mass", [True, False])
+def test_fv_tp_2d_dropin_damping_matches_oracle(cuda, cube_prob, nord, damp_c, with_mass):
+    """deln_flux added to the fluxes: mass-weighted with mass fluxes, unweighted without them."""
+    P = cube_prob
+    t, k = 4, 2
+    g, q, cx, cy, xfx, yfx, rax, ray, mfx, mfy = _tile_inputs(P, t=t, k=k)
+    mass = np.ascontiguousarray(P.dp[t, k].numpy())
+    mx, my = (mfx, mfy) if with_mass else (None, None)
+    fx_r, fy_r, _ = O.fv_tp_2d(q, cx, cy, 8, xfx, yfx, g, rax, ray, mx, my, mass=mass, nord=nord, damp_c=damp_c)
+    fx0, fy0, _ = O.fv_tp_2d(q, cx, cy, 8, xfx, yfx, g, rax, ray, mx, my)
+    assert rel_l2(fx_r, fx0) > 1e-6  # the damping is visible at this tolerance
+    n = P.n
+    fx = np.zeros((n, n + 1))
+    fy = np.zeros((n + 1, n))
+    api.fv_tp_2d(q.copy(), cx, cy, n + 1, n + 1, 8, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax,
+                 ray, 1.0, mx, my, mass, nord, damp_c)
+    assert rel_l2(fx, fx_r) <= FP64_TOL
+    assert rel_l2(fy, fy_r) <= FP64_TOL
+
+
+@pytest.mark.parametrize("nord_tr,trdm", [(0, 0.0), (1, 0.1)])
+def test_tracer_2d_dropin_matches_oracle_with_halo_callback(cuda, cube_prob, nord_tr, trdm):
     P = cube_prob
     t = 2
     g = P.geoms[t]
@@ -165,11 +221,11 @@ def test_tracer_2d_dropin_matches_oracle_with_halo_callback(cuda, cube_prob):
 
     args = [np.ascontiguousarray(a[t].numpy()) for a in (P.dp, P.mfx, P.mfy, P.cx, P.cy)]
     ref = O.tracer_2d(q0, *args, g, hord=8, q_split=3, halo_fn=lambda p, nq, npz, ctx: refresh(
-        np.ctypeslib.as_array(p, shape=q0.shape)))
+        np.ctypeslib.as_array(p, shape=q0.shape)), nord_tr=nord_tr, trdm=trdm)
     qg = q0.copy()
     dp, mfx, mfy, cx, cy = (a.copy() for a in args)
     ns = api.tracer_2d(qg, dp, mfx, mfy, cx, cy, api.GridStruct(g), api.bounds_for(P.n), P.n + 1, P.n + 1, P.npz,
-                       P.nq, 8, 3, P.dt, halo_update=refresh)
+                       P.nq, 8, 3, P.dt, nord_tr=nord_tr, trdm=trdm, halo_update=refresh)
     assert ns == ref[6] == 3
     assert rel_l2(interior(qg, P.n), interior(ref[0], P.n)) <= FP64_TOL
     assert rel_l2(interior(dp, P.n), interior(ref[1], P.n)) <= FP64_TOL
@@ -243,9 +299,16 @@ def test_errors_are_reported_not_fatal(cuda, cube_prob):
     from fv3atm_gb300._lib import Fv3gError
     with pytest.raises(Fv3gError, match="hord 6"):
         api.fv_tp_2d(q, cx, cy, n + 1, n + 1, 6, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray)
-    with pytest.raises(Fv3gError, match="nord"):
+    with pytest.raises(Fv3gError, match="nord"):  # del-8 needs more than the 3-cell halo
         api.fv_tp_2d(q, cx, cy, n + 1, n + 1, 8, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray,
-                     1.0, None, None, 1)
+                     1.0, None, None, None, 3, 0.1)
+    with pytest.raises(Fv3gError, match="lim_fac"):
+        api.fv_tp_2d(q, cx, cy, n + 1, n + 1, 1, fx, fy, xfx, yfx, api.GridStruct(g), api.bounds_for(n), rax, ray,
+                     0.0)
+    with pytest.raises(Fv3gError, match="damping"):
+        st = api.CubeState(P.n, P.npz, P.nq, trdm=0.1)
+        st.upload("Q", P.q.numpy())  # no grid: the damping metrics are missing
+        st.tracer_2d(1)
     with pytest.raises(Fv3gError, match="kord 7"):
         api.CubeState(P.n, P.npz, P.nq, kord=7)
 
