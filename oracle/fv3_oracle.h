@@ -16,7 +16,11 @@
  *   - Lin (2004, MWR 132): the "fast" monotonicity constraint of the edge
  *     deviations (hord=8) and Lagrangian-to-Eulerian remapping;
  *   - Putman & Lin (2007, JCP 227): one-sided, dxa-weighted edge values at
- *     cube-face edges and the rotated corner fill of the cubed sphere.
+ *     cube-face edges and the rotated corner fill of the cubed sphere;
+ *   - the GFDL_atmos_cubed_sphere tp_core algorithm for the details those
+ *     papers leave open: the hord 1 / 5 two-dx filter, the one-sided
+ *     interface constants next to a cube edge (s11, s14, s15 for hord 8;
+ *     c1, c2, c3 below it), and the deln_flux del-2(nord+1) tracer damping.
  * Call signatures and argument shapes follow the documented FV3 interfaces
  * (fv_tp_2d, tracer_2d, map_scalar, map1_ppm), with Fortran lower bounds given
  * explicitly.  All 2-D arrays are column-major with i fastest.
