@@ -387,6 +387,7 @@ def main():
     # --------------------------------------------------- mixed headline leg
     st = build_state(P, "mixed", a.nq, a.npz, a.n, a.warps)
     warps = a.warps if a.warps > 0 else st.autotune()
+    ring_warps = st.widths()[1]
     m0 = st.mass("Q")
     st.step(a.q_split, use_graph=False)
     st.sync()
@@ -523,7 +524,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 stencils; f64 pe/overlap schedule/mass sums", "data": "synthetic (seeded; no public dataset)",
-        "config": {**workload(a), "precision": "mixed", "replicas": world, "warps_per_cta": warps},
+        "config": {**workload(a), "precision": "mixed", "replicas": world, "warps_per_cta": warps,
+                   "warps_per_cta_edge_ring": ring_warps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "k_substep<float,8> (fused fv_tp_2d + flux-form update), interior + edge-ring launch "

@@ -219,10 +219,16 @@ class CubeState:
         _lib.call("fv3g_fillz_batched", self._h, _stream(stream))
 
     def autotune(self) -> int:
-        """Pick the advection CTA width by timing a substep; returns it."""
+        """Pick the advection CTA widths by timing a substep; returns the interior width."""
         w = C.c_int(0)
         _lib.call("fv3g_state_autotune", self._h, C.byref(w))
         return w.value
+
+    def widths(self) -> tuple:
+        """(interior, edge-ring) advection CTA widths in warps."""
+        w, r = C.c_int(0), C.c_int(0)
+        _lib.call("fv3g_state_widths", self._h, C.byref(w), C.byref(r))
+        return w.value, r.value
 
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
         _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))

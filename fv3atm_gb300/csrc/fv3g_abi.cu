@@ -126,6 +126,7 @@ struct fv3g_state {
   void* dx = nullptr; void* dy = nullptr; void* sin4 = nullptr;
   void* del6u = nullptr; void* del6v = nullptr;  // tracer-damping metrics
   int del6_tiles = 0;                            // tiles whose damping metrics were set
+  int warps_ring = 0;                            // edge-ring CTA width (0: warps_per_cta), set by autotune
   double da_min = 0.0;
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
@@ -256,6 +257,7 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.topo = st->topo;
   a.eflux = (T*)st->eflux;
   a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
+  a.warps_ring = st->warps_ring;
   return a;
 }
 
@@ -647,40 +649,68 @@ int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
 }
 
 // Time one substep (interior + edge-ring launches, halo fill and prologue)
-// for each candidate CTA width and keep the fastest.  Reads the home tracer
-// buffer and writes only scratch buffers; the logical state is unchanged.
+// for each candidate CTA width and keep the fastest; then the same for the
+// width of the edge-ring launch alone (its CTAs need more registers and
+// shared memory, so a narrower CTA can fit twice per SM).  Reads the home
+// tracer buffer and writes only scratch buffers; the logical state is
+// unchanged.
 int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   const int cand[] = {4, 5, 6, 8, 10};
-  const int saved_w = st->d.warps_per_cta, q_cur = st->q_cur, dp_start = st->dp_start, dp_end = st->dp_end;
+  const int saved_w = st->d.warps_per_cta, saved_r = st->warps_ring, q_cur = st->q_cur, dp_start = st->dp_start,
+            dp_end = st->dp_end;
   const bool remapped = st->remapped, timing = st->timing;
   st->timing = false;
   cudaEvent_t e0, e1;
   FV3G_CUDA(cudaEventCreate(&e0));
   FV3G_CUDA(cudaEventCreate(&e1));
-  int best = 0;
-  float best_ms = 0.f;
   int rc = 0;
-  for (int w : cand) {
-    st->d.warps_per_cta = w;
+  // one timed substep at the current widths; returns a negative time when the width does not fit
+  auto time_one = [&](float& ms) -> int {
     int r = fv3g_tracer_2d_batched(st, 1, st->stream);  // warm-up; rejects widths that do not fit
-    if (r == FV3G_E_ARG) continue;
-    if (r) { rc = r; break; }
-    float ms = 1e30f;
-    for (int rep = 0; rep < 2 && !rc; ++rep) {
+    if (r == FV3G_E_ARG) {
+      ms = -1.f;
+      return 0;
+    }
+    if (r) return r;
+    ms = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
       cudaEventRecord(e0, st->stream);
-      rc = fv3g_tracer_2d_batched(st, 1, st->stream);
+      r = fv3g_tracer_2d_batched(st, 1, st->stream);
       cudaEventRecord(e1, st->stream);
-      if (!rc && cudaEventSynchronize(e1) == cudaSuccess) {
+      if (r) return r;
+      if (cudaEventSynchronize(e1) == cudaSuccess) {
         float t = 0.f;
         cudaEventElapsedTime(&t, e0, e1);
         ms = std::min(ms, t);
       }
     }
-    if (rc) break;
+    return 0;
+  };
+  int best = 0, best_r = 0;
+  float best_ms = 0.f;
+  st->warps_ring = 0;
+  for (int w : cand) {
+    st->d.warps_per_cta = w;
+    float ms;
+    if ((rc = time_one(ms))) break;
+    if (ms < 0.f) continue;
     if (best == 0 || ms < best_ms) {
       best = w;
       best_ms = ms;
+    }
+  }
+  if (!rc && best > 0) {
+    st->d.warps_per_cta = best;
+    for (int w : cand) {
+      if (w == best) continue;
+      st->warps_ring = w;
+      float ms;
+      if ((rc = time_one(ms))) break;
+      if (ms >= 0.f && ms < best_ms) {
+        best_r = w;
+        best_ms = ms;
+      }
     }
   }
   cudaEventDestroy(e0);
@@ -692,14 +722,24 @@ int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
   st->remapped = remapped;
   if (rc || best == 0) {
     st->d.warps_per_cta = saved_w;
+    st->warps_ring = saved_r;
     return rc ? rc : set_error(FV3G_E_ARG, "no advection CTA width fits this precision");
   }
   st->d.warps_per_cta = best;
+  st->warps_ring = best_r;
   if (st->gexec) {  // the captured step was built for the old width
     cudaGraphExecDestroy(st->gexec);
     st->gexec = nullptr;
   }
   if (warps_out) *warps_out = best;
+  return 0;
+}
+
+int fv3g_state_widths(fv3g_state* st, int* warps, int* warps_ring) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  const int w = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
+  if (warps) *warps = w;
+  if (warps_ring) *warps_ring = st->warps_ring > 0 ? st->warps_ring : w;
   return 0;
 }
 

@@ -85,6 +85,7 @@ struct AdvArgs {
   T* fy_out;
   long long sFlux;
   double lim_fac;  // hord 1: 2-dx filter factor (upstream default 1)
+  int warps_ring;  // warps per CTA of the edge-ring launch (0: as the interior launch)
   // del-2(nord+1) tracer damping (deln_flux), run after the substep kernel
   const T* del6_u;  // [tile] planes: y-face metric (isd:ied, jsd:jed+1)
   const T* del6_v;  // x-face metric (isd:ied+1, jsd:jed)

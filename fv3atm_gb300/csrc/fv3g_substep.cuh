@@ -572,6 +572,7 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
   const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
   const int nt = a.cube ? 6 : 1;
+  const int wr = a.warps_ring > 0 ? a.warps_ring : warps;  // edge-ring CTAs may run narrower
   if (nint > 0) {
     dim3 grid(nint, a.npz, nt);
     k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false), s>>>(a, bm);
@@ -579,7 +580,7 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   }
   if (nring > 0) {
     dim3 grid(nring, a.npz, nt);
-    k_substep<T, HORD, FLUXES, true><<<grid, 32 * warps, substep_smem_bytes<T>(warps, true), s>>>(a, bm);
+    k_substep<T, HORD, FLUXES, true><<<grid, 32 * wr, substep_smem_bytes<T>(wr, true), s>>>(a, bm);
     FV3G_CUDA(cudaGetLastError());
   }
   return 0;
@@ -617,8 +618,9 @@ static void set_attrs(cudaError_t& err) {
 template <typename T, int HORD>
 int launch_substep_hord(const AdvArgs<T>& a, bool flux_mode, int warps, cudaStream_t s) {
   const int mw = max_warps<T>();
-  if (warps < 1 || warps > mw)
-    return set_error(FV3G_E_ARG, "this precision supports 1..%d advection warps per CTA (got %d)", mw, warps);
+  if (warps < 1 || warps > mw || a.warps_ring < 0 || a.warps_ring > mw)
+    return set_error(FV3G_E_ARG, "this precision supports 1..%d advection warps per CTA (got %d, ring %d)", mw,
+                     warps, a.warps_ring);
   return flux_mode ? launch_one<T, HORD, true>(a, warps, s) : launch_one<T, HORD, false>(a, warps, s);
 }
 

@@ -294,6 +294,9 @@ int fv3g_stream_sync(fv3g_state* st, void* stream);
  * state (warps_out may be NULL).  Side-effect free on the state's fields.
  * Call it outside stream capture, after the inputs are uploaded. */
 int fv3g_state_autotune(fv3g_state* st, int* warps_out);
+/* The advection CTA widths in use: interior CTAs and the CTAs whose window
+ * holds a cube-face edge (the autotuner may run those narrower). */
+int fv3g_state_widths(fv3g_state* st, int* warps, int* warps_ring);
 /* fillz on the state's remapped tracers (every interior column and tracer). */
 int fv3g_fillz_batched(fv3g_state* st, void* stream);
 
