@@ -233,6 +233,15 @@ class CubeState:
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
         _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))
 
+    def step_host(self, q_split: int, q_in: int, fields: dict, q_out: int, host_f32: bool, groups: int = 0,
+                  stream=None) -> None:
+        """fv3g_step_host: host pointers (ints) of Q, of fields["DELP"/"CX"/"CY"/"MFX"/"MFY"] and of the output;
+        transfers of tracer groups overlap the compute.  With a stream the call only enqueues."""
+        s = None if stream is None else _stream(stream)
+        _lib.call("fv3g_step_host", self._h, q_split, C.c_void_p(q_in), C.c_void_p(fields["DELP"]),
+                  C.c_void_p(fields["CX"]), C.c_void_p(fields["CY"]), C.c_void_p(fields["MFX"]),
+                  C.c_void_p(fields["MFY"]), C.c_void_p(q_out), int(host_f32), groups, s)
+
     def handle(self):
         return self._h
 

@@ -135,6 +135,8 @@ struct fv3g_state {
   int* err = nullptr;
   double* stage = nullptr; size_t stage_bytes = 0;  // FP64 staging for uploads
   cudaStream_t stream = nullptr;
+  cudaStream_t up = nullptr, down = nullptr;  // fv3g_step_host: upload and download streams
+  std::vector<cudaEvent_t> pev;               // fv3g_step_host: its events
   int q_cur = 0;      // buffer holding the latest tracer field
   int dp_start = 0;   // buffer holding dp at the start of the last substep
   int dp_end = 0;     // buffer holding dp at the end of the last substep
@@ -291,13 +293,14 @@ int field_shape(fv3g_state* st, int field, FieldShape& fs, bool for_upload) {
 
 // Copy a field between its device planes and a contiguous (nplanes, nj, ni)
 // buffer of the state's element type; to_buf selects the direction.
-int plane_copy(fv3g_state* st, const FieldShape& fs, void* buf, bool to_buf, cudaMemcpyKind kind, cudaStream_t s) {
+int plane_copy(fv3g_state* st, const FieldShape& fs, void* buf, bool to_buf, cudaMemcpyKind kind, cudaStream_t s,
+               int max_ctas = 0) {
   const size_t es = st->esz;
   char* dev = (char*)fs.dev + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es;
   const size_t dp = (size_t)st->pg.pitch * es, ds = (size_t)st->plane * es;
   const size_t bp = (size_t)fs.ni * es, bs = (size_t)fs.ni * fs.nj * es;
-  if (to_buf) return copy_planes(buf, bp, bs, dev, dp, ds, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s);
-  return copy_planes(dev, dp, ds, buf, bp, bs, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s);
+  if (to_buf) return copy_planes(buf, bp, bs, dev, dp, ds, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s, max_ctas);
+  return copy_planes(dev, dp, ds, buf, bp, bs, (size_t)fs.ni * es, fs.nj, fs.nplanes, kind, s, max_ctas);
 }
 
 int ensure_stage(fv3g_state* st, size_t bytes) {
@@ -335,13 +338,14 @@ int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t 
   return 0;
 }
 
+// Prologue of tracer_2d: scaled work copies of cx, cy, mfx, mfy and the area
+// fluxes, shared by every tracer.
 template <typename T>
-int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
+int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   if (st->d.trdm > 1e-4 && (st->del6_tiles != (1 << st->nt) - 1 || !(st->da_min > 0.0)))
     return set_error(FV3G_E_ARG, "tracer damping (trdm > 1e-4) needs every tile's grid with del6_u, del6_v, da_min");
   const long long fsz = st->plane * st->npz * st->nt;
   const size_t fb = (size_t)fsz * sizeof(T);
-  // scaled work copies and area fluxes
   FV3G_CUDA(cudaMemcpyAsync(st->cxs, st->cx, fb, cudaMemcpyDeviceToDevice, s));
   FV3G_CUDA(cudaMemcpyAsync(st->cys, st->cy, fb, cudaMemcpyDeviceToDevice, s));
   FV3G_CUDA(cudaMemcpyAsync(st->mfxs, st->mfx, fb, cudaMemcpyDeviceToDevice, s));
@@ -352,18 +356,31 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
                             st->n, 1, st->n, st->nt, st->npz, frac, s));
   CHECK(mark(st, K_PROLOGUE, s, 1));
-  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
+  return 0;
+}
+
+// The substeps of tracer_2d for tracers [g0, g0+ng) (every tracer is
+// advected independently; the layer thicknesses they write are the same).
+template <typename T>
+int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
+  // a CTA advances one tracer per warp: no wider than the group
+  const int warps = std::min(ng, st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10));
+  const long long gofs = (long long)g0 * st->plane * st->npz;  // element offset of the group in a tile
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
     const int dst = (src == 1) ? 2 : 1;
     const int dpo = (dpi == 1) ? 2 : 1;
     AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
+    a.q_in += gofs;
+    a.q_out += gofs;
+    a.nq = ng;
+    a.warps_ring = std::min(a.warps_ring, ng);
     if (st->nt == 6) {
-      CHECK(launch_cube_halo<T>((T*)st->q[src], a.sQt, st->plane, st->nq * st->npz, st->pg, st->n, st->topo, s));
+      CHECK(launch_cube_halo<T>((T*)st->q[src] + gofs, a.sQt, st->plane, ng * st->npz, st->pg, st->n, st->topo, s));
       CHECK(mark(st, K_HALO, s));
     } else if (src != 0) {  // the prescribed ring of the home buffer, held over the step
-      CHECK(launch_copy_halo_ring<T>((T*)st->q[src], (const T*)st->q[0], st->plane, st->nq * st->npz, st->pg,
-                                     st->n, s));
+      CHECK(launch_copy_halo_ring<T>((T*)st->q[src] + gofs, (const T*)st->q[0] + gofs, st->plane, ng * st->npz,
+                                     st->pg, st->n, s));
       CHECK(mark(st, K_HALO, s));
     }
     CHECK(launch_substep<T>(a, st->d.hord, false, warps, s));
@@ -395,17 +412,26 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
 }
 
 template <typename T>
-int remap_t(fv3g_state* st, cudaStream_t s) {
+int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
+  CHECK(prologue_t<T>(st, nsplt, s));
+  return substeps_t<T>(st, nsplt, 0, st->nq, s);
+}
+
+// Remap of tracers [g0, g0+ng) from the Lagrangian levels onto ak + bk ps.
+template <typename T>
+int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1) {
   if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  if (ng < 0) ng = st->nq;
+  const long long gofs = (long long)g0 * st->plane * st->npz;
   RemapArgs<T> r{};
-  r.q_in = (const T*)st->q[st->q_cur];
-  r.q_out = (T*)st->q[0];
+  r.q_in = (const T*)st->q[st->q_cur] + gofs;
+  r.q_out = (T*)st->q[0] + gofs;
   if (st->q_cur == 0) return set_error(FV3G_E_ARG, "remap needs an advected field (run tracer_2d first)");
   r.sQk = st->plane;
   r.sQq = st->plane * st->npz;
   r.sQt = r.sQq * st->nq;
   r.sQqo = r.sQq;
-  r.nfield = st->nq;
+  r.nfield = ng;
   r.dp = (const T*)st->dp[st->dp_end];
   r.dp_out = (T*)st->dp_eul;
   r.sFk = st->plane;
@@ -422,6 +448,26 @@ int remap_t(fv3g_state* st, cudaStream_t s) {
   CHECK(mark(st, K_REMAP, s));
   st->q_cur = 0;
   st->remapped = true;
+  return 0;
+}
+
+// Copy tracers [g0, g0+ng) of every tile between a host (ntiles, nq, npz, nd,
+// nd) array of the state's element type and the planes of q[0].
+int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaStream_t s, int max_ctas) {
+  const size_t es = st->esz, nd = (size_t)st->nd;
+  const size_t hplane = nd * nd * es, dplane = (size_t)st->plane * es;
+  for (int t = 0; t < st->nt; ++t) {
+    const long long p0 = ((long long)t * st->nq + g0) * st->npz;  // first plane of the group in tile t
+    char* dev = (char*)st->q[0] + p0 * dplane;
+    char* h = (char*)host + p0 * hplane;
+    const size_t pitch = (size_t)st->pg.pitch * es;
+    if (to_host)
+      CHECK(copy_planes(h, nd * es, hplane, dev, pitch, dplane, nd * es, nd, (long long)ng * st->npz,
+                        cudaMemcpyDeviceToHost, s, max_ctas));
+    else
+      CHECK(copy_planes(dev, pitch, dplane, h, nd * es, hplane, nd * es, nd, (long long)ng * st->npz,
+                        cudaMemcpyHostToDevice, s, max_ctas));
+  }
   return 0;
 }
 
@@ -529,6 +575,9 @@ int fv3g_state_destroy(fv3g_state* st) {
   if (st->stream) cudaStreamSynchronize(st->stream);
   if (st->gexec) cudaGraphExecDestroy(st->gexec);
   for (cudaEvent_t e : st->ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : st->pev) cudaEventDestroy(e);
+  if (st->up) cudaStreamDestroy(st->up);
+  if (st->down) cudaStreamDestroy(st->down);
   for (void* p : st->allocs) cudaFree(p);
   if (st->stage) cudaFree(st->stage);
   if (st->stream) cudaStreamDestroy(st->stream);
@@ -1007,6 +1056,93 @@ int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, voi
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
   CHECK(plane_copy(st, fs, host, true, cudaMemcpyDeviceToHost, s));
+  return 0;
+}
+
+// One tracer_2d + remap step from host arrays to host arrays, transfers
+// overlapped with compute: the per-level inputs go first, then the tracers in
+// groups; group g is advected and remapped on the state's stream while group
+// g+1 uploads (a grid-capped copy kernel reading page-locked host memory) and
+// group g-1 downloads (copy engine), each on its own stream.
+int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* delp, const void* cx, const void* cy,
+                   const void* mfx, const void* mfy, void* q_out, int host_f32, int groups, void* stream) {
+  if (!st || !q_in || !delp || !cx || !cy || !mfx || !mfy || !q_out) return set_error(FV3G_E_ARG, "null argument");
+  if (q_split < 1 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 1..64 on the batched path");
+  if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
+  if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
+  int G = groups > 0 ? groups : std::max(1, st->nq / warps);
+  G = std::min(G, st->nq);
+  // The copy streams run at the highest priority: a compute kernel's grid is
+  // far larger than the GPU, and without priority the copy kernels' CTAs
+  // would only be dispatched after the last compute CTA; with it they take
+  // the first free slots and then stay resident beside the compute CTAs.
+  if (!st->up || !st->down) {
+    int least = 0, greatest = 0;
+    FV3G_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    if (!st->up) FV3G_CUDA(cudaStreamCreateWithPriority(&st->up, cudaStreamNonBlocking, greatest));
+    if (!st->down) FV3G_CUDA(cudaStreamCreateWithPriority(&st->down, cudaStreamNonBlocking, greatest));
+  }
+  const size_t need = 2 + 2 * (size_t)G;  // start, levels, then per group: uploaded, computed
+  while (st->pev.size() < need + 1) {
+    cudaEvent_t e;
+    FV3G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    st->pev.push_back(e);
+  }
+  cudaStream_t caller = stream ? (cudaStream_t)stream : st->stream;
+  cudaStream_t cs = st->stream, us = st->up, ds = st->down;
+  cudaEvent_t ev_start = st->pev[0], ev_lev = st->pev[1], ev_end = st->pev[need];
+  // everything after the caller's prior work on its stream
+  FV3G_CUDA(cudaEventRecord(ev_start, caller));
+  FV3G_CUDA(cudaStreamWaitEvent(us, ev_start, 0));
+  FV3G_CUDA(cudaStreamWaitEvent(cs, ev_start, 0));
+  FV3G_CUDA(cudaStreamWaitEvent(ds, ev_start, 0));
+  st->nev = 0;
+  CHECK(mark(st, -1, cs));
+  constexpr int kCopyCtas = 152;  // one copy CTA per SM beside the compute kernels
+  const int lev_fields[] = {FV3G_FIELD_DELP, FV3G_FIELD_CX, FV3G_FIELD_CY, FV3G_FIELD_MFX, FV3G_FIELD_MFY};
+  const void* lev_src[] = {delp, cx, cy, mfx, mfy};
+  for (int f = 0; f < 5; ++f) {
+    FieldShape fs;
+    CHECK(field_shape(st, lev_fields[f], fs, true));
+    CHECK(plane_copy(st, fs, (void*)lev_src[f], false, cudaMemcpyHostToDevice, us));
+  }
+  FV3G_CUDA(cudaEventRecord(ev_lev, us));
+  auto group = [&](int g, int& g0, int& ng) {
+    g0 = (int)((long long)st->nq * g / G);
+    ng = (int)((long long)st->nq * (g + 1) / G) - g0;
+  };
+  for (int g = 0; g < G; ++g) {
+    int g0, ng;
+    group(g, g0, ng);
+    CHECK(q_group_copy(st, g0, ng, (void*)q_in, false, us, g == 0 ? 0 : kCopyCtas));
+    FV3G_CUDA(cudaEventRecord(st->pev[2 + 2 * g], us));
+  }
+  FV3G_CUDA(cudaStreamWaitEvent(cs, ev_lev, 0));
+  CHECK(st->fp64 ? prologue_t<double>(st, q_split, cs) : prologue_t<float>(st, q_split, cs));
+  for (int g = 0; g < G; ++g) {
+    int g0, ng;
+    group(g, g0, ng);
+    FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + 2 * g], 0));
+    if (st->fp64) {
+      CHECK(substeps_t<double>(st, q_split, g0, ng, cs));
+      CHECK(remap_t<double>(st, cs, g0, ng));
+    } else {
+      CHECK(substeps_t<float>(st, q_split, g0, ng, cs));
+      CHECK(remap_t<float>(st, cs, g0, ng));
+    }
+    FV3G_CUDA(cudaEventRecord(st->pev[3 + 2 * g], cs));
+    FV3G_CUDA(cudaStreamWaitEvent(ds, st->pev[3 + 2 * g], 0));
+    CHECK(q_group_copy(st, g0, ng, q_out, true, ds, kCopyCtas));
+  }
+  // join the three streams into the caller's
+  FV3G_CUDA(cudaEventRecord(ev_end, ds));
+  FV3G_CUDA(cudaStreamWaitEvent(caller, ev_end, 0));
+  FV3G_CUDA(cudaEventRecord(ev_end, cs));
+  FV3G_CUDA(cudaStreamWaitEvent(caller, ev_end, 0));
+  FV3G_CUDA(cudaEventRecord(ev_end, us));
+  FV3G_CUDA(cudaStreamWaitEvent(caller, ev_end, 0));
+  if (!stream) FV3G_CUDA(cudaStreamSynchronize(caller));
   return 0;
 }
 

@@ -26,7 +26,10 @@ namespace {
 constexpr long long kChunk = 256;
 
 // One warp per row of one plane (rows in a grid-stride loop, one integer
-// division per row), the row's words across the lanes: coalesced rows.
+// division per row), the row's words across the lanes: coalesced rows.  Each
+// lane loads four words before storing them, so a warp keeps 512 bytes of
+// reads in flight (reads of host memory over the link have microseconds of
+// latency).
 __global__ void k_copy_planes(unsigned* dst, long long dpitch, long long dslice, const unsigned* src, long long spitch,
                               long long sslice, int width, int height, long long nplanes) {
   const long long rows = (long long)height * nplanes;
@@ -38,7 +41,19 @@ __global__ void k_copy_planes(unsigned* dst, long long dpitch, long long dslice,
     const long long y = r - p * height;
     unsigned* d = dst + p * dslice + y * dpitch;
     const unsigned* sp = src + p * sslice + y * spitch;
-    for (int x = lane; x < width; x += 32) d[x] = sp[x];
+    for (int x0 = 0; x0 < width; x0 += 128) {
+      unsigned v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = x0 + 32 * u + lane;
+        if (x < width) v[u] = sp[x];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = x0 + 32 * u + lane;
+        if (x < width) d[x] = v[u];
+      }
+    }
   }
 }
 }  // namespace
@@ -59,10 +74,10 @@ thread_local Staging g_staging;
 constexpr size_t kStageBytes = size_t(256) << 20;
 
 int device_words(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
-                 size_t width_bytes, size_t height, long long nplanes, cudaStream_t s) {
-  const int width = (int)(width_bytes / 4);
+                 size_t width_bytes, size_t height, long long nplanes, cudaStream_t s, int max_ctas = 0) {
   const long long rows = (long long)height * nplanes;
-  const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((rows + 7) / 8, 152LL * 16));
+  const long long cap = max_ctas > 0 ? max_ctas : 152LL * 16;
+  const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((rows + 7) / 8, cap));
   k_copy_planes<<<grid, 256, 0, s>>>((unsigned*)dst, (long long)(dpitch / 4), (long long)(dslice / 4),
                                      (const unsigned*)src, (long long)(spitch / 4), (long long)(sslice / 4),
                                      (int)(width_bytes / 4), (int)height, nplanes);
@@ -72,7 +87,7 @@ int device_words(void* dst, size_t dpitch, size_t dslice, const void* src, size_
 
 // dense host stack <-> pitched device stack through the staging buffer
 int staged_copy(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
-                size_t width_bytes, size_t height, long long nplanes, bool h2d, cudaStream_t s) {
+                size_t width_bytes, size_t height, long long nplanes, bool h2d, cudaStream_t s, int max_ctas) {
   Staging& g = g_staging;
   const size_t plane = width_bytes * height;
   const long long per = std::max<long long>(1, (long long)(kStageBytes / plane));
@@ -94,10 +109,10 @@ int staged_copy(void* dst, size_t dpitch, size_t dslice, const void* src, size_t
     if (h2d) {
       FV3G_CUDA(cudaMemcpyAsync(g.buf, (const char*)src + p0 * sslice, np * plane, cudaMemcpyHostToDevice, s));
       CHECK_RC(device_words((char*)dst + p0 * dslice, dpitch, dslice, g.buf, width_bytes, plane, width_bytes, height,
-                            np, s));
+                            np, s, max_ctas));
     } else {
       CHECK_RC(device_words(g.buf, width_bytes, plane, (const char*)src + p0 * sslice, spitch, sslice, width_bytes,
-                            height, np, s));
+                            height, np, s, max_ctas));
       FV3G_CUDA(cudaMemcpyAsync((char*)dst + p0 * dslice, g.buf, np * plane, cudaMemcpyDeviceToHost, s));
     }
   }
@@ -107,7 +122,8 @@ int staged_copy(void* dst, size_t dpitch, size_t dslice, const void* src, size_t
 }  // namespace
 
 int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
-                size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s) {
+                size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s,
+                int max_ctas) {
   if (nplanes <= 0 || width_bytes == 0 || height == 0) return 0;
   if (kind == cudaMemcpyDeviceToDevice) {
     if ((dpitch | dslice | spitch | sslice | width_bytes | (size_t)dst | (size_t)src) & 3)
@@ -120,7 +136,8 @@ int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t
     if (qe != cudaSuccess) cudaGetLastError();  // pageable memory on older drivers: clear and stage
     const bool aligned = !((dpitch | dslice | spitch | sslice | width_bytes | (size_t)dst | (size_t)src) & 3);
     if (qe == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer != nullptr && aligned)
-      return device_words(dst, dpitch, dslice, at.devicePointer, spitch, sslice, width_bytes, height, nplanes, s);
+      return device_words(dst, dpitch, dslice, at.devicePointer, spitch, sslice, width_bytes, height, nplanes, s,
+                          max_ctas);
   }
   {  // dense pageable host side: staged
     const bool h2d = kind == cudaMemcpyHostToDevice;
@@ -129,7 +146,7 @@ int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t
     const void* dev = h2d ? dst : src;
     const bool aligned = !((dp | ds | width_bytes | (size_t)dev) & 3);
     if (hp == width_bytes && hs == width_bytes * height && aligned)
-      return staged_copy(dst, dpitch, dslice, src, spitch, sslice, width_bytes, height, nplanes, h2d, s);
+      return staged_copy(dst, dpitch, dslice, src, spitch, sslice, width_bytes, height, nplanes, h2d, s, max_ctas);
   }
   for (long long p0 = 0; p0 < nplanes; p0 += kChunk) {
     const long long np = std::min(kChunk, nplanes - p0);

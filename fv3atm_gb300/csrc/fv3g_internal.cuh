@@ -220,10 +220,13 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
                        int ie, int js, int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s);
 
 // Copy nplanes planes of width_bytes x height between pitched buffers
-// (slice = bytes from one plane to the next); device-to-device by a kernel,
-// host copies in chunks of cudaMemcpy3DAsync.
+// (slice = bytes from one plane to the next); device-to-device and uploads
+// from page-locked host memory by a kernel (max_ctas > 0 caps its grid, for
+// copies that run beside compute kernels), other host copies staged or in
+// chunks of cudaMemcpy3DAsync.
 int copy_planes(void* dst, size_t dpitch, size_t dslice, const void* src, size_t spitch, size_t sslice,
-                size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s);
+                size_t width_bytes, size_t height, long long nplanes, cudaMemcpyKind kind, cudaStream_t s,
+                int max_ctas = 0);
 
 int prepare_kernels();
 BlockMap block_map(int is, int ie, int js, int je, int npx, int npy, int nested);

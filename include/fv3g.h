@@ -289,6 +289,19 @@ int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream);
 int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32, void* stream);
 int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream);
 int fv3g_stream_sync(fv3g_state* st, void* stream);
+/* One tracer_2d + remap step from host arrays to host arrays with the
+ * transfers overlapped with the compute: the per-level inputs are uploaded
+ * first, then the tracers move in `groups` groups (0: nq / warps_per_cta), and
+ * group g is advected and remapped while group g+1 uploads and group g-1
+ * downloads.  q_in, q_out: (ntiles, nq, npz, nd, nd); delp, cx, cy, mfx, mfy:
+ * the FV3G_FIELD_* shapes; element type float (host_f32 = 1, MIXED states) or
+ * double (FP64 states); page-locked host memory for full bandwidth.  With a
+ * stream the work is ordered after the stream's prior work and the call
+ * returns once it is enqueued (the stream waits for its end); with NULL it
+ * returns when q_out holds the result. */
+int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* delp, const void* cx,
+                   const void* cy, const void* mfx, const void* mfy, void* q_out, int host_f32,
+                   int groups, void* stream);
 /* Choose the advection CTA width (warps per CTA) by timing one substep of
  * the loaded fields at each candidate width; the fastest is kept for the
  * state (warps_out may be NULL).  Side-effect free on the state's fields.

@@ -313,6 +313,28 @@ def test_errors_are_reported_not_fatal(cuda, cube_prob):
         api.CubeState(P.n, P.npz, P.nq, kord=7)
 
 
+@pytest.mark.parametrize("precision,groups", [("mixed", 1), ("mixed", 2), ("mixed", 3), ("fp64", 2)])
+def test_step_host_pipelined_equals_device_step(cuda, cube_prob, precision, groups):
+    """fv3g_step_host (host arrays in and out, tracer groups overlapping their transfers with the compute)
+    gives the device-resident step's result bit for bit, also when called again."""
+    import torch
+    P = cube_prob
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    st.load_problem(P)
+    st.step(3)
+    want = st.download("Q_REMAPPED")
+    src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
+    host = {k: torch.as_tensor(v).to(dt).contiguous().pin_memory() for k, v in src.items()}
+    out = torch.zeros(st.field_shape("Q_REMAPPED"), dtype=dt).pin_memory()
+    for _ in range(2):
+        out.zero_()
+        st.step_host(3, host["Q"].data_ptr(), {k: h.data_ptr() for k, h in host.items()}, out.data_ptr(),
+                     precision == "mixed", groups)
+        assert np.array_equal(out.numpy().astype(np.float64), want)
+    st.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_field_copies_roundtrip_many_planes(cuda, precision):
     """6 x 9 x 127 planes through the device, pinned-host and FP64-host copy paths."""
