@@ -285,15 +285,22 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
 template <typename T>
 __host__ __device__ constexpr int pk(int k) { return k + (k >> (sizeof(T) == 8 ? 4 : 5)); }
 
+// Fields per pass of the warp kernel: FP32 columns advance two fields at a
+// time, so the lane-to-lane scans of both interleave (the scans are latency
+// chains of shuffles); FP64 keeps one (its ring has three slots).
+template <typename T>
+__host__ __device__ constexpr int fields_per_pass() { return sizeof(T) == 4 ? 2 : 1; }
+
 template <typename T, int NPL>
 struct ColSmem {
+  static constexpr int FP = fields_per_pass<T>();
   double pe1[pk<double>(32 * NPL) + 1];
   T dp[pk<T>(32 * NPL)];
-  T pl[pk<T>(32 * NPL)];  // sub-grid parabola of every source layer: left, right edge and curvature
-  T pr[pk<T>(32 * NPL)];
-  T p6[pk<T>(32 * NPL)];
-  float mh[pk<float>(32 * NPL) + 1];  // FP32 fields: cumulative layer mass at every source interface,
-  float ml[pk<float>(32 * NPL) + 1];  // as an unevaluated sum hi + lo (float-float)
+  T pl[FP][pk<T>(32 * NPL)];  // sub-grid parabola of every source layer: left, right edge and curvature
+  T pr[FP][pk<T>(32 * NPL)];
+  T p6[FP][pk<T>(32 * NPL)];
+  float mh[FP][pk<float>(32 * NPL) + 1];  // FP32 fields: cumulative layer mass at every source interface,
+  float ml[FP][pk<float>(32 * NPL) + 1];  // as an unevaluated sum hi + lo (float-float)
 };
 
 // Float-float arithmetic (an unevaluated sum of two floats, ~48-bit
@@ -384,6 +391,49 @@ __device__ __forceinline__ Mat2<T> shfl_up_mat(const Mat2<T>& m, int o) {
 // backward (lane+o first); both return the exclusive prefix's offset, i.e.
 // the recurrence value entering this lane's first (forward) or last
 // (backward) element, given that the chain starts with a constant map.
+// The same scans on N independent chains, level by level (their shuffles
+// and multiplies interleave).
+template <typename T, int N>
+__device__ __forceinline__ void affine_enter_fwd_n(T (&al)[N], T (&be)[N], T (&out)[N], int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T pa[N], pb[N];
+#pragma unroll
+    for (int h = 0; h < N; ++h) {
+      pa[h] = __shfl_up_sync(0xffffffffu, al[h], o);
+      pb[h] = __shfl_up_sync(0xffffffffu, be[h], o);
+    }
+#pragma unroll
+    for (int h = 0; h < N; ++h)
+      if (lane >= o) {
+        be[h] = al[h] * pb[h] + be[h];
+        al[h] = al[h] * pa[h];
+      }
+  }
+#pragma unroll
+  for (int h = 0; h < N; ++h) out[h] = __shfl_up_sync(0xffffffffu, be[h], 1);
+}
+template <typename T, int N>
+__device__ __forceinline__ void affine_enter_bwd_n(T (&al)[N], T (&be)[N], T (&out)[N], int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T pa[N], pb[N];
+#pragma unroll
+    for (int h = 0; h < N; ++h) {
+      pa[h] = __shfl_down_sync(0xffffffffu, al[h], o);
+      pb[h] = __shfl_down_sync(0xffffffffu, be[h], o);
+    }
+#pragma unroll
+    for (int h = 0; h < N; ++h)
+      if (lane + o < 32) {
+        be[h] = al[h] * pb[h] + be[h];
+        al[h] = al[h] * pa[h];
+      }
+  }
+#pragma unroll
+  for (int h = 0; h < N; ++h) out[h] = __shfl_down_sync(0xffffffffu, be[h], 1);
+}
+
 template <typename T>
 __device__ __forceinline__ T affine_enter_fwd(T al, T be, int lane) {
 #pragma unroll
@@ -450,7 +500,7 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
     cp_async_commit();
   };
 #pragma unroll
-  for (int f = 0; f < RING - 1; ++f) issue(f);
+  for (int f = 0; f < RING - fields_per_pass<T>(); ++f) issue(f);
 
   // ------------------------------------------------ interface pressures pe1
   if (a.pe1 != nullptr) {
@@ -576,69 +626,98 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
   T rdpk[NPL];
 #pragma unroll
   for (int j = 0; j < NPL; ++j) rdpk[j] = T(1) / dpk[j];
-  for (int f = 0; f < a.nfield; ++f) {
-    __syncthreads();  // every warp is done with field f-1, whose slot is refilled now
-    issue(f + RING - 1);
-    cp_async_wait<RING - 1>();
-    __syncthreads();  // field f is in its slot
-    const T* Q = ring + ((f % RING) * 8 + warp) * RP;
-    T* q2 = a.q_out + qo + f * a.sQqo;
-    T qv[NPL], st[NPL];
+  constexpr int FP = fields_per_pass<T>();
+  for (int f0 = 0; f0 < a.nfield; f0 += FP) {
+    __syncthreads();  // every warp is done with the previous pass, whose slots are refilled now
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) qv[j] = (u0 + j < km) ? Q[pk<T>(u0 + j)] : T(0);
+    for (int h = 0; h < FP; ++h) issue(f0 + RING - FP + h);
+    cp_async_wait<RING - FP>();
+    __syncthreads();  // the pass's fields are in their slots
+    // a pass past the last field repeats it and stores nothing
+    const T* Q[FP];
+    T* q2[FP];
+    bool store[FP];
+#pragma unroll
+    for (int h = 0; h < FP; ++h) {
+      const int f = min(f0 + h, a.nfield - 1);
+      Q[h] = ring + ((f % RING) * 8 + warp) * RP;
+      q2[h] = a.q_out + qo + f * a.sQqo;
+      store[h] = real && f0 + h < a.nfield;
+    }
+    T qv[FP][NPL], st[FP][NPL];
+#pragma unroll
+    for (int h = 0; h < FP; ++h)
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) qv[h][j] = (u0 + j < km) ? Q[h][pk<T>(u0 + j)] : T(0);
     // -------------------------------------------- interface values a[0..km]
     if (km == 1) {
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) st[j] = qv[0];
-    } else {
-      T rhs[NPL], qa[NPL], qb[NPL];
-      T al = T(1), be = T(0);
+      for (int h = 0; h < FP; ++h)
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) {
-        qa[j] = Q[pk<T>(ia[j])];
-        qb[j] = Q[pk<T>(ib[j])];
-        rhs[j] = wa[j] * qa[j] + wb[j] * qb[j] + wc[j] * qsv;
-        const T aj = -mco[j] * rdv[j];
-        be = aj * be + rhs[j] * rdv[j];
-        al = aj * al;
-      }
-      T y[NPL];
-      {
-        T yp = affine_enter_fwd<T>(al, be, lane);
+        for (int j = 0; j < NPL; ++j) st[h][j] = qv[h][0];
+    } else {
+      T rhs[FP][NPL], qa[FP][NPL], qb[FP][NPL], al[FP], be[FP];
+#pragma unroll
+      for (int h = 0; h < FP; ++h) {
+        al[h] = T(1);
+        be[h] = T(0);
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
-          yp = (rhs[j] - mco[j] * yp) * rdv[j];
-          y[j] = yp;
+          qa[h][j] = Q[h][pk<T>(ia[j])];
+          qb[h][j] = Q[h][pk<T>(ib[j])];
+          rhs[h][j] = wa[j] * qa[h][j] + wb[j] * qb[h][j] + wc[j] * qsv;
+          const T aj = -mco[j] * rdv[j];
+          be[h] = aj * be[h] + rhs[h][j] * rdv[j];
+          al[h] = aj * al[h];
         }
       }
-      al = T(1);
-      be = T(0);
+      T y[FP][NPL];
+      {
+        T yp[FP];
+        affine_enter_fwd_n<T, FP>(al, be, yp, lane);
 #pragma unroll
-      for (int j = NPL - 1; j >= 0; --j) {
-        be = -cpb[j] * be + y[j];
-        al = -cpb[j] * al;
-      }
-      T av = affine_enter_bwd<T>(al, be, lane);
+        for (int h = 0; h < FP; ++h)
 #pragma unroll
-      for (int j = NPL - 1; j >= 0; --j) {
-        const int u = u0 + j;
-        av = y[j] - cpb[j] * av;
-        const bool clampit = KORD == 9 && u <= km && !(u == km && a.iv == -2);
-        st[j] = clampit ? clamp2(av, qa[j], qb[j]) : av;
+          for (int j = 0; j < NPL; ++j) {
+            yp[h] = (rhs[h][j] - mco[j] * yp[h]) * rdv[j];
+            y[h][j] = yp[h];
+          }
       }
+#pragma unroll
+      for (int h = 0; h < FP; ++h) {
+        al[h] = T(1);
+        be[h] = T(0);
+#pragma unroll
+        for (int j = NPL - 1; j >= 0; --j) {
+          be[h] = -cpb[j] * be[h] + y[h][j];
+          al[h] = -cpb[j] * al[h];
+        }
+      }
+      T av[FP];
+      affine_enter_bwd_n<T, FP>(al, be, av, lane);
+#pragma unroll
+      for (int h = 0; h < FP; ++h)
+#pragma unroll
+        for (int j = NPL - 1; j >= 0; --j) {
+          const int u = u0 + j;
+          av[h] = y[h][j] - cpb[j] * av[h];
+          const bool clampit = KORD == 9 && u <= km && !(u == km && a.iv == -2);
+          st[h][j] = clampit ? clamp2(av[h], qa[h][j], qb[h][j]) : av[h];
+        }
     }
     // ------------------------------------------ sub-grid parabolas of layers
-    {
-      const T st_next = __shfl_down_sync(0xffffffffu, st[0], 1);
+#pragma unroll
+    for (int h = 0; h < FP; ++h) {
+      const T st_next = __shfl_down_sync(0xffffffffu, st[h][0], 1);
 #pragma unroll
       for (int j = 0; j < NPL; ++j) {
         const int u = u0 + j;
-        const Profile<T> p = layer_profile_sel<T, KORD>(qv[j], st[j], j + 1 < NPL ? st[j + 1] : st_next, a.iv,
-                                                        floor_v);
+        const Profile<T> p = layer_profile_sel<T, KORD>(qv[h][j], st[h][j], j + 1 < NPL ? st[h][j + 1] : st_next,
+                                                        a.iv, floor_v);
         if (u < km) {
-          S.pl[pk<T>(u)] = p.l;
-          S.pr[pk<T>(u)] = p.r;
-          S.p6[pk<T>(u)] = p.s6;
+          S.pl[h][pk<T>(u)] = p.l;
+          S.pr[h][pk<T>(u)] = p.r;
+          S.p6[h][pk<T>(u)] = p.s6;
         }
       }
     }
@@ -647,73 +726,89 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
       // interface (layer masses q*dp are exact as float-float products), so a
       // target layer's mass is a difference of two cumulative values and the
       // column mass telescopes; only the final division rounds per value.
-      FF m[NPL], tot{0.f, 0.f};
+      FF m[FP][NPL], ex[FP];
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) {
-        m[j] = (u0 + j < km) ? ff_prod((float)qv[j], (float)S.dp[pk<T>(u0 + j)]) : FF{0.f, 0.f};
-        tot = ff_add(tot, m[j]);
+      for (int h = 0; h < FP; ++h) {
+        ex[h] = FF{0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+          m[h][j] = (u0 + j < km) ? ff_prod((float)qv[h][j], (float)S.dp[pk<T>(u0 + j)]) : FF{0.f, 0.f};
+          ex[h] = ff_add(ex[h], m[h][j]);
+        }
       }
-      FF ex = tot;  // inclusive scan of the lane totals, then shifted by one lane
+      // inclusive scan of the lane totals, then shifted by one lane
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const FF p{__shfl_up_sync(0xffffffffu, ex.hi, o), __shfl_up_sync(0xffffffffu, ex.lo, o)};
-        if (lane >= o) ex = ff_add(p, ex);
-      }
-      FF run{__shfl_up_sync(0xffffffffu, ex.hi, 1), __shfl_up_sync(0xffffffffu, ex.lo, 1)};
-      if (lane == 0) run = FF{0.f, 0.f};
+        FF p[FP];
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) {
-        if (u0 + j <= km) {
-          S.mh[pk<float>(u0 + j)] = run.hi;
-          S.ml[pk<float>(u0 + j)] = run.lo;
+        for (int h = 0; h < FP; ++h)
+          p[h] = FF{__shfl_up_sync(0xffffffffu, ex[h].hi, o), __shfl_up_sync(0xffffffffu, ex[h].lo, o)};
+#pragma unroll
+        for (int h = 0; h < FP; ++h)
+          if (lane >= o) ex[h] = ff_add(p[h], ex[h]);
+      }
+#pragma unroll
+      for (int h = 0; h < FP; ++h) {
+        FF run{__shfl_up_sync(0xffffffffu, ex[h].hi, 1), __shfl_up_sync(0xffffffffu, ex[h].lo, 1)};
+        if (lane == 0) run = FF{0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+          if (u0 + j <= km) {
+            S.mh[h][pk<float>(u0 + j)] = run.hi;
+            S.ml[h][pk<float>(u0 + j)] = run.lo;
+          }
+          run = ff_add(run, m[h][j]);
         }
-        run = ff_add(run, m[j]);
       }
     }
     __syncwarp();
     // ------------------------------------------------------- integration
-    if (Single<T>::value) {
-      FF cm[NPL + 1];  // cumulative mass at this lane's target interfaces
 #pragma unroll
-      for (int j = 0; j <= NPL; ++j) {
-        const int L = Ls[j];
-        const float X = (float)Xs[j];
-        const int il = pk<float>(L), iu = pk<float>(L + 1);
-        FF c{S.mh[il], S.ml[il]};
-        if (X >= 1.f) {
-          c = FF{S.mh[iu], S.ml[iu]};
-        } else if (X > 0.f) {
-          const int it = pk<T>(L);
-          const float part = (float)S.dp[it] * X * (float)pmean(S.pl[it], S.pr[it], S.p6[it], T(0), T(X));
-          c = ff_add(c, FF{part, 0.f});
+    for (int h = 0; h < FP; ++h) {
+      if (Single<T>::value) {
+        FF cm[NPL + 1];  // cumulative mass at this lane's target interfaces
+#pragma unroll
+        for (int j = 0; j <= NPL; ++j) {
+          const int L = Ls[j];
+          const float X = (float)Xs[j];
+          const int il = pk<float>(L), iu = pk<float>(L + 1);
+          FF c{S.mh[h][il], S.ml[h][il]};
+          if (X >= 1.f) {
+            c = FF{S.mh[h][iu], S.ml[h][iu]};
+          } else if (X > 0.f) {
+            const int it = pk<T>(L);
+            const float part =
+                (float)S.dp[it] * X * (float)pmean(S.pl[h][it], S.pr[h][it], S.p6[h][it], T(0), T(X));
+            c = ff_add(c, FF{part, 0.f});
+          }
+          cm[j] = c;
         }
-        cm[j] = c;
-      }
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) {
-        const int t = u0 + j;
-        const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
-        if (real && t < kn) q2[(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
-      }
-    } else {
+        for (int j = 0; j < NPL; ++j) {
+          const int t = u0 + j;
+          const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
+          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
+        }
+      } else {
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) {
-        const int t = u0 + j;
-        const int Lt = Ls[j], Lb = Ls[j + 1];
-        const T Xt = Xs[j], Xb = Xs[j + 1];
-        const bool inside = (Lb == Lt) || (Lb == Lt + 1 && Xb == T(0));
-        const int it = pk<T>(Lt), ib_ = pk<T>(Lb);
-        const T qt = Q[it], dpt = S.dp[it];
-        const T pm1 = pmean(S.pl[it], S.pr[it], S.p6[it], Xt, (inside && Lb == Lt) ? Xb : T(1));
-        const T vin = (Xt == T(0) && (Lb == Lt + 1 || Xb == T(1))) ? qt : pm1;
-        T mass = Xt == T(0) ? qt * dpt : (dpt * (T(1) - Xt)) * pm1;
-        for (int mm = Lt + 1; mm < Lb; ++mm) mass = mass + Q[pk<T>(mm)] * S.dp[pk<T>(mm)];
-        const T qb_ = Q[ib_], dpb = S.dp[ib_];
-        const T pm2 = pmean(S.pl[ib_], S.pr[ib_], S.p6[ib_], T(0), Xb);
-        const T bot = Xb >= T(1) ? qb_ * (dpb * Xb) : (Xb > T(0) ? (dpb * Xb) * pm2 : T(0));
-        mass = mass + bot;
-        const T out = inside ? vin : mass * rdpk[j];
-        if (real && t < kn) q2[(long long)t * a.sQk] = out;
+        for (int j = 0; j < NPL; ++j) {
+          const int t = u0 + j;
+          const int Lt = Ls[j], Lb = Ls[j + 1];
+          const T Xt = Xs[j], Xb = Xs[j + 1];
+          const bool inside = (Lb == Lt) || (Lb == Lt + 1 && Xb == T(0));
+          const int it = pk<T>(Lt), ib_ = pk<T>(Lb);
+          const T qt = Q[h][it], dpt = S.dp[it];
+          const T pm1 = pmean(S.pl[h][it], S.pr[h][it], S.p6[h][it], Xt, (inside && Lb == Lt) ? Xb : T(1));
+          const T vin = (Xt == T(0) && (Lb == Lt + 1 || Xb == T(1))) ? qt : pm1;
+          T mass = Xt == T(0) ? qt * dpt : (dpt * (T(1) - Xt)) * pm1;
+          for (int mm = Lt + 1; mm < Lb; ++mm) mass = mass + Q[h][pk<T>(mm)] * S.dp[pk<T>(mm)];
+          const T qb_ = Q[h][ib_], dpb = S.dp[ib_];
+          const T pm2 = pmean(S.pl[h][ib_], S.pr[h][ib_], S.p6[h][ib_], T(0), Xb);
+          const T bot = Xb >= T(1) ? qb_ * (dpb * Xb) : (Xb > T(0) ? (dpb * Xb) * pm2 : T(0));
+          mass = mass + bot;
+          const T out = inside ? vin : mass * rdpk[j];
+          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = out;
+        }
       }
     }
   }
