@@ -417,12 +417,15 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   return substeps_t<T>(st, nsplt, 0, st->nq, s);
 }
 
-// Remap of tracers [g0, g0+ng) from the Lagrangian levels onto ak + bk ps.
+// Remap of tracers [g0, g0+ng) of tiles [t0, t0+ntl) from the Lagrangian
+// levels onto ak + bk ps.
 template <typename T>
-int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1) {
+int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1, int t0 = 0, int ntl = -1) {
   if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
   if (ng < 0) ng = st->nq;
-  const long long gofs = (long long)g0 * st->plane * st->npz;
+  if (ntl < 0) ntl = st->nt;
+  const long long tq = (long long)t0 * st->plane * st->npz * st->nq, tf = (long long)t0 * st->plane * st->npz;
+  const long long gofs = (long long)g0 * st->plane * st->npz + tq;
   RemapArgs<T> r{};
   r.q_in = (const T*)st->q[st->q_cur] + gofs;
   r.q_out = (T*)st->q[0] + gofs;
@@ -432,31 +435,35 @@ int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1) {
   r.sQt = r.sQq * st->nq;
   r.sQqo = r.sQq;
   r.nfield = ng;
-  r.dp = (const T*)st->dp[st->dp_end];
-  r.dp_out = (T*)st->dp_eul;
+  r.dp = (const T*)st->dp[st->dp_end] + tf;
+  r.dp_out = (T*)st->dp_eul + tf;
   r.sFk = st->plane;
   r.sFt = st->plane * st->npz;
   r.ak = st->ak;
   r.bk = st->bk;
   r.pg = st->pg;
   r.i1 = 1; r.j1 = 1; r.ni = st->n; r.nj = st->n;
-  r.ncol = (long long)st->nt * st->n * st->n;
+  r.ncol = (long long)ntl * st->n * st->n;
   r.km = st->npz; r.kn = st->npz;
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
   CHECK(launch_remap<T>(r, st->d.kord, s));
   CHECK(mark(st, K_REMAP, s));
-  st->q_cur = 0;
-  st->remapped = true;
+  if (t0 + ntl == st->nt) {  // the last tile range of the field: the state now holds the remapped field
+    st->q_cur = 0;
+    st->remapped = true;
+  }
   return 0;
 }
 
-// Copy tracers [g0, g0+ng) of every tile between a host (ntiles, nq, npz, nd,
-// nd) array of the state's element type and the planes of q[0].
-int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaStream_t s, int max_ctas) {
+// Copy tracers [g0, g0+ng) of tiles [t0, t1) between a host (ntiles, nq,
+// npz, nd, nd) array of the state's element type and the planes of q[0].
+int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaStream_t s, int max_ctas, int t0 = 0,
+                 int t1 = -1) {
   const size_t es = st->esz, nd = (size_t)st->nd;
   const size_t hplane = nd * nd * es, dplane = (size_t)st->plane * es;
-  for (int t = 0; t < st->nt; ++t) {
+  if (t1 < 0) t1 = st->nt;
+  for (int t = t0; t < t1; ++t) {
     const long long p0 = ((long long)t * st->nq + g0) * st->npz;  // first plane of the group in tile t
     char* dev = (char*)st->q[0] + p0 * dplane;
     char* h = (char*)host + p0 * hplane;
@@ -1083,7 +1090,7 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
     if (!st->up) FV3G_CUDA(cudaStreamCreateWithPriority(&st->up, cudaStreamNonBlocking, greatest));
     if (!st->down) FV3G_CUDA(cudaStreamCreateWithPriority(&st->down, cudaStreamNonBlocking, greatest));
   }
-  const size_t need = 2 + 2 * (size_t)G;  // start, levels, then per group: uploaded, computed
+  const size_t need = 2 + (size_t)G * (1 + st->nt);  // start, levels, per group: uploaded, each tile remapped
   while (st->pev.size() < need + 1) {
     cudaEvent_t e;
     FV3G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1116,24 +1123,24 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
     int g0, ng;
     group(g, g0, ng);
     CHECK(q_group_copy(st, g0, ng, (void*)q_in, false, us, g == 0 ? 0 : kCopyCtas));
-    FV3G_CUDA(cudaEventRecord(st->pev[2 + 2 * g], us));
+    FV3G_CUDA(cudaEventRecord(st->pev[2 + g], us));
   }
   FV3G_CUDA(cudaStreamWaitEvent(cs, ev_lev, 0));
   CHECK(st->fp64 ? prologue_t<double>(st, q_split, cs) : prologue_t<float>(st, q_split, cs));
   for (int g = 0; g < G; ++g) {
     int g0, ng;
     group(g, g0, ng);
-    FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + 2 * g], 0));
-    if (st->fp64) {
-      CHECK(substeps_t<double>(st, q_split, g0, ng, cs));
-      CHECK(remap_t<double>(st, cs, g0, ng));
-    } else {
-      CHECK(substeps_t<float>(st, q_split, g0, ng, cs));
-      CHECK(remap_t<float>(st, cs, g0, ng));
+    FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + g], 0));
+    CHECK(st->fp64 ? substeps_t<double>(st, q_split, g0, ng, cs) : substeps_t<float>(st, q_split, g0, ng, cs));
+    // the remap runs tile by tile, each tile's download starting as soon as it is remapped, so only the
+    // last tile of the last group waits for its download at the end
+    for (int t = 0; t < st->nt; ++t) {
+      CHECK(st->fp64 ? remap_t<double>(st, cs, g0, ng, t, 1) : remap_t<float>(st, cs, g0, ng, t, 1));
+      cudaEvent_t done = st->pev[2 + G + (size_t)g * st->nt + t];
+      FV3G_CUDA(cudaEventRecord(done, cs));
+      FV3G_CUDA(cudaStreamWaitEvent(ds, done, 0));
+      CHECK(q_group_copy(st, g0, ng, q_out, true, ds, kCopyCtas, t, t + 1));
     }
-    FV3G_CUDA(cudaEventRecord(st->pev[3 + 2 * g], cs));
-    FV3G_CUDA(cudaStreamWaitEvent(ds, st->pev[3 + 2 * g], 0));
-    CHECK(q_group_copy(st, g0, ng, q_out, true, ds, kCopyCtas));
   }
   // join the three streams into the caller's
   FV3G_CUDA(cudaEventRecord(ev_end, ds));
