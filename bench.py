@@ -85,6 +85,47 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def op_ceiling(q_split: int, updates_per_s: float, sm_max_mhz):
+    """Secondary (compute) ceiling: the oracle's counted operations per update (tests/golden/op_counts.json,
+    written by tests/golden/make_golden.py) times the update rate, against the nominal FP32 (non-tensor)
+    rate of the GPU's SMs at their maximum clock."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "op_counts.json")) as f:
+            c = json.load(f)
+    except (OSError, ValueError):
+        return None
+    flops = q_split * c["flops_per_substep_cell"] + c["flops_per_remap_level"]
+    ops = q_split * c["ops_per_substep_cell"] + c["ops_per_remap_level"]
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
+    mhz = float(sm_max_mhz) if sm_max_mhz else 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12  # 128 FP32 lanes per SM, an FMA counted as two flops
+    achieved = updates_per_s * flops / 1e12
+    return {"flops_per_update": flops, "ops_per_update": ops, "achieved_tflops": achieved,
+            "achieved_tops": updates_per_s * ops / 1e12, "peak_tflops_fp32_nominal": peak,
+            "frac": achieved / peak,
+            "source": "oracle op-counting scalar: +,-,*,/ on tracer values (ops adds min/max/sign)",
+            "peak_kind": f"nominal: {sms} SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz"}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def committed_traffic(precision: str):
     """DRAM bytes of one substep (interior + edge-ring launches) at this workload from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "substep_kernel_C384L127x20.txt")
@@ -348,7 +389,7 @@ def run_reference(a, world, rank):
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": 1e3 * info["seconds"] / max(a.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": cfg,
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                              "sample": info["sample"] + " (C++ FP64 oracle, OpenMP; the upstream Fortran is absent)"},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -535,7 +576,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         rate, info = cpu_oracle_rate(a.n, 4, 2, a.q_split, a.cpu_seconds)
-        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+        cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port", "cpu_model": cpu_model(),
                "sample": info["sample"] + f", {info['seconds']:.1f} s (C++ FP64 oracle, OpenMP)"}
 
     if rank != 0:
@@ -556,6 +597,7 @@ def main():
                      "alg_bytes_per_substep": ab["substep"], "avg_substep_ms": sub_avg,
                      "launches_per_substep": sub_n / (a.steps * a.q_split), "peak_kind": peak_kind},
         "step_hbm": {"alg_bytes_per_update": ab["per_update"], "achieved_gbs": step_gbs, "frac": step_gbs / peak},
+        "step_ops": op_ceiling(a.q_split, value / world, (clocks or {}).get("sm_max_mhz")),
         "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern.items()},
         "gpu_launches": launches,
         "clocks": clocks,

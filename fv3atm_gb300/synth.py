@@ -187,6 +187,8 @@ def fill_cube_halo(x, n: int, ng: int, topo: np.ndarray):
     dst, src = _halo_index(n, ng, topo)
     nd = n + 2 * ng
     v = x.movedim(0, -3).reshape(*x.shape[1:-2], 6 * nd * nd)
+    if v.data_ptr() == x.data_ptr():  # the reshape returned a view (one plane per tile): work on a copy
+        v = v.clone()
     d = torch.as_tensor(dst, device=x.device)
     s = torch.as_tensor(src, device=x.device)
     v[..., d] = v[..., s]

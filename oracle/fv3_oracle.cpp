@@ -31,6 +31,37 @@ inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d
 inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
 inline double val(double a) { return a; }
 inline double val(const Dual& a) { return a.v; }
+// Op-counting scalar (for the flop ceiling of the measurement): every +, -,
+// *, / on it and every min / max / sign transfer is tallied in g_ops; a
+// negation and |.| are free (operand modifiers on the GPU).  Counting runs
+// are single-threaded.
+struct OpTally {
+  unsigned long long add = 0, mul = 0, div = 0, cmp = 0;
+};
+OpTally g_ops;
+struct Cnt {
+  double v;
+  Cnt() : v(0) {}
+  Cnt(double a) : v(a) {}
+};
+inline Cnt operator+(Cnt a, Cnt b) { ++g_ops.add; return Cnt(a.v + b.v); }
+inline Cnt operator-(Cnt a, Cnt b) { ++g_ops.add; return Cnt(a.v - b.v); }
+inline Cnt operator-(Cnt a) { return Cnt(-a.v); }
+inline Cnt operator*(Cnt a, Cnt b) { ++g_ops.mul; return Cnt(a.v * b.v); }
+inline Cnt operator/(Cnt a, Cnt b) { ++g_ops.div; return Cnt(a.v / b.v); }
+inline double val(const Cnt& a) { return a.v; }
+inline Cnt tmin(Cnt a, Cnt b) { ++g_ops.cmp; return b.v < a.v ? b : a; }
+inline Cnt tmax(Cnt a, Cnt b) { ++g_ops.cmp; return b.v > a.v ? b : a; }
+inline Cnt tabs(Cnt a) { return a.v < 0 ? Cnt(-a.v) : a; }
+inline Cnt tsign(Cnt a, Cnt b) { ++g_ops.cmp; return b.v < 0 ? Cnt(-std::fabs(a.v)) : Cnt(std::fabs(a.v)); }
+// ops done on the values of T (limiter tests), tallied for the counting scalar only
+template <class T> inline void tally(int, int, int) {}
+template <> inline void tally<Cnt>(int add, int mul, int cmp) {
+  g_ops.add += add;
+  g_ops.mul += mul;
+  g_ops.cmp += cmp;
+}
+
 template <class T> inline T tmin(T a, T b) { return val(b) < val(a) ? b : a; }
 template <class T> inline T tmax(T a, T b) { return val(b) > val(a) ? b : a; }
 template <class T> inline T tabs(T a) { return val(a) < 0 ? -a : a; }
@@ -55,6 +86,7 @@ template <class T> View2<T> v2(T* p, int ilo, int ihi, int jlo) { return View2<T
 // edge value on the overshooting side so that the parabola's extremum sits on
 // the opposite edge.
 template <class T> inline void cw84(T& bl, T& br) {
+  tally<T>(3, 4, 3);  // bl br, 3 (br - bl)(bl + br), (br - bl)^2, the tests and the -2 factor
   if (val(bl) * val(br) >= 0.0) {
     bl = T(0.0);
     br = T(0.0);
@@ -181,6 +213,7 @@ void ppm_line(int hord, double lim_fac, const T* x, const double* c, const doubl
       BR(m) = AL(m + 1) - X(m);
       if (hord == 5) smt[m - m0] = val(BL(m)) * val(BR(m)) < 0.0;
       else smt[m - m0] = std::fabs(lim_fac * val(BL(m) + BR(m))) < std::fabs(val(BL(m) - BR(m)));
+      tally<T>(hord == 5 ? 0 : 2, 1, 1);
     }
   }
 
@@ -188,6 +221,7 @@ void ppm_line(int hord, double lim_fac, const T* x, const double* c, const doubl
   for (int f = flo; f <= fhi; ++f) {
     double cf = c[f - flo];
     const bool high = hord == 8 || smt[f - 1 - m0] || smt[f - m0];
+    tally<T>(1, 0, 1);  // 1 -+ c and the upwind selection
     if (cf > 0.0) {
       T b0 = BL(f - 1) + BR(f - 1);
       flux[f - flo] = high ? X(f - 1) + T(1.0 - cf) * (BR(f - 1) - T(cf) * b0) : X(f - 1);
@@ -642,6 +676,33 @@ void orc_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int 
                   const double* mass, int nord, double damp_c) {
   fv_tp_2d_t<double>(q, crx, cry, npx, npy, hord, fx, fy, xfx, yfx, g, bd, ra_x, ra_y, lim_fac, mfx, mfy, mass, nord,
                      damp_c);
+}
+
+void orc_count_fv_tp_2d(const double* q, const double* crx, const double* cry, int npx, int npy, int hord,
+                        const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
+                        const double* ra_x, const double* ra_y, const double* mfx, const double* mfy,
+                        unsigned long long* counts) {
+  Dom d(bd);
+  std::vector<Cnt> qq(d.plane), fx(d.nmx), fy(d.nmy);
+  for (size_t n = 0; n < d.plane; ++n) qq[n] = Cnt(q[n]);
+  g_ops = OpTally{};
+  fv_tp_2d_t<Cnt>(qq.data(), crx, cry, npx, npy, hord, fx.data(), fy.data(), xfx, yfx, g, bd, ra_x, ra_y, 1.0, mfx,
+                  mfy, nullptr, 0, 0.0);
+  counts[0] = g_ops.add;
+  counts[1] = g_ops.mul;
+  counts[2] = g_ops.div;
+  counts[3] = g_ops.cmp;
+}
+
+void orc_count_remap_column(int km, const double* pe1, const double* q1, int kn, const double* pe2, int iv, int kord,
+                            unsigned long long* counts) {
+  std::vector<Cnt> c1(q1, q1 + km), c2(kn);
+  g_ops = OpTally{};
+  remap_column_t<Cnt>(km, pe1, c1.data(), 0.0, kn, pe2, c2.data(), iv, kord, 0.0);
+  counts[0] = g_ops.add;
+  counts[1] = g_ops.mul;
+  counts[2] = g_ops.div;
+  counts[3] = g_ops.cmp;
 }
 
 void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const double* cry, int npx,

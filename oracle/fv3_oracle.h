@@ -143,6 +143,16 @@ void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const
                      const double* ra_x, const double* ra_y, double lim_fac, const double* mfx,
                      const double* mfy, const double* mass, int nord, double damp_c);
 
+/* Operation counts (counts[0..3] = add/sub, mul, div, min/max/sign) of one
+ * fv_tp_2d call (q not modified) and of one column remap, on the tracer-valued
+ * quantities: the figure behind the flop ceiling of the measurement. */
+void orc_count_fv_tp_2d(const double* q, const double* crx, const double* cry, int npx, int npy, int hord,
+                        const double* xfx, const double* yfx, const orc_grid* g, const orc_bounds* bd,
+                        const double* ra_x, const double* ra_y, const double* mfx, const double* mfy,
+                        unsigned long long* counts);
+void orc_count_remap_column(int km, const double* pe1, const double* q1, int kn, const double* pe2, int iv,
+                            int kord, unsigned long long* counts);
+
 #ifdef __cplusplus
 }
 #endif

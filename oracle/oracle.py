@@ -128,6 +128,27 @@ def fv_tp_2d_tl(q, dq, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx=None, mfy
     return dfx, dfy
 
 
+def count_fv_tp_2d(q, crx, cry, hord, xfx, yfx, geom, ra_x, ra_y, mfx, mfy, ng: int = 3) -> dict:
+    """Operation counts of one fv_tp_2d call on one tile level (the counting scalar of the oracle)."""
+    q = _f64(q)
+    n = q.shape[-1] - 2 * ng
+    g = GridRef(geom)
+    arrs = [_f64(a) for a in (crx, cry, xfx, yfx, ra_x, ra_y, mfx, mfy)]
+    c = (C.c_ulonglong * 4)()
+    lib().orc_count_fv_tp_2d(_p(q), _p(arrs[0]), _p(arrs[1]), n + 1, n + 1, hord, _p(arrs[2]), _p(arrs[3]),
+                             C.byref(g.struct), C.byref(bounds_for(n, ng)), _p(arrs[4]), _p(arrs[5]), _p(arrs[6]),
+                             _p(arrs[7]), c)
+    return dict(zip(("add", "mul", "div", "cmp"), (int(v) for v in c)))
+
+
+def count_remap_column(pe1, q1, pe2, iv=0, kord=9) -> dict:
+    """Operation counts of the remap of one column (tracer-valued quantities only)."""
+    pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
+    c = (C.c_ulonglong * 4)()
+    lib().orc_count_remap_column(q1.shape[0], _p(pe1), _p(q1), pe2.shape[0] - 1, _p(pe2), iv, kord, c)
+    return dict(zip(("add", "mul", "div", "cmp"), (int(v) for v in c)))
+
+
 def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3, nord_tr=0, trdm=0.0,
               lim_fac=1.0):
     """Single-domain tracer_2d.  q (nq, npz, nd, nd).  Returns (q, dp1, mfx, mfy, cx, cy, nsplt)."""

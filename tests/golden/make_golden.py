@@ -79,9 +79,49 @@ def c48_bell_norms():
                        "norms_l1_l2_linf": list(_c48.norms(P, q, t))}, indent=1)
 
 
+def op_counts():
+    """Operation counts of the oracle's hord-8 fv_tp_2d on a C48 tile level and of its kord-9 remap of one
+    127-level column (the counting scalar), normalised per tracer-cell-level; bench.py reads the per-update
+    figures for its flop ceiling."""
+    import json
+    from fv3atm_gb300 import grid as G
+    from tests._helpers import area_fluxes, ra_xy
+    P = S.make_problem(48, 1, 1, seed=5, cmax=0.8)
+    t = 1
+    g = P.geoms[t]
+    cx, cy = P.cx[t, 0].numpy(), P.cy[t, 0].numpy()
+    xfx, yfx = area_fluxes(cx, cy, g)
+    rax, ray = ra_xy(xfx, yfx, g)
+    q = np.ascontiguousarray(P.q[t, 0, 0].numpy())
+    adv = O.count_fv_tp_2d(q, cx, cy, 8, xfx, yfx, g, rax, ray, P.mfx[t, 0].numpy(), P.mfy[t, 0].numpy())
+    km = 127
+    ak, bk = G.hybrid_levels(km)
+    rng = np.random.default_rng(1)
+    dp = (np.diff(ak) + np.diff(bk) * 1e5) * (1 + 0.1 * rng.uniform(-1, 1, km))
+    pe1 = np.concatenate([[ak[0]], ak[0] + np.cumsum(dp)])
+    pe2 = ak + bk * pe1[-1]
+    q1 = np.abs(rng.standard_normal(km)).cumsum() * 0.01
+    rem = O.count_remap_column(pe1, q1, pe2)
+    cells = 48 * 48
+    update = {"add": 4, "mul": 2, "div": 1, "cmp": 0}  # q <- (q dp1 + div F rarea) / dp2 per cell
+    per_cell = {k: (adv[k] + update[k] * cells) / cells for k in adv}
+    per_level = {k: rem[k] / km for k in rem}
+    flops = lambda d: d["add"] + d["mul"] + d["div"]
+    ops = lambda d: flops(d) + d["cmp"]
+    return json.dumps({
+        "what": "oracle op counts (add/sub, mul, div on tracer values; cmp = min/max/sign): fv_tp_2d hord 8 + the "
+                "flux-form update on one C48 tile level, and the kord-9 remap of one 127-level column",
+        "fv_tp_2d_c48": adv, "remap_column_l127": rem,
+        "per_tracer_cell_level_substep": per_cell, "per_tracer_column_level_remap": per_level,
+        "flops_per_substep_cell": flops(per_cell), "ops_per_substep_cell": ops(per_cell),
+        "flops_per_remap_level": flops(per_level), "ops_per_remap_level": ops(per_level)}, indent=1)
+
+
 if __name__ == "__main__":
     np.savez_compressed(os.path.join(HERE, "cube_c12_l2.npz"), **cube_fixture())
     np.savez_compressed(os.path.join(HERE, "remap_columns_l63.npz"), **remap_fixture())
     with open(os.path.join(HERE, "c48_bell_norms.json"), "w") as f:
         f.write(c48_bell_norms() + "\n")
+    with open(os.path.join(HERE, "op_counts.json"), "w") as f:
+        f.write(op_counts() + "\n")
     print("written")
