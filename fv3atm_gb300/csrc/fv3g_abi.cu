@@ -448,7 +448,10 @@ int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1, int t0 = 0,
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
   CHECK(launch_remap<T>(r, st->d.kord, s));
-  CHECK(mark(st, K_REMAP, s));
+  if (st->d.fill)  // Lagrangian_to_Eulerian's fillz of the remapped tracers
+    CHECK(launch_fillz_planes<T>(r.q_out, r.dp_out, st->n, ntl, st->npz, ng, r.sQt, r.sQq, r.sQk, r.sFt, r.sFk,
+                                 st->pg, s));
+  CHECK(mark(st, K_REMAP, s, st->d.fill ? 2 : 1));
   if (t0 + ntl == st->nt) {  // the last tile range of the field: the state now holds the remapped field
     st->q_cur = 0;
     st->remapped = true;

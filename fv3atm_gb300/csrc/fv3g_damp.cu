@@ -20,6 +20,8 @@
 // 3-cell halo holds nord <= 2 (upstream's limit without extra ghosting).
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "fv3g_stencil.cuh"
 
 namespace fv3g {
@@ -35,7 +37,8 @@ struct SmemDamp {
 
 template <typename T, int NORD, bool FLUXES>
 __global__ void __launch_bounds__(256) k_damp(const AdvArgs<T> a, int nbx) {
-  __shared__ SmemDamp<T> S;
+  extern __shared__ __align__(16) unsigned char damp_raw[];
+  SmemDamp<T>& S = *reinterpret_cast<SmemDamp<T>*>(damp_raw);
   const int t = blockIdx.z, k = blockIdx.y;
   const int bx = blockIdx.x % nbx, by = blockIdx.x / nbx;
   const int i0 = a.is + bx * TW, j0 = a.js + by * TW;
@@ -171,14 +174,39 @@ int launch_damp(const AdvArgs<T>& a, bool flux_mode, cudaStream_t s) {
   if (!flux_mode && (!a.q_out || !a.dp2)) return set_error(FV3G_E_ARG, "damping of q needs q_out and dp2");
   const int nbx = (a.ie - a.is + TW) / TW, nby = (a.je - a.js + TW) / TW;
   const dim3 grid((unsigned)(nbx * nby), (unsigned)a.npz, a.cube ? 6u : 1u);
+  constexpr size_t smem = sizeof(SmemDamp<T>);
   switch (a.nord * 2 + (flux_mode ? 1 : 0)) {
-    case 0: k_damp<T, 0, false><<<grid, 256, 0, s>>>(a, nbx); break;
-    case 1: k_damp<T, 0, true><<<grid, 256, 0, s>>>(a, nbx); break;
-    case 2: k_damp<T, 1, false><<<grid, 256, 0, s>>>(a, nbx); break;
-    case 3: k_damp<T, 1, true><<<grid, 256, 0, s>>>(a, nbx); break;
-    case 4: k_damp<T, 2, false><<<grid, 256, 0, s>>>(a, nbx); break;
-    default: k_damp<T, 2, true><<<grid, 256, 0, s>>>(a, nbx); break;
+    case 0: k_damp<T, 0, false><<<grid, 256, smem, s>>>(a, nbx); break;
+    case 1: k_damp<T, 0, true><<<grid, 256, smem, s>>>(a, nbx); break;
+    case 2: k_damp<T, 1, false><<<grid, 256, smem, s>>>(a, nbx); break;
+    case 3: k_damp<T, 1, true><<<grid, 256, smem, s>>>(a, nbx); break;
+    case 4: k_damp<T, 2, false><<<grid, 256, smem, s>>>(a, nbx); break;
+    default: k_damp<T, 2, true><<<grid, 256, smem, s>>>(a, nbx); break;
   }
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Tangent-linear damping fluxes (value/tangent pairs, flux mode) for the
+// tangent-linear and adjoint fv_tp_2d: del-2 only, whose stencil (the two
+// cells beside a face, no corner fill) lies inside the advection's.
+int launch_damp_tl(const AdvArgs<Dual<double>>& a, cudaStream_t s) {
+  if (a.nord != 0)
+    return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint fv_tp_2d damps with nord 0 only (got %d)",
+                     a.nord);
+  constexpr size_t smem = sizeof(SmemDamp<Dual<double>>);
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    err = cudaFuncSetAttribute(k_damp<Dual<double>, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+  });
+  if (err != cudaSuccess) return cuda_error(err, "cudaFuncSetAttribute(k_damp)");
+  if (!a.del6_u || !a.del6_v || !a.fx_out || !a.fy_out || (a.damp_mass && !a.dp1))
+    return set_error(FV3G_E_ARG, "tangent-linear damping needs del6_u, del6_v, flux planes and the mass");
+  const int nbx = (a.ie - a.is + TW) / TW, nby = (a.je - a.js + TW) / TW;
+  const dim3 grid((unsigned)(nbx * nby), (unsigned)a.npz, 1u);
+  k_damp<Dual<double>, 0, true><<<grid, 256, smem, s>>>(a, nbx);
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }

@@ -196,6 +196,7 @@ void prepare_substep_hord(cudaError_t& err);
 // tile-edge fluxes; runs after the substep kernel on the same stream.
 template <typename T>
 int launch_damp(const AdvArgs<T>& a, bool flux_mode, cudaStream_t s);
+int launch_damp_tl(const AdvArgs<Dual<double>>& a, cudaStream_t s);  // nord 0, flux mode
 // damp = (damp_c da_min)^(nord+1), as the product upstream's integer power is
 double damp_coefficient(double damp_c, double da_min, int nord);
 

@@ -123,9 +123,48 @@ int check_tp_args(const fv3g_bounds* bd, int npx, int npy, int hord, const fv3g_
   if (hord != 1 && hord != 5 && hord != 8)
     return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", hord);
   if (hord == 1 && !(lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", lim_fac);
-  if (damp_c > 1e-4 && (mfx == nullptr || mass != nullptr))
-    return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint fv_tp_2d has no tracer damping (damp_c=%g)",
-                     damp_c);
+  return 0;
+}
+
+// Damping of the tangent-linear / adjoint fv_tp_2d (as upstream: damp_c > 1e-4,
+// with mass fluxes only if mass is given): del-2 only.
+int check_tp_damping(bool damping, int nord, const fv3g_grid* grid) {
+  if (!damping) return 0;
+  if (nord != 0)
+    return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint fv_tp_2d damps with nord 0 only (got %d)",
+                     nord);
+  if (!grid->del6_u || !grid->del6_v) return set_error(FV3G_E_ARG, "tracer damping needs grid del6_u and del6_v");
+  if (!(grid->da_min > 0.0)) return set_error(FV3G_E_ARG, "tracer damping needs grid da_min > 0");
+  return 0;
+}
+
+// The frozen damping inputs (del6_u, del6_v, mass) as value planes with zero
+// tangent, and the damping arguments of the tangent-linear launch.
+int damping_args(AdvArgs<D2>& ad, D2* d6u, D2* d6v, D2* dms, double* stage, const PlaneGeom& pg,
+                 const fv3g_bounds* bd, const fv3g_grid* grid, const double* mfx, const double* mass, double damp_c,
+                 cudaStream_t s) {
+  const long long P = pg.plane();
+  const int isd = bd->isd, ied = bd->ied, jsd = bd->jsd, jed = bd->jed;
+  struct Item {
+    D2* dst;
+    const double* src;
+    int ihi, jhi;
+  } items[] = {{d6u, grid->del6_u, ied, jed + 1},
+               {d6v, grid->del6_v, ied + 1, jed},
+               {dms, mfx ? mass : nullptr, ied, jed}};
+  for (const Item& it : items) {
+    if (!it.src) continue;
+    FV3G_CUDA(cudaMemsetAsync(stage, 0, sizeof(double) * P, s));
+    CHECK(h2d_planes(stage, pg, it.src, isd, it.ihi, jsd, it.jhi, 1, s));
+    k_pack_dual<<<grid_1d(P), 256, 0, s>>>(it.dst, stage, nullptr, P);
+    FV3G_CUDA(cudaGetLastError());
+  }
+  ad.del6_u = d6u;
+  ad.del6_v = d6v;
+  ad.damp = D2(damp_coefficient(damp_c, grid->da_min, 0));
+  ad.nord = 0;
+  ad.damp_mass = mfx != nullptr;
+  ad.dp1 = mfx ? dms : nullptr;
   return 0;
 }
 
@@ -309,19 +348,21 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
                      const double* yfx, const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x,
                      const double* ra_y, double lim_fac, const double* mfx, const double* mfy, const double* mass,
                      int nord, double damp_c) {
-  (void)nord;
   CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, mfx, mass, damp_c));
+  const bool damping = damp_c > 1e-4 && (mfx == nullptr || mass != nullptr);
+  CHECK(check_tp_damping(damping, nord, grid));
   if (!q || !q_tl || !crx || !cry || !xfx || !yfx || !ra_x || !ra_y || !fx_tl || !fy_tl)
     return set_error(FV3G_E_ARG, "null array argument");
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
-  CHECK(g_ctx.begin(3 * padded(P, 8) + 14 * padded(P, 16)));
+  CHECK(g_ctx.begin(3 * padded(P, 8) + 17 * padded(P, 16)));
   cudaStream_t s = g_ctx.stream;
   double *stage = g_ctx.take<double>(P), *qv = g_ctx.take<double>(P), *qd = g_ctx.take<double>(P);
   FrozenTp f;
   D2** slots[] = {&f.cx, &f.cy, &f.xf, &f.yf, &f.rx, &f.ry, &f.mx, &f.my, &f.dxa, &f.dya, &f.area};
   for (D2** sl : slots) *sl = g_ctx.take<D2>(P);
   D2 *dq = g_ctx.take<D2>(P), *dfx = g_ctx.take<D2>(P), *dfy = g_ctx.take<D2>(P);
+  D2 *d6u = g_ctx.take<D2>(P), *d6v = g_ctx.take<D2>(P), *dms = g_ctx.take<D2>(P);
   FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
   CHECK(upload_frozen(f, stage, pg, bd, crx, cry, xfx, yfx, ra_x, ra_y, mfx, mfy, grid, s));
   CHECK(h2d_planes(qv, pg, q, bd->isd, bd->ied, bd->jsd, bd->jed, 1, s));
@@ -336,6 +377,11 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
   a.fx_out = dfx;
   a.fy_out = dfy;
   CHECK(launch_substep_tl(a, hord, s));
+  if (damping) {
+    AdvArgs<D2> ad = a;
+    CHECK(damping_args(ad, d6u, d6v, dms, stage, pg, bd, grid, mfx, mass, damp_c, s));
+    CHECK(launch_damp_tl(ad, s));
+  }
   double* out_v = qv;
   double* out_d = qd;
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je;
@@ -356,14 +402,15 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
                      double* fx_ad, double* fy_ad, const double* xfx, const double* yfx, const fv3g_grid* grid,
                      const fv3g_bounds* bd, const double* ra_x, const double* ra_y, double lim_fac,
                      const double* mfx, const double* mfy, const double* mass, int nord, double damp_c) {
-  (void)nord;
   CHECK(check_tp_args(bd, npx, npy, hord, grid, lim_fac, mfx, mass, damp_c));
+  const bool damping = damp_c > 1e-4 && (mfx == nullptr || mass != nullptr);
+  CHECK(check_tp_damping(damping, nord, grid));
   if (!q || !q_ad || !crx || !cry || !xfx || !yfx || !ra_x || !ra_y || !fx_ad || !fy_ad)
     return set_error(FV3G_E_ARG, "null array argument");
   constexpr int NC = 42;  // colours per input: 7 x 6
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
-  CHECK(g_ctx.begin(7 * padded(P, 8) + 11 * padded(P, 16) + 4 * padded(P * NC, 16)));
+  CHECK(g_ctx.begin(7 * padded(P, 8) + 14 * padded(P, 16) + 4 * padded(P * NC, 16)));
   cudaStream_t s = g_ctx.stream;
   double *stage = g_ctx.take<double>(P), *qx = g_ctx.take<double>(P), *qy = g_ctx.take<double>(P);
   double *fxa = g_ctx.take<double>(P), *fya = g_ctx.take<double>(P), *gx = g_ctx.take<double>(P);
@@ -372,6 +419,7 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
   D2** slots[] = {&f.cx, &f.cy, &f.xf, &f.yf, &f.rx, &f.ry, &f.mx, &f.my, &f.dxa, &f.dya, &f.area};
   for (D2** sl : slots) *sl = g_ctx.take<D2>(P);
   D2 *in_x = g_ctx.take<D2>(P * NC), *in_y = g_ctx.take<D2>(P * NC), *fl = g_ctx.take<D2>(P * NC * 2);
+  D2 *d6u = g_ctx.take<D2>(P), *d6v = g_ctx.take<D2>(P), *dms = g_ctx.take<D2>(P);
   FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
   CHECK(upload_frozen(f, stage, pg, bd, crx, cry, xfx, yfx, ra_x, ra_y, mfx, mfy, grid, s));
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
@@ -395,6 +443,10 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
   a.lim_fac = lim_fac;
   a.fx_out = fl;
   a.fy_out = fl + P * NC;
+  // the del-2 damping reads the y-sweep input's strip and interior cells (the two cells beside each face),
+  // inside the boxes the gather below reads for that input
+  AdvArgs<D2> ad = a;
+  if (damping) CHECK(damping_args(ad, d6u, d6v, dms, stage, pg, bd, grid, mfx, mass, damp_c, s));
   for (int pass = 0; pass < 2; ++pass) {  // 0: x-sweep input, 1: y-sweep input
     const int px = pass == 0 ? 7 : 6, py = pass == 0 ? 6 : 7;
     const long long n = (long long)P * NC;
@@ -403,6 +455,7 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
     FV3G_CUDA(cudaGetLastError());
     FV3G_CUDA(cudaMemsetAsync(fl, 0, sizeof(D2) * P * NC * 2, s));
     CHECK(launch_substep_tl(a, hord, s));
+    if (damping) CHECK(launch_damp_tl(ad, s));
     // face boxes holding a cell: x input fx [i-2, i+3] x {j}, fy [i-3, i+3] x [j-2, j+3];
     // y input fx [i-2, i+3] x [j-3, j+3], fy {i} x [j-2, j+3]
     const FaceBox bxf = pass == 0 ? FaceBox{-2, 3, 0, 0} : FaceBox{-2, 3, -3, 3};

@@ -171,8 +171,8 @@ int fv3g_fv_tp_2d_tl(const double* q, const double* q_tl, const double* crx, con
 
 /* fv_tp_2d adjoint at trajectory q: q_ad (isd:ied, jsd:jed) += J^T (fx_ad, fy_ad);
  * fx_ad (is:ie+1, js:je) and fy_ad (is:ie, js:je+1) are set to zero.
- * Damping (damp_c > 1e-4 where it applies) is not differentiated here:
- * both entries return FV3G_E_UNSUPPORTED for it. */
+ * Damping (damp_c > 1e-4 where it applies) is differentiated for nord 0
+ * (del-2); higher orders return FV3G_E_UNSUPPORTED. */
 int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const double* cry, int npx, int npy,
                      int hord, double* fx_ad, double* fy_ad, const double* xfx, const double* yfx,
                      const fv3g_grid* grid, const fv3g_bounds* bd, const double* ra_x, const double* ra_y,
@@ -241,6 +241,7 @@ typedef struct {
   int nord_tr;    /* tracer damping order 0..2 (del-2(nord_tr+1)) */
   double trdm;    /* damping coefficient; > 1e-4 damps the first substep (needs the grid's del6_u/v) */
   double lim_fac; /* hord 1 filter factor; 0 means 1 */
+  int fill;       /* 1: fillz the remapped tracers in every remap (fv_core_nml fill) */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */

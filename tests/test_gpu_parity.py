@@ -313,6 +313,27 @@ def test_errors_are_reported_not_fatal(cuda, cube_prob):
         api.CubeState(P.n, P.npz, P.nq, kord=7)
 
 
+def test_step_with_fill_matches_oracle_remap_then_fillz(cuda, cube_prob):
+    """desc.fill: the remap of the step is followed by fillz, as Lagrangian_to_Eulerian does with fill on.
+    hord 5 (unlimited) leaves undershoots below zero next to the clipped bells, which fillz removes."""
+    P = cube_prob
+    q1, dp_last, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=5, q_split=3)
+    dpf = final_dp(dp_last, P.mfx.numpy(), P.mfy.numpy(), P.geoms, ns, P.n)
+    q2, dp2, _, _ = remap_reference(q1, dpf, P.ak, P.bk, P.n)
+    n, s = P.n, slice(3, 3 + P.n)
+    assert (q2[..., s, s] < 0).any()  # the case exercises the filler
+    # oracle fillz on every interior column: (im, km, nq) with i fastest
+    qc = np.ascontiguousarray(q2[..., s, s].transpose(1, 2, 0, 3, 4).reshape(P.nq, P.npz, -1))
+    dpc = np.ascontiguousarray(dp2.transpose(1, 0, 2, 3).reshape(P.npz, -1))  # interior columns only
+    qf = O.fillz(qc, dpc)
+    st = api.CubeState(P.n, P.npz, P.nq, precision="fp64", hord=5, fill=True)
+    st.load_problem(P)
+    st.step(3)
+    got = st.download("Q_REMAPPED")[..., s, s].transpose(1, 2, 0, 3, 4).reshape(P.nq, P.npz, -1)
+    assert rel_l2(got, qf) <= FP64_TOL
+    st.close()
+
+
 @pytest.mark.parametrize("precision,groups", [("mixed", 1), ("mixed", 2), ("mixed", 3), ("fp64", 2)])
 def test_step_host_pipelined_equals_device_step(cuda, cube_prob, precision, groups):
     """fv3g_step_host (host arrays in and out, tracer groups overlapping their transfers with the compute)

@@ -90,8 +90,9 @@ def test_fv_tp_2d_tl_matches_oracle(cuda, tile_prob, hord):
     assert rel_l2(fx, ffx) <= TL_TOL and rel_l2(fy, ffy) <= TL_TOL  # the trajectory fluxes
 
 
-def test_fv_tp_2d_tl_is_linear_and_rejects_damping(cuda, tile_prob):
-    """hord 5's 2-dx filter is frozen at the trajectory, so the tangent-linear model is a linear map."""
+def test_fv_tp_2d_tl_is_linear_and_rejects_higher_order_damping(cuda, tile_prob):
+    """hord 5's 2-dx filter is frozen at the trajectory, so the tangent-linear model is a linear map; its
+    damping is del-2 only."""
     d = _inputs(tile_prob)
     rng = np.random.default_rng(2)
     x, y = rng.standard_normal(d["q"].shape), rng.standard_normal(d["q"].shape)
@@ -100,10 +101,39 @@ def test_fv_tp_2d_tl_is_linear_and_rejects_damping(cuda, tile_prob):
         assert rel_l2(tz[c], 2.0 * tx[c] - 3.0 * ty[c]) <= TL_TOL
     from fv3atm_gb300._lib import Fv3gError
     n = d["n"]
-    with pytest.raises(Fv3gError, match="damping"):
+    with pytest.raises(Fv3gError, match="nord 0 only"):
         api.fv_tp_2d_tl(d["q"], x, d["cx"], d["cy"], n + 1, n + 1, 8, None, np.zeros((n, n + 1)), None,
                         np.zeros((n + 1, n)), d["xfx"], d["yfx"], api.GridStruct(d["g"]), api.bounds_for(n), d["rax"],
-                        d["ray"], 1.0, d["mfx"], d["mfy"], np.ones_like(d["q"]), 0, 0.1)
+                        d["ray"], 1.0, d["mfx"], d["mfy"], np.ones_like(d["q"]), 1, 0.1)
+
+
+@pytest.mark.parametrize("with_mfx", [True, False])
+def test_fv_tp_2d_tl_ad_with_del2_damping(cuda, tile_prob, with_mfx):
+    """damp_c > 1e-4, nord 0: the tangent-linear fluxes equal the oracle's (damping included, mass-weighted
+    with mass fluxes), and the adjoint passes the dot-product test."""
+    d = _inputs(tile_prob, t=4, k=2, iq=1, smooth=True)
+    n = d["n"]
+    mass = np.ascontiguousarray(tile_prob.dp[4, 2].numpy())
+    mx, my = (d["mfx"], d["mfy"]) if with_mfx else (None, None)
+    rng = np.random.default_rng(11)
+    dq = rng.standard_normal(d["q"].shape)
+    gs = api.GridStruct(d["g"])
+    fx, fxt, fy, fyt = np.zeros((n, n + 1)), np.zeros((n, n + 1)), np.zeros((n + 1, n)), np.zeros((n + 1, n))
+    api.fv_tp_2d_tl(d["q"], dq, d["cx"], d["cy"], n + 1, n + 1, 8, fx, fxt, fy, fyt, d["xfx"], d["yfx"], gs,
+                    api.bounds_for(n), d["rax"], d["ray"], 1.0, mx, my, mass, 0, 0.12)
+    rfx, rfy = O.fv_tp_2d_tl(d["q"], dq, d["cx"], d["cy"], 8, d["xfx"], d["yfx"], d["g"], d["rax"], d["ray"], mx,
+                             my, mass=mass, nord=0, damp_c=0.12)
+    r0x, _ = O.fv_tp_2d_tl(d["q"], dq, d["cx"], d["cy"], 8, d["xfx"], d["yfx"], d["g"], d["rax"], d["ray"], mx, my)
+    assert rel_l2(rfx, r0x) > 1e-6  # the damping is visible at this tolerance
+    assert rel_l2(fxt, rfx) <= TL_TOL and rel_l2(fyt, rfy) <= TL_TOL
+    wx, wy = rng.standard_normal((n, n + 1)), rng.standard_normal((n + 1, n))
+    q_ad = np.zeros_like(d["q"])
+    fx_ad, fy_ad = wx.copy(), wy.copy()
+    api.fv_tp_2d_ad(d["q"], q_ad, d["cx"], d["cy"], n + 1, n + 1, 8, fx_ad, fy_ad, d["xfx"], d["yfx"], gs,
+                    api.bounds_for(n), d["rax"], d["ray"], 1.0, mx, my, mass, 0, 0.12)
+    lhs = float((fxt * wx).sum() + (fyt * wy).sum())
+    rhs = float((q_ad * dq).sum())
+    assert abs(lhs - rhs) <= DOT_TOL * abs(lhs), (lhs, rhs)
 
 
 @pytest.mark.parametrize("hord", [1, 5, 8])
