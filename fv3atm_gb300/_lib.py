@@ -24,7 +24,7 @@ EXPORTS = (
     "fv3g_tracer_2d_batched", "fv3g_remap_batched", "fv3g_step", "fv3g_mass_sum", "fv3g_state_error",
     "fv3g_field_info", "fv3g_upload_async", "fv3g_download_async", "fv3g_stream_sync", "fv3g_set_timing",
     "fv3g_kernel_times", "fv3g_remap_columns_noalloc", "fv3g_fv_tp_2d_tl", "fv3g_fv_tp_2d_ad", "fv3g_map1_ppm_tl",
-    "fv3g_map1_ppm_ad", "fv3g_state_autotune", "fv3g_state_widths", "fv3g_step_host", "fv3g_ensemble_create", "fv3g_ensemble_step",
+    "fv3g_map1_ppm_ad", "fv3g_state_autotune", "fv3g_state_widths", "fv3g_step_host", "fv3g_tracer_2d_1L", "fv3g_ensemble_create", "fv3g_ensemble_step",
     "fv3g_ensemble_destroy", "fv3g_fillz", "fv3g_pressure_vars", "fv3g_fillz_batched",
 )
 

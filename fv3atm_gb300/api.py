@@ -76,6 +76,22 @@ def tracer_2d(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, npx,
     return nsplt.value
 
 
+def tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, npx, npy, npz, nq, hord, q_split,
+                 dt, nord_tr=0, trdm=0.0, lim_fac=1.0, halo_update=None) -> int:
+    """tracer_2d_1L: levels advanced one at a time with their own substep counts; returns the largest."""
+    shape = q.shape
+    cb = _lib.HALO_FN()
+    if halo_update is not None:
+        def _cb(ptr, nq_, npz_, ctx):
+            halo_update(np.ctypeslib.as_array(ptr, shape=shape))
+        cb = _lib.HALO_FN(_cb)
+    nsplt = C.c_int(0)
+    _lib.call("fv3g_tracer_2d_1L", _p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(gridstruct.struct),
+              C.byref(bd), npx, npy, npz, nq, hord, q_split, C.c_double(dt), nord_tr, C.c_double(trdm),
+              C.c_double(lim_fac), cb, None, C.byref(nsplt))
+    return nsplt.value
+
+
 def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min) -> None:
     _lib.call("fv3g_map_scalar", km, _p(pe1), _p(q1), _p(qs), kn, _p(pe2), _p(q2), i1, i2, j, ibeg, iend, jbeg, jend,
               iv, kord, C.c_double(q_min))

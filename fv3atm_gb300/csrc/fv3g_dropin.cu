@@ -136,10 +136,13 @@ int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int 
   return 0;
 }
 
-int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const fv3g_grid* grid,
-                   const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
-                   int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out) {
-  (void)dt;
+// tracer_2d (one substep count for all levels) or, per_level, tracer_2d_1L
+// (each level with its own count from its own Courant maximum, its fluxes
+// scaled by its own 1/nsplt, halos refreshed before each of its substeps).
+static int tracer_2d_impl(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                          const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord,
+                          int q_split, int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn,
+                          void* halo_ctx, int* nsplt_out, bool per_level) {
   CHECK(check_bounds(bd, npx, npy));
   if (!q || !dp1 || !mfx || !mfy || !cx || !cy || !grid) return set_error(FV3G_E_ARG, "null array argument");
   if (!grid->dx || !grid->dy || !grid->dxa || !grid->dya || !grid->area || !grid->rarea || !grid->sin_sg)
@@ -184,6 +187,95 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   if (damping) {
     CHECK(h2d_planes(d6u, pg, grid->del6_u, isd, ied, jsd, jed + 1, 1, s));
     CHECK(h2d_planes(d6v, pg, grid->del6_v, isd, ied + 1, jsd, jed, 1, s));
+  }
+
+  if (per_level) {
+    const int nif = ie - is + 2, njd = jed - jsd + 1, nid = ied - isd + 1, njf = je - js + 2;
+    const size_t hplane = (size_t)nid * njd;
+    std::vector<int> ns(npz);
+    int nmax = 1;
+    for (int k = 0; k < npz; ++k) {  // the level's Courant maximum over the compute domain
+      double cmax = 0.0;
+      for (int j = js; j <= je; ++j)
+        for (int i = is; i <= ie; ++i) {
+          cmax = std::max(cmax, std::fabs(cx[(size_t)(i - is) + (size_t)(j - jsd) * nif + (size_t)k * nif * njd]));
+          cmax = std::max(cmax, std::fabs(cy[(size_t)(i - isd) + (size_t)(j - js) * nid + (size_t)k * nid * njf]));
+        }
+      if (!std::isfinite(cmax)) return set_error(FV3G_E_NONFINITE, "non-finite Courant number (level %d)", k + 1);
+      ns[k] = q_split > 0 ? q_split : (int)(1.0 + cmax);
+      if (ns[k] > 64)
+        return set_error(FV3G_E_COURANT, "Courant number too large (level %d: nsplt=%d > 64)", k + 1, ns[k]);
+      nmax = std::max(nmax, ns[k]);
+    }
+    if (nsplt_out) *nsplt_out = nmax;
+    const long long PL = (long long)P;
+    for (int k = 0; k < npz; ++k) {
+      const long long ko = (long long)k * PL;
+      const double frac = (ns[k] == 1) ? 1.0 : 1.0 / ns[k];
+      CHECK(launch_area_flux<double>(dcx + ko, dcy + ko, dxf + ko, dyf + ko, dmx + ko, dmy + ko, ddxa, ddya, ddx,
+                                     ddy, dsin, 0, PL, 0, PL, pg, is, ie, js, je, 1, 1, frac, s));
+      int dpi = 0, dp_start = 0;
+      for (int it = 0; it < ns[k]; ++it) {
+        if (halo_fn) {  // the caller refreshes halos; only this level's planes change meanwhile
+          for (int iq = 0; iq < nq; ++iq)
+            CHECK(d2h_planes(q + ((size_t)iq * npz + k) * hplane, qa + ((long long)iq * npz + k) * PL, pg, isd, ied,
+                             jsd, jed, 1, s));
+          FV3G_CUDA(cudaStreamSynchronize(s));
+          halo_fn(q, nq, npz, halo_ctx);
+          for (int iq = 0; iq < nq; ++iq)
+            CHECK(h2d_planes(qa + ((long long)iq * npz + k) * PL, pg, q + ((size_t)iq * npz + k) * hplane, isd, ied,
+                             jsd, jed, 1, s));
+        }
+        const int dpo = (dpi == 1) ? 2 : 1;
+        AdvArgs<double> a{};
+        a.q_in = qa + ko; a.q_out = qb + ko;
+        a.sQk = PL; a.sQq = PL * npz; a.sQt = 0;
+        a.cx = dcx + ko; a.cy = dcy + ko; a.xfx = dxf + ko; a.yfx = dyf + ko; a.mfx = dmx + ko; a.mfy = dmy + ko;
+        a.dp1 = dpb[dpi] + ko; a.dp2 = dpb[dpo] + ko;
+        a.sFk = PL; a.sFt = 0;
+        a.area = dar; a.rarea = drar; a.dxa = ddxa; a.dya = ddya; a.sMt = 0;
+        a.pg = pg;
+        a.is = is; a.ie = ie; a.js = js; a.je = je;
+        a.npx = npx; a.npy = npy;
+        a.nq = nq; a.npz = 1;
+        a.corners = corner_mask(grid);
+        a.nested = grid->nested;
+        a.cube = 0;
+        a.lim_fac = lim_fac;
+        CHECK(launch_substep<double>(a, hord, false, std::min(nq, 4), s));
+        if (damping && it == 0) {
+          a.del6_u = d6u;
+          a.del6_v = d6v;
+          a.damp = damp_coefficient(trdm, grid->da_min, nord_tr);
+          a.nord = nord_tr;
+          a.damp_mass = 1;
+          CHECK(launch_damp<double>(a, false, s));
+        }
+        // the level's updated compute domain, every tracer, back into the halo-carrying buffer
+        const size_t pitch = (size_t)pg.pitch * 8, slice = (size_t)PL * npz * 8;
+        CHECK(copy_planes(qa + ko + pg.at(is, js), pitch, slice, qb + ko + pg.at(is, js), pitch, slice,
+                          (size_t)(ie - is + 1) * 8, je - js + 1, nq, cudaMemcpyDeviceToDevice, s));
+        dp_start = dpi;
+        dpi = dpo;
+      }
+      // this level's dp1: the thickness at the start of its last substep (compute domain)
+      const int ni = ie - is + 1, nj = je - js + 1;
+      CHECK(copy_planes(dp1 + k * hplane + (is - isd) + (size_t)(js - jsd) * nid, (size_t)nid * 8, hplane * 8,
+                        dpb[dp_start] + ko + pg.at(is, js), (size_t)pg.pitch * 8, (size_t)PL * 8, (size_t)ni * 8, nj,
+                        1, cudaMemcpyDeviceToHost, s));
+    }
+    if (!grid->nested && corner_mask(grid)) {
+      const long long np = (long long)nqp;
+      k_corners<<<(unsigned)((np * 36 + 255) / 256), 256, 0, s>>>(qa, pg, npx, npy, corner_mask(grid), 1, np);
+      FV3G_CUDA(cudaGetLastError());
+    }
+    CHECK(d2h_planes(q, qa, pg, isd, ied, jsd, jed, (long long)nqp, s));
+    CHECK(d2h_planes(cx, dcx, pg, is, ie + 1, jsd, jed, npz, s));
+    CHECK(d2h_planes(cy, dcy, pg, isd, ied, js, je + 1, npz, s));
+    CHECK(d2h_planes(mfx, dmx, pg, is, ie + 1, js, je, npz, s));
+    CHECK(d2h_planes(mfy, dmy, pg, is, ie, js, je + 1, npz, s));
+    FV3G_CUDA(cudaStreamSynchronize(s));
+    return 0;
   }
 
   int nsplt = q_split;
@@ -263,6 +355,23 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   CHECK(d2h_planes(mfy, dmy, pg, is, ie, js, je + 1, npz, s));
   FV3G_CUDA(cudaStreamSynchronize(s));
   return 0;
+}
+
+int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const fv3g_grid* grid,
+                   const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
+                   int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out) {
+  (void)dt;
+  return tracer_2d_impl(q, dp1, mfx, mfy, cx, cy, grid, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm,
+                        lim_fac, halo_fn, halo_ctx, nsplt_out, false);
+}
+
+int fv3g_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                      const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord,
+                      int q_split, double dt, int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn,
+                      void* halo_ctx, int* nsplt_out) {
+  (void)dt;
+  return tracer_2d_impl(q, dp1, mfx, mfy, cx, cy, grid, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm,
+                        lim_fac, halo_fn, halo_ctx, nsplt_out, true);
 }
 
 static int map_common(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,

@@ -123,6 +123,20 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
                    int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
                    fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out);
 
+/* tracer_2d_1L (fv_tracer2d.F90; used with fv_core_nml z_tracer): as
+ * fv3g_tracer_2d, but the levels are advanced one at a time, each with its
+ * own substep count (q_split > 0, or 1 + that level's Courant maximum) and its
+ * cx, cy, mfx, mfy scaled by its own 1/nsplt; halo_fn runs before every
+ * substep of every level (only that level's planes change in between).
+ * nsplt_out receives the largest count.
+ * Replaces: tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, gridstruct, bd, domain,
+ *           npx, npy, npz, nq, hord, q_split, dt, id_divg, q_pack, dp1_pack,
+ *           nord_tr, trdm, lim_fac). */
+int fv3g_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                      const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq,
+                      int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
+                      fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out);
+
 /* map_scalar (fv_mapz.F90): remap row j of a 3-D field, FP64.
  *   pe1 (i1:i2, km+1)  pe2 (i1:i2, kn+1)  qs (i1:i2)
  *   q1 (ibeg:iend, jbeg:jend, km) in    q2 (ibeg:iend, jbeg:jend, kn) inout

@@ -762,6 +762,53 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
   return nsplt;
 }
 
+// tracer_2d_1L: the levels one at a time, each with its own substep count
+// from its own Courant maximum (or q_split), its fluxes scaled by its own
+// 1/nsplt; the halo callback runs before every substep of every level.
+int orc_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
+                     const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
+                     int nord_tr, double trdm, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx,
+                     int* nsplt_levels) {
+  (void)dt;
+  Dom d(bd);
+  std::vector<double> fx(d.nmx), fy(d.nmy);
+  int nmax = 0;
+  for (int k = 0; k < npz; ++k) {
+    double *cxk = cx + k * d.nxf, *cyk = cy + k * d.nyf, *mxk = mfx + k * d.nmx, *myk = mfy + k * d.nmy;
+    double* dpk = dp1 + k * d.plane;
+    Level L;
+    L.xfx.assign(d.nxf, 0.0);
+    L.yfx.assign(d.nyf, 0.0);
+    area_fluxes(cxk, cyk, L.xfx.data(), L.yfx.data(), g, bd);
+    const int nsplt = q_split > 0 ? q_split : (int)(1.0 + max_courant(cxk, cyk, d, 1));
+    if (nsplt != 1) {
+      const double frac = 1.0 / nsplt;
+      scale_fluxes(mxk, myk, cxk, cyk, d, 1, frac);
+      for (auto& v : L.xfx) v *= frac;
+      for (auto& v : L.yfx) v *= frac;
+    }
+    for (int it = 0; it < nsplt; ++it) {
+      if (halo_fn) halo_fn(q, nq, npz, halo_ctx);
+      level_setup(L, dpk, mxk, myk, g, d);
+      for (int iq = 0; iq < nq; ++iq) {
+        double* qk = q + ((size_t)iq * npz + k) * d.plane;
+        fv_tp_2d_t<double>(qk, cxk, cyk, npx, npy, hord, fx.data(), fy.data(), L.xfx.data(), L.yfx.data(), g, bd,
+                           L.rax.data(), L.ray.data(), lim_fac, mxk, myk, dpk, nord_tr, it == 0 ? trdm : 0.0);
+        flux_update(qk, dpk, L, fx.data(), fy.data(), g, d);
+      }
+      if (it < nsplt - 1) {
+        View2<double> DP{dpk, d.isd, d.jsd, d.nid};
+        View2<const double> D2{L.dp2.data(), d.isd, d.jsd, d.nid};
+        for (int j = d.js; j <= d.je; ++j)
+          for (int i = d.is; i <= d.ie; ++i) DP(i, j) = D2(i, j);
+      }
+    }
+    if (nsplt_levels) nsplt_levels[k] = nsplt;
+    nmax = std::max(nmax, nsplt);
+  }
+  return nmax;
+}
+
 // Edge halo strips of six tiles from their neighbours' interiors.
 void orc_cube_halo_fill(double* q, int n, int ng, int nplanes, const int* topo) {
   const int nid = n + 2 * ng;

@@ -87,6 +87,15 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
                   int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
                   orc_halo_fn halo_fn, void* halo_ctx);
 
+/* tracer_2d_1L: the levels one at a time, each with its own substep count
+ * (q_split > 0, or 1 + the level's Courant maximum) and its fluxes scaled by
+ * its own 1/nsplt; halo_fn runs before every substep of every level.
+ * nsplt_levels (npz, may be NULL) receives the counts; returns their maximum. */
+int orc_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                     const orc_grid* g, const orc_bounds* bd, int npx, int npy, int npz, int nq,
+                     int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
+                     orc_halo_fn halo_fn, void* halo_ctx, int* nsplt_levels);
+
 /* Fill the edge halo strips of six tiles (all levels/tracers stacked in nplanes
  * planes of (isd:ied, jsd:jed) per tile; tile stride = nplanes planes). */
 void orc_cube_halo_fill(double* q, int n, int ng, int nplanes, const int* topo);

@@ -164,6 +164,23 @@ def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, n
     return q, dp1, mfx, mfy, cx, cy, nsplt
 
 
+def tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3, nord_tr=0,
+                 trdm=0.0, lim_fac=1.0):
+    """Single-domain tracer_2d_1L (per-level substep counts).  Returns (q, dp1, mfx, mfy, cx, cy, nsplt_levels)."""
+    q = _f64(q).copy()
+    dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
+    nq, npz = q.shape[0], q.shape[1]
+    n = q.shape[-1] - 2 * ng
+    g = GridRef(geom)
+    cb = HALO_FN(halo_fn) if halo_fn is not None else HALO_FN()
+    ns = np.zeros(npz, dtype=np.int32)
+    lib().orc_tracer_2d_1L(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(g.struct),
+                           C.byref(bounds_for(n, ng)), n + 1, n + 1, npz, nq, hord, q_split, C.c_double(0.0),
+                           nord_tr, C.c_double(trdm), C.c_double(lim_fac), cb, None,
+                           ns.ctypes.data_as(C.POINTER(C.c_int)))
+    return q, dp1, mfx, mfy, cx, cy, ns
+
+
 def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=True, ng: int = 3,
                    nord_tr=0, trdm=0.0, lim_fac=1.0):
     """Six-tile tracer_2d.  q (6, nq, npz, nd, nd).  Returns (q, dp1, nsplt)."""

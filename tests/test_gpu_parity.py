@@ -233,6 +233,37 @@ def test_tracer_2d_dropin_matches_oracle_with_halo_callback(cuda, cube_prob, nor
         assert rel_l2(got, want) <= 1e-15
 
 
+@pytest.mark.parametrize("trdm", [0.0, 0.1])
+def test_tracer_2d_1L_dropin_matches_oracle(cuda, trdm):
+    """Per-level substep counts (winds scaled by level so the counts differ), a halo callback that restores
+    the prescribed ring, and optional damping: the drop-in equals the oracle's tracer_2d_1L."""
+    P = S.make_problem(30, 4, 2, seed=13, cmax=0.9, ntiles=1)
+    g = P.geoms[0]
+    f = np.array([0.5, 1.5, 2.5, 1.0])
+    args = [np.ascontiguousarray(a[0].numpy()) for a in (P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy)]
+    for idx in (2, 3, 4, 5):
+        args[idx] = np.ascontiguousarray(args[idx] * f[:, None, None])
+    halo = args[0].copy()
+
+    def refresh(qarr):
+        n, ng = P.n, 3
+        keep = qarr[..., ng:ng + n, ng:ng + n].copy()
+        qarr[...] = halo
+        qarr[..., ng:ng + n, ng:ng + n] = keep
+
+    ref = O.tracer_2d_1L(*args, g, hord=8, nord_tr=0, trdm=trdm,
+                         halo_fn=lambda p, nq, npz, ctx: refresh(np.ctypeslib.as_array(p, shape=halo.shape)))
+    assert len(set(ref[6].tolist())) > 1
+    q, dp, mfx, mfy, cx, cy = (a.copy() for a in args)
+    ns = api.tracer_2d_1L(q, dp, mfx, mfy, cx, cy, api.GridStruct(g), api.bounds_for(P.n), P.n + 1, P.n + 1, P.npz,
+                          P.nq, 8, 0, P.dt, nord_tr=0, trdm=trdm, halo_update=refresh)
+    assert ns == int(ref[6].max())
+    assert rel_l2(interior(q, P.n), interior(ref[0], P.n)) <= FP64_TOL
+    assert rel_l2(interior(dp, P.n), interior(ref[1], P.n)) <= FP64_TOL
+    for got, want in zip((mfx, mfy, cx, cy), ref[2:6]):
+        assert rel_l2(got, want) <= 1e-15
+
+
 def test_tracer_2d_dropin_derives_nsplt(cuda, cube_prob):
     P = cube_prob
     t = 0

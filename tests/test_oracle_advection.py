@@ -284,3 +284,29 @@ def test_tangent_linear_hord8_matches_finite_differences_on_a_monotone_field():
         errs.append(max(np.linalg.norm((f1x - f0x) / eps - dfx) / np.linalg.norm(dfx),
                         np.linalg.norm((f1y - f0y) / eps - dfy) / np.linalg.norm(dfy)))
     assert min(errs) < 1e-6, errs
+
+
+def _level_scaled(P, factors):
+    """The single-tile problem's winds and mass fluxes scaled per level (Courant maxima differ by level)."""
+    f = np.asarray(factors, dtype=np.float64)
+    args = [np.ascontiguousarray(a[0].numpy()) for a in (P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy)]
+    for idx in (2, 3, 4, 5):
+        args[idx] = np.ascontiguousarray(args[idx] * f[:, None, None])
+    return args
+
+
+def test_tracer_2d_1L_is_tracer_2d_level_by_level():
+    """tracer_2d_1L advances each level with its own substep count: level k equals a one-level tracer_2d call."""
+    P = S.make_problem(24, 4, 2, seed=3, cmax=0.9, ntiles=1)
+    args = _level_scaled(P, [0.5, 1.5, 2.5, 1.0])
+    q, dp, mfx, mfy, cx, cy, ns = O.tracer_2d_1L(*args, P.geoms[0], hord=8)
+    assert len(set(ns.tolist())) > 1, ns
+    for k in range(P.npz):
+        one = [args[0][:, k:k + 1]] + [a[k:k + 1] for a in args[1:]]
+        r = O.tracer_2d(*[np.ascontiguousarray(a) for a in one], P.geoms[0], hord=8)
+        assert r[6] == ns[k]
+        assert np.array_equal(q[:, k], r[0][:, 0]) and np.array_equal(dp[k], r[1][0])
+    # a fixed q_split gives tracer_2d itself
+    a1 = O.tracer_2d_1L(*args, P.geoms[0], hord=8, q_split=3)
+    a2 = O.tracer_2d(*args, P.geoms[0], hord=8, q_split=3)
+    assert np.array_equal(a1[0], a2[0]) and np.array_equal(a1[1], a2[1])
