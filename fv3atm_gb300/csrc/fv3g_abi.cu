@@ -344,17 +344,17 @@ template <typename T>
 int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   if (st->d.trdm > 1e-4 && (st->del6_tiles != (1 << st->nt) - 1 || !(st->da_min > 0.0)))
     return set_error(FV3G_E_ARG, "tracer damping (trdm > 1e-4) needs every tile's grid with del6_u, del6_v, da_min");
-  const long long fsz = st->plane * st->npz * st->nt;
-  const size_t fb = (size_t)fsz * sizeof(T);
-  FV3G_CUDA(cudaMemcpyAsync(st->cxs, st->cx, fb, cudaMemcpyDeviceToDevice, s));
-  FV3G_CUDA(cudaMemcpyAsync(st->cys, st->cy, fb, cudaMemcpyDeviceToDevice, s));
-  FV3G_CUDA(cudaMemcpyAsync(st->mfxs, st->mfx, fb, cudaMemcpyDeviceToDevice, s));
-  FV3G_CUDA(cudaMemcpyAsync(st->mfys, st->mfy, fb, cudaMemcpyDeviceToDevice, s));
+  // scaled copies of cx, cy, mfx, mfy (read from the inputs, written scaled) and the area fluxes
   const T frac = (nsplt == 1) ? T(1) : T(1.0 / nsplt);
+  AreaFluxSrc<T> src;
+  src.cx = (const T*)st->cx;
+  src.cy = (const T*)st->cy;
+  src.mfx = (const T*)st->mfx;
+  src.mfy = (const T*)st->mfy;
   CHECK(launch_area_flux<T>((T*)st->cxs, (T*)st->cys, (T*)st->xfx, (T*)st->yfx, (T*)st->mfxs, (T*)st->mfys,
                             (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
-                            st->n, 1, st->n, st->nt, st->npz, frac, s));
+                            st->n, 1, st->n, st->nt, st->npz, frac, s, src));
   CHECK(mark(st, K_PROLOGUE, s, 1));
   return 0;
 }

@@ -128,7 +128,13 @@ __global__ void k_edge_fix(const AdvArgs<T> a, int n) {
 template <typename T>
 __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa, const T* dya,
                             const T* dx, const T* dy, const T* sin_sg, long long sFt, long long sFk,
-                            long long sMt, long long sSin, PlaneGeom pg, int is, int ie, int js, int je, T frac) {
+                            long long sMt, long long sSin, PlaneGeom pg, int is, int ie, int js, int je, T frac,
+                            AreaFluxSrc<T> src) {
+  // unscaled inputs: src when given (the scaled copies are written), else cx.. themselves (in place)
+  const T* cxi = src.cx ? src.cx : cx;
+  const T* cyi = src.cy ? src.cy : cy;
+  const T* mxi = src.mfx ? src.mfx : mfx;
+  const T* myi = src.mfy ? src.mfy : mfy;
   const int t = blockIdx.z, k = blockIdx.y;
   const int nid = pg.pitch;  // loop over the data-domain rectangle of faces
   const int ni = ie - is + 1 + 2 * NG + 1, nj = je - js + 1 + 2 * NG + 1;
@@ -144,23 +150,23 @@ __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const 
     const long long p = pg.at(i, j);
     // x faces: i in is..ie+1, rows jsd..jed
     if (i >= is && i <= ie + 1 && j <= je + NG) {
-      const T c = cx[fo + p];
+      const T c = cxi[fo + p];
       T v;
       if (c > T(0)) v = c * dxa[mo + pg.at(i - 1, j)] * dy[mo + p] * s_e[pg.at(i - 1, j)];
       else v = c * dxa[mo + p] * dy[mo + p] * s_w[p];
       xfx[fo + p] = v * frac;
       cx[fo + p] = c * frac;
-      if (j >= js && j <= je) mfx[fo + p] *= frac;
+      if (j >= js && j <= je) mfx[fo + p] = mxi[fo + p] * frac;
     }
     // y faces: j in js..je+1, cols isd..ied
     if (j >= js && j <= je + 1 && i <= ie + NG) {
-      const T c = cy[fo + p];
+      const T c = cyi[fo + p];
       T v;
       if (c > T(0)) v = c * dya[mo + pg.at(i, j - 1)] * dx[mo + p] * s_n[pg.at(i, j - 1)];
       else v = c * dya[mo + p] * dx[mo + p] * s_s[p];
       yfx[fo + p] = v * frac;
       cy[fo + p] = c * frac;
-      if (i >= is && i <= ie) mfy[fo + p] *= frac;
+      if (i >= is && i <= ie) mfy[fo + p] = myi[fo + p] * frac;
     }
   }
 }
@@ -313,11 +319,12 @@ int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s) {
 template <typename T>
 int launch_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa, const T* dya, const T* dx,
                      const T* dy, const T* sin_sg, long long sFt, long long sFk, long long sMt, long long sSin,
-                     PlaneGeom pg, int is, int ie, int js, int je, int ntiles, int npz, T frac, cudaStream_t s) {
+                     PlaneGeom pg, int is, int ie, int js, int je, int ntiles, int npz, T frac, cudaStream_t s,
+                     AreaFluxSrc<T> src) {
   const int ncell = (ie - is + 2 + 2 * NG) * (je - js + 2 + 2 * NG);
   dim3 grid((ncell + 255) / 256, npz, ntiles);
   k_area_flux<T><<<grid, 256, 0, s>>>(cx, cy, xfx, yfx, mfx, mfy, dxa, dya, dx, dy, sin_sg, sFt, sFk, sMt, sSin,
-                                      pg, is, ie, js, je, frac);
+                                      pg, is, ie, js, je, frac, src);
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }
@@ -339,7 +346,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
   template int launch_copy_halo_ring<T>(T*, const T*, long long, int, PlaneGeom, int, cudaStream_t);             \
   template int launch_area_flux<T>(T*, T*, T*, T*, T*, T*, const T*, const T*, const T*, const T*, const T*, \
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \
-                                   int, T, cudaStream_t);                                                    \
+                                   int, T, cudaStream_t, AreaFluxSrc<T>);                                    \
   template int launch_max_courant<T>(const T*, const T*, long long, long long, PlaneGeom, int, int, int, int, int, \
                                      int, unsigned int*, cudaStream_t);
 FV3G_INST(float)

@@ -211,11 +211,22 @@ template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s);
 template <typename T>
 int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s);
+// Unscaled Courant numbers and mass fluxes to read instead of scaling in place.
+template <typename T>
+struct AreaFluxSrc {
+  const T* cx = nullptr;
+  const T* cy = nullptr;
+  const T* mfx = nullptr;
+  const T* mfy = nullptr;
+};
+// xfx, yfx from the Courant numbers with the upwind metrics, and cx, cy, mfx,
+// mfy scaled by frac (tracer_2d's prologue); with src, read from src and write
+// the scaled values into cx.. (copies) instead of scaling in place.
 template <typename T>
 int launch_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa, const T* dya,
                      const T* dx, const T* dy, const T* sin_sg, long long sFt, long long sFk,
                      long long sMt, long long sSin, PlaneGeom pg, int is, int ie, int js, int je,
-                     int ntiles, int npz, T frac, cudaStream_t s);
+                     int ntiles, int npz, T frac, cudaStream_t s, AreaFluxSrc<T> src = AreaFluxSrc<T>{});
 template <typename T>
 int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is,
                        int ie, int js, int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s);
