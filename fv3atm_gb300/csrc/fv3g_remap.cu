@@ -331,6 +331,11 @@ __device__ __forceinline__ FF ff_prod(float a, float b) {
 template <typename T>
 __host__ __device__ constexpr int ring_slots() { return sizeof(T) == 8 ? 3 : 4; }
 
+// Columns (warps) per CTA of the warp remap; its threads copy one level of
+// all RCOL columns at a time (8 FP32 columns: one 32-byte sector; 4 measured
+// 9 % slower at C384 L127 x 20).
+constexpr int RCOL = 8;
+
 // Slot pitch per column: room for the padded levels, and a residue (4 mod 32
 // floats, 2 mod 16 doubles) that spreads the 8 columns of one copy
 // instruction over distinct banks.
@@ -343,7 +348,7 @@ __host__ __device__ constexpr int ring_pitch() {
 
 template <typename T, int NPL>
 __host__ __device__ constexpr size_t remap_warp_smem() {
-  return 8 * sizeof(ColSmem<T, NPL>) + (size_t)ring_slots<T>() * 8 * ring_pitch<T, NPL>() * sizeof(T);
+  return RCOL * sizeof(ColSmem<T, NPL>) + (size_t)ring_slots<T>() * RCOL * ring_pitch<T, NPL>() * sizeof(T);
 }
 
 template <typename T>
@@ -460,14 +465,14 @@ __device__ __forceinline__ T affine_enter_bwd(T al, T be, int lane) {
 }
 
 template <typename T, int KORD, int NPL>
-__global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
+__global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) {
   constexpr int RING = ring_slots<T>(), RP = ring_pitch<T, NPL>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   ColSmem<T, NPL>& S = reinterpret_cast<ColSmem<T, NPL>*>(smem_raw)[warp];
-  T* const ring = reinterpret_cast<T*>(smem_raw + 8 * sizeof(ColSmem<T, NPL>));
+  T* const ring = reinterpret_cast<T*>(smem_raw + RCOL * sizeof(ColSmem<T, NPL>));
   const int nc = (int)a.ncol;  // launch_remap checks that it fits in an int
-  const int col0 = blockIdx.x * 8;
+  const int col0 = blockIdx.x * RCOL;
   // the last CTA's surplus warps repeat the last column and store nothing
   const bool real = col0 + warp < nc;
   const int col = real ? col0 + warp : nc - 1;
@@ -484,13 +489,13 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
   const int u0 = lane * NPL;  // first interface / layer of this lane
 
   // cooperative field copy: this thread's column and levels
-  const int cc = threadIdx.x & 7, kk = threadIdx.x >> 3;
+  const int cc = threadIdx.x % RCOL, kk = threadIdx.x / RCOL;
   long long fo_c, qo_c;
   offsets(min(col0 + cc, nc - 1), fo_c, qo_c);
   auto issue = [&](int f) {
     if (f < a.nfield) {
       const T* src = a.q_in + qo_c + f * a.sQq;
-      T* dst = ring + ((f % RING) * 8 + cc) * RP;
+      T* dst = ring + ((f % RING) * RCOL + cc) * RP;
 #pragma unroll
       for (int r = 0; r < NPL; ++r) {
         const int k = kk + 32 * r;
@@ -640,7 +645,7 @@ __global__ void __launch_bounds__(256) k_remap_warp(const RemapArgs<T> a) {
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
       const int f = min(f0 + h, a.nfield - 1);
-      Q[h] = ring + ((f % RING) * 8 + warp) * RP;
+      Q[h] = ring + ((f % RING) * RCOL + warp) * RP;
       q2[h] = a.q_out + qo + f * a.sQqo;
       store[h] = real && f0 + h < a.nfield;
     }
@@ -838,8 +843,8 @@ int prepare_remap_kernels() {
 template <typename T, int KORD, int NPL>
 static cudaError_t launch_warp_npl(const RemapArgs<T>& a, cudaStream_t s) {
   constexpr size_t smem = remap_warp_smem<T, NPL>();
-  const unsigned nb = (unsigned)((a.ncol + 7) / 8);
-  k_remap_warp<T, KORD, NPL><<<nb, 256, smem, s>>>(a);
+  const unsigned nb = (unsigned)((a.ncol + RCOL - 1) / RCOL);
+  k_remap_warp<T, KORD, NPL><<<nb, 32 * RCOL, smem, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -303,6 +303,37 @@ def test_map_scalar_dropin_matches_oracle(cuda, kord, iv):
     assert np.count_nonzero(got[:, j, :2]) == 0 and np.count_nonzero(got[:, :j]) == 0
 
 
+def test_map_scalar_rows_from_concurrent_threads(cuda):
+    """Lagrangian_to_Eulerian calls map_scalar row by row from OpenMP threads: rows remapped from 8 host
+    threads at once (each thread has its own stream and device arena) equal the rows remapped one by one."""
+    from concurrent.futures import ThreadPoolExecutor
+    from fv3atm_gb300 import grid as G
+    rng = np.random.default_rng(9)
+    km, ni, nj = 127, 48, 16
+    ak, bk = G.hybrid_levels(km)
+    ps = rng.uniform(95000, 103000, (nj, ni))
+    dref = np.diff(ak)[:, None, None] + np.diff(bk)[:, None, None] * ps[None]
+    dp = dref * (1 + 0.1 * rng.uniform(-1, 1, dref.shape))
+    q1 = np.ascontiguousarray(np.abs(rng.standard_normal((km, nj, ni))) + 0.1)
+    pe1 = np.concatenate([np.full((1, nj, ni), ak[0]), ak[0] + np.cumsum(dp, 0)])
+    pe2 = ak[:, None, None] + bk[:, None, None] * pe1[-1][None]
+    qs = np.zeros(ni)
+
+    def row(j, out):
+        p1 = np.ascontiguousarray(pe1[:, j, :])
+        p2 = np.ascontiguousarray(pe2[:, j, :])
+        api.map_scalar(km, p1, q1, qs, km, p2, out, 1, ni, j + 1, 1, ni, 1, nj, 0, 9, 0.0)
+
+    serial = np.zeros_like(q1)
+    for j in range(nj):
+        row(j, serial)
+    outs = [np.zeros_like(q1) for _ in range(nj)]
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        list(ex.map(lambda j: row(j, outs[j]), range(nj)))
+    for j in range(nj):
+        assert np.array_equal(outs[j][:, j, :], serial[:, j, :])
+
+
 def test_map_scalar_3d_matches_rows(cuda):
     rng = np.random.default_rng(9)
     from fv3atm_gb300 import grid as G
