@@ -74,6 +74,20 @@ def test_cube_hord5_matches_oracle(cuda, cube_prob):
     assert rel_l2(interior(q, P.n), interior(q_ref, P.n)) <= FP64_TOL
 
 
+@pytest.mark.parametrize("n", [27, 28, 53])
+@pytest.mark.parametrize("hord", [5, 8])
+def test_cube_edge_at_the_window_border(cuda, n, hord):
+    """Tile sizes whose east/north cube edge falls at window face 30 or 31 of the last full CTA tile (the next
+    tile holds one or two cells): the one-sided edge values still reach the faces next to the edge."""
+    P = S.make_problem(n, 2, 2, seed=17, cmax=0.8)
+    q_ref, _, _ = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=hord, q_split=2)
+    st = api.CubeState(n, 2, 2, precision="fp64", hord=hord)
+    st.load_problem(P)
+    st.tracer_2d(2)
+    assert rel_l2(interior(st.download("Q"), n), interior(q_ref, n)) <= FP64_TOL
+    st.close()
+
+
 # (hord, nord_tr, trdm, lim_fac): the hord-1 / hord-5 filters, and del-2 / del-4 / del-6 damping of
 # the first substep
 SCHEMES = [(1, 0, 0.0, 3.0), (5, 0, 0.0, 1.0), (8, 0, 0.12, 1.0), (8, 1, 0.1, 1.0), (8, 2, 0.1, 1.0),
