@@ -24,8 +24,9 @@ EXPORTS = (
     "fv3g_tracer_2d_batched", "fv3g_remap_batched", "fv3g_step", "fv3g_mass_sum", "fv3g_state_error",
     "fv3g_field_info", "fv3g_upload_async", "fv3g_download_async", "fv3g_stream_sync", "fv3g_set_timing",
     "fv3g_kernel_times", "fv3g_remap_columns_noalloc", "fv3g_fv_tp_2d_tl", "fv3g_fv_tp_2d_ad", "fv3g_map1_ppm_tl",
-    "fv3g_map1_ppm_ad", "fv3g_state_autotune", "fv3g_state_widths", "fv3g_step_host", "fv3g_tracer_2d_1L", "fv3g_ensemble_create", "fv3g_ensemble_step",
-    "fv3g_ensemble_destroy", "fv3g_fillz", "fv3g_pressure_vars", "fv3g_fillz_batched",
+    "fv3g_map1_ppm_ad", "fv3g_state_autotune", "fv3g_state_widths", "fv3g_step_host", "fv3g_tracer_2d_1L", "fv3g_ensemble_create",
+    "fv3g_ensemble_step", "fv3g_ensemble_destroy", "fv3g_fillz", "fv3g_pressure_vars", "fv3g_fillz_batched",
+    "fv3g_tracer_2d_nested",
 )
 
 
@@ -50,6 +51,11 @@ class StateDesc(C.Structure):
                 ("hord", C.c_int), ("kord", C.c_int), ("iv", C.c_int), ("q_min", C.c_double),
                 ("warps_per_cta", C.c_int), ("nord_tr", C.c_int), ("trdm", C.c_double), ("lim_fac", C.c_double),
                 ("fill", C.c_int)]
+
+
+class NestBC(C.Structure):
+    _fields_ = [(k, DP) for k in ("west_t0", "west_t1", "east_t0", "east_t1", "south_t0", "south_t1", "north_t0",
+                                  "north_t1")]
 
 
 HALO_FN = C.CFUNCTYPE(None, DP, C.c_int, C.c_int, VP)

@@ -17,10 +17,10 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DP, Bounds, Grid, StateDesc
+from ._lib import DP, Bounds, Grid, NestBC, StateDesc
 
-__all__ = ["Bounds", "GridStruct", "fv_tp_2d", "tracer_2d", "map_scalar", "map1_ppm", "map_scalar_3d", "CubeState",
-           "bounds_for"]
+__all__ = ["Bounds", "GridStruct", "fv_tp_2d", "tracer_2d", "tracer_2d_1L", "tracer_2d_nested", "NestBoundary",
+           "map_scalar", "map1_ppm", "map_scalar_3d", "CubeState", "bounds_for"]
 
 
 def _p(a):
@@ -90,6 +90,51 @@ def tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, n
               C.byref(bd), npx, npy, npz, nq, hord, q_split, C.c_double(dt), nord_tr, C.c_double(trdm),
               C.c_double(lim_fac), cb, None, C.byref(nsplt))
     return nsplt.value
+
+
+class NestBoundary:
+    """neststruct%q_BC of every tracer: {side: (t0, t1)} for the sides "west", "east", "south", "north", each
+    array (nq, npz, rows, cols) float64 in C order, i.e. per tracer the Fortran strip west (isd:0, jsd:jed, npz),
+    east (npx:ied, jsd:jed, npz), south (isd:ied, jsd:0, npz) or north (isd:ied, npy:jed, npz).  A side the
+    domain does not read may be left out."""
+
+    SIDES = ("west", "east", "south", "north")
+
+    def __init__(self, strips: dict):
+        self.arrays = {k: tuple(np.ascontiguousarray(a, dtype=np.float64) for a in v) for k, v in strips.items()}
+        nq = {a.shape[0] for v in self.arrays.values() for a in v}
+        if len(nq) != 1:
+            raise ValueError("boundary strips disagree on the tracer count")
+        self.nq = nq.pop()
+        self.structs = (NestBC * self.nq)()
+        for iq in range(self.nq):
+            ptrs = []
+            for side in self.SIDES:
+                pair = self.arrays.get(side)
+                ptrs += [pair[t][iq].ctypes.data_as(DP) if pair is not None else None for t in range(2)]
+            self.structs[iq] = NestBC(*ptrs)
+
+
+def tracer_2d_nested(q, dp1, mfx, mfy, cx, cy, gridstruct: GridStruct, bd: Bounds, npx, npy, npz, nq, hord,
+                     q_split, dt, nord_tr=0, trdm=0.0, k_split=1, q_bc: NestBoundary | None = None,
+                     nest_timestep: int = 0, lim_fac=1.0, halo_update=None) -> tuple[int, int]:
+    """tracer_2d_nested: on a nested grid the outer-side halos take q_bc interpolated to each substep's start.
+    Returns (nsplt, the advanced nest_timestep)."""
+    if q_bc is not None and q_bc.nq != nq:
+        raise ValueError(f"q_bc holds {q_bc.nq} tracers, nq is {nq}")
+    shape = q.shape
+    cb = _lib.HALO_FN()
+    if halo_update is not None:
+        def _cb(ptr, nq_, npz_, ctx):
+            halo_update(np.ctypeslib.as_array(ptr, shape=shape))
+        cb = _lib.HALO_FN(_cb)
+    nsplt = C.c_int(0)
+    counter = C.c_int(nest_timestep)
+    _lib.call("fv3g_tracer_2d_nested", _p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(gridstruct.struct),
+              C.byref(bd), npx, npy, npz, nq, hord, q_split, C.c_double(dt), nord_tr, C.c_double(trdm), k_split,
+              q_bc.structs if q_bc is not None else None, C.byref(counter), C.c_double(lim_fac), cb, None,
+              C.byref(nsplt))
+    return nsplt.value, counter.value
 
 
 def map_scalar(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, q_min) -> None:

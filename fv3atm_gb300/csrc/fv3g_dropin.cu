@@ -1,5 +1,6 @@
 // fv3g_dropin.cu -- exact-shape (host-array) entries: fv3g_fv_tp_2d,
-// fv3g_tracer_2d, fv3g_map_scalar, fv3g_map1_ppm, fv3g_map_scalar_3d.
+// fv3g_tracer_2d, fv3g_tracer_2d_1L, fv3g_tracer_2d_nested, fv3g_map_scalar,
+// fv3g_map1_ppm, fv3g_map_scalar_3d.
 //
 // Each entry keeps the upstream Fortran argument list (fv_tp_2d / tracer_2d
 // of tp_core.F90 / fv_tracer2d.F90, map_scalar / map1_ppm of fv_mapz.F90 in
@@ -38,6 +39,78 @@ int check_damping(const fv3g_grid* grid, int nord, bool need_rarea) {
   if (!(grid->da_min > 0.0)) return set_error(FV3G_E_ARG, "tracer damping needs grid da_min > 0");
   if (need_rarea && !grid->rarea) return set_error(FV3G_E_ARG, "tracer damping needs grid rarea");
   return 0;
+}
+
+// One outer side of a nested domain: the boundary states of every (tracer,
+// level) plane at t0 and t1, ni x nj cells from (i0, j0), i fastest.
+struct NestSide {
+  const double* t0;
+  const double* t1;
+  int i0, j0, ni, nj;
+};
+struct NestSides {
+  NestSide side[4];
+  int n;
+};
+
+// nested_grid_BC_apply_intT on every plane: q = (t0·(split − step) + step·t1)
+// · (1/split) at the outer-side halo cells, rounded after every operation as
+// the unfused expression is (w0 = split − step and denom = 1/split come from
+// the host).  blockIdx.y picks the side.
+__global__ void k_nest_bc(double* q, PlaneGeom pg, long long plane, NestSides ns, long long nplanes, double step,
+                          double w0, double denom) {
+  const NestSide sd = ns.side[blockIdx.y];
+  const long long cells = (long long)sd.ni * sd.nj, total = cells * nplanes;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long p = t / cells;
+    const int c = (int)(t - p * cells);
+    const int i = sd.i0 + c % sd.ni, j = sd.j0 + c / sd.ni;
+    q[p * plane + pg.at(i, j)] = __dmul_rn(__dadd_rn(__dmul_rn(sd.t0[t], w0), __dmul_rn(step, sd.t1[t])), denom);
+  }
+}
+
+// The outer sides of a rank's domain that a nested grid's boundary states
+// cover, as nested_grid_BC_apply_intT picks them: west/east over the data
+// domain's full height when is == 1 / ie == npx-1; south/north over i = is..ie
+// on an outer side (isd/ied toward a neighbour rank) when js == 1 / je == npy-1.
+// off[] is where each side's cells start inside its host strip and pitch[] the
+// strip's row length: west (isd:0, jsd:jed), east (npx:ied, jsd:jed), south
+// (isd:ied, jsd:0), north (isd:ied, npy:jed).
+struct NestLayout {
+  NestSides ns{};
+  int which[4];  // 0 west, 1 east, 2 south, 3 north
+  size_t off[4], pitch[4], slice[4];
+  size_t cells = 0;  // per plane, all sides
+};
+
+NestLayout nest_layout(const fv3g_bounds* bd, int npx, int npy) {
+  NestLayout L;
+  const int nid = bd->ied - bd->isd + 1, njd = bd->jed - bd->jsd + 1;
+  const int i0 = (bd->is == 1) ? bd->is : bd->isd, i1 = (bd->ie == npx - 1) ? bd->ie : bd->ied;
+  auto add = [&](int w, int ilo, int jlo, int ni, int nj, size_t off, size_t pitch, size_t slice) {
+    NestSide& sd = L.ns.side[L.ns.n];
+    sd.i0 = ilo; sd.j0 = jlo; sd.ni = ni; sd.nj = nj;
+    L.which[L.ns.n] = w;
+    L.off[L.ns.n] = off; L.pitch[L.ns.n] = pitch; L.slice[L.ns.n] = slice;
+    L.cells += (size_t)ni * nj;
+    ++L.ns.n;
+  };
+  const int nw = 1 - bd->isd, ne = bd->ied - npx + 1, nsr = 1 - bd->jsd, nnr = bd->jed - npy + 1;
+  if (bd->is == 1) add(0, bd->isd, bd->jsd, nw, njd, 0, nw, (size_t)nw * njd);
+  if (bd->ie == npx - 1) add(1, npx, bd->jsd, ne, njd, 0, ne, (size_t)ne * njd);
+  if (bd->js == 1) add(2, i0, bd->jsd, i1 - i0 + 1, nsr, (size_t)(i0 - bd->isd), nid, (size_t)nid * nsr);
+  if (bd->je == npy - 1) add(3, i0, npy, i1 - i0 + 1, nnr, (size_t)(i0 - bd->isd), nid, (size_t)nid * nnr);
+  return L;
+}
+
+void nest_strips(const fv3g_nest_bc& bc, int w, const double** t0, const double** t1) {
+  switch (w) {
+    case 0: *t0 = bc.west_t0; *t1 = bc.west_t1; break;
+    case 1: *t0 = bc.east_t0; *t1 = bc.east_t1; break;
+    case 2: *t0 = bc.south_t0; *t1 = bc.south_t1; break;
+    default: *t0 = bc.north_t0; *t1 = bc.north_t1; break;
+  }
 }
 
 }  // namespace
@@ -142,7 +215,8 @@ int fv3g_fv_tp_2d(double* q, const double* crx, const double* cry, int npx, int 
 static int tracer_2d_impl(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
                           const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord,
                           int q_split, int nord_tr, double trdm, double lim_fac, fv3g_halo_fn halo_fn,
-                          void* halo_ctx, int* nsplt_out, bool per_level) {
+                          void* halo_ctx, int* nsplt_out, bool per_level, const fv3g_nest_bc* q_bc = nullptr,
+                          int* nest_timestep = nullptr, int k_split = 1) {
   CHECK(check_bounds(bd, npx, npy));
   if (!q || !dp1 || !mfx || !mfy || !cx || !cy || !grid) return set_error(FV3G_E_ARG, "null array argument");
   if (!grid->dx || !grid->dy || !grid->dxa || !grid->dya || !grid->area || !grid->rarea || !grid->sin_sg)
@@ -152,10 +226,25 @@ static int tracer_2d_impl(double* q, double* dp1, double* mfx, double* mfy, doub
   // damping of the first substep, weighted by its starting thickness
   const bool damping = trdm > 1e-4;
   if (damping) CHECK(check_damping(grid, nord_tr, false));
+  // boundary states of a nested grid, applied before every substep
+  const bool nest = nest_timestep != nullptr && grid->nested;
+  NestLayout nl;
+  if (nest) {
+    if (!q_bc) return set_error(FV3G_E_ARG, "a nested grid needs q_bc boundary states");
+    if (k_split < 1) return set_error(FV3G_E_ARG, "k_split must be positive (got %d)", k_split);
+    nl = nest_layout(bd, npx, npy);
+    for (int iq = 0; iq < nq; ++iq)
+      for (int m = 0; m < nl.ns.n; ++m) {
+        const double *t0, *t1;
+        nest_strips(q_bc[iq], nl.which[m], &t0, &t1);
+        if (!t0 || !t1) return set_error(FV3G_E_ARG, "q_bc(%d) lacks the strips of an outer side", iq + 1);
+      }
+  }
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
   const size_t nqp = (size_t)nq * npz;
-  CHECK(g_ctx.begin(padded(P * nqp, 8) * 2 + padded(P * npz, 8) * 9 + padded(P, 8) * 14 + 256));
+  CHECK(g_ctx.begin(padded(P * nqp, 8) * 2 + padded(P * npz, 8) * 9 + padded(P, 8) * 14 + 256 +
+                    (nest ? 2 * padded(nl.cells * nqp, 8) + 8 * 256 : 0)));
   cudaStream_t s = g_ctx.stream;
   double* qa = g_ctx.take<double>(P * nqp);
   double* qb = g_ctx.take<double>(P * nqp);
@@ -187,6 +276,23 @@ static int tracer_2d_impl(double* q, double* dp1, double* mfx, double* mfy, doub
   if (damping) {
     CHECK(h2d_planes(d6u, pg, grid->del6_u, isd, ied, jsd, jed + 1, 1, s));
     CHECK(h2d_planes(d6v, pg, grid->del6_v, isd, ied + 1, jsd, jed, 1, s));
+  }
+  if (nest) {  // each side's t0 and t1 for every (tracer, level) plane, packed
+    for (int m = 0; m < nl.ns.n; ++m) {
+      NestSide& sd = nl.ns.side[m];
+      const size_t cells = (size_t)sd.ni * sd.nj;
+      double* dev[2] = {g_ctx.take<double>(cells * nqp), g_ctx.take<double>(cells * nqp)};
+      for (int iq = 0; iq < nq; ++iq) {
+        const double* src[2];
+        nest_strips(q_bc[iq], nl.which[m], &src[0], &src[1]);
+        for (int t = 0; t < 2; ++t)
+          CHECK(copy_planes(dev[t] + (size_t)iq * npz * cells, (size_t)sd.ni * 8, cells * 8, src[t] + nl.off[m],
+                            nl.pitch[m] * 8, nl.slice[m] * 8, (size_t)sd.ni * 8, sd.nj, npz,
+                            cudaMemcpyHostToDevice, s));
+      }
+      sd.t0 = dev[0];
+      sd.t1 = dev[1];
+    }
   }
 
   if (per_level) {
@@ -305,6 +411,18 @@ static int tracer_2d_impl(double* q, double* dp1, double* mfx, double* mfy, doub
       halo_fn(q, nq, npz, halo_ctx);
       CHECK(h2d_planes(qa, pg, q, isd, ied, jsd, jed, (long long)nqp, s));
     }
+    if (nest) {
+      const double step = (double)*nest_timestep, split = (double)nsplt * k_split;
+      if (nl.ns.n > 0) {
+        size_t most = 0;
+        for (int m = 0; m < nl.ns.n; ++m) most = std::max(most, (size_t)nl.ns.side[m].ni * nl.ns.side[m].nj);
+        const unsigned bx = (unsigned)std::min<size_t>((most * nqp + 255) / 256, 1024);
+        k_nest_bc<<<dim3(bx, nl.ns.n), 256, 0, s>>>(qa, pg, (long long)P, nl.ns, (long long)nqp, step,
+                                                     split - step, 1.0 / split);
+        FV3G_CUDA(cudaGetLastError());
+      }
+      ++*nest_timestep;
+    }
     const int dpo = (dpi == 1) ? 2 : 1;
     AdvArgs<double> a{};
     a.q_in = qa; a.q_out = qb;
@@ -363,6 +481,22 @@ int fv3g_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx,
   (void)dt;
   return tracer_2d_impl(q, dp1, mfx, mfy, cx, cy, grid, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm,
                         lim_fac, halo_fn, halo_ctx, nsplt_out, false);
+}
+
+int fv3g_tracer_2d_nested(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                          const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq, int hord,
+                          int q_split, double dt, int nord_tr, double trdm, int k_split, const fv3g_nest_bc* q_bc,
+                          int* nest_timestep, double lim_fac, fv3g_halo_fn halo_fn, void* halo_ctx,
+                          int* nsplt_out) {
+  (void)dt;
+  if (!nest_timestep) return set_error(FV3G_E_ARG, "nest_timestep must not be NULL");
+  if (!grid) return set_error(FV3G_E_ARG, "null array argument");
+  // the counter advances only when the call succeeds
+  int counter = *nest_timestep;
+  CHECK(tracer_2d_impl(q, dp1, mfx, mfy, cx, cy, grid, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm,
+                       lim_fac, halo_fn, halo_ctx, nsplt_out, false, q_bc, &counter, k_split));
+  *nest_timestep = counter;
+  return 0;
 }
 
 int fv3g_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,

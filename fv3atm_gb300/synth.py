@@ -406,3 +406,14 @@ def c48_single_tile(n: int = 48, npz: int = 63, seed: int = 0, cmax: float = 0.4
         return out
 
     return P, exact
+
+
+def nest_strips(field_t0, field_t1, isd: int, jsd: int, npx: int, npy: int) -> dict:
+    """Boundary states of a nested domain cut from two full fields (nq, npz, njd, nid) at the parent times t0
+    and t1: {side: (t0, t1)} with the strips laid out as a nest's q_BC holds them, west (isd:0, jsd:jed),
+    east (npx:ied, jsd:jed), south (isd:ied, jsd:0), north (isd:ied, npy:jed), each (nq, npz, rows, cols)."""
+    out = {}
+    for name, cut in (("west", np.s_[..., :, :1 - isd]), ("east", np.s_[..., :, npx - isd:]),
+                      ("south", np.s_[..., :1 - jsd, :]), ("north", np.s_[..., npy - jsd:, :])):
+        out[name] = tuple(np.ascontiguousarray(np.asarray(f)[cut], dtype=np.float64) for f in (field_t0, field_t1))
+    return out

@@ -137,6 +137,42 @@ int fv3g_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* 
                       int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
                       fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out);
 
+/* Boundary states of a nested grid for one tracer, neststruct%q_BC(iq), at
+ * the parent times t0 and t1 (HOST pointers, i fastest, npz levels each), as
+ * allocate_fv_nest_BC_type lays them out for an unstaggered field
+ * (moving_nest/fv_moving_nest.F90:2005-2008):
+ *   west  (isd:0,   jsd:jed, npz)   read when is == 1
+ *   east  (npx:ied, jsd:jed, npz)   read when ie == npx-1
+ *   south (isd:ied, jsd:0,   npz)   read when js == 1
+ *   north (isd:ied, npy:jed, npz)   read when je == npy-1
+ * South and north are read over i = is..ie on an outer side of the domain
+ * and to isd/ied toward a neighbour rank; the corner blocks come from west and
+ * east.  The strips of a side that is not read may be NULL. */
+typedef struct {
+  const double *west_t0, *west_t1, *east_t0, *east_t1;
+  const double *south_t0, *south_t1, *north_t0, *north_t1;
+} fv3g_nest_bc;
+
+/* tracer_2d_nested (fv_tracer2d.F90; the variant fv_dynamics calls on a
+ * nested grid or on a grid with nests): fv3g_tracer_2d, and on a nested grid
+ * (grid->nested = 1) the halo cells on the domain's outer sides are set before
+ * every substep, after halo_fn, from q_bc[0..nq) interpolated in time as
+ *   q = (t0*(split - step) + step*t1) * (1/split),
+ *   split = nsplt*k_split, step = *nest_timestep,
+ * the count of tracer substeps taken since the parent's t0
+ * (neststruct%tracer_nest_timestep, moving_nest/fv_moving_nest.F90:1781);
+ * it advances by one per substep and is written back on success.  On a grid
+ * that is not nested q_bc may be NULL and the count is left as it is.
+ * Replaces (argument list as documented upstream): tracer_2d_nested(q, dp1,
+ *           mfx, mfy, cx, cy, gridstruct, bd, domain, npx, npy, npz, nq,
+ *           hord, q_split, dt, id_divg, q_pack, dp1_pack, nord_tr, trdm,
+ *           k_split, neststruct, parent_grid, n_map, lim_fac). */
+int fv3g_tracer_2d_nested(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                          const fv3g_grid* grid, const fv3g_bounds* bd, int npx, int npy, int npz, int nq,
+                          int hord, int q_split, double dt, int nord_tr, double trdm, int k_split,
+                          const fv3g_nest_bc* q_bc, int* nest_timestep, double lim_fac,
+                          fv3g_halo_fn halo_fn, void* halo_ctx, int* nsplt_out);
+
 /* map_scalar (fv_mapz.F90): remap row j of a 3-D field, FP64.
  *   pe1 (i1:i2, km+1)  pe2 (i1:i2, kn+1)  qs (i1:i2)
  *   q1 (ibeg:iend, jbeg:jend, km) in    q2 (ibeg:iend, jbeg:jend, kn) inout

@@ -719,10 +719,64 @@ void orc_fv_tp_2d_tl(const double* q, const double* dq, const double* crx, const
   for (size_t n = 0; n < d.nmy; ++n) dfy[n] = fy[n].d;
 }
 
-int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
-                  const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
-                  int nord_tr, double trdm, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx) {
-  (void)dt;
+// nested_grid_BC_apply_intT for one 3-D field with no staggering: the halo
+// cells on the outer sides of the nested domain get the boundary state
+// interpolated in time, (t0·(split − step) + step·t1)·(1/split).  West and
+// east take the full height of the data domain (the corner blocks with them);
+// south and north take the columns between, i = is..ie on a side that is an
+// outer side and isd/ied where the rank has a neighbour.  The strips are laid
+// out as allocate_fv_nest_BC_type allocates them with istag = jstag = 0
+// (moving_nest/fv_moving_nest.F90:2005-2008): west (isd:0, jsd:jed), east
+// (npx:ied, jsd:jed), south (isd:ied, jsd:0), north (isd:ied, npy:jed), each
+// with npz levels.
+static void nest_bc_apply(double* var, const Dom& d, int npx, int npy, int npz, const orc_nest_bc& bc, double step,
+                          double split) {
+  const double denom = 1.0 / split;
+  auto blend = [&](const double* t0, const double* t1, size_t n) {
+    return (t0[n] * (split - step) + step * t1[n]) * denom;
+  };
+  const int nwest = 1 - d.isd, neast = d.ied - npx + 1, nsouth = 1 - d.jsd, nnorth = d.jed - npy + 1;
+  const int i0 = (d.is == 1) ? d.is : d.isd, i1 = (d.ie == npx - 1) ? d.ie : d.ied;
+  for (int k = 0; k < npz; ++k) {
+    View2<double> V{var + (size_t)k * d.plane, d.isd, d.jsd, d.nid};
+    if (d.is == 1)
+      for (int j = d.jsd; j <= d.jed; ++j)
+        for (int i = d.isd; i <= 0; ++i)
+          V(i, j) = blend(bc.west_t0, bc.west_t1,
+                          (size_t)(i - d.isd) + (size_t)(j - d.jsd) * nwest + (size_t)k * nwest * d.njd);
+    if (d.ie == npx - 1)
+      for (int j = d.jsd; j <= d.jed; ++j)
+        for (int i = npx; i <= d.ied; ++i)
+          V(i, j) = blend(bc.east_t0, bc.east_t1,
+                          (size_t)(i - npx) + (size_t)(j - d.jsd) * neast + (size_t)k * neast * d.njd);
+    if (d.js == 1)
+      for (int j = d.jsd; j <= 0; ++j)
+        for (int i = i0; i <= i1; ++i)
+          V(i, j) = blend(bc.south_t0, bc.south_t1,
+                          (size_t)(i - d.isd) + (size_t)(j - d.jsd) * d.nid + (size_t)k * d.nid * nsouth);
+    if (d.je == npy - 1)
+      for (int j = npy; j <= d.jed; ++j)
+        for (int i = i0; i <= i1; ++i)
+          V(i, j) = blend(bc.north_t0, bc.north_t1,
+                          (size_t)(i - d.isd) + (size_t)(j - npy) * d.nid + (size_t)k * d.nid * nnorth);
+  }
+}
+
+void orc_nest_bc_apply(double* var, const orc_bounds* bd, int npx, int npy, int npz, const orc_nest_bc* bc,
+                       double step, double split) {
+  nest_bc_apply(var, Dom(bd), npx, npy, npz, *bc, step, split);
+}
+
+// The substep loop of tracer_2d; on a nested grid with boundary states, they
+// are applied to every tracer after the halo refresh of each substep, at the
+// time of the substep's start: step = the count of tracer substeps taken since
+// the parent's t0 (neststruct%tracer_nest_timestep, passed to
+// setup_nested_grid_BCs at moving_nest/fv_moving_nest.F90:1781), split =
+// nsplt·k_split; the count advances by one per substep of a nested grid.
+static int tracer_2d_run(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
+                         const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split,
+                         int nord_tr, double trdm, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx,
+                         const orc_nest_bc* q_bc, int* nest_timestep, int k_split) {
   Dom d(bd);
   std::vector<double> xfx(d.nxf * npz), yfx(d.nyf * npz);
   for (int k = 0; k < npz; ++k) area_fluxes(cx + k * d.nxf, cy + k * d.nyf, xfx.data() + k * d.nxf,
@@ -737,6 +791,13 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
   std::vector<double> fx(d.nmx), fy(d.nmy);
   for (int it = 0; it < nsplt; ++it) {
     if (halo_fn) halo_fn(q, nq, npz, halo_ctx);
+    if (nest_timestep && g->nested) {
+      if (q_bc)
+        for (int iq = 0; iq < nq; ++iq)
+          nest_bc_apply(q + (size_t)iq * npz * d.plane, d, npx, npy, npz, q_bc[iq], (double)*nest_timestep,
+                        (double)nsplt * k_split);
+      ++*nest_timestep;
+    }
 #pragma omp parallel for schedule(dynamic) firstprivate(fx, fy)
     for (int k = 0; k < npz; ++k) {
       Level L;
@@ -759,6 +820,26 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
       }
     }
   }
+  return nsplt;
+}
+
+int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy, const orc_grid* g,
+                  const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord, int q_split, double dt,
+                  int nord_tr, double trdm, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx) {
+  (void)dt;
+  return tracer_2d_run(q, dp1, mfx, mfy, cx, cy, g, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm, lim_fac,
+                       halo_fn, halo_ctx, nullptr, nullptr, 1);
+}
+
+int orc_tracer_2d_nested(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                         const orc_grid* g, const orc_bounds* bd, int npx, int npy, int npz, int nq, int hord,
+                         int q_split, double dt, int nord_tr, double trdm, int k_split, const orc_nest_bc* q_bc,
+                         int* nest_timestep, double lim_fac, orc_halo_fn halo_fn, void* halo_ctx) {
+  (void)dt;
+  int counter = nest_timestep ? *nest_timestep : 0;
+  const int nsplt = tracer_2d_run(q, dp1, mfx, mfy, cx, cy, g, bd, npx, npy, npz, nq, hord, q_split, nord_tr, trdm,
+                                  lim_fac, halo_fn, halo_ctx, q_bc, &counter, k_split);
+  if (nest_timestep) *nest_timestep = counter;
   return nsplt;
 }
 

@@ -87,6 +87,31 @@ int orc_tracer_2d(double* q, double* dp1, double* mfx, double* mfy, double* cx, 
                   int hord, int q_split, double dt, int nord_tr, double trdm, double lim_fac,
                   orc_halo_fn halo_fn, void* halo_ctx);
 
+/* Boundary states of a nested grid for one tracer (neststruct%q_BC(iq)) at
+ * the parent times t0 and t1, each with npz levels, i fastest:
+ *   west (isd:0, jsd:jed)   east (npx:ied, jsd:jed)
+ *   south (isd:ied, jsd:0)  north (isd:ied, npy:jed)
+ * Only the outer sides of the domain are read. */
+typedef struct {
+  const double *west_t0, *west_t1, *east_t0, *east_t1;
+  const double *south_t0, *south_t1, *north_t0, *north_t1;
+} orc_nest_bc;
+
+/* nested_grid_BC_apply_intT for one 3-D field (var (isd:ied,jsd:jed,npz)):
+ * the outer-side halo cells become (t0*(split-step) + step*t1)/split. */
+void orc_nest_bc_apply(double* var, const orc_bounds* bd, int npx, int npy, int npz, const orc_nest_bc* bc,
+                       double step, double split);
+
+/* tracer_2d_nested: tracer_2d whose substeps, on a nested grid (g->nested),
+ * apply the boundary states q_bc[0..nq) after halo_fn, with step =
+ * *nest_timestep and split = nsplt*k_split; *nest_timestep advances by one
+ * per substep of a nested grid.  Returns nsplt. */
+int orc_tracer_2d_nested(double* q, double* dp1, double* mfx, double* mfy, double* cx, double* cy,
+                         const orc_grid* g, const orc_bounds* bd, int npx, int npy, int npz, int nq,
+                         int hord, int q_split, double dt, int nord_tr, double trdm, int k_split,
+                         const orc_nest_bc* q_bc, int* nest_timestep, double lim_fac,
+                         orc_halo_fn halo_fn, void* halo_ctx);
+
 /* tracer_2d_1L: the levels one at a time, each with its own substep count
  * (q_split > 0, or 1 + the level's Courant maximum) and its fluxes scaled by
  * its own 1/nsplt; halo_fn runs before every substep of every level.

@@ -29,7 +29,28 @@ class Grid(C.Structure):
                 ("nested", C.c_int), ("del6_u", DP), ("del6_v", DP), ("da_min", C.c_double)]
 
 
+class NestBC(C.Structure):
+    _fields_ = [(k, DP) for k in ("west_t0", "west_t1", "east_t0", "east_t1", "south_t0", "south_t1", "north_t0",
+                                  "north_t1")]
+
+
 HALO_FN = C.CFUNCTYPE(None, DP, C.c_int, C.c_int, C.c_void_p)
+
+NEST_SIDES = ("west", "east", "south", "north")
+
+
+def nest_bc_structs(bc: dict, nq: int):
+    """(NestBC * nq) for boundary states given as {side: (t0, t1)} with t0, t1 of shape (nq, npz, rows, cols),
+    C-contiguous float64; a missing side gives NULL pointers."""
+    arr = (NestBC * nq)()
+    for iq in range(nq):
+        ptrs = []
+        for side in NEST_SIDES:
+            pair = bc.get(side)
+            for t in range(2):
+                ptrs.append(_p(pair[t][iq]) if pair is not None else None)
+        arr[iq] = NestBC(*ptrs)
+    return arr
 
 
 def build(force: bool = False) -> str:
@@ -47,6 +68,7 @@ def lib():
         L.orc_fv_tp_2d.restype = None
         L.orc_tracer_2d.restype = C.c_int
         L.orc_tracer_2d_cube.restype = C.c_int
+        L.orc_tracer_2d_nested.restype = C.c_int
         L.orc_mass_sum.restype = C.c_double
         L.orc_mass_sum.argtypes = [DP, DP, DP, C.c_long, C.c_long]
     return _lib
@@ -162,6 +184,37 @@ def tracer_2d(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, n
                                 C.byref(bounds_for(n, ng)), n + 1, n + 1, npz, nq, hord, q_split, C.c_double(0.0),
                                 nord_tr, C.c_double(trdm), C.c_double(lim_fac), cb, None)
     return q, dp1, mfx, mfy, cx, cy, nsplt
+
+
+def nest_bc_apply(var, bc: dict, step: float, split: float, bounds: Bounds, npx: int, npy: int, iq: int = 0):
+    """nested_grid_BC_apply_intT of tracer iq's boundary states on var (npz, njd, nid); returns a copy."""
+    var = _f64(var).copy()
+    arr = nest_bc_structs(bc, iq + 1)
+    lib().orc_nest_bc_apply(_p(var), C.byref(bounds), npx, npy, var.shape[0], C.byref(arr[iq]), C.c_double(step),
+                            C.c_double(split))
+    return var
+
+
+def tracer_2d_nested(q, dp1, mfx, mfy, cx, cy, geom, bc, nest_timestep=0, k_split=1, hord=8, q_split=0,
+                     halo_fn=None, nord_tr=0, trdm=0.0, lim_fac=1.0, nested=1, bounds: Bounds | None = None,
+                     npx: int | None = None, npy: int | None = None, da_min=None, ng: int = 3):
+    """tracer_2d_nested on one domain.  q (nq, npz, njd, nid); bc {side: (t0, t1)} (see nest_bc_structs) or
+    None.  bounds default to a whole n x n domain.  Returns (q, dp1, mfx, mfy, cx, cy, nsplt, nest_timestep)."""
+    q = _f64(q).copy()
+    dp1, mfx, mfy, cx, cy = (_f64(a).copy() for a in (dp1, mfx, mfy, cx, cy))
+    nq, npz = q.shape[0], q.shape[1]
+    if bounds is None:
+        n = q.shape[-1] - 2 * ng
+        bounds, npx, npy = bounds_for(n, ng), n + 1, n + 1
+    g = GridRef(geom, nested=nested, da_min=da_min)
+    cb = HALO_FN(halo_fn) if halo_fn is not None else HALO_FN()
+    arr = nest_bc_structs(bc, nq) if bc is not None else None
+    counter = C.c_int(nest_timestep)
+    nsplt = lib().orc_tracer_2d_nested(_p(q), _p(dp1), _p(mfx), _p(mfy), _p(cx), _p(cy), C.byref(g.struct),
+                                       C.byref(bounds), npx, npy, npz, nq, hord, q_split, C.c_double(0.0), nord_tr,
+                                       C.c_double(trdm), k_split, arr, C.byref(counter), C.c_double(lim_fac), cb,
+                                       None)
+    return q, dp1, mfx, mfy, cx, cy, nsplt, counter.value
 
 
 def tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None, ng: int = 3, nord_tr=0,

@@ -82,3 +82,28 @@ def cube_mass(q, dp, geoms, n: int, ng: int = 3):
 
 def problem(n=30, npz=5, nq=3, seed=3, **kw) -> S.Problem:
     return S.make_problem(n, npz, nq, seed=seed, **kw)
+
+
+class _SubGeom:
+    """The metric arrays of one rank's part of a tile (attributes as TileGeom's)."""
+
+
+def sub_domain(P: S.Problem, t: int, is_: int, ie: int, js: int, je: int, ng: int = 3):
+    """The arrays of the rank that owns cells [is_, ie] x [js, je] (1-based) of tile t with its own ng-cell halo:
+    (geom, [q, dp, mfx, mfy, cx, cy]) shaped as that rank's Fortran arguments, halos from the full tile."""
+    g = P.geoms[t]
+    ci, cj = slice(is_ - 1, ie + 2 * ng), slice(js - 1, je + 2 * ng)          # data-domain cells
+    fi, fj = slice(is_ - 1, ie + 2 * ng + 1), slice(js - 1, je + 2 * ng + 1)  # faces bounding them
+    sg = _SubGeom()
+    sg.dx, sg.del6_u = g.dx[fj, ci], g.del6_u[fj, ci]
+    sg.dy, sg.del6_v = g.dy[cj, fi], g.del6_v[cj, fi]
+    for name in ("dxa", "dya", "area", "rarea"):
+        setattr(sg, name, getattr(g, name)[cj, ci])
+    sg.sin_sg = g.sin_sg[:, cj, ci]
+    q = P.q[t].numpy()[..., cj, ci]
+    dp = P.dp[t].numpy()[..., cj, ci]
+    mfx = P.mfx[t].numpy()[..., js - 1:je, is_ - 1:ie + 1]
+    mfy = P.mfy[t].numpy()[..., js - 1:je + 1, is_ - 1:ie]
+    cx = P.cx[t].numpy()[..., cj, is_ - 1:ie + 1]
+    cy = P.cy[t].numpy()[..., js - 1:je + 1, ci]
+    return sg, [np.ascontiguousarray(a, dtype=np.float64) for a in (q, dp, mfx, mfy, cx, cy)]
