@@ -14,7 +14,7 @@ VP = C.c_void_p
 FV3G_FP64, FV3G_MIXED = 0, 1
 FIELDS = dict(Q=0, DELP=1, CX=2, CY=3, MFX=4, MFY=5, Q_REMAPPED=6, DELP_OUT=7)
 ERRORS = {-1: "FV3G_E_ARG", -2: "FV3G_E_CUDA", -3: "FV3G_E_COURANT", -4: "FV3G_E_NONFINITE", -5: "FV3G_E_DELP",
-          -6: "FV3G_E_UNSUPPORTED", -7: "FV3G_E_NOMEM"}
+          -6: "FV3G_E_UNSUPPORTED", -7: "FV3G_E_NOMEM", -8: "FV3G_E_CHECKSUM"}
 
 # every symbol include/fv3g.h declares (checked by the test-suite)
 EXPORTS = (
@@ -26,7 +26,8 @@ EXPORTS = (
     "fv3g_kernel_times", "fv3g_remap_columns_noalloc", "fv3g_fv_tp_2d_tl", "fv3g_fv_tp_2d_ad", "fv3g_map1_ppm_tl",
     "fv3g_map1_ppm_ad", "fv3g_state_autotune", "fv3g_state_widths", "fv3g_step_host", "fv3g_tracer_2d_1L", "fv3g_ensemble_create",
     "fv3g_ensemble_step", "fv3g_ensemble_destroy", "fv3g_fillz", "fv3g_pressure_vars", "fv3g_fillz_batched",
-    "fv3g_tracer_2d_nested",
+    "fv3g_tracer_2d_nested", "fv3g_nc_open", "fv3g_nc_close", "fv3g_nc_nvars", "fv3g_nc_var_info", "fv3g_nc_checksum",
+    "fv3g_nc_read", "fv3g_state_read_restart", "fv3g_state_write_restart",
 )
 
 

@@ -483,6 +483,32 @@ int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaS
 
 }  // namespace
 
+int fv3g::state_field_view(fv3g_state* st, int field, bool loading, StateFieldView* v) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (field != FV3G_FIELD_Q && field != FV3G_FIELD_DELP)
+    return set_error(FV3G_E_ARG, "restart files carry the tracers (FV3G_FIELD_Q) and delp (FV3G_FIELD_DELP)");
+  if (loading && field == FV3G_FIELD_Q) {
+    if (st->q_cur != 0) {
+      FV3G_CUDA(cudaMemcpyAsync(st->q[0], st->q[st->q_cur], (size_t)st->nt * st->nq * st->npz * st->plane * st->esz,
+                                cudaMemcpyDeviceToDevice, st->stream));
+      st->q_cur = 0;
+    }
+    st->remapped = false;
+  }
+  FieldShape fs;
+  CHECK(field_shape(st, field, fs, loading));
+  v->dev = fs.dev;
+  v->esz = (int)st->esz;
+  v->pg = st->pg;
+  v->plane = st->plane;
+  v->n = st->n;
+  v->npz = st->npz;
+  v->nq = st->nq;
+  v->ntiles = st->nt;
+  v->stream = st->stream;
+  return 0;
+}
+
 extern "C" {
 
 int fv3g_version(void) { return 100; }

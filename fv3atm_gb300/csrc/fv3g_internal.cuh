@@ -172,6 +172,22 @@ __device__ __forceinline__ T ppm_flux(T c, T xl, T bll, T brl, T xr, T blr, T br
 int set_error(int code, const char* fmt, ...);
 int cuda_error(cudaError_t e, const char* what);
 
+// A field of a batched state as the restart reader and writer see it: planes
+// of the state's element type (esz 4 or 8) stacked [tile][tracer][level] (Q)
+// or [tile][level] (DELP), the compute domain at pg.at(1..n, 1..n).
+struct StateFieldView {
+  void* dev;
+  int esz;
+  PlaneGeom pg;
+  long long plane;
+  int n, npz, nq, ntiles;
+  cudaStream_t stream;
+};
+// loading: the field is about to be overwritten in part (Q: the latest tracer
+// buffer becomes the home buffer first, so tracers not loaded keep their
+// values); otherwise the field's latest values are viewed for writing out.
+int state_field_view(fv3g_state* st, int field, bool loading, StateFieldView* v);
+
 #define FV3G_CUDA(call)                                         \
   do {                                                          \
     cudaError_t e__ = (call);                                   \

@@ -41,6 +41,7 @@ extern "C" {
 #define FV3G_E_DELP -5       /* a layer thickness became non-positive */
 #define FV3G_E_UNSUPPORTED -6 /* option outside the implemented set */
 #define FV3G_E_NOMEM -7      /* device allocation failed */
+#define FV3G_E_CHECKSUM -8   /* a restart variable's data disagree with its checksum attribute */
 
 /* ------------------------------------------------------------ precision -- */
 #define FV3G_FP64 0   /* FP64 throughout */
@@ -387,6 +388,56 @@ int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind)
 int fv3g_state_error(fv3g_state* st, int* code);
 /* Device pointer and element strides of a field (for zero-copy harnesses). */
 int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch);
+
+/* ------------------------------------------------------- restart files -- */
+/* The restart files of the path, fv_tracer.res.tile<t>.nc (the tracers) and
+ * fv_core.res.tile<t>.nc (delp), which fv3atm reads at start-up and writes at
+ * restart times (atmos_model.F90:105,1149-1166), in the layout of the write
+ * component (io/module_write_restart_netcdf.F90:244-317): dimensions xaxis_1,
+ * yaxis_1, zaxis_1 and the unlimited Time, every field (Time, zaxis_1,
+ * yaxis_1, xaxis_1) with a 'checksum' attribute, FMS mpp_chksum written as
+ * '(Z16)' (:444-530): the sum modulo 2^64 of the values' bit patterns taken
+ * as 64-bit integers (FP64 data) or as sign-extended 32-bit integers (FP32).
+ * Containers: netCDF classic (CDF-1), 64-bit offset (CDF-2) and 64-bit data
+ * (CDF-5).  netCDF-4/HDF5 files are refused with FV3G_E_UNSUPPORTED (convert
+ * them with nccopy -k cdf5 first).  Host-side calls (open, info, checksum,
+ * read) need no GPU. */
+typedef struct fv3g_ncfile fv3g_ncfile;
+#define FV3G_NC_FLOAT 5
+#define FV3G_NC_DOUBLE 6
+int fv3g_nc_open(const char* path, fv3g_ncfile** out);
+int fv3g_nc_close(fv3g_ncfile* f);
+int fv3g_nc_nvars(fv3g_ncfile* f, int* nvars);
+/* Variable idx (0-based): its name (NUL-terminated, cut to len), netCDF type
+ * (1 byte ... 6 double, 7..11 the CDF-5 types), rank and shape (slowest
+ * first, at most 8 entries written; the record dimension counts the file's
+ * records) and whether it is a record variable. */
+int fv3g_nc_var_info(fv3g_ncfile* f, int idx, char* name, int len, int* nc_type, int* ndims, long long* shape,
+                     int* is_record);
+/* The variable's 'checksum' attribute; present = 0 when it has none. */
+int fv3g_nc_checksum(fv3g_ncfile* f, const char* name, unsigned long long* checksum, int* present);
+/* Host read of one record (ignored for a fixed variable) converted to FP64;
+ * count must equal the variable's values per record. */
+int fv3g_nc_read(fv3g_ncfile* f, const char* name, int record, double* out, long long count);
+/* Load record 0 of nvars variables, each (zaxis, yaxis, xaxis) = (npz, n, n),
+ * into tile `tile` (0-based) of a state field: FV3G_FIELD_Q with slots[v]
+ * the tracer index of variable v, or FV3G_FIELD_DELP (one variable, slots
+ * NULL).  The file's bytes go to the GPU as they are; one kernel swaps the
+ * byte order, converts to the state's precision, places the values in the
+ * halo-padded planes (halos untouched) and sums the checksum.  verify != 0: a
+ * checksum attribute that disagrees fails with FV3G_E_CHECKSUM (fv3atm's
+ * ignore_rst_cksum = .false.).  checksums (nvars, may be NULL) receive the
+ * sums.  Loading Q makes the latest tracer buffer the home buffer first, so
+ * tracers not loaded keep their latest values.  Synchronous. */
+int fv3g_state_read_restart(fv3g_state* st, int field, int tile, fv3g_ncfile* f, const char* const* names,
+                            const int* slots, int nvars, int verify, unsigned long long* checksums);
+/* Write the latest values of tile `tile` of a state field (slots as above)
+ * to a new file at path in the write component's layout, as nc_type
+ * FV3G_NC_FLOAT or FV3G_NC_DOUBLE in container version 1, 2 or 5 (CDF-1,
+ * CDF-2, CDF-5); checksums (nvars, may be NULL) receive the sums written into
+ * the attributes.  Synchronous. */
+int fv3g_state_write_restart(fv3g_state* st, int field, int tile, const char* path, const char* const* names,
+                             const int* slots, int nvars, int nc_type, int version, unsigned long long* checksums);
 
 #ifdef __cplusplus
 }
