@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--warps", type=int, default=0,
                     help="advection warps per CTA (0 = chosen by fv3g_state_autotune)")
+    ap.add_argument("--restart", action="store_true",
+                    help="instead of the step: time writing and reading one tile's fv_tracer.res file")
+    ap.add_argument("--restart-tracers", type=int, default=4)
+    ap.add_argument("--restart-dir", default="", help="where the restart leg writes its file (default: a temp dir)")
     return ap.parse_args()
 
 
@@ -395,11 +399,58 @@ def run_reference(a, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def restart_leg(a) -> None:
+    """Write and read back tile 1's fv_tracer.res file of a mixed state (C{n} L{npz}, restart_tracers tracers)
+    through the library, FP64 and FP32 files; the best of three wall times of each call, over the file's bytes.
+    The read follows the write, so its file is served from the page cache."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from fv3atm_gb300 import restart as R
+    from fv3atm_gb300 import synth as S
+    nq = a.restart_tracers
+    P = S.make_problem(a.n, a.npz, nq, seed=2000, cmax=0.8, device="cuda")
+    st = build_state(P, "mixed", nq, a.npz, a.n)
+    names = [f"tracer{i + 1}" for i in range(nq)]
+    d = tempfile.mkdtemp(prefix="fv3g_restart_", dir=a.restart_dir or None)
+    path = os.path.join(d, "fv_tracer.res.tile1.nc")
+    legs = {}
+    try:
+        for dtype in ("double", "float"):
+            tw, tr = [], []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                sums_w = R.write_state(st, "Q", 0, path, names, dtype=dtype)
+                tw.append(time.perf_counter() - t0)
+                t0 = time.perf_counter()
+                sums_r = R.read_state(st, "Q", 0, path, names)
+                tr.append(time.perf_counter() - t0)
+                assert sums_r == sums_w
+            size = os.path.getsize(path)
+            legs[dtype] = {"file_bytes": size, "write_GBps": round(size / min(tw) / 1e9, 2),
+                           "read_GBps": round(size / min(tr) / 1e9, 2), "write_s": round(min(tw), 4),
+                           "read_s": round(min(tr), 4)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    torch.cuda.synchronize()
+    print(json.dumps({"metric": "fv_tracer.res write and read throughput, one tile", "unit": "GB/s of file",
+                      "config": {"workload": f"tile 1 of C{a.n} L{a.npz}, {nq} tracers, FP32-mixed state, CDF-2"},
+                      "legs": legs, "device": torch.cuda.get_device_name(0)}))
+
+
 def main():
     a = parse()
     world, rank, local = dist_setup()
     if a.impl == "reference":
         run_reference(a, world, rank)
+        return
+    if a.restart:
+        if rank == 0:
+            restart_leg(a)
         return
     import numpy as np
     import torch
