@@ -56,16 +56,30 @@ struct SmemWarp {
   T qi[TW][PQ];   // q_i; then q dp1/rarea + x-flux divergence (or the x fluxes)
 };
 
-// Per-warp shared memory; edge CTAs add the deviations of two lines at two
-// edges, [2][16][32] values.
+// Per-warp shared memory; edge CTAs add the edge deviations of two lines,
+// [2][slots][32] values: 8 slots (bl, br of the 4 cells beside one edge) when
+// no window holds both edges of a direction, 16 when one can (a compute
+// domain of at most 28 cells in x or y).
 template <typename T>
-__host__ __device__ constexpr size_t warp_smem_bytes(bool edges) {
-  return sizeof(SmemWarp<T>) + (edges ? 2 * 16 * 32 * sizeof(T) : 0);
+__host__ __device__ constexpr size_t warp_smem_bytes(bool edges, bool two_edges) {
+  return sizeof(SmemWarp<T>) + (edges ? 2 * (two_edges ? 16 : 8) * 32 * sizeof(T) : 0);
+}
+
+__host__ __device__ __forceinline__ bool windows_hold_two_edges(int is, int ie, int js, int je) {
+  return ie - is + 1 <= WIN - 4 || je - js + 1 <= WIN - 4;
 }
 
 template <typename T>
-size_t substep_smem_bytes(int warps, bool edges) {
-  return sizeof(SmemLevel<T>) + warps * warp_smem_bytes<T>(edges);
+size_t substep_smem_bytes(int warps, bool edges, bool two_edges) {
+  return sizeof(SmemLevel<T>) + warps * warp_smem_bytes<T>(edges, two_edges);
+}
+
+// Edge-ring CTAs of FP32 states run as k_substep_ring32, capped at 8 warps
+// and 128 registers so that two 8-warp CTAs fit an SM; FP64 and dual-number
+// ones keep 10 warps.
+template <typename T>
+__host__ __device__ constexpr int ring_max_warps() {
+  return sizeof(T) == 4 ? 8 : 10;
 }
 
 // ------------------------------------------------------- PPM line stream ---
@@ -189,10 +203,11 @@ __device__ __forceinline__ T dm_clamp(T xm, T x0, T xp) {
 struct EdgeSel {
   unsigned mask;
   int eA, eB;
+  int sb;  // first slot of edge B: 8 when a window can hold both edges, else 0
 };
-__device__ __forceinline__ EdgeSel edge_sel(int eA, int eB) {
+__device__ __forceinline__ EdgeSel edge_sel(int eA, int eB, int sb) {
   auto bits = [](int e) { return (e >= 0 && e < 32) ? (0xFu << e) : 0u; };
-  return EdgeSel{bits(eA) | bits(eB), eA, eB};
+  return EdgeSel{bits(eA) | bits(eB), eA, eB, sb};
 }
 
 template <typename T, int HORD>
@@ -207,7 +222,7 @@ struct Line {
     psm = true;
   }
 
-  // ed: this lane's edge deviations (16 lane-strided slots: edge A bl0..3 br0..3, then edge B)
+  // ed: this lane's edge deviations (lane-strided slots: edge A bl0..3 br0..3, then edge B from slot sb)
   template <bool EDGES>
   __device__ __forceinline__ T step(int m, T x, T c, const T* ed, const EdgeSel& es) {
     T alc, bl, br;
@@ -226,7 +241,7 @@ struct Line {
     }
     if (EDGES && ((es.mask >> m) & 1u)) {  // cell m-2 is cell e-2+d of an edge
       const int dA = m - es.eA;
-      const int slot = (unsigned)dA < 4u ? dA : 8 + (m - es.eB);
+      const int slot = (unsigned)dA < 4u ? dA : es.sb + (m - es.eB);
       bl = ed[slot * 32];
       br = ed[(slot + 4) * 32];
     }
@@ -261,7 +276,7 @@ template <typename T, int HORD, bool FLUXES, bool EDGES>
 __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>& L, SmemWarp<T>& S, int t, int k,
                                                T* eds, int iq, int i0, int j0, int ni, int nj, int lane, int exA,
                                                int exB, int eyA, int eyB, bool corner_block,
-                                               long long efo, long long efe) {
+                                               long long efo, long long efe, int nslot) {
   const PlaneGeom& pg = a.pg;
   const int n = a.npx - 1;
   // Cube-corner halo blocks of the window, which copy_corners fills by a
@@ -293,10 +308,11 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
   __syncwarp();
 
   T fyr[NF];  // inner y flux of this lane's column at faces 3..29 (S1 -> S3)
-  const EdgeSel esx = edge_sel(exA, exB), esy = edge_sel(eyA, eyB);
-  // edge deviations of the lines in flight: eds[line][16][32], lines 0 (and 1 in S2)
+  const int sb = nslot - 8;
+  const EdgeSel esx = edge_sel(exA, exB, sb), esy = edge_sel(eyA, eyB, sb);
+  // edge deviations of the lines in flight: eds[line][nslot][32], lines 0 (and 1 in S2)
   T* const ed0 = eds + lane;
-  T* const ed1 = eds + 16 * 32 + lane;
+  T* const ed1 = eds + nslot * 32 + lane;
   // ------------------------------------------------ S1: inner y, q_i ------
   {
     const int w = lane;
@@ -306,7 +322,7 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       auto edA = [&L, w, eyA](int m) { return L.edy[0][m - eyA + 2][w]; };
       auto edB = [&L, w, eyB](int m) { return L.edy[1][m - eyB + 2][w]; };
       edge_devs<T, HORD>(eyA, false, ex, edA, ed0);
-      edge_devs<T, HORD>(eyB, true, ex, edB, ed0 + 8 * 32);
+      edge_devs<T, HORD>(eyB, true, ex, edB, ed0 + sb * 32);
     }
     Line<T, HORD> ln;
     ln.init(T(a.lim_fac));
@@ -348,10 +364,10 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       auto edA = [&L, r, exA](int m) { return L.edx[0][m - exA + 2][r]; };
       auto edB = [&L, r, exB](int m) { return L.edx[1][m - exB + 2][r]; };
       edge_devs<T, HORD>(exA, false, exi, edA, ed0);
-      edge_devs<T, HORD>(exB, true, exi, edB, ed0 + 8 * 32);
+      edge_devs<T, HORD>(exB, true, exi, edB, ed0 + sb * 32);
       if (outer) {
         edge_devs<T, HORD>(exA, false, exo, edA, ed1);
-        edge_devs<T, HORD>(exB, true, exo, edB, ed1 + 8 * 32);
+        edge_devs<T, HORD>(exB, true, exo, edB, ed1 + sb * 32);
       }
     }
     const bool efw = EDGES && a.cube && a.eflux != nullptr && outer && ro < nj;
@@ -402,7 +418,7 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       auto edA = [&L, c, eyA](int m) { return L.edy[0][m - eyA + 2][c + 3]; };
       auto edB = [&L, c, eyB](int m) { return L.edy[1][m - eyB + 2][c + 3]; };
       edge_devs<T, HORD>(eyA, false, ex, edA, ed0);
-      edge_devs<T, HORD>(eyB, true, ex, edB, ed0 + 8 * 32);
+      edge_devs<T, HORD>(eyB, true, ex, edB, ed0 + sb * 32);
     }
     const int ig = i0 + c;
     const bool valid_c = c < ni;
@@ -447,11 +463,12 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
 // not need.  Interior CTAs cover the rectangle [bx0, bx0+nbxi) x [by0,
 // by0+nbyi) of CTA tiles; edge CTAs enumerate the ring around it row by row.
 template <typename T, int HORD, bool FLUXES, bool EDGES>
-__global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const BlockMap bm) {
+__device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap& bm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES);
+  const bool two = EDGES && windows_hold_two_edges(a.is, a.ie, a.js, a.je);
+  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES, two);
   SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
   T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
 
@@ -564,7 +581,17 @@ __global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const Block
 
   for (int iq = warp; iq < a.nq; iq += W)
     advance_tracer<T, HORD, FLUXES, EDGES>(a, L, S, t, k, eds, iq, i0, j0, ni, nj, lane, exA, exB, eyA, eyB,
-                                           corner_block, efo, efe);
+                                           corner_block, efo, efe, two ? 16 : 8);
+}
+
+template <typename T, int HORD, bool FLUXES, bool EDGES>
+__global__ void __launch_bounds__(320) k_substep(const AdvArgs<T> a, const BlockMap bm) {
+  substep_body<T, HORD, FLUXES, EDGES>(a, bm);
+}
+
+template <int HORD, bool FLUXES>
+__global__ void __launch_bounds__(256, 2) k_substep_ring32(const AdvArgs<float> a, const BlockMap bm) {
+  substep_body<float, HORD, FLUXES, true>(a, bm);
 }
 
 template <typename T, int HORD, bool FLUXES>
@@ -572,15 +599,20 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
   const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
   const int nt = a.cube ? 6 : 1;
-  const int wr = a.warps_ring > 0 ? a.warps_ring : warps;  // edge-ring CTAs may run narrower
+  // edge-ring CTAs may run narrower (and at most ring_max_warps wide)
+  const int wr = std::min(a.warps_ring > 0 ? a.warps_ring : warps, ring_max_warps<T>());
+  const bool two = windows_hold_two_edges(a.is, a.ie, a.js, a.je);
   if (nint > 0) {
     dim3 grid(nint, a.npz, nt);
-    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false), s>>>(a, bm);
+    k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false, false), s>>>(a, bm);
     FV3G_CUDA(cudaGetLastError());
   }
   if (nring > 0) {
     dim3 grid(nring, a.npz, nt);
-    k_substep<T, HORD, FLUXES, true><<<grid, 32 * wr, substep_smem_bytes<T>(wr, true), s>>>(a, bm);
+    if constexpr (sizeof(T) == 4)
+      k_substep_ring32<HORD, FLUXES><<<grid, 32 * wr, substep_smem_bytes<T>(wr, true, two), s>>>(a, bm);
+    else
+      k_substep<T, HORD, FLUXES, true><<<grid, 32 * wr, substep_smem_bytes<T>(wr, true, two), s>>>(a, bm);
     FV3G_CUDA(cudaGetLastError());
   }
   return 0;
@@ -590,14 +622,17 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
 template <typename T>
 static int max_warps() {
   int w = 10;
-  while (w > 1 && substep_smem_bytes<T>(w, true) > 227 * 1024) --w;
+  while (w > 1 && substep_smem_bytes<T>(w, true, true) > 227 * 1024) --w;
   return w;
 }
 
 template <typename T, int HORD, bool FLUXES, bool EDGES>
 static cudaError_t set_smem_attr() {
-  const int mx = (int)substep_smem_bytes<T>(max_warps<T>(), EDGES);
-  return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  const int mx = (int)substep_smem_bytes<T>(max_warps<T>(), EDGES, true);
+  if constexpr (EDGES && sizeof(T) == 4)
+    return cudaFuncSetAttribute(k_substep_ring32<HORD, FLUXES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  else
+    return cudaFuncSetAttribute(k_substep<T, HORD, FLUXES, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 template <typename T, int HORD>
@@ -617,10 +652,11 @@ static void set_attrs(cudaError_t& err) {
 
 template <typename T, int HORD>
 int launch_substep_hord(const AdvArgs<T>& a, bool flux_mode, int warps, cudaStream_t s) {
-  const int mw = max_warps<T>();
-  if (warps < 1 || warps > mw || a.warps_ring < 0 || a.warps_ring > mw)
-    return set_error(FV3G_E_ARG, "this precision supports 1..%d advection warps per CTA (got %d, ring %d)", mw,
-                     warps, a.warps_ring);
+  const int mw = max_warps<T>(), mr = std::min(mw, ring_max_warps<T>());
+  if (warps < 1 || warps > mw || a.warps_ring < 0 || a.warps_ring > mr)
+    return set_error(FV3G_E_ARG,
+                     "this precision supports 1..%d advection warps per CTA and 1..%d per edge-ring CTA (got %d, %d)",
+                     mw, mr, warps, a.warps_ring);
   return flux_mode ? launch_one<T, HORD, true>(a, warps, s) : launch_one<T, HORD, false>(a, warps, s);
 }
 
