@@ -824,7 +824,8 @@ int fv3g_state_widths(fv3g_state* st, int* warps, int* warps_ring) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   const int w = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
   if (warps) *warps = w;
-  if (warps_ring) *warps_ring = st->warps_ring > 0 ? st->warps_ring : w;
+  // the edge-ring launch is capped (8 warps for FP32 states, 10 otherwise)
+  if (warps_ring) *warps_ring = std::min(st->warps_ring > 0 ? st->warps_ring : w, ring_max_warps((int)st->esz));
   return 0;
 }
 

@@ -38,6 +38,10 @@ struct Topo {
   signed char rev[6][4];
 };
 
+// Widest edge-ring CTA (warps) of a state's element size: the FP32 ring
+// kernel is capped at 128 registers so that two 8-warp CTAs fit an SM.
+__host__ __device__ constexpr int ring_max_warps(int element_bytes) { return element_bytes == 4 ? 8 : 10; }
+
 struct PlaneGeom {
   int pitch;  // elements per row
   int rows;   // rows per plane

@@ -76,11 +76,7 @@ size_t substep_smem_bytes(int warps, bool edges, bool two_edges) {
 
 // Edge-ring CTAs of FP32 states run as k_substep_ring32, capped at 8 warps
 // and 128 registers so that two 8-warp CTAs fit an SM; FP64 and dual-number
-// ones keep 10 warps.
-template <typename T>
-__host__ __device__ constexpr int ring_max_warps() {
-  return sizeof(T) == 4 ? 8 : 10;
-}
+// ones keep 10 warps (ring_max_warps).
 
 // ------------------------------------------------------- PPM line stream ---
 // Deviations (bl, br) of the four cells e-2..e+1 around a cube-face edge at
@@ -600,7 +596,7 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
   const int nt = a.cube ? 6 : 1;
   // edge-ring CTAs may run narrower (and at most ring_max_warps wide)
-  const int wr = std::min(a.warps_ring > 0 ? a.warps_ring : warps, ring_max_warps<T>());
+  const int wr = std::min(a.warps_ring > 0 ? a.warps_ring : warps, ring_max_warps((int)sizeof(T)));
   const bool two = windows_hold_two_edges(a.is, a.ie, a.js, a.je);
   if (nint > 0) {
     dim3 grid(nint, a.npz, nt);
@@ -652,7 +648,7 @@ static void set_attrs(cudaError_t& err) {
 
 template <typename T, int HORD>
 int launch_substep_hord(const AdvArgs<T>& a, bool flux_mode, int warps, cudaStream_t s) {
-  const int mw = max_warps<T>(), mr = std::min(mw, ring_max_warps<T>());
+  const int mw = max_warps<T>(), mr = std::min(mw, ring_max_warps((int)sizeof(T)));
   if (warps < 1 || warps > mw || a.warps_ring < 0 || a.warps_ring > mr)
     return set_error(FV3G_E_ARG,
                      "this precision supports 1..%d advection warps per CTA and 1..%d per edge-ring CTA (got %d, %d)",

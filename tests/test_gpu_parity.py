@@ -615,6 +615,7 @@ def test_autotune_picks_a_width_and_leaves_results_unchanged(cuda, cube_prob):
     st.load_problem(P)
     w = st.autotune()
     assert w in (4, 5, 6, 8, 10)
+    assert st.widths()[0] == w and st.widths()[1] <= 8  # FP32 edge-ring CTAs are capped at 8 warps
     st.step(3)
     got = st.download("Q_REMAPPED")
     want = _run_cube(P, "mixed", remap=True, graph=True, warps=4).download("Q_REMAPPED")
