@@ -260,6 +260,7 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.eflux = (T*)st->eflux;
   a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
   a.warps_ring = st->warps_ring;
+  a.err = st->err;
   return a;
 }
 
@@ -351,6 +352,7 @@ int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   src.cy = (const T*)st->cy;
   src.mfx = (const T*)st->mfx;
   src.mfy = (const T*)st->mfy;
+  src.err = st->err;
   CHECK(launch_area_flux<T>((T*)st->cxs, (T*)st->cys, (T*)st->xfx, (T*)st->yfx, (T*)st->mfxs, (T*)st->mfys,
                             (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
                             (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,

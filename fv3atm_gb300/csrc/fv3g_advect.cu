@@ -125,6 +125,14 @@ __global__ void k_edge_fix(const AdvArgs<T> a, int n) {
 // ------------------------------------------------------------- prologue ---
 // Area fluxes from Courant numbers with the upwind metric, then scaling of
 // cx, cy, xfx, yfx, mfx, mfy by 1/nsplt (tracer_2d before its substep loop).
+// A compute face's inputs: finite, and the Courant number of one substep
+// (c * frac) at most 1 in magnitude (the swept region stays in the upwind cell).
+template <typename T>
+__device__ __forceinline__ void face_check(T c, T m, T frac, int* err) {
+  if (!isfinite(c) || !isfinite(m)) raise_error(err, FV3G_E_NONFINITE);
+  else if (fabs(c * frac) > T(1)) raise_error(err, FV3G_E_COURANT);
+}
+
 template <typename T>
 __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa, const T* dya,
                             const T* dx, const T* dy, const T* sin_sg, long long sFt, long long sFk,
@@ -156,7 +164,11 @@ __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const 
       else v = c * dxa[mo + p] * dy[mo + p] * s_w[p];
       xfx[fo + p] = v * frac;
       cx[fo + p] = c * frac;
-      if (j >= js && j <= je) mfx[fo + p] = mxi[fo + p] * frac;
+      if (j >= js && j <= je) {
+        const T m = mxi[fo + p];
+        mfx[fo + p] = m * frac;
+        if (src.err != nullptr) face_check(c, m, frac, src.err);
+      }
     }
     // y faces: j in js..je+1, cols isd..ied
     if (j >= js && j <= je + 1 && i <= ie + NG) {
@@ -166,7 +178,11 @@ __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const 
       else v = c * dya[mo + p] * dx[mo + p] * s_s[p];
       yfx[fo + p] = v * frac;
       cy[fo + p] = c * frac;
-      if (i >= is && i <= ie) mfy[fo + p] = myi[fo + p] * frac;
+      if (i >= is && i <= ie) {
+        const T m = myi[fo + p];
+        mfy[fo + p] = m * frac;
+        if (src.err != nullptr) face_check(c, m, frac, src.err);
+      }
     }
   }
 }

@@ -96,7 +96,13 @@ struct AdvArgs {
   T damp;           // (damp_c da_min)^(nord+1)
   int nord;
   int damp_mass;    // 1: field q, flux weighted by damp times the face mean of dp1; 0: field damp q
+  int* err;         // optional sticky error word: FV3G_E_DELP when a compute cell's dp2 is not positive
 };
+
+// First error of a batched step into its sticky word (later ones are dropped).
+__device__ __forceinline__ void raise_error(int* err, int code) {
+  if (err != nullptr) atomicCAS(err, 0, code);
+}
 
 // CTA tiles of a substep launch: the interior rectangle [bx0, bx0+nbxi) x
 // [by0, by0+nbyi) of the nbx x nby tiles holds those whose 32-cell window
@@ -238,6 +244,9 @@ struct AreaFluxSrc {
   const T* cy = nullptr;
   const T* mfx = nullptr;
   const T* mfy = nullptr;
+  // optional sticky error word: FV3G_E_NONFINITE for a non-finite Courant number or mass flux on a compute
+  // face, FV3G_E_COURANT for a scaled Courant number above 1 in magnitude
+  int* err = nullptr;
 };
 // xfx, yfx from the Courant numbers with the upwind metrics, and cx, cy, mfx,
 // mfy scaled by frac (tracer_2d's prologue); with src, read from src and write

@@ -554,7 +554,10 @@ __device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap
                          ld_field(my, pg, i, j + 1)) * ra;
       L.dpa[r][c] = d1 / ra;
       L.ub[r][c] = ra / d2;
-      if (r < nj && c < ni && dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
+      if (r < nj && c < ni) {
+        if (dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
+        if (!(d2 > T(0))) raise_error(a.err, FV3G_E_DELP);
+      }
     }
     if (EDGES) {  // metrics of the one-sided edge values: dxa across x edges, dya across y edges
       const T* dxa = a.dxa + t * a.sMt;

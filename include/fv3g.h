@@ -384,7 +384,12 @@ int fv3g_ensemble_destroy(fv3g_ensemble* ens);
 #define FV3G_KERNEL_KINDS 5
 int fv3g_set_timing(fv3g_state* st, int enable);
 int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind);
-/* Sticky device error word of the state (0 = none); cleared by reading. */
+/* Sticky device error word of the state (0 = none), the first of: FV3G_E_NONFINITE
+ * (a non-finite Courant number or mass flux on a compute face), FV3G_E_COURANT
+ * (a Courant number over q_split above 1 in magnitude), FV3G_E_DELP (a layer
+ * thickness not positive after a substep's mass fluxes), raised on the device
+ * by the steps since the last read; the step runs to its end regardless.
+ * Synchronous; cleared by reading. */
 int fv3g_state_error(fv3g_state* st, int* code);
 /* Device pointer and element strides of a field (for zero-copy harnesses). */
 int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch);

@@ -74,17 +74,21 @@ def test_cube_hord5_matches_oracle(cuda, cube_prob):
     assert rel_l2(interior(q, P.n), interior(q_ref, P.n)) <= FP64_TOL
 
 
-@pytest.mark.parametrize("n", [27, 28, 53])
+@pytest.mark.parametrize("n", [8, 27, 28, 29, 30, 53])
 @pytest.mark.parametrize("hord", [5, 8])
-def test_cube_edge_at_the_window_border(cuda, n, hord):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cube_edge_at_the_window_border(cuda, n, hord, precision):
     """Tile sizes whose east/north cube edge falls at window face 30 or 31 of the last full CTA tile (the next
-    tile holds one or two cells): the one-sided edge values still reach the faces next to the edge."""
+    tile holds one or two cells), or where windows hold both edges of a direction (n <= 28, the edge CTAs'
+    16-slot layout; n >= 29 uses 8 slots): the one-sided edge values still reach the faces next to the edge,
+    on the FP64 ring kernel and on the register-capped FP32 one."""
     P = S.make_problem(n, 2, 2, seed=17, cmax=0.8)
     q_ref, _, _ = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=hord, q_split=2)
-    st = api.CubeState(n, 2, 2, precision="fp64", hord=hord)
+    st = api.CubeState(n, 2, 2, precision=precision, hord=hord)
     st.load_problem(P)
     st.tracer_2d(2)
-    assert rel_l2(interior(st.download("Q"), n), interior(q_ref, n)) <= FP64_TOL
+    tol = FP64_TOL if precision == "fp64" else (MIXED_TOL if hord == 8 else FILTER_MIXED_TOL)
+    assert rel_l2(interior(st.download("Q"), n), interior(q_ref, n)) <= tol
     st.close()
 
 
@@ -457,6 +461,33 @@ def test_errors_are_reported_not_fatal(cuda, cube_prob):
         st.tracer_2d(1)
     with pytest.raises(Fv3gError, match="kord 7"):
         api.CubeState(P.n, P.npz, P.nq, kord=7)
+
+
+@pytest.mark.parametrize("fault,code", [("none", 0), ("nan_cx", -4), ("courant", -3), ("inf_mfx", -4),
+                                        ("mass", -5)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_state_error_word_reports_bad_inputs(cuda, fault, code, precision):
+    """The batched step's sticky error word: a non-finite Courant number or mass flux on a compute face, a
+    Courant number above q_split, or a mass flux that empties a cell; read once, then cleared."""
+    P = S.make_problem(30, 3, 2, seed=23, cmax=0.5)
+    cx, mfx = P.cx.numpy().copy(), P.mfx.numpy().copy()
+    # tile 2, level 1, the x face between cells i = 5 and 6 of row j = 8
+    if fault == "nan_cx":
+        cx[2, 1, 10, 5] = np.nan
+    elif fault == "courant":
+        cx[2, 1, 10, 5] = 2.5  # 1.25 per substep at q_split 2
+    elif fault == "inf_mfx":
+        mfx[2, 1, 7, 5] = np.inf
+    elif fault == "mass":
+        mfx[2, 1, 7, 5] = 1e15  # drains cell (5, 8) far beyond its mass
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    st.load_problem(P)
+    st.upload("CX", cx)
+    st.upload("MFX", mfx)
+    st.tracer_2d(2)
+    assert st.error_code() == code
+    assert st.error_code() == 0  # cleared by the read
+    st.close()
 
 
 def test_step_with_fill_matches_oracle_remap_then_fillz(cuda, cube_prob):
