@@ -498,6 +498,7 @@ def main():
     with ClockSampler(local) as clk:
         ms, kern = timed_steps(st, a, world, a.steps, a.warmup, stream)
     clocks = clk.summary()
+    device_error = st.error_code()  # sticky word of the steps: 0 = inputs finite, Courant <= 1, dp > 0
     value = world * units * a.steps / (ms / 1e3)
     ab = alg_bytes(a, 4, 4)
     # one substep = the interior launch + the edge-ring launch of k_substep
@@ -651,6 +652,7 @@ def main():
         "step_ops": op_ceiling(a.q_split, value / world, (clocks or {}).get("sm_max_mhz")),
         "kernel_ms_per_step": {k: v[0] / a.steps for k, v in kern.items()},
         "gpu_launches": launches,
+        "device_error": device_error,
         "clocks": clocks,
         "fp64": out.get("fp64"),
         "mixed_over_fp64": (value / out["fp64"]["value"]) if "fp64" in out else None,
