@@ -1193,8 +1193,13 @@ int fv3g_stream_sync(fv3g_state* st, void* stream) {
 
 int fv3g_state_error(fv3g_state* st, int* code) {
   if (!st || !code) return set_error(FV3G_E_ARG, "null argument");
-  FV3G_CUDA(cudaMemcpy(code, st->err, sizeof(int), cudaMemcpyDeviceToHost));
-  FV3G_CUDA(cudaMemset(st->err, 0, sizeof(int)));
+  // read and clear in order after the work queued on the state's streams (they do not
+  // synchronise with the default stream)
+  for (cudaStream_t s : {st->up, st->down})
+    if (s) FV3G_CUDA(cudaStreamSynchronize(s));
+  FV3G_CUDA(cudaMemcpyAsync(code, st->err, sizeof(int), cudaMemcpyDeviceToHost, st->stream));
+  FV3G_CUDA(cudaMemsetAsync(st->err, 0, sizeof(int), st->stream));
+  FV3G_CUDA(cudaStreamSynchronize(st->stream));
   return 0;
 }
 

@@ -389,7 +389,8 @@ int fv3g_kernel_times(fv3g_state* st, double* ms_by_kind, int* launches_by_kind)
  * (a Courant number over q_split above 1 in magnitude), FV3G_E_DELP (a layer
  * thickness not positive after a substep's mass fluxes), raised on the device
  * by the steps since the last read; the step runs to its end regardless.
- * Synchronous; cleared by reading. */
+ * Waits for the work queued on the state's own streams (work queued on a
+ * caller's stream must be complete first); cleared by reading. */
 int fv3g_state_error(fv3g_state* st, int* code);
 /* Device pointer and element strides of a field (for zero-copy harnesses). */
 int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch);
