@@ -69,6 +69,13 @@ __host__ __device__ __forceinline__ bool windows_hold_two_edges(int is, int ie, 
   return ie - is + 1 <= WIN - 4 || je - js + 1 <= WIN - 4;
 }
 
+// Edge CTAs of FP64 and dual-number states keep 16 slots everywhere (their
+// shared memory does not limit them; the fixed layout keeps their registers).
+template <typename T>
+__host__ __device__ __forceinline__ bool edge_slots16(int is, int ie, int js, int je) {
+  return sizeof(T) != 4 || windows_hold_two_edges(is, ie, js, je);
+}
+
 template <typename T>
 size_t substep_smem_bytes(int warps, bool edges, bool two_edges) {
   return sizeof(SmemLevel<T>) + warps * warp_smem_bytes<T>(edges, two_edges);
@@ -463,7 +470,7 @@ __device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  const bool two = EDGES && windows_hold_two_edges(a.is, a.ie, a.js, a.je);
+  const bool two = EDGES && edge_slots16<T>(a.is, a.ie, a.js, a.je);
   unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES, two);
   SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
   T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
@@ -600,7 +607,7 @@ static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const int nt = a.cube ? 6 : 1;
   // edge-ring CTAs may run narrower (and at most ring_max_warps wide)
   const int wr = std::min(a.warps_ring > 0 ? a.warps_ring : warps, ring_max_warps((int)sizeof(T)));
-  const bool two = windows_hold_two_edges(a.is, a.ie, a.js, a.je);
+  const bool two = edge_slots16<T>(a.is, a.ie, a.js, a.je);
   if (nint > 0) {
     dim3 grid(nint, a.npz, nt);
     k_substep<T, HORD, FLUXES, false><<<grid, 32 * warps, substep_smem_bytes<T>(warps, false, false), s>>>(a, bm);
