@@ -151,7 +151,9 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        # the raw samples; FV3G_CLOCKS_DIR picks where they are kept (default: the temp directory)
+        import tempfile
+        self.path = os.path.join(os.environ.get("FV3G_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_rank{index}.csv")
 
     def __enter__(self):
         try:
