@@ -1,6 +1,6 @@
 // fv3_oracle.cpp -- FP64 CPU restatement of the FV3 tracer-transport path.
 //
-// TEST INFRASTRUCTURE ONLY (the checker for the CUDA path).  See fv3_oracle.h
+// TEST INFRASTRUCTURE ONLY (the oracle the CUDA path is compared with).  See fv3_oracle.h
 // for the method references and the parity status (unpinned: the upstream
 // Fortran is an empty submodule in the reference tree, .gitmodules:1-4).
 //

@@ -1,7 +1,7 @@
 /*
  * fv3_oracle.h -- FP64 CPU restatement of the FV3 tracer-transport path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA path in
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the CUDA path in
  * fv3atm_gb300/ is compared against.  Only tests/, __graft_entry__.smoke() and
  * bench.py's CPU-baseline leg may load it.  It is never part of the product.
  *

@@ -1,6 +1,6 @@
 """ctypes bindings of the FP64 CPU oracle (oracle/fv3_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY: the checker that the CUDA path is compared against.
+TEST INFRASTRUCTURE ONLY: the oracle that the CUDA path is compared against.
 The library is built by ``make -C oracle`` (``build()`` below does it).
 Parity against the upstream Fortran is unpinned (its source is absent).
 """

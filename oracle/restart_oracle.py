@@ -1,6 +1,6 @@
 """FMS ``mpp_chksum`` and the text of a restart file's ``checksum`` attribute, restated in numpy.
 
-TEST INFRASTRUCTURE ONLY: the checker for the restart reader and writer.
+TEST INFRASTRUCTURE ONLY: the oracle of the restart reader and writer.
 
 ``mpp_chksum`` (FMS, called by io/module_write_restart_netcdf.F90:444-500 on the field it writes) sums the
 values' bit patterns as integers: an FP64 array as 64-bit integers, an FP32 array as 32-bit integers widened

@@ -45,7 +45,7 @@ def test_barrier_and_max_over_ranks_on_gloo(tmp_path):
 
 @pytest.mark.timeout(600)
 def test_reference_arm_under_torchrun_prints_once():
-    """`bench.py --impl reference` launched as the driver launches N > 1 (torchrun, 127.0.0.1): rank 0 times
+    """`bench.py --impl reference` launched as a multi-GPU run launches it (torchrun, 127.0.0.1): rank 0 times
     the CPU oracle and prints one JSON line, rank 1 exits 0 without output."""
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="2")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
