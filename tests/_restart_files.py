@@ -55,3 +55,57 @@ def read_fields(path) -> dict:
                 ck = getattr(v, "checksum", None)
                 out[name] = (np.array(v[0]), ck.decode() if isinstance(ck, bytes) else ck)
     return out
+
+
+def write_cdf5(path, fields: dict, checksum: bool = True):
+    """A CDF-5 (64-bit data) file in the write component's layout, packed by hand from the published format
+    (scipy writes CDF-1/2 only): big-endian, 8-byte counts, sizes, dimension ids and offsets."""
+    import struct
+    first = next(iter(fields.values()))
+    npz, n = first.shape[0], first.shape[-1]
+    dims = [("xaxis_1", n), ("yaxis_1", n), ("zaxis_1", npz), ("Time", 0)]
+
+    def name(s):
+        b = s.encode()
+        return struct.pack(">q", len(b)) + b + b"\0" * (-len(b) % 4)
+
+    def text_attr(k, v):
+        b = v.encode()
+        return name(k) + struct.pack(">iq", 2, len(b)) + b + b"\0" * (-len(b) % 4)
+
+    # (name, dimids, attrs, nc_type, bytes per record or in all, record, data bytes)
+    vars_ = [(a, [i], [("axis", a[0].upper())], 6, 8 * ln, False,
+              np.arange(1, ln + 1, dtype=">f8").tobytes()) for i, (a, ln) in enumerate(dims[:3])]
+    vars_.append(("Time", [3], [("cartesian_axis", "T")], 6, 8, True, np.array([1.0], ">f8").tobytes()))
+    for k, a in fields.items():
+        t = 6 if a.dtype == np.float64 else 5
+        attrs = [("checksum", z16(mpp_chksum(a)))] if checksum else []
+        vars_.append((k, [3, 2, 1, 0], attrs, t, a.nbytes, True, a.astype(a.dtype.newbyteorder(">")).tobytes()))
+
+    def header(begins):
+        h = b"CDF\x05" + struct.pack(">q", 1)
+        h += struct.pack(">iq", 10, len(dims)) + b"".join(name(d) + struct.pack(">q", ln) for d, ln in dims)
+        h += struct.pack(">iq", 0, 0)  # no global attributes
+        h += struct.pack(">iq", 11, len(vars_))
+        for (vn, ids, attrs, t, nb, rec, _), beg in zip(vars_, begins):
+            h += name(vn) + struct.pack(">q", len(ids)) + b"".join(struct.pack(">q", i) for i in ids)
+            h += (struct.pack(">iq", 12, len(attrs)) + b"".join(text_attr(k, v) for k, v in attrs)) if attrs \
+                else struct.pack(">iq", 0, 0)
+            h += struct.pack(">iqq", t, nb + (-nb % 4), beg)
+        return h
+
+    off = len(header([0] * len(vars_)))
+    begins = [0] * len(vars_)
+    for i, v in enumerate(vars_):  # the fixed variables first, then the record section
+        if not v[5]:
+            begins[i] = off
+            off += v[4] + (-v[4] % 4)
+    for i, v in enumerate(vars_):
+        if v[5]:
+            begins[i] = off
+            off += v[4] + (-v[4] % 4)
+    with open(path, "wb") as f:
+        f.write(header(begins))
+        for (vn, ids, attrs, t, nb, rec, data), beg in zip(vars_, begins):
+            f.seek(beg)
+            f.write(data + b"\0" * (-len(data) % 4))

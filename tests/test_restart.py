@@ -82,3 +82,20 @@ def test_refusals_are_errors_not_crashes(tmp_path):
     with R.NcFile(good) as f:
         with pytest.raises(Fv3gError, match="no variable"):
             f.read("rainwat")
+
+
+def test_reader_parses_a_cdf5_file(tmp_path):
+    """64-bit counts, sizes, dimension ids and offsets (CDF-5), FP64 and FP32 fields."""
+    from ._restart_files import write_cdf5
+    rng = np.random.default_rng(9)
+    fields = {"sphum": rng.random((3, 5, 5)), "o3mr": rng.random((3, 5, 5)).astype(np.float32)}
+    path = str(tmp_path / "cdf5.nc")
+    write_cdf5(path, fields)
+    with R.NcFile(path) as f:
+        v = f.variables()
+        assert list(v) == ["xaxis_1", "yaxis_1", "zaxis_1", "Time", "sphum", "o3mr"]
+        assert v["o3mr"] == (np.dtype(np.float32), (1, 3, 5, 5), True)
+        for k, a in fields.items():
+            assert np.array_equal(f.read(k), a.astype(np.float64))
+            assert f.checksum(k) == mpp_chksum(a)
+        assert np.array_equal(f.read("zaxis_1"), np.arange(1.0, 4.0))
