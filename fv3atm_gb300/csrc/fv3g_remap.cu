@@ -396,44 +396,54 @@ __device__ __forceinline__ Mat2<T> shfl_up_mat(const Mat2<T>& m, int o) {
 // backward (lane+o first); both return the exclusive prefix's offset, i.e.
 // the recurrence value entering this lane's first (forward) or last
 // (backward) element, given that the chain starts with a constant map.
-// The same scans on N independent chains, level by level (their shuffles
-// and multiplies interleave).
+//
+// The multipliers of the remap's substitution scans depend on the column only
+// (the LU factors), not on the field: their values entering each of the five
+// scan steps are computed once per column (scan_muls_*), and each field's
+// scans then move only their offsets, N chains interleaved (one shuffle and
+// one multiply-add per step and chain).
+template <typename T>
+__device__ __forceinline__ void scan_muls_fwd(T al, T (&m)[5], int lane) {
+#pragma unroll
+  for (int o = 1, s = 0; o < 32; o <<= 1, ++s) {
+    m[s] = al;
+    const T pa = __shfl_up_sync(0xffffffffu, al, o);
+    if (lane >= o) al = al * pa;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void scan_muls_bwd(T al, T (&m)[5], int lane) {
+#pragma unroll
+  for (int o = 1, s = 0; o < 32; o <<= 1, ++s) {
+    m[s] = al;
+    const T pa = __shfl_down_sync(0xffffffffu, al, o);
+    if (lane + o < 32) al = al * pa;
+  }
+}
 template <typename T, int N>
-__device__ __forceinline__ void affine_enter_fwd_n(T (&al)[N], T (&be)[N], T (&out)[N], int lane) {
+__device__ __forceinline__ void affine_enter_fwd_m(const T (&m)[5], T (&be)[N], T (&out)[N], int lane) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    T pa[N], pb[N];
+  for (int o = 1, s = 0; o < 32; o <<= 1, ++s) {
+    T pb[N];
 #pragma unroll
-    for (int h = 0; h < N; ++h) {
-      pa[h] = __shfl_up_sync(0xffffffffu, al[h], o);
-      pb[h] = __shfl_up_sync(0xffffffffu, be[h], o);
-    }
+    for (int h = 0; h < N; ++h) pb[h] = __shfl_up_sync(0xffffffffu, be[h], o);
 #pragma unroll
     for (int h = 0; h < N; ++h)
-      if (lane >= o) {
-        be[h] = al[h] * pb[h] + be[h];
-        al[h] = al[h] * pa[h];
-      }
+      if (lane >= o) be[h] = m[s] * pb[h] + be[h];
   }
 #pragma unroll
   for (int h = 0; h < N; ++h) out[h] = __shfl_up_sync(0xffffffffu, be[h], 1);
 }
 template <typename T, int N>
-__device__ __forceinline__ void affine_enter_bwd_n(T (&al)[N], T (&be)[N], T (&out)[N], int lane) {
+__device__ __forceinline__ void affine_enter_bwd_m(const T (&m)[5], T (&be)[N], T (&out)[N], int lane) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    T pa[N], pb[N];
+  for (int o = 1, s = 0; o < 32; o <<= 1, ++s) {
+    T pb[N];
 #pragma unroll
-    for (int h = 0; h < N; ++h) {
-      pa[h] = __shfl_down_sync(0xffffffffu, al[h], o);
-      pb[h] = __shfl_down_sync(0xffffffffu, be[h], o);
-    }
+    for (int h = 0; h < N; ++h) pb[h] = __shfl_down_sync(0xffffffffu, be[h], o);
 #pragma unroll
     for (int h = 0; h < N; ++h)
-      if (lane + o < 32) {
-        be[h] = al[h] * pb[h] + be[h];
-        al[h] = al[h] * pa[h];
-      }
+      if (lane + o < 32) be[h] = m[s] * pb[h] + be[h];
   }
 #pragma unroll
   for (int h = 0; h < N; ++h) out[h] = __shfl_down_sync(0xffffffffu, be[h], 1);
@@ -631,6 +641,20 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
   T rdpk[NPL];
 #pragma unroll
   for (int j = 0; j < NPL; ++j) rdpk[j] = T(1) / dpk[j];
+  // the substitution scans' multipliers (column constants): forward a_j = -mco_j rd_j, backward -cp_j
+  T ajv[NPL], mf[5], mb[5];
+  {
+    T alf = T(1), alb = T(1);
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+      ajv[j] = -mco[j] * rdv[j];
+      alf = ajv[j] * alf;
+    }
+#pragma unroll
+    for (int j = NPL - 1; j >= 0; --j) alb = -cpb[j] * alb;
+    scan_muls_fwd(alf, mf, lane);
+    scan_muls_bwd(alb, mb, lane);
+  }
   constexpr int FP = fields_per_pass<T>();
   for (int f0 = 0; f0 < a.nfield; f0 += FP) {
     __syncthreads();  // every warp is done with the previous pass, whose slots are refilled now
@@ -661,25 +685,22 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
 #pragma unroll
         for (int j = 0; j < NPL; ++j) st[h][j] = qv[h][0];
     } else {
-      T rhs[FP][NPL], qa[FP][NPL], qb[FP][NPL], al[FP], be[FP];
+      T rhs[FP][NPL], qa[FP][NPL], qb[FP][NPL], be[FP];
 #pragma unroll
       for (int h = 0; h < FP; ++h) {
-        al[h] = T(1);
         be[h] = T(0);
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
           qa[h][j] = Q[h][pk<T>(ia[j])];
           qb[h][j] = Q[h][pk<T>(ib[j])];
           rhs[h][j] = wa[j] * qa[h][j] + wb[j] * qb[h][j] + wc[j] * qsv;
-          const T aj = -mco[j] * rdv[j];
-          be[h] = aj * be[h] + rhs[h][j] * rdv[j];
-          al[h] = aj * al[h];
+          be[h] = ajv[j] * be[h] + rhs[h][j] * rdv[j];
         }
       }
       T y[FP][NPL];
       {
         T yp[FP];
-        affine_enter_fwd_n<T, FP>(al, be, yp, lane);
+        affine_enter_fwd_m<T, FP>(mf, be, yp, lane);
 #pragma unroll
         for (int h = 0; h < FP; ++h)
 #pragma unroll
@@ -690,16 +711,12 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
       }
 #pragma unroll
       for (int h = 0; h < FP; ++h) {
-        al[h] = T(1);
         be[h] = T(0);
 #pragma unroll
-        for (int j = NPL - 1; j >= 0; --j) {
-          be[h] = -cpb[j] * be[h] + y[h][j];
-          al[h] = -cpb[j] * al[h];
-        }
+        for (int j = NPL - 1; j >= 0; --j) be[h] = -cpb[j] * be[h] + y[h][j];
       }
       T av[FP];
-      affine_enter_bwd_n<T, FP>(al, be, av, lane);
+      affine_enter_bwd_m<T, FP>(mb, be, av, lane);
 #pragma unroll
       for (int h = 0; h < FP; ++h)
 #pragma unroll
@@ -792,7 +809,7 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
         for (int j = 0; j < NPL; ++j) {
           const int t = u0 + j;
           const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
-          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
+          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) * (float)rdpk[j]);
         }
       } else {
 #pragma unroll
