@@ -809,7 +809,9 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
         for (int j = 0; j < NPL; ++j) {
           const int t = u0 + j;
           const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
-          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) * (float)rdpk[j]);
+          // a division, not a product with the rounded reciprocal: that rounding is shared by every tracer
+          // of the layer and biased the global mass (+5e-10 per step at C384 L127 x20)
+          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
         }
       } else {
 #pragma unroll
