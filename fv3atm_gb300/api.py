@@ -286,6 +286,12 @@ class CubeState:
         _lib.call("fv3g_state_autotune", self._h, C.byref(w))
         return w.value
 
+    def nsplt(self) -> int:
+        """Substeps of the last tracer_2d (q_split, or the count derived from the Courant maximum)."""
+        n = C.c_int(0)
+        _lib.call("fv3g_state_nsplt", self._h, C.byref(n))
+        return n.value
+
     def widths(self) -> tuple:
         """(interior, edge-ring) advection CTA widths in warps."""
         w, r = C.c_int(0), C.c_int(0)

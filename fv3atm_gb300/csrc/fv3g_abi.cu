@@ -131,7 +131,8 @@ struct fv3g_state {
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
   double* partials = nullptr; double* mass_out = nullptr;
-  unsigned int* cmax = nullptr;
+  unsigned long long* cmax = nullptr;  // bits of the Courant maximum (q_split 0)
+  int last_nsplt = 0;                  // substeps of the last tracer_2d
   int* err = nullptr;
   double* stage = nullptr; size_t stage_bytes = 0;  // FP64 staging for uploads
   cudaStream_t stream = nullptr;
@@ -413,6 +414,35 @@ int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
   return 0;
 }
 
+// The substep count of a tracer_2d call: q_split when it is given, else
+// tracer_2d's int(1 + max |Courant|) over every tile's compute cells (the
+// unscaled inputs), read back once; non-finite Courant numbers and counts
+// above 64 are errors.
+int resolve_nsplt(fv3g_state* st, int q_split, cudaStream_t s, int* nsplt) {
+  if (q_split < 0 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 0..64 on the batched path");
+  if (q_split > 0) {
+    *nsplt = q_split;
+    return 0;
+  }
+  FV3G_CUDA(cudaMemsetAsync(st->cmax, 0, sizeof(unsigned long long), s));
+  if (st->fp64)
+    CHECK(launch_max_courant<double>((const double*)st->cx, (const double*)st->cy, st->plane * st->npz, st->plane,
+                                     st->pg, 1, st->n, 1, st->n, st->nt, st->npz, st->cmax, s));
+  else
+    CHECK(launch_max_courant<float>((const float*)st->cx, (const float*)st->cy, st->plane * st->npz, st->plane,
+                                    st->pg, 1, st->n, 1, st->n, st->nt, st->npz, st->cmax, s));
+  unsigned long long bits = 0;
+  FV3G_CUDA(cudaMemcpyAsync(&bits, st->cmax, sizeof bits, cudaMemcpyDeviceToHost, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  double cmax;
+  memcpy(&cmax, &bits, sizeof cmax);
+  if (!std::isfinite(cmax)) return set_error(FV3G_E_NONFINITE, "non-finite Courant number");
+  const int n = (int)(1.0 + cmax);
+  if (n > 64) return set_error(FV3G_E_COURANT, "Courant number too large (nsplt=%d > 64)", n);
+  *nsplt = n;
+  return 0;
+}
+
 template <typename T>
 int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   CHECK(prologue_t<T>(st, nsplt, s));
@@ -594,7 +624,7 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);
   if (!rc) rc = dalloc(st, (void**)&st->mass_out, sizeof(double) * d.nq);
-  if (!rc) rc = dalloc(st, (void**)&st->cmax, sizeof(unsigned));
+  if (!rc) rc = dalloc(st, (void**)&st->cmax, sizeof(unsigned long long));
   if (!rc) rc = dalloc(st, (void**)&st->err, sizeof(int));
   if (!rc) {
     e = cudaStreamSynchronize(st->stream);
@@ -730,9 +760,17 @@ int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4,
 
 int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
-  if (q_split < 1 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 1..64 on the batched path");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
-  return st->fp64 ? tracer_2d_t<double>(st, q_split, s) : tracer_2d_t<float>(st, q_split, s);
+  int nsplt = q_split;
+  CHECK(resolve_nsplt(st, q_split, s, &nsplt));
+  st->last_nsplt = nsplt;
+  return st->fp64 ? tracer_2d_t<double>(st, nsplt, s) : tracer_2d_t<float>(st, nsplt, s);
+}
+
+int fv3g_state_nsplt(fv3g_state* st, int* nsplt) {
+  if (!st || !nsplt) return set_error(FV3G_E_ARG, "null argument");
+  *nsplt = st->last_nsplt;
+  return 0;
 }
 
 // Time one substep (interior + edge-ring launches, halo fill and prologue)
@@ -889,6 +927,8 @@ int fv3g_ensemble_create(fv3g_state* const* members, int n, fv3g_ensemble** out)
 
 int fv3g_ensemble_step(fv3g_ensemble* e, int q_split, void* stream) {
   if (!e) return set_error(FV3G_E_ARG, "null ensemble");
+  // one graph for every member: the count is fixed (no read of the Courant maximum inside a capture)
+  if (q_split < 1 || q_split > 64) return set_error(FV3G_E_ARG, "the ensemble step needs q_split 1..64");
   for (fv3g_state* st : e->m) {
     if (!st->levels_set) return set_error(FV3G_E_ARG, "a member has no levels (fv3g_state_set_levels)");
     if (st->timing) return set_error(FV3G_E_ARG, "per-kernel timing is not available inside an ensemble step");
@@ -955,6 +995,9 @@ int fv3g_remap_batched(fv3g_state* st, void* stream) {
 int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  if (q_split == 0) {  // the count first (one read of the Courant maximum), then the step for that count
+    CHECK(resolve_nsplt(st, 0, s, &q_split));
+  }
   if (!use_graph) {
     st->nev = 0;
     CHECK(mark(st, -1, s));
@@ -987,6 +1030,7 @@ int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
   FV3G_CUDA(cudaGraphLaunch(st->gexec, s));
   st->q_cur = 0;
   st->remapped = true;
+  st->last_nsplt = q_split;
   return 0;
 }
 
@@ -1106,7 +1150,7 @@ int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, voi
 int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* delp, const void* cx, const void* cy,
                    const void* mfx, const void* mfy, void* q_out, int host_f32, int groups, void* stream) {
   if (!st || !q_in || !delp || !cx || !cy || !mfx || !mfy || !q_out) return set_error(FV3G_E_ARG, "null argument");
-  if (q_split < 1 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 1..64 on the batched path");
+  if (q_split < 0 || q_split > 64) return set_error(FV3G_E_ARG, "q_split must be 0..64 on the batched path");
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
   if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
   const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
@@ -1147,6 +1191,9 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
     CHECK(plane_copy(st, fs, (void*)lev_src[f], false, cudaMemcpyHostToDevice, us));
   }
   FV3G_CUDA(cudaEventRecord(ev_lev, us));
+  // q_split 0: the count from the uploaded Courant numbers (the host waits for the per-level uploads)
+  if (q_split == 0) CHECK(resolve_nsplt(st, 0, us, &q_split));
+  st->last_nsplt = q_split;
   auto group = [&](int g, int& g0, int& ng) {
     g0 = (int)((long long)st->nq * g / G);
     ng = (int)((long long)st->nq * (g + 1) / G) - g0;

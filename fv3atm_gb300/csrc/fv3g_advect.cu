@@ -189,17 +189,24 @@ __global__ void k_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const 
 
 template <typename T>
 __global__ void k_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is, int ie,
-                              int js, int je, unsigned int* out) {
+                              int js, int je, unsigned long long* out) {
+  // max(|cx|, |cy|) over the compute cells (tracer_2d's cmax), exact in FP64; a non-finite value wins
+  // (NaN compares false, so it is carried explicitly)
   const int t = blockIdx.z, k = blockIdx.y;
   const int ni = ie - is + 1, nj = je - js + 1;
-  float m = 0.f;
+  double m = 0.0;
+  bool bad = false;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ni * nj; e += gridDim.x * blockDim.x) {
     const int i = is + e % ni, j = js + e / ni;
     const long long p = t * sFt + k * sFk + pg.at(i, j);
-    m = fmaxf(m, fmaxf(fabsf((float)cx[p]), fabsf((float)cy[p])));
+    const double a = fabs((double)cx[p]), b = fabs((double)cy[p]);
+    bad = bad || !isfinite(a) || !isfinite(b);
+    m = fmax(m, fmax(a, b));
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+  if (bad) m = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // non-negative doubles order as their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
 // ------------------------------------------------------------ launchers ---
@@ -347,7 +354,7 @@ int launch_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa,
 
 template <typename T>
 int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is, int ie, int js,
-                       int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s) {
+                       int je, int ntiles, int npz, unsigned long long* d_out, cudaStream_t s) {
   const int ncell = (ie - is + 1) * (je - js + 1);
   dim3 grid(std::min((ncell + 255) / 256, 64), npz, ntiles);
   k_max_courant<T><<<grid, 256, 0, s>>>(cx, cy, sFt, sFk, pg, is, ie, js, je, d_out);
@@ -364,7 +371,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \
                                    int, T, cudaStream_t, AreaFluxSrc<T>);                                    \
   template int launch_max_courant<T>(const T*, const T*, long long, long long, PlaneGeom, int, int, int, int, int, \
-                                     int, unsigned int*, cudaStream_t);
+                                     int, unsigned long long*, cudaStream_t);
 FV3G_INST(float)
 FV3G_INST(double)
 #undef FV3G_INST

@@ -258,7 +258,7 @@ int launch_area_flux(T* cx, T* cy, T* xfx, T* yfx, T* mfx, T* mfy, const T* dxa,
                      int ntiles, int npz, T frac, cudaStream_t s, AreaFluxSrc<T> src = AreaFluxSrc<T>{});
 template <typename T>
 int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, PlaneGeom pg, int is,
-                       int ie, int js, int je, int ntiles, int npz, unsigned int* d_out, cudaStream_t s);
+                       int ie, int js, int je, int ntiles, int npz, unsigned long long* d_out, cudaStream_t s);
 
 // Copy nplanes planes of width_bytes x height between pitched buffers
 // (slice = bytes from one plane to the next); device-to-device and uploads

@@ -323,12 +323,18 @@ int fv3g_download(fv3g_state* st, int field, double* host);
 int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream);
 int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream);
 
-/* One tracer_2d call on device data (nsplt = q_split; q_split must be > 0). */
+/* One tracer_2d call on device data: nsplt = q_split (1..64), or with
+ * q_split = 0 tracer_2d's int(1 + max |Courant|) over every tile's compute
+ * cells of CX and CY (one device-to-host read, so the call waits for the
+ * stream; FV3G_E_NONFINITE / FV3G_E_COURANT for a non-finite maximum or a
+ * count above 64).  fv3g_state_nsplt returns the count used last. */
 int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream);
+int fv3g_state_nsplt(fv3g_state* st, int* nsplt);
 /* Remap every tracer from the Lagrangian levels of DELP_OUT to ak + bk*ps. */
 int fv3g_remap_batched(fv3g_state* st, void* stream);
 /* tracer_2d + remap; with use_graph the step is captured once as a CUDA graph
- * and replayed on later calls with the same q_split. */
+ * and replayed on later calls with the same substep count (q_split 0: the
+ * count is derived first, as in fv3g_tracer_2d_batched). */
 int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream);
 /* Compensated FP64 global tracer mass sum(q*delp*area) over 6 tiles, per
  * tracer, of the field (FV3G_FIELD_Q with DELP, or Q_REMAPPED with the
@@ -350,7 +356,9 @@ int fv3g_stream_sync(fv3g_state* st, void* stream);
  * double (FP64 states); page-locked host memory for full bandwidth.  With a
  * stream the work is ordered after the stream's prior work and the call
  * returns once it is enqueued (the stream waits for its end); with NULL it
- * returns when q_out holds the result. */
+ * returns when q_out holds the result.  q_split 0 derives the substep count
+ * from the uploaded Courant numbers (the call then waits for the per-level
+ * uploads before it enqueues the rest). */
 int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* delp, const void* cx,
                    const void* cy, const void* mfx, const void* mfy, void* q_out, int host_f32,
                    int groups, void* stream);

@@ -533,6 +533,46 @@ def test_step_host_pipelined_equals_device_step(cuda, cube_prob, precision, grou
     st.close()
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_batched_q_split_zero_derives_the_substep_count(cuda, precision, tol):
+    """q_split 0 on the batched path (fv_core_nml's default): nsplt = int(1 + max |Courant|) as tracer_2d
+    derives it, the same result as passing that count, through tracer_2d, the graph step and the host step."""
+    import torch
+    P = S.make_problem(24, 3, 2, seed=29, cmax=1.6)
+    q_ref, _, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=8, q_split=0)
+    assert ns >= 2
+    a = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    b = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    a.load_problem(P)
+    b.load_problem(P)
+    a.tracer_2d(0)
+    b.tracer_2d(ns)
+    assert a.nsplt() == ns and b.nsplt() == ns
+    assert rel_l2(interior(a.download("Q"), P.n), interior(q_ref, P.n)) <= tol
+    assert np.array_equal(a.download("Q"), b.download("Q"))
+    for st in (a, b):
+        st.load_problem(P)
+    a.step(0)
+    b.step(ns)
+    want = b.download("Q_REMAPPED")
+    assert a.nsplt() == ns and np.array_equal(a.download("Q_REMAPPED"), want)
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
+    host = {k: torch.as_tensor(v).to(dt).contiguous().pin_memory() for k, v in src.items()}
+    out = torch.zeros(a.field_shape("Q_REMAPPED"), dtype=dt).pin_memory()
+    a.step_host(0, host["Q"].data_ptr(), {k: h.data_ptr() for k, h in host.items()}, out.data_ptr(),
+                precision == "mixed", 2)
+    assert a.nsplt() == ns and np.array_equal(out.numpy().astype(np.float64), want)
+    from fv3atm_gb300._lib import Fv3gError
+    cx = P.cx.numpy().copy()
+    cx[1, 0, 9, 4] = np.nan
+    a.upload("CX", cx)
+    with pytest.raises(Fv3gError, match="non-finite"):
+        a.tracer_2d(0)
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_field_copies_roundtrip_many_planes(cuda, precision):
     """6 x 9 x 127 planes through the device, pinned-host and FP64-host copy paths."""
