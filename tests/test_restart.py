@@ -99,3 +99,15 @@ def test_reader_parses_a_cdf5_file(tmp_path):
             assert np.array_equal(f.read(k), a.astype(np.float64))
             assert f.checksum(k) == mpp_chksum(a)
         assert np.array_equal(f.read("zaxis_1"), np.arange(1.0, 4.0))
+
+
+def test_truncated_data_is_an_error(tmp_path):
+    """A file whose header is whole but whose values stop early: the host read reports a short read."""
+    good = str(tmp_path / "good.nc")
+    write_fields(good, {"sphum": np.ones((4, 6, 6))})
+    data = open(good, "rb").read()
+    cut = tmp_path / "cut.nc"
+    cut.write_bytes(data[:-100])
+    with R.NcFile(str(cut)) as f:
+        with pytest.raises(Fv3gError, match="short read"):
+            f.read("sphum")
