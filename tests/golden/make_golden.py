@@ -50,6 +50,32 @@ def cube_fixture():
     return {**d, **out, "n": np.array(12)}
 
 
+# tracer_2d_nested cases of the nested fixture: name -> oracle keyword arguments
+NESTED_CASES = {
+    "h8": dict(hord=8, q_split=2),
+    "h5_nord1": dict(hord=5, q_split=2, nord_tr=1, trdm=0.1),
+}
+
+
+def nested_fixture():
+    """One C12-sized nested domain (no cube edges or corners), 2 levels, 2 tracers: boundary states at t0 (the
+    initial halo) and t1, k_split 2, the substep count entering at 1."""
+    P = S.make_problem(12, 2, 2, seed=303, cmax=0.8, ntiles=1)
+    d = {k: getattr(P, k)[0].numpy() for k in ("q", "dp", "cx", "cy", "mfx", "mfy")}
+    g = P.geoms[0]
+    for f in GEOM_FIELDS:
+        d["geom_" + f] = getattr(g, f)
+    strips = S.nest_strips(d["q"], d["q"] * 1.25 + 0.05, -2, -2, 13, 13)
+    for side, (t0, t1) in strips.items():
+        d[f"bc_{side}_t0"], d[f"bc_{side}_t1"] = t0, t1
+    out = {}
+    for name, kw in NESTED_CASES.items():
+        r = O.tracer_2d_nested(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], g, strips, nest_timestep=1,
+                               k_split=2, **kw)
+        out[f"q_{name}"], out[f"dp_{name}"], out[f"count_{name}"] = r[0], r[1][..., 3:15, 3:15], np.array(r[7])
+    return {**d, **out, "n": np.array(12)}
+
+
 def remap_fixture():
     from fv3atm_gb300 import grid as G
     rng = np.random.default_rng(202)
@@ -120,6 +146,7 @@ def op_counts():
 if __name__ == "__main__":
     np.savez_compressed(os.path.join(HERE, "cube_c12_l2.npz"), **cube_fixture())
     np.savez_compressed(os.path.join(HERE, "remap_columns_l63.npz"), **remap_fixture())
+    np.savez_compressed(os.path.join(HERE, "nested_c12_l2.npz"), **nested_fixture())
     with open(os.path.join(HERE, "c48_bell_norms.json"), "w") as f:
         f.write(c48_bell_norms() + "\n")
     with open(os.path.join(HERE, "op_counts.json"), "w") as f:

@@ -42,6 +42,30 @@ def test_oracle_reproduces_cube_fixture(name):
     assert np.array_equal(dp_last[..., 3:3 + n, 3:3 + n], d[f"dplast_{name}"])
 
 
+NESTED_CASES = {
+    "h8": dict(hord=8, q_split=2),
+    "h5_nord1": dict(hord=5, q_split=2, nord_tr=1, trdm=0.1),
+}
+
+
+def load_nested():
+    d = dict(np.load(os.path.join(HERE, "nested_c12_l2.npz")))
+    geom = types.SimpleNamespace(**{f: d["geom_" + f] for f in GEOM_FIELDS}, n=int(d["n"]), ng=3)
+    strips = {side: (d[f"bc_{side}_t0"], d[f"bc_{side}_t1"]) for side in ("west", "east", "south", "north")}
+    return d, geom, strips
+
+
+@pytest.mark.parametrize("name", sorted(NESTED_CASES))
+def test_oracle_reproduces_nested_fixture(name):
+    d, geom, strips = load_nested()
+    r = O.tracer_2d_nested(d["q"], d["dp"], d["mfx"], d["mfy"], d["cx"], d["cy"], geom, strips, nest_timestep=1,
+                           k_split=2, **NESTED_CASES[name])
+    n = int(d["n"])
+    assert np.array_equal(r[0], d[f"q_{name}"])
+    assert np.array_equal(r[1][..., 3:3 + n, 3:3 + n], d[f"dp_{name}"])
+    assert r[7] == int(d[f"count_{name}"]) == 3
+
+
 @pytest.mark.parametrize("kord,iv,qmin", [(9, 0, 0.0), (9, 1, 0.05), (4, 0, 0.0), (4, -1, 0.0), (4, -2, 0.0),
                                           (4, 1, 0.05)])
 def test_oracle_reproduces_remap_fixture(kord, iv, qmin):

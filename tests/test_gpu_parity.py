@@ -653,6 +653,24 @@ def test_cube_matches_committed_golden_fixture(cuda):
         assert rel_l2(q, d[f"q_h{hord}"]) <= FP64_TOL, hord
 
 
+@pytest.mark.parametrize("name", ["h8", "h5_nord1"])
+def test_nested_matches_committed_golden_fixture(cuda, name):
+    """fv3g_tracer_2d_nested on the committed nested fixture (tests/golden/nested_c12_l2.npz)."""
+    from .test_golden import NESTED_CASES, load_nested
+    d, geom, strips = load_nested()
+    n = int(d["n"])
+    kw = NESTED_CASES[name]
+    q, dp, mfx, mfy, cx, cy = (np.ascontiguousarray(d[k]).copy() for k in ("q", "dp", "mfx", "mfy", "cx", "cy"))
+    da = float(np.min(d["geom_area"][3:3 + n, 3:3 + n]))
+    ns, count = api.tracer_2d_nested(q, dp, mfx, mfy, cx, cy, api.GridStruct(geom, nested=1, da_min=da),
+                                     api.bounds_for(n), n + 1, n + 1, q.shape[1], q.shape[0], kw["hord"],
+                                     kw["q_split"], 0.0, nord_tr=kw.get("nord_tr", 0), trdm=kw.get("trdm", 0.0),
+                                     k_split=2, q_bc=api.NestBoundary(strips), nest_timestep=1)
+    assert (ns, count) == (2, int(d[f"count_{name}"]))
+    assert rel_l2(q, d[f"q_{name}"]) <= FP64_TOL
+    assert rel_l2(interior(dp, n), d[f"dp_{name}"]) <= FP64_TOL
+
+
 def test_remap_matches_committed_golden_fixture(cuda):
     import os
     d = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "remap_columns_l63.npz")))
