@@ -527,7 +527,7 @@ int fv3g::state_field_view(fv3g_state* st, int field, bool loading, StateFieldVi
     }
     st->remapped = false;
   }
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, loading));
   v->dev = fs.dev;
   v->esz = (int)st->esz;
@@ -700,7 +700,7 @@ int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk) {
 
 int fv3g_upload(fv3g_state* st, int field, const double* host) {
   if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, true));
   if (field == FV3G_FIELD_Q_REMAPPED || field == FV3G_FIELD_DELP_OUT)
     return set_error(FV3G_E_ARG, "field %d is an output", field);
@@ -716,14 +716,14 @@ int fv3g_upload(fv3g_state* st, int field, const double* host) {
 
 int fv3g_download(fv3g_state* st, int field, double* host) {
   if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, false));
   return st->fp64 ? download_t<double>(st, fs, host, st->stream) : download_t<float>(st, fs, host, st->stream);
 }
 
 int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream) {
   if (!st || !dptr) return set_error(FV3G_E_ARG, "null argument");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   CHECK(plane_copy(st, fs, const_cast<void*>(dptr), false, cudaMemcpyDeviceToDevice, s));
@@ -736,7 +736,7 @@ int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream
 
 int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream) {
   if (!st || !dptr) return set_error(FV3G_E_ARG, "null argument");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   CHECK(plane_copy(st, fs, dptr, true, cudaMemcpyDeviceToDevice, s));
@@ -745,7 +745,7 @@ int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream) {
 
 int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4, int* pitch) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, false));
   if (dptr) *dptr = fs.dev;
   if (pitch) *pitch = st->pg.pitch;
@@ -1115,7 +1115,7 @@ int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32,
   if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
   if (field == FV3G_FIELD_Q_REMAPPED || field == FV3G_FIELD_DELP_OUT)
     return set_error(FV3G_E_ARG, "field %d is an output", field);
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) == !st->fp64) {  // same element type: one pitched copy
@@ -1134,7 +1134,7 @@ int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32,
 
 int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream) {
   if (!st || !host) return set_error(FV3G_E_ARG, "null argument");
-  FieldShape fs;
+  FieldShape fs{};
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
@@ -1186,7 +1186,7 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
   const int lev_fields[] = {FV3G_FIELD_DELP, FV3G_FIELD_CX, FV3G_FIELD_CY, FV3G_FIELD_MFX, FV3G_FIELD_MFY};
   const void* lev_src[] = {delp, cx, cy, mfx, mfy};
   for (int f = 0; f < 5; ++f) {
-    FieldShape fs;
+    FieldShape fs{};
     CHECK(field_shape(st, lev_fields[f], fs, true));
     CHECK(plane_copy(st, fs, (void*)lev_src[f], false, cudaMemcpyHostToDevice, us));
   }
