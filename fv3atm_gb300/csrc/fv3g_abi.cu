@@ -401,7 +401,7 @@ int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
       const int nint = bm.nbxi * bm.nbyi;
       CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint) + (damp ? 1 : 0)));
     }
-    if (st->nt == 6) {
+    if (st->nt == 6 && st->eflux != nullptr) {
       CHECK(launch_edge_fix<T>(a, st->n, s));
       CHECK(mark(st, K_EDGEFIX, s));
     }
@@ -575,7 +575,8 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (d.trdm > 1e-4 && (d.nord_tr < 0 || d.nord_tr > 2))
     return set_error(FV3G_E_UNSUPPORTED, "tracer damping supports nord_tr 0..2 (got %d)", d.nord_tr);
   if (d.kord != 4 && d.kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented", d.kord);
-  if (d.iv < -2 || d.iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", d.iv);
+  if (d.iv < -1 || d.iv > 1)
+    return set_error(FV3G_E_ARG, "iv %d outside -1..1 (iv -2 needs per-column surface values qs)", d.iv);
   fv3g_state* st = new (std::nothrow) fv3g_state();
   if (!st) return set_error(FV3G_E_NOMEM, "host allocation failed");
   st->d = d;
@@ -619,7 +620,8 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   for (void** m : metrics)
     if (!rc) rc = dalloc(st, m, P * nt);
   if (!rc) rc = dalloc(st, &st->sin4, P * nt * 4);
-  if (!rc && nt == 6) rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
+  if (!rc && nt == 6 && d.edge_sync)
+    rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
   if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);

@@ -518,6 +518,7 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
     return set_error(FV3G_E_ARG, "row/column range outside the array bounds");
   if (kord != 4 && kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
   if (iv < -2 || iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", iv);
+  if (iv == -2 && qs == nullptr) return set_error(FV3G_E_ARG, "iv -2 needs the surface values qs");
   const int ni = i2 - i1 + 1, nj = j2 - j1 + 1;
   const long long ncol = (long long)ni * nj;
   // device copy of the selected columns, planes of ni x nj per (field, level)

@@ -6,9 +6,13 @@
 // OpenACC that hands its device arrays over with host_data use_device) and
 // forbids other allocations inside its time loop, or code that must not
 // trigger the implicit device synchronisation of cudaMalloc/cudaFree.  For
-// them, fv3g_remap_columns_noalloc runs the same column-remap kernel as every
-// other remap entry, with its scratch held in one file-scope __device__ array
-// of fixed size instead of a buffer obtained from cudaMalloc.
+// them, fv3g_remap_columns_noalloc runs the thread-per-column remap kernel
+// (k_remap_scratch, which the tangent-linear remap also uses; map_scalar,
+// map1_ppm and the batched remap run the warp-per-column kernel, and the
+// tests check this entry against one of those) with its scratch held in one
+// file-scope __device__ array of fixed size instead of a buffer obtained
+// from cudaMalloc.  The addresses of that array are looked up once per
+// device and kept: a device reset after the first call is not supported.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -74,6 +78,7 @@ extern "C" int fv3g_remap_columns_noalloc(int ncol, int km, const double* pe1, c
   if (nfield < 1) return set_error(FV3G_E_ARG, "nfield must be positive");
   if (kord != 4 && kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
   if (iv < -2 || iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -2..1", iv);
+  if (iv == -2 && qs == nullptr) return set_error(FV3G_E_ARG, "iv -2 needs the surface values qs");
   double* scratch = nullptr;
   unsigned char* sched = nullptr;
   int rc = device_scratch(&scratch, &sched);

@@ -11,8 +11,9 @@
 //     contains it and its fractional position (FP64 differences, stored in T);
 //   * the LU factors of the tridiagonal interface system (they depend on the
 //     layer thicknesses only).
-// Per field: forward/back substitution for the interface values, the kord
-// constraints, and the integration of the sub-grid parabolas over the
+// Per field: the interface values (kord 9: forward/back substitution of the
+// C1 system; kord 4: the explicit PPM stencil), the kord constraints
+// (fv3g_profile.cuh), and the integration of the sub-grid parabolas over the
 // overlaps.  Column-constant arrays and the interface values live in a
 // scratch buffer laid out [level][column] (coalesced, L2-resident).
 #include <algorithm>
@@ -20,64 +21,15 @@
 #include <mutex>
 
 #include "fv3g_internal.cuh"
+#include "fv3g_profile.cuh"
 #include "fv3g_remap.cuh"
 
 namespace fv3g {
 
-template <typename T> __device__ __forceinline__ T clampv(T a, T x0, T x1) { return clamp2(a, x0, x1); }
 
 // mean of the parabola (aL, aR, a6) over the fractional interval [x1, x2]
 template <typename T> __device__ __forceinline__ T pmean(T l, T r, T s6, T x1, T x2) {
   return l + T(0.5) * (x1 + x2) * ((r - l) + s6) - s6 * ((x2 * x2 + x1 * x2 + x1 * x1) * T(1.0 / 3.0));
-}
-
-template <typename T>
-struct Profile {  // sub-grid parabola of one source layer
-  T q, l, r, s6;
-};
-
-// cw84 with selects in place of branches (the same values): no divergence
-// when the lanes of a warp take different cases.
-template <typename T> __device__ __forceinline__ void cw84_sel(T& bl, T& br) {
-  const bool flat = bl * br >= T(0);
-  const T d = br - bl;
-  const T t = T(3) * d * (bl + br);
-  const T d2 = d * d;
-  const bool lo = -t > d2, hi = !lo && t > d2;
-  const T nbl = lo ? T(-2) * br : bl, nbr = hi ? T(-2) * bl : br;
-  bl = flat ? T(0) : nbl;
-  br = flat ? T(0) : nbr;
-}
-
-template <typename T, int KORD>
-__device__ __forceinline__ Profile<T> layer_profile_sel(T q, T aL, T aR, int iv, T floor_v) {
-  if (KORD != 9 && iv >= 0) {
-    aL = tmax(aL, floor_v);
-    aR = tmax(aR, floor_v);
-  }
-  T bl = aL - q, br = aR - q;
-  cw84_sel(bl, br);
-  if (KORD != 9 && iv >= 0) {
-    const bool flat = (q + bl < floor_v) || (q + br < floor_v);
-    bl = flat ? T(0) : bl;
-    br = flat ? T(0) : br;
-  }
-  return Profile<T>{q, q + bl, q + br, T(-3) * (bl + br)};
-}
-
-template <typename T, int KORD>
-__device__ __forceinline__ Profile<T> layer_profile(T q, T aL, T aR, int iv, T floor_v) {
-  if (KORD != 9 && iv >= 0) {
-    aL = tmax(aL, floor_v);
-    aR = tmax(aR, floor_v);
-  }
-  T bl = aL - q, br = aR - q;
-  cw84(bl, br);
-  if (KORD != 9 && iv >= 0 && (q + bl < floor_v || q + br < floor_v)) {  // keep the floor: flatten
-    bl = T(0);
-    br = T(0);
-  }
-  return Profile<T>{q, q + bl, q + br, T(-3) * (bl + br)};
 }
 
 // Thread-per-column form with a global scratch (the caller's fixed buffer);
@@ -147,8 +99,8 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
       SC(s_x, k2) = Single<T>::value ? T(float(p - lo) / float(hi - lo)) : T((p - lo) / (hi - lo));
     }
   }
-  // LU factors of the interface system (rows 0..km), see the oracle restatement
-  if (km > 1) {
+  // LU factors of the kord 9 interface system (rows 0..km)
+  if (KORD == 9 && km > 1) {
     const T g = SC(s_dp, 1) / SC(s_dp, 0);
     T di = g, up = g + T(1);
     T cp = up / di;
@@ -181,11 +133,13 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
     const T* q1 = a.q_in + qo + f * a.sQq;
     T* q2 = a.q_out + qo + f * a.sQqo;
     const T qsv = a.qs ? T(a.qs[col]) : T(0);
+    auto qf = [&](int k) -> T { return q1[(long long)min(max(k, 0), km - 1) * a.sQk]; };
+    auto hf = [&](int k) -> T { return SC(s_dp, min(max(k, 0), km - 1)); };
     // -------------------------------------------- interface values a[0..km]
     if (km == 1) {
       SC(s_a, 0) = q1[0];
       SC(s_a, 1) = q1[0];
-    } else {
+    } else if (KORD == 9) {
       const T g = SC(s_dp, 1) / SC(s_dp, 0);
       T qm = q1[0], qk = q1[a.sQk];
       T ap = ((g * (T(2) * g + T(3))) * qm + qk) / (g + T(1)) * SC(s_rd, 0);
@@ -203,24 +157,27 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
         const T gb = SC(s_d, km);
         rhs = ((gb * (T(2) * gb + T(3))) * q1[(km - 1) * a.sQk] + q1[(km - 2) * a.sQk]) / (gb + T(1));
       }
+      // back substitution on the raw values; each interface is limited on its own
       T av = (rhs - SC(s_cp, km) * ap) * SC(s_rd, km);
-      SC(s_a, km) = (KORD == 9 && a.iv != -2) ? clampv(av, q1[(km - 2) * a.sQk], q1[(km - 1) * a.sQk]) : av;
+      SC(s_a, km) = k9_interface(av, km, km, a.iv, floor_v, qf);
       for (int k = km - 1; k >= 0; --k) {
         av = SC(s_a, k) - SC(s_cp, k) * av;
-        T st = av;
-        if (KORD == 9) {
-          if (k == 0) st = clampv(av, q1[0], q1[a.sQk]);
-          else st = clampv(av, q1[(k - 1) * a.sQk], q1[k * a.sQk]);
-        }
-        SC(s_a, k) = st;
+        SC(s_a, k) = k9_interface(av, k, km, a.iv, floor_v, qf);
       }
+    } else {
+      // kord 4: the layer slopes (kept in s_d), then the PPM interfaces
+      for (int k = 0; k < km; ++k) SC(s_d, k) = ppm_slope<T>(k, km, qf, hf);
+      for (int u = 0; u <= km; ++u)
+        SC(s_a, u) = ppm_interface<T>(u, km, a.iv, qsv, u >= 1 ? SC(s_d, u - 1) : T(0), u < km ? SC(s_d, u) : T(0),
+                                      qf, hf);
     }
     // ------------------------------------------------------- integration
     int kc = -1;  // layer whose profile is cached
     Profile<T> P{};
     auto prof = [&](int k) -> const Profile<T>& {
       if (k != kc) {
-        P = layer_profile<T, KORD>(q1[k * a.sQk], SC(s_a, k), SC(s_a, k + 1), a.iv, floor_v);
+        P = layer_profile<T, KORD>(k, km, q1[k * a.sQk], SC(s_a, k), SC(s_a, k + 1), KORD == 9 ? T(0) : SC(s_d, k),
+                                   a.iv, floor_v, qf);
         kc = k;
       }
       return P;
@@ -475,7 +432,7 @@ __device__ __forceinline__ T affine_enter_bwd(T al, T be, int lane) {
 }
 
 template <typename T, int KORD, int NPL>
-__global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) {
+__global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_warp(const RemapArgs<T> a) {
   constexpr int RING = ring_slots<T>(), RP = ring_pitch<T, NPL>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -578,7 +535,8 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
   // ------------------------------------------- LU of the interface system
   // Row u of the system: rhs_u = wa q[ia] + wb q[ib] + wc qs, forward step
   // y_u = (rhs_u - mco_u y_{u-1}) rd_u, back step a_u = y_u - cpb_u a_{u+1};
-  // rows above km have rd = 0.  The clamp of kord 9 uses the same two layers.
+  // rows above km have rd = 0.  kord 4 has no system: its interfaces are an
+  // explicit stencil.
   T wa[NPL], wb[NPL], wc[NPL], mco[NPL], rdv[NPL], cpb[NPL];
   int ia[NPL], ib[NPL];
 #pragma unroll
@@ -588,7 +546,7 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
     ib[j] = max(min(u == 0 ? 1 : (u == km ? km - 2 : u), km - 1), 0);
     wa[j] = wb[j] = wc[j] = mco[j] = rdv[j] = cpb[j] = T(0);
   }
-  if (km > 1) {
+  if (KORD == 9 && km > 1) {
     const T g = S.dp[pk<T>(1)] / S.dp[pk<T>(0)];
     T dd[NPL];
     Mat2<T> m{T(1), T(0), T(0), T(1)};
@@ -679,22 +637,30 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
 #pragma unroll
       for (int j = 0; j < NPL; ++j) qv[h][j] = (u0 + j < km) ? Q[h][pk<T>(u0 + j)] : T(0);
     // -------------------------------------------- interface values a[0..km]
+    // st[h][j]: the limited interface u0 + j (kord 9) or the PPM one (kord 4);
+    // the interface after the lane's last layer is the next lane's first
+    // (kord 9) or computed here as well (kord 4, st_end).
+    T st_end[FP], dmv[FP][NPL];
     if (km == 1) {
 #pragma unroll
-      for (int h = 0; h < FP; ++h)
+      for (int h = 0; h < FP; ++h) {
+        st_end[h] = qv[h][0];
 #pragma unroll
-        for (int j = 0; j < NPL; ++j) st[h][j] = qv[h][0];
-    } else {
-      T rhs[FP][NPL], qa[FP][NPL], qb[FP][NPL], be[FP];
+        for (int j = 0; j < NPL; ++j) {
+          st[h][j] = qv[h][0];
+          dmv[h][j] = T(0);
+        }
+      }
+    } else if (KORD == 9) {
+      T rhs[FP][NPL], be[FP];
 #pragma unroll
       for (int h = 0; h < FP; ++h) {
         be[h] = T(0);
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
-          qa[h][j] = Q[h][pk<T>(ia[j])];
-          qb[h][j] = Q[h][pk<T>(ib[j])];
-          rhs[h][j] = wa[j] * qa[h][j] + wb[j] * qb[h][j] + wc[j] * qsv;
+          rhs[h][j] = wa[j] * Q[h][pk<T>(ia[j])] + wb[j] * Q[h][pk<T>(ib[j])] + wc[j] * qsv;
           be[h] = ajv[j] * be[h] + rhs[h][j] * rdv[j];
+          dmv[h][j] = T(0);
         }
       }
       T y[FP][NPL];
@@ -718,24 +684,44 @@ __global__ void __launch_bounds__(32 * RCOL) k_remap_warp(const RemapArgs<T> a) 
       T av[FP];
       affine_enter_bwd_m<T, FP>(mb, be, av, lane);
 #pragma unroll
-      for (int h = 0; h < FP; ++h)
+      for (int h = 0; h < FP; ++h) {
+        const T* Qh = Q[h];
+        auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
 #pragma unroll
         for (int j = NPL - 1; j >= 0; --j) {
-          const int u = u0 + j;
           av[h] = y[h][j] - cpb[j] * av[h];
-          const bool clampit = KORD == 9 && u <= km && !(u == km && a.iv == -2);
-          st[h][j] = clampit ? clamp2(av[h], qa[h][j], qb[h][j]) : av[h];
+          st[h][j] = k9_interface(av[h], min(u0 + j, km), km, a.iv, floor_v, qf);
         }
+        st_end[h] = __shfl_down_sync(0xffffffffu, st[h][0], 1);
+      }
+    } else {
+#pragma unroll
+      for (int h = 0; h < FP; ++h) {
+        const T* Qh = Q[h];
+        auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
+        auto hf = [&S, km](int k) -> T { return S.dp[pk<T>(min(max(k, 0), km - 1))]; };
+        T dml = ppm_slope<T>(u0 - 1, km, qf, hf);
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+          const T dmr = ppm_slope<T>(u0 + j, km, qf, hf);
+          st[h][j] = ppm_interface<T>(min(u0 + j, km), km, a.iv, qsv, dml, dmr, qf, hf);
+          dmv[h][j] = dmr;
+          dml = dmr;
+        }
+        st_end[h] = ppm_interface<T>(min(u0 + NPL, km), km, a.iv, qsv, dml, ppm_slope<T>(u0 + NPL, km, qf, hf), qf,
+                                     hf);
+      }
     }
     // ------------------------------------------ sub-grid parabolas of layers
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
-      const T st_next = __shfl_down_sync(0xffffffffu, st[h][0], 1);
+      const T* Qh = Q[h];
+      auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
 #pragma unroll
       for (int j = 0; j < NPL; ++j) {
         const int u = u0 + j;
-        const Profile<T> p = layer_profile_sel<T, KORD>(qv[h][j], st[h][j], j + 1 < NPL ? st[h][j + 1] : st_next,
-                                                        a.iv, floor_v);
+        const Profile<T> p = layer_profile<T, KORD>(u, km, qv[h][j], st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h],
+                                                    dmv[h][j], a.iv, floor_v, qf);
         if (u < km) {
           S.pl[h][pk<T>(u)] = p.l;
           S.pr[h][pk<T>(u)] = p.r;

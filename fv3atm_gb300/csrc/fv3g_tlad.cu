@@ -284,6 +284,7 @@ int fv3g_map1_ppm_tl(int km, const double* pe1, const double* q1, const double* 
                      int jbeg, int jend, int iv, int kord) {
   CHECK(check_map_args(km, kn, i1, i2, j, ibeg, iend, jbeg, jend));
   if (!pe1 || !q1 || !q1_tl || !pe2 || !q2_tl) return set_error(FV3G_E_ARG, "null array argument");
+  if (iv == -2 && qs == nullptr) return set_error(FV3G_E_ARG, "iv -2 needs the surface values qs");
   const int ncol = i2 - i1 + 1;
   const size_t nib = (size_t)(iend - ibeg + 1), plane = nib * (size_t)(jend - jbeg + 1);
   const size_t row = (size_t)(j - jbeg) * nib;
@@ -314,6 +315,7 @@ int fv3g_map1_ppm_ad(int km, const double* pe1, const double* q1, double* q1_ad,
                      int iv, int kord) {
   CHECK(check_map_args(km, kn, i1, i2, j, ibeg, iend, jbeg, jend));
   if (!pe1 || !q1 || !q1_ad || !pe2 || !q2_ad) return set_error(FV3G_E_ARG, "null array argument");
+  if (iv == -2 && qs == nullptr) return set_error(FV3G_E_ARG, "iv -2 needs the surface values qs");
   const int ncol = i2 - i1 + 1;
   const size_t nib = (size_t)(iend - ibeg + 1), plane = nib * (size_t)(jend - jbeg + 1);
   const size_t row = (size_t)(j - jbeg) * nib;

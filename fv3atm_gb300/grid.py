@@ -8,9 +8,15 @@ in-tree users are ``atmos_model.F90:578-614``) and the six-tile connectivity tha
 the on-device halo gather and the tile-edge flux reconciliation use.
 
 Arrays are numpy float64 with shape ``(nj, ni)`` in C order, so memory is
-i-fastest exactly like a Fortran ``(i, j)`` array.  Halo metrics are those of the
-extended gnomonic grid of the same face (the synthetic problem does not need
-them to equal the neighbour's), which requires ``n >= 12`` with a 3-cell halo.
+i-fastest exactly like a Fortran ``(i, j)`` array.  ``tile_geometry`` gives one
+face on its extended gnomonic grid (halo included), which requires ``n >= 12``
+with a 3-cell halo.  ``cube_geometry`` then replaces the halo metrics of the six
+faces by those of the cells they stand for, as FV3's halo updates of the grid
+do: an edge-strip cell takes the neighbouring tile's metrics (rotated into the
+tile's directions), a cube-corner cell those of the cell that the copy_corners
+rotation of the sweep direction puts there (x metrics by the x-sweep rotation,
+y metrics by the y-sweep one).  Both tiles beside a cube edge then see the
+same cells on either side of it, so they compute the same face fluxes.
 """
 from __future__ import annotations
 
@@ -184,8 +190,169 @@ def da_min(geoms) -> float:
     return float(min(g.area[g.ng:g.ng + g.n, g.ng:g.ng + g.n].min() for g in geoms))
 
 
+def edge_matrix(topo: np.ndarray, n: int, t: int, e: int) -> np.ndarray:
+    """2x2 integer matrix taking a displacement (di, dj) in tile t's edge-e halo strip to the neighbour tile's
+    (di, dj) at the cells the strip stands for."""
+    # a strip cell at depth 2, position 2: its four neighbours stay in the strip
+    if e == W:
+        c = (-1, 2)
+    elif e == E:
+        c = (n + 2, 2)
+    elif e == S:
+        c = (2, -1)
+    else:
+        c = (2, n + 2)
+    _, i0, j0 = halo_source(topo, n, t, *c)
+    _, i1, j1 = halo_source(topo, n, t, c[0] + 1, c[1])
+    _, i2, j2 = halo_source(topo, n, t, c[0], c[1] + 1)
+    return np.array([[i1 - i0, i2 - i0], [j1 - j0, j2 - j0]], dtype=np.int64)
+
+
+def corner_source(n: int, i: int, j: int, direction: int) -> tuple:
+    """The edge-strip cell of the same tile that copy_corners puts at cube-corner halo cell (i, j) for a sweep
+    in `direction` (1 = x, 2 = y), and the matrix taking displacements at (i, j) to displacements there
+    (a quarter turn about the corner point)."""
+    su = -1 if i < 1 else 1
+    sv = -1 if j < 1 else 1
+    cx2 = 1 if su < 0 else 2 * n + 1  # doubled corner coordinates
+    cy2 = 1 if sv < 0 else 2 * n + 1
+    u, v = 2 * i - cx2, 2 * j - cy2
+    plus = (su == -sv) if direction == 1 else (su == sv)
+    if plus:
+        u2, v2, R = -v, u, np.array([[0, -1], [1, 0]], dtype=np.int64)
+    else:
+        u2, v2, R = v, -u, np.array([[0, 1], [-1, 0]], dtype=np.int64)
+    return (u2 + cx2) // 2, (v2 + cy2) // 2, R
+
+
+def resolve_cell(topo: np.ndarray, n: int, t: int, i: int, j: int, direction: int) -> tuple:
+    """(tile, i, j, M) of the interior cell that data-domain cell (i, j) of tile t stands for, and the matrix
+    taking displacements at (i, j) to displacements there; cube-corner cells use the copy_corners rotation of
+    `direction`."""
+    oi, oj = i < 1 or i > n, j < 1 or j > n
+    if not oi and not oj:
+        return t, i, j, np.eye(2, dtype=np.int64)
+    if oi and oj:
+        i2, j2, R = corner_source(n, i, j, direction)
+        tt, i3, j3, M = resolve_cell(topo, n, t, i2, j2, direction)
+        return tt, i3, j3, M @ R
+    e = (W if i < 1 else E) if oi else (S if j < 1 else N)
+    tt, i2, j2 = halo_source(topo, n, t, i, j)
+    return tt, i2, j2, edge_matrix(topo, n, t, e)
+
+
+# sin_sg slots of the four cell edges by outward direction
+_SIN_SLOT = {(-1, 0): 0, (0, -1): 1, (1, 0): 2, (0, 1): 3}
+
+
+def _face_of(tt: int, i: int, j: int, d: tuple) -> tuple:
+    """('x' or 'y', i, j) of the face of cell (i, j) in direction d: x faces are west faces, y faces south."""
+    if d == (-1, 0):
+        return "x", i, j
+    if d == (1, 0):
+        return "x", i + 1, j
+    if d == (0, -1):
+        return "y", i, j
+    return "y", i, j + 1
+
+
+def face_source(topo: np.ndarray, n: int, t: int, kind: str, i: int, j: int) -> tuple:
+    """The face of an interior cell that halo face (kind, i, j) of tile t stands for: (tile, kind, i, j, sign),
+    sign = -1 where the neighbour's positive direction across the face is the opposite one.  x face (i, j)
+    separates cells (i-1, j) and (i, j); y face (i, j) cells (i, j-1) and (i, j).  Returns None for a face of
+    the tile itself (both cells interior, or one interior: a tile-edge face)."""
+    cells = [(i - 1, j), (i, j)] if kind == "x" else [(i, j - 1), (i, j)]
+    inside = [1 <= a <= n and 1 <= b <= n for a, b in cells]
+    if any(inside):
+        return None
+    strip = [not ((a < 1 or a > n) and (b < 1 or b > n)) for a, b in cells]
+    k = 1 if strip[1] else (0 if strip[0] else 1)
+    c = cells[k]
+    d = (-1, 0) if kind == "x" else (0, -1)
+    if k == 0:
+        d = (-d[0], -d[1])
+    direction = 1 if kind == "x" else 2
+    tt, ci, cj, M = resolve_cell(topo, n, t, c[0], c[1], direction)
+    md = tuple(int(v) for v in M @ np.array(d))
+    fk, fi, fj = _face_of(tt, ci, cj, md)
+    # the tile's positive direction across the face, +i (x) or +j (y), in the neighbour's frame
+    pos = M @ (np.array([1, 0]) if kind == "x" else np.array([0, 1]))
+    sign = int(pos[0] + pos[1])
+    return tt, fk, fi, fj, sign
+
+
+def fill_halo_metrics(geoms: list, topo: np.ndarray) -> None:
+    """Replace the halo metrics of six faces in place by those of the cells they stand for (module docstring)."""
+    g0 = geoms[0]
+    n, ng = g0.n, g0.ng
+    src = [dict(dxa=g.dxa.copy(), dya=g.dya.copy(), area=g.area.copy(), sin_sg=g.sin_sg.copy(), dx=g.dx.copy(),
+                dy=g.dy.copy(), del6_u=g.del6_u.copy(), del6_v=g.del6_v.copy()) for g in geoms]
+    o = ng - 1  # array index of tile index i is i + o
+    rng_ = range(1 - ng, n + ng + 1)
+    for t, g in enumerate(geoms):
+        for j in rng_:
+            for i in rng_:
+                if 1 <= i <= n and 1 <= j <= n:
+                    continue
+                for direction in (1, 2):
+                    tt, ci, cj, M = resolve_cell(topo, n, t, i, j, direction)
+                    s = src[tt]
+                    along_i = M[0, 0] != 0 if direction == 1 else M[0, 1] != 0
+                    if direction == 1:
+                        g.dxa[j + o, i + o] = s["dxa" if along_i else "dya"][cj + o, ci + o]
+                        g.area[j + o, i + o] = s["area"][cj + o, ci + o]
+                    else:
+                        g.dya[j + o, i + o] = s["dxa" if along_i else "dya"][cj + o, ci + o]
+                    for d in (((-1, 0), (1, 0)) if direction == 1 else ((0, -1), (0, 1))):
+                        md = tuple(int(v) for v in M @ np.array(d))
+                        g.sin_sg[_SIN_SLOT[d], j + o, i + o] = s["sin_sg"][_SIN_SLOT[md], cj + o, ci + o]
+                    for slot in range(4, 9):
+                        g.sin_sg[slot, j + o, i + o] = s["sin_sg"][slot, cj + o, ci + o]
+        # faces: dx, del6_u on y faces (rows jsd..jed+1), dy, del6_v on x faces (cols isd..ied+1)
+        for kind in ("x", "y"):
+            fi_rng = range(1 - ng, n + ng + 2) if kind == "x" else rng_
+            fj_rng = rng_ if kind == "x" else range(1 - ng, n + ng + 2)
+            for j in fj_rng:
+                for i in fi_rng:
+                    r = face_source(topo, n, t, kind, i, j)
+                    if r is None:
+                        continue
+                    tt, fk, fi, fj, _ = r
+                    s = src[tt]
+                    names = ("dy", "del6_v") if kind == "x" else ("dx", "del6_u")
+                    snames = ("dy", "del6_v") if fk == "x" else ("dx", "del6_u")
+                    for a_, b_ in zip(names, snames):
+                        getattr(g, a_)[j + o, i + o] = s[b_][fj + o, fi + o]
+        g.rarea[...] = 1.0 / g.area
+    # tile-edge faces: one value, the lower-numbered tile's
+    for t, g in enumerate(geoms):
+        for e in range(4):
+            nt, ne, rev = (int(v) for v in topo[t, e])
+            if nt > t:
+                continue
+            for sidx in range(n):
+                own = _edge_face_slots(n, ng, e, sidx)
+                other = _edge_face_slots(n, ng, ne, n - 1 - sidx if rev else sidx)
+                for key, (name, idx) in own.items():
+                    oname, oidx = other[key]
+                    getattr(g, name)[idx] = getattr(geoms[nt], oname)[oidx]
+
+
+def _edge_face_slots(n: int, ng: int, e: int, s: int) -> dict:
+    """Array name and index of the length and damping metric of face s (0-based) along tile edge e."""
+    o = ng - 1
+    if e in (W, E):
+        idx = (s + 1 + o, (1 if e == W else n + 1) + o)
+        return {"len": ("dy", idx), "del6": ("del6_v", idx)}
+    idx = ((1 if e == S else n + 1) + o, s + 1 + o)
+    return {"len": ("dx", idx), "del6": ("del6_u", idx)}
+
+
 def cube_geometry(n: int, ng: int = 3, radius: float = RADIUS) -> list:
-    return [tile_geometry(n, t, ng, radius) for t in range(6)]
+    """The six faces with the halo metrics of the cells they stand for (module docstring)."""
+    geoms = [tile_geometry(n, t, ng, radius) for t in range(6)]
+    fill_halo_metrics(geoms, cube_topology())
+    return geoms
 
 
 def hybrid_levels(km: int, ptop: float = 100.0, p0: float = 1.0e5, eta_c: float = 0.2) -> tuple:

@@ -205,7 +205,7 @@ def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, c
     rng = np.random.default_rng(seed)
     nd = n + 2 * ng
     topo = G.cube_topology()
-    geoms = [G.tile_geometry(n, t, ng) for t in range(ntiles if ntiles == 6 else 1)]
+    geoms = G.cube_geometry(n, ng) if ntiles == 6 else [G.tile_geometry(n, 0, ng)]
     ak, bk = G.hybrid_levels(npz)
 
     # stream function: solid body + optional random perturbation
@@ -287,6 +287,7 @@ def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, c
     if T == 6:
         _sync_edges(mfx, mfy, n, topo, row_off=0)
         _sync_edges(cx3, cy3, n, topo, row_off=ng)
+        fill_courant_halo(cx3, cy3, n, ng, topo)
 
     # tracers
     qrng = np.random.default_rng(seed + 31)
@@ -306,6 +307,24 @@ def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, c
     return Problem(n=n, ng=ng, npz=npz, nq=nq, ntiles=T, geoms=geoms, topo=topo, ak=ak, bk=bk, dt=dt, q=q, dp=dp,
                    cx=cx3, cy=cy3, mfx=mfx, mfy=mfy, meta=dict(seed=seed, cmax=cmax, u0=u0, pert_amp=pert_amp,
                                                             centers=centers))
+
+
+def fill_courant_halo(cx, cy, n: int, ng: int, topo: np.ndarray) -> None:
+    """Courant numbers of the halo faces of six tiles from the faces they stand for (grid.face_source), as a
+    halo update of the winds gives them: cx (6, npz, nd, n+1) on the halo rows, cy (6, npz, n+1, nd) on the
+    halo columns."""
+    o = ng - 1
+    for t in range(6):
+        for j in list(range(1 - ng, 1)) + list(range(n + 1, n + ng + 1)):
+            for i in range(1, n + 2):
+                tt, fk, fi, fj, sign = G.face_source(topo, n, t, "x", i, j)
+                src = cx[tt, :, fj + o, fi - 1] if fk == "x" else cy[tt, :, fj - 1, fi + o]
+                cx[t, :, j + o, i - 1] = sign * src
+        for i in list(range(1 - ng, 1)) + list(range(n + 1, n + ng + 1)):
+            for j in range(1, n + 2):
+                tt, fk, fi, fj, sign = G.face_source(topo, n, t, "y", i, j)
+                src = cx[tt, :, fj + o, fi - 1] if fk == "x" else cy[tt, :, fj - 1, fi + o]
+                cy[t, :, j - 1, i + o] = sign * src
 
 
 def _sync_edges(xf, yf, n: int, topo: np.ndarray, row_off: int) -> None:

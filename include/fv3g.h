@@ -13,7 +13,7 @@
  *
  * Conventions
  *  - Everything is plain C: pointers, sizes and doubles/ints, callable from
- *    Fortran through ISO_C_BINDING (bind(C) interfaces in INTEGRATION.md).
+ *    Fortran through ISO_C_BINDING bind(C) interfaces.
  *  - Arrays passed to the exact-shape entries are HOST arrays in Fortran
  *    (column-major, i fastest) order with the bounds documented per argument;
  *    the library copies them to the GPU and back.
@@ -177,7 +177,7 @@ int fv3g_tracer_2d_nested(double* q, double* dp1, double* mfx, double* mfy, doub
 /* map_scalar (fv_mapz.F90): remap row j of a 3-D field, FP64.
  *   pe1 (i1:i2, km+1)  pe2 (i1:i2, kn+1)  qs (i1:i2)
  *   q1 (ibeg:iend, jbeg:jend, km) in    q2 (ibeg:iend, jbeg:jend, kn) inout
- *   iv: -2 (bottom value qs), -1, 0 (positive), 1 (floor q_min)
+ *   iv: -2 (bottom value qs, which must then be given), -1, 0 (positive), 1 (floor q_min)
  *   kord: 4 (C1 spline, CW84 limiter) or 9 (monotone)
  *   pe2(1) must equal pe1(1) and pe2(kn+1) must equal pe1(km+1).
  * Thread-safe: may be called concurrently from OpenMP threads (per-thread
@@ -266,7 +266,10 @@ int fv3g_pressure_vars(int im, int km, double ptop, double akap, const double* d
  * GPU that loads the library until exit) shared by all calls, so calls that
  * overlap on the GPU (on different streams or host threads) race; serialise
  * them.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The looked-up addresses are kept for the life of the process: resetting a
+ * device (cudaDeviceReset) after the first call is not supported.
+ * iv == -2 needs qs (FV3G_E_ARG otherwise). */
 int fv3g_remap_columns_noalloc(int ncol, int km, const double* pe1, const double* q1, const double* qs,
                                int kn, const double* pe2, double* q2, int nfield, int iv, int kord,
                                double q_min, void* stream);
@@ -286,13 +289,17 @@ typedef struct {
   int precision;  /* FV3G_FP64 or FV3G_MIXED */
   int hord;       /* 1, 5 or 8 (see fv3g_fv_tp_2d) */
   int kord;       /* 4 or 9 */
-  int iv;         /* remap iv (see fv3g_map_scalar) */
+  int iv;         /* remap iv (see fv3g_map_scalar): -1, 0 or 1; -2 needs a per-column qs, which a state does not hold */
   double q_min;   /* remap floor for iv == 1 */
   int warps_per_cta; /* advection CTA width in warps (0 = default) */
   int nord_tr;    /* tracer damping order 0..2 (del-2(nord_tr+1)) */
   double trdm;    /* damping coefficient; > 1e-4 damps the first substep (needs the grid's del6_u/v) */
   double lim_fac; /* hord 1 filter factor; 0 means 1 */
   int fill;       /* 1: fillz the remapped tracers in every remap (fv_core_nml fill) */
+  int edge_sync;  /* six tiles: 1 makes each shared tile-edge face carry one flux, the upwind tile's (the
+                     downwind tile's edge cell is corrected); 0 (upstream behaviour) keeps each tile's own
+                     value.  With halos that hold the neighbours' cells, metrics and winds the two values
+                     already agree to round-off; the option removes that round-off from the global mass. */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */

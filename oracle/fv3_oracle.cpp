@@ -537,72 +537,197 @@ void flux_update(double* qk, const double* dp1k, const Level& L, const double* f
 }
 
 // ------------------------------------------------------------------ remap ---
-// Column reconstruction.  Interface values come from the C1 ("cubic-spline")
+// Column reconstruction: the sub-grid parabola (aL, aR, a6) of every source
+// layer, in the two families of fv_mapz.
+//
+// kord >= 7 (cs_profile).  Interface values come from the C1 ("cubic-spline")
 // condition: the sub-grid parabolas of adjacent layers have equal slopes at
 // their shared interface, which on layers of thickness h_{k-1}, h_k gives
 //   a_{k-1} + 2(1+d) a_k + d a_{k+1} = 3 (q_{k-1} + d q_k),   d = h_{k-1}/h_k.
 // The top and bottom rows require the outermost interface pair to agree with
 // one parabola through the two outermost layer means (exact for quadratics).
-// iv == -2 replaces the bottom row by a_km = qs.  Constraints:
-//   kord 9: every interface value is clamped to the range of its two adjacent
-//           layer means (boundary interfaces: the two outermost means), then
-//           the CW84 cell constraint -- monotone, no new extrema;
-//   kord 4: no clamp; edge values floored at the iv floor (iv >= 0), then CW84;
-//           a layer whose corrected edges still fall below the floor is
-//           flattened (its mean is kept).
+// iv == -2 replaces the bottom row by a_km = qs.  The kord 9 constraints,
+// restated from Lin (2004), the FV3 documentation (Harris et al. 2021) and
+// Huynh's second constraint (Suresh & Huynh 1997), with D_u = q_u - q_{u-1}
+// the jump of the layer means across interface u:
+//   interfaces 1..km-1, with extremum detection: where the neighbouring jumps
+//     D_{u-1} and D_{u+1} have one sign (a monotone stretch) the value is
+//     clamped into the range of its two layer means; next to a local maximum
+//     (D_{u-1} > 0, D_{u+1} <= 0) it is only kept at or above the smaller
+//     mean, next to a local minimum only at or below the larger one (and at
+//     or above the floor for iv >= 0).  At u = 1 and u = km-1 the missing
+//     jump is the one across u itself.  The outermost interfaces are clamped
+//     into the range of the two outermost means (not a_km when iv == -2);
+//   layers: the two at each end take the CW84 constraint; an interior layer
+//     that is a local extremum beside another one (a two-grid-length wave) is
+//     flattened; otherwise, when its parabola has an interior extremum
+//     (|a6| > |aR - aL|), the right edge is bounded to the range of q,
+//     q + 2 D_k and q + 2 D_k - 1.5 D_{k-1} (upper-limit and large-curvature
+//     values) and the left edge to the range of q, q - 2 D_{k+1} and
+//     q - 2 D_{k+1} + 1.5 D_{k+2}.
+//
+// kord < 7 (ppm_profile).  Slopes of Colella & Woodward (1984) eq. 1.7 on the
+// layer thicknesses, as half increments dm limited by the range of the layer
+// and its two neighbours (Lin et al. 1994; dm = 0 in the end layers);
+// interfaces 2..km-2 from CW84 eq. 1.6 with the limited slopes; interfaces 1
+// and km-1 from the parabola through the three nearest layer means (exact
+// for quadratic profiles), clamped into the range of their two means; the
+// outermost interfaces make the end layers linear (a_0 = 2 q_0 - a_1, a_km
+// likewise, or qs when iv == -2).  Layers 2..km-3 take the kord 4 constraint
+// of Lin (2004): each edge deviation at most |2 dm| with the sign of dm; the
+// two layers at each end take CW84.
+//
+// Both families, iv >= 0: a layer whose edges or interior minimum fall below
+// the floor (0, or q_min when iv == 1) is flattened (its mean is kept).
+template <class T>
+void cs_interfaces(const T* q, const double* dp, int km, int iv, double qs, T* a) {
+  std::vector<T> rhs(km + 1);
+  std::vector<double> cp(km + 1), lo(km + 1), di(km + 1), up(km + 1);
+  double g = dp[1] / dp[0];
+  di[0] = g; up[0] = g + 1.0; lo[0] = 0.0;
+  rhs[0] = (T(g * (2.0 * g + 3.0)) * q[0] + q[1]) / T(g + 1.0);
+  for (int k = 1; k < km; ++k) {
+    double d = dp[k - 1] / dp[k];
+    lo[k] = 1.0; di[k] = 2.0 * (1.0 + d); up[k] = d;
+    rhs[k] = T(3.0) * (q[k - 1] + T(d) * q[k]);
+  }
+  if (iv == -2) {
+    lo[km] = 0.0; di[km] = 1.0; up[km] = 0.0;
+    rhs[km] = T(qs);
+  } else {
+    double gb = dp[km - 2] / dp[km - 1];
+    lo[km] = gb + 1.0; di[km] = gb; up[km] = 0.0;
+    rhs[km] = (T(gb * (2.0 * gb + 3.0)) * q[km - 1] + q[km - 2]) / T(gb + 1.0);
+  }
+  // Thomas algorithm
+  cp[0] = up[0] / di[0];
+  a[0] = rhs[0] / T(di[0]);
+  for (int k = 1; k <= km; ++k) {
+    double den = di[k] - lo[k] * cp[k - 1];
+    cp[k] = up[k] / den;
+    a[k] = (rhs[k] - T(lo[k]) * a[k - 1]) / T(den);
+  }
+  for (int k = km - 1; k >= 0; --k) a[k] = a[k] - T(cp[k]) * a[k + 1];
+}
+
+// kord 9 interface constraint with extremum detection (see above)
+template <class T>
+void k9_interface_limits(const T* q, int km, int iv, double floor_v, T* a) {
+  auto D = [&](int u) { return val(q[u]) - val(q[u - 1]); };  // jump across interface u (1..km-1)
+  a[0] = clamp2(a[0], q[0], q[1]);
+  for (int u = 1; u < km; ++u) {
+    const double dl = D(u > 1 ? u - 1 : u), dr = D(u < km - 1 ? u + 1 : u);
+    tally<T>(0, 1, 1);
+    if (dl * dr > 0.0) {
+      a[u] = clamp2(a[u], q[u - 1], q[u]);
+    } else if (dl > 0.0) {
+      a[u] = tmax(a[u], tmin(q[u - 1], q[u]));
+    } else {
+      a[u] = tmin(a[u], tmax(q[u - 1], q[u]));
+      if (iv >= 0) a[u] = tmax(a[u], T(floor_v));
+    }
+  }
+  if (iv != -2) a[km] = clamp2(a[km], q[km - 2], q[km - 1]);
+}
+
+// Value at the interface between an end layer (mean q0, thickness h0) and the
+// next layer (q1, h1) of the parabola whose means over those two layers and
+// the one after them (q2, h2) are the layer means: the derivative at that
+// interface of the cubic through the cumulative masses.
+template <class T>
+T quad3_interface(T q0, T q1, T q2, double h0, double h1, double h2) {
+  const double w0 = h1 * (h1 + h2) / ((h0 + h1) * (h0 + h1 + h2));
+  const double w2 = -h0 * h1 / ((h0 + h1 + h2) * (h1 + h2));
+  const double w1 = 1.0 - w0 - w2;
+  return T(w0) * q0 + T(w1) * q1 + T(w2) * q2;
+}
+
+// PPM interfaces and half-increment slopes (kord < 7, see above)
+template <class T>
+void ppm_interfaces(const T* q, const double* dp, int km, int iv, double qs, T* a, T* dm) {
+  for (int k = 0; k < km; ++k) dm[k] = T(0.0);
+  for (int k = 1; k < km - 1; ++k) {
+    const double d0 = dp[k - 1], d1 = dp[k], d2 = dp[k + 1];
+    const T dq = T(d1 / (d0 + d1 + d2)) * (T((2.0 * d0 + d1) / (d2 + d1)) * (q[k + 1] - q[k]) +
+                                            T((d1 + 2.0 * d2) / (d0 + d1)) * (q[k] - q[k - 1]));
+    const T mx = tmax(tmax(q[k - 1], q[k]), q[k + 1]) - q[k];
+    const T mn = q[k] - tmin(tmin(q[k - 1], q[k]), q[k + 1]);
+    dm[k] = tsign(tmin(tmin(T(0.5) * tabs(dq), mx), mn), dq);
+  }
+  for (int u = 2; u <= km - 2; ++u) {
+    const int j = u - 1;
+    const double hm = dp[j - 1], h0 = dp[j], h1 = dp[j + 1], h2 = dp[j + 2];
+    const double s01 = h0 + h1, sall = hm + h0 + h1 + h2;
+    const double c0 = h0 / s01;
+    const double c1 = 2.0 * h1 * h0 / s01 * ((hm + h0) / (2.0 * h0 + h1) - (h2 + h1) / (2.0 * h1 + h0)) / sall;
+    const double c2 = h0 * (hm + h0) / (2.0 * h0 + h1) / sall;
+    const double c3 = h1 * (h1 + h2) / (h0 + 2.0 * h1) / sall;
+    const T dq = q[j + 1] - q[j];
+    a[u] = q[j] + T(c0 + c1) * dq - T(2.0 * c2) * dm[j + 1] + T(2.0 * c3) * dm[j];
+  }
+  if (km == 2) {
+    a[1] = (q[0] * T(dp[1]) + q[1] * T(dp[0])) / T(dp[0] + dp[1]);
+  } else {
+    a[1] = clamp2(quad3_interface(q[0], q[1], q[2], dp[0], dp[1], dp[2]), q[0], q[1]);
+    a[km - 1] = clamp2(quad3_interface(q[km - 1], q[km - 2], q[km - 3], dp[km - 1], dp[km - 2], dp[km - 3]),
+                       q[km - 2], q[km - 1]);
+  }
+  a[0] = T(2.0) * q[0] - a[1];
+  a[km] = (iv == -2) ? T(qs) : T(2.0) * q[km - 1] - a[km - 1];
+}
+
 template <class T>
 void column_profile_t(const T* q, const double* dp, int km, int iv, int kord, double qs, double q_min,
                       T* aL, T* aR, T* a6) {
-  std::vector<T> a(km + 1), rhs(km + 1);
-  std::vector<double> cp(km + 1), lo(km + 1), di(km + 1), up(km + 1);
-  if (km == 1) {
-    a[0] = q[0];
-    a[1] = q[0];
-  } else {
-    double g = dp[1] / dp[0];
-    di[0] = g; up[0] = g + 1.0; lo[0] = 0.0;
-    rhs[0] = (T(g * (2.0 * g + 3.0)) * q[0] + q[1]) / T(g + 1.0);
-    for (int k = 1; k < km; ++k) {
-      double d = dp[k - 1] / dp[k];
-      lo[k] = 1.0; di[k] = 2.0 * (1.0 + d); up[k] = d;
-      rhs[k] = T(3.0) * (q[k - 1] + T(d) * q[k]);
-    }
-    if (iv == -2) {
-      lo[km] = 0.0; di[km] = 1.0; up[km] = 0.0;
-      rhs[km] = T(qs);
-    } else {
-      double gb = dp[km - 2] / dp[km - 1];
-      lo[km] = gb + 1.0; di[km] = gb; up[km] = 0.0;
-      rhs[km] = (T(gb * (2.0 * gb + 3.0)) * q[km - 1] + q[km - 2]) / T(gb + 1.0);
-    }
-    // Thomas algorithm
-    cp[0] = up[0] / di[0];
-    a[0] = rhs[0] / T(di[0]);
-    for (int k = 1; k <= km; ++k) {
-      double den = di[k] - lo[k] * cp[k - 1];
-      cp[k] = up[k] / den;
-      a[k] = (rhs[k] - T(lo[k]) * a[k - 1]) / T(den);
-    }
-    for (int k = km - 1; k >= 0; --k) a[k] = a[k] - T(cp[k]) * a[k + 1];
-  }
   const double floor_v = (iv == 1) ? q_min : 0.0;
-  if (kord == 9 && km > 1) {
-    a[0] = clamp2(a[0], q[0], q[1]);
-    for (int k = 1; k < km; ++k) a[k] = clamp2(a[k], q[k - 1], q[k]);
-    if (iv != -2) a[km] = clamp2(a[km], q[km - 2], q[km - 1]);
+  if (km == 1) {
+    aL[0] = q[0];
+    aR[0] = q[0];
+    a6[0] = T(0.0);
+    return;
   }
+  std::vector<T> a(km + 1), dm(km);
+  if (kord >= 7) {
+    cs_interfaces(q, dp, km, iv, qs, a.data());
+    k9_interface_limits(q, km, iv, floor_v, a.data());
+  } else {
+    ppm_interfaces(q, dp, km, iv, qs, a.data(), dm.data());
+  }
+  auto D = [&](int u) { return val(q[u]) - val(q[u - 1]); };
+  auto extm = [&](int k) { return k >= 1 && k <= km - 2 && D(k) * D(k + 1) < 0.0; };
   for (int k = 0; k < km; ++k) {
-    T l = a[k], r = a[k + 1];
-    if (kord != 9 && iv >= 0) {
-      l = tmax(l, T(floor_v));
-      r = tmax(r, T(floor_v));
+    T bl = a[k] - q[k], br = a[k + 1] - q[k];
+    const bool end_layer = k < 2 || k > km - 3;
+    if (end_layer) {
+      cw84(bl, br);
+    } else if (kord >= 7) {
+      tally<T>(0, 2, 3);
+      if (extm(k) && (extm(k - 1) || extm(k + 1))) {
+        bl = T(0.0);
+        br = T(0.0);
+      } else {
+        tally<T>(2, 1, 1);
+        if (3.0 * std::fabs(val(bl) + val(br)) > std::fabs(val(br) - val(bl))) {
+          const T pr = T(2.0) * (q[k] - q[k - 1]), lr = pr - T(1.5) * (q[k - 1] - q[k - 2]);
+          const T pl = T(-2.0) * (q[k + 1] - q[k]), ll = pl + T(1.5) * (q[k + 2] - q[k + 1]);
+          br = tmin(tmax(br, tmin(tmin(T(0.0), pr), lr)), tmax(tmax(T(0.0), pr), lr));
+          bl = tmin(tmax(bl, tmin(tmin(T(0.0), pl), ll)), tmax(tmax(T(0.0), pl), ll));
+        }
+      }
+    } else {
+      const T xt = T(2.0) * dm[k];
+      bl = -tsign(tmin(tabs(xt), tabs(bl)), xt);
+      br = tsign(tmin(tabs(xt), tabs(br)), xt);
     }
-    T bl = l - q[k], br = r - q[k];
-    cw84(bl, br);
-    // the overshoot correction can move an edge below the floor: flatten
-    if (kord != 9 && iv >= 0 && (val(q[k] + bl) < floor_v || val(q[k] + br) < floor_v)) {
-      bl = T(0.0);
-      br = T(0.0);
+    if (iv >= 0) {  // keep the reconstruction at or above the floor: flatten
+      const double l = val(q[k]) + val(bl), r = val(q[k]) + val(br);
+      const double s6 = -3.0 * (val(bl) + val(br)), da = val(br) - val(bl);
+      bool low = l < floor_v || r < floor_v;
+      if (!low && -s6 > std::fabs(da)) low = val(q[k]) + s6 / 12.0 + da * da / (4.0 * s6) < floor_v;
+      if (low) {
+        bl = T(0.0);
+        br = T(0.0);
+      }
     }
     aL[k] = q[k] + bl;
     aR[k] = q[k] + br;

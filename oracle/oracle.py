@@ -234,7 +234,7 @@ def tracer_2d_1L(q, dp1, mfx, mfy, cx, cy, geom, hord=8, q_split=0, halo_fn=None
     return q, dp1, mfx, mfy, cx, cy, ns
 
 
-def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=True, ng: int = 3,
+def tracer_2d_cube(q, dp1, mfx, mfy, cx, cy, geoms, topo, hord=8, q_split=0, sync_edges=False, ng: int = 3,
                    nord_tr=0, trdm=0.0, lim_fac=1.0):
     """Six-tile tracer_2d.  q (6, nq, npz, nd, nd).  Returns (q, dp1, nsplt)."""
     q = _f64(q).copy()

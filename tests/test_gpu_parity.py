@@ -59,6 +59,28 @@ def test_cube_tracer_2d_matches_oracle(cuda, cube_prob, cube_oracle, precision, 
     assert rel_l2(interior(dp, n), interior(dp_ref, n)) <= tol
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+@pytest.mark.parametrize("hord,nord,trdm", [(8, 0, 0.0), (8, 1, 0.1)])
+def test_cube_edge_sync_option_matches_oracle(cuda, cube_prob, precision, tol, hord, nord, trdm):
+    """edge_sync = 1 (each shared tile-edge face carries the upwind tile's flux; k_edge_fix) against the oracle
+    run the same way; the FP64 global mass is conserved with and without it."""
+    P = cube_prob
+    q_ref, dp_last, ns = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=hord,
+                                          q_split=3, sync_edges=True, nord_tr=nord, trdm=trdm)
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision, hord=hord, nord_tr=nord, trdm=trdm, edge_sync=True)
+    st.load_problem(P)
+    st.tracer_2d(3)
+    q = st.download("Q")
+    for iq in range(P.nq):
+        assert rel_l2(interior(q[:, iq], P.n), interior(q_ref[:, iq], P.n)) <= tol
+    if precision == "fp64":
+        dpf = final_dp(dp_last, P.mfx.numpy(), P.mfy.numpy(), P.geoms, ns, P.n)
+        m0 = cube_mass(P.q.numpy(), P.dp.numpy(), P.geoms, P.n)
+        m1 = cube_mass(q, dpf, P.geoms, P.n)
+        assert np.all(np.abs(m1 - m0) <= 1e-13 * np.abs(m0)), (m1 - m0) / m0
+    st.close()
+
+
 @pytest.mark.parametrize("warps", [1, 3])
 def test_cube_warps_per_cta_do_not_change_results(cuda, cube_prob, warps):
     P = cube_prob
@@ -127,11 +149,12 @@ def test_cube_schemes_and_damping_match_oracle(cuda, cube_prob, precision, tol, 
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
-def test_cube_remap_matches_oracle(cuda, cube_prob, cube_oracle, precision, tol):
+@pytest.mark.parametrize("kord", [9, 4])
+def test_cube_remap_matches_oracle(cuda, cube_prob, cube_oracle, precision, tol, kord):
     P = cube_prob
     q_adv, dpf = cube_oracle
-    q_ref, dp2_ref, _, _ = remap_reference(q_adv, dpf, P.ak, P.bk, P.n)
-    st = _run_cube(P, precision, remap=True)
+    q_ref, dp2_ref, _, _ = remap_reference(q_adv, dpf, P.ak, P.bk, P.n, kord=kord)
+    st = _run_cube(P, precision, remap=True, kord=kord)
     q = st.download("Q_REMAPPED")
     for iq in range(P.nq):
         e = rel_l2(interior(q[:, iq], P.n), interior(q_ref[:, iq], P.n))
@@ -365,8 +388,11 @@ def test_tracer_2d_dropin_derives_nsplt(cuda, cube_prob):
     assert rel_l2(interior(q, P.n), interior(ref[0], P.n)) <= FP64_TOL
 
 
-@pytest.mark.parametrize("kord,iv", [(9, 0), (9, 1), (4, 0), (4, -1), (4, -2)])
-def test_map_scalar_dropin_matches_oracle(cuda, kord, iv):
+@pytest.mark.parametrize("kind", ["noise", "smooth"])
+@pytest.mark.parametrize("kord,iv", [(9, 0), (9, 1), (9, -1), (9, -2), (4, 0), (4, 1), (4, -1), (4, -2)])
+def test_map_scalar_dropin_matches_oracle(cuda, kord, iv, kind):
+    """Columns of noise (many two-grid-length waves and single extrema) and smooth columns with resolved
+    extrema (kord 9's Huynh bounds act there) through every iv case."""
     rng = np.random.default_rng(5)
     from fv3atm_gb300 import grid as G
     km, ni, nj = 63, 20, 7
@@ -375,7 +401,12 @@ def test_map_scalar_dropin_matches_oracle(cuda, kord, iv):
     dref = np.diff(ak)[:, None, None] + np.diff(bk)[:, None, None] * ps[None]
     dp = dref * (1 + 0.1 * rng.uniform(-1, 1, dref.shape))
     dp *= dref.sum(0) / dp.sum(0)
-    q1 = np.ascontiguousarray(np.abs(rng.standard_normal((km, nj, ni))) + 0.1)
+    if kind == "noise":
+        q1 = np.ascontiguousarray(np.abs(rng.standard_normal((km, nj, ni))) + 0.1)
+    else:
+        z = np.linspace(0.0, 1.0, km)[:, None, None]
+        q1 = np.ascontiguousarray(1.2 + np.sin(2 * np.pi * (2 + rng.uniform(0, 2, (1, nj, ni))) * z +
+                                               rng.uniform(0, 6, (1, nj, ni))))
     pe1 = np.concatenate([np.full((1, nj, ni), ak[0]), ak[0] + np.cumsum(dp, 0)])
     pe2 = ak[:, None, None] + bk[:, None, None] * pe1[-1][None]
     qs = rng.uniform(0, 1, (nj, ni))

@@ -32,25 +32,40 @@ def _columns(seed, km, ncol, nfield):
     return pe1, pe2, q1
 
 
-def _noalloc(pe1, q1, pe2, iv, kord, q_min):
+def _device(pe1, q1, pe2, qs):
     import torch
-    nfield, km, ncol = q1.shape
-    kn = pe2.shape[0] - 1
     d = {k: torch.as_tensor(v, device="cuda") for k, v in (("pe1", pe1), ("pe2", pe2), ("q1", q1))}
-    q2 = torch.full((nfield, kn, ncol), -1.0, dtype=torch.float64, device="cuda")
+    if qs is not None:
+        d["qs"] = torch.as_tensor(qs, device="cuda")
+    nfield, _, ncol = q1.shape
+    d["q2"] = torch.full((nfield, pe2.shape[0] - 1, ncol), -1.0, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
+    return d
+
+
+def _call(d, iv, kord, q_min):
+    nfield, km, ncol = d["q1"].shape
+    kn = d["pe2"].shape[0] - 1
+    qs = C.c_void_p(d["qs"].data_ptr()) if "qs" in d else None
     _lib.call("fv3g_remap_columns_noalloc", ncol, km, C.c_void_p(d["pe1"].data_ptr()),
-              C.c_void_p(d["q1"].data_ptr()), None, kn, C.c_void_p(d["pe2"].data_ptr()), C.c_void_p(q2.data_ptr()),
-              nfield, iv, kord, C.c_double(q_min), None)
+              C.c_void_p(d["q1"].data_ptr()), qs, kn, C.c_void_p(d["pe2"].data_ptr()),
+              C.c_void_p(d["q2"].data_ptr()), nfield, iv, kord, C.c_double(q_min), None)
+
+
+def _noalloc(pe1, q1, pe2, iv, kord, q_min, qs=None):
+    import torch
+    d = _device(pe1, q1, pe2, qs)
+    _call(d, iv, kord, q_min)
     torch.cuda.synchronize()
-    return q2.cpu().numpy()
+    return d["q2"].cpu().numpy()
 
 
-def _allocating(pe1, q1, pe2, iv, kord, q_min):
+def _allocating(pe1, q1, pe2, iv, kord, q_min, qs=None):
     nfield, km, ncol = q1.shape
     kn = pe2.shape[0] - 1
     q2 = np.zeros((nfield, kn, 1, ncol))
-    api.map_scalar_3d(km, pe1, np.ascontiguousarray(q1[:, :, None, :]), None, kn, pe2, q2, 1, ncol, 1, 1, 1, ncol,
+    qsa = None if qs is None else np.ascontiguousarray(qs[None, :])
+    api.map_scalar_3d(km, pe1, np.ascontiguousarray(q1[:, :, None, :]), qsa, kn, pe2, q2, 1, ncol, 1, 1, 1, ncol,
                       1, 1, nfield, iv, kord, q_min)
     return q2[:, :, 0, :]
 
@@ -67,6 +82,38 @@ def test_noalloc_remap_matches_allocating_entry_twice(cuda):
         assert _rel(got, want) <= FP64_TOL, (call, _rel(got, want))
 
 
+def test_noalloc_remap_at_its_limits_with_surface_values(cuda):
+    """The full fixed array (1024 columns, 128 layers on both sides) and iv = -2, whose bottom interface is the
+    caller's device array qs, against fv3g_map_scalar_3d given the same qs."""
+    rng = np.random.default_rng(11)
+    for call, kord in enumerate((4, 9)):
+        pe1, pe2, q1 = _columns(20 + call, 128, 1024, 2)
+        qs = q1[:, -1, :].mean(0) + 0.01 * rng.standard_normal(1024)
+        got = _noalloc(pe1, q1, pe2, -2, kord, 0.0, qs=qs)
+        want = _allocating(pe1, q1, pe2, -2, kord, 0.0, qs=qs)
+        assert _rel(got, want) <= FP64_TOL, (kord, _rel(got, want))
+
+
+def test_noalloc_remap_allocates_no_device_memory(cuda):
+    """After a first call (which looks up the fixed array's address), further calls leave the device's free
+    memory and torch's allocator untouched."""
+    import torch
+    pe1, pe2, q1 = _columns(5, 127, 1000, 3)
+    d = _device(pe1, q1, pe2, None)
+    _call(d, 0, 9, 0.0)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for _ in range(3):
+        _call(d, 0, 9, 0.0)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0
+    for key in ("allocation.all.allocated", "reserved_bytes.all.current", "allocated_bytes.all.current"):
+        assert stats1.get(key) == stats0.get(key), key
+
+
 def test_noalloc_remap_rejects_oversized_requests(cuda):
     with pytest.raises(_lib.Fv3gError, match="1024 columns"):
         _lib.call("fv3g_remap_columns_noalloc", 1025, 10, C.c_void_p(8), C.c_void_p(8), None, 10, C.c_void_p(8),
@@ -74,3 +121,6 @@ def test_noalloc_remap_rejects_oversized_requests(cuda):
     with pytest.raises(_lib.Fv3gError, match="layers"):
         _lib.call("fv3g_remap_columns_noalloc", 10, 129, C.c_void_p(8), C.c_void_p(8), None, 10, C.c_void_p(8),
                   C.c_void_p(8), 1, 0, 9, C.c_double(0.0), None)
+    with pytest.raises(_lib.Fv3gError, match="qs"):
+        _lib.call("fv3g_remap_columns_noalloc", 10, 10, C.c_void_p(8), C.c_void_p(8), None, 10, C.c_void_p(8),
+                  C.c_void_p(8), 1, -2, 9, C.c_double(0.0), None)
