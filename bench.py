@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fv3g", choices=["fv3g", "reference"])
-    ap.add_argument("--n", type=int, default=384)
+    ap.add_argument("--resolution", dest="n", type=int, default=384, help="cells per tile edge (C_n)")
     ap.add_argument("--npz", type=int, default=127)
     ap.add_argument("--nq", type=int, default=20)
     ap.add_argument("--q-split", type=int, default=3)
@@ -234,7 +234,8 @@ ENSEMBLE = [(48, 32)] * 16 + [(96, 64)] * 10 + [(192, 127)] * 6
 
 def ensemble_leg(a, stream):
     """All members advanced by one CUDA graph per step (fv3g_ensemble_step), mixed precision, each member's
-    CTA width autotuned for its size; per-member error of one step against the FP64 path."""
+    CTA width autotuned for its size; per-member error of one step against the FP64 path (each member against
+    the oracle: tests/test_gpu_configs.py)."""
     import numpy as np
     import torch
     from fv3atm_gb300 import api
@@ -347,47 +348,71 @@ CPU_SAMPLE_NQ = 2
 CPU_SAMPLE_STEPS = 2
 
 
-def cpu_oracle_rate(n, npz, nq, q_split, seconds, steps=None, warmup=0):
-    """Updates/s of the FP64 C++ oracle (OpenMP, all host threads) on a bounded sample.
+def headline_problem(a, rank: int = 0, nq: int = 0):
+    """The seeded synthetic problem of the workload (six C{n} tiles, npz levels, nq tracers -- the workload's
+    when 0), generated on the GPU when there is one.  Tracers are drawn one by one, so the first tracers of a
+    smaller problem equal those of the workload's."""
+    import torch
+    from fv3atm_gb300 import synth as S
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    return S.make_problem(a.n, a.npz, nq or a.nq, seed=2000 + rank, cmax=0.8, pert_amp=10.0, dp_noise=0.10,
+                          device=dev)
 
-    The sample keeps the six C{n} tiles and the workload's generator settings
-    and reduces levels/tracers; `steps` timed steps (or as many as fit in
-    `seconds`) follow `warmup` untimed ones."""
+
+def oracle_sample(P, ntr: int) -> dict:
+    """Host FP64 copies of the fields of the CPU sample: tracers 0..ntr-1 of P and every per-level field."""
+    import numpy as np
+    host = lambda t: np.ascontiguousarray(t.detach().to("cpu", dtype=__import__("torch").float64).numpy())  # noqa: E731
+    return {"q": host(P.q[:, :ntr]), "dp": host(P.dp), "mfx": host(P.mfx), "mfy": host(P.mfy), "cx": host(P.cx),
+            "cy": host(P.cy), "geoms": P.geoms, "topo": P.topo, "ak": P.ak, "bk": P.bk, "n": P.n, "npz": P.npz,
+            "nq": ntr}
+
+
+def cpu_oracle_rate(smp: dict, q_split: int, steps: int, warmup: int = 0):
+    """Updates/s of the FP64 C++ oracle (OpenMP, all host threads) on the sample, one step = tracer_2d (q_split
+    substeps) + the kord-9 remap of every sample tracer; also returns the remapped tracers of the last step
+    (ntr, npz, 6, n, n)."""
     import numpy as np
     import oracle as O
-    from fv3atm_gb300 import synth as S
-    P = S.make_problem(n, npz, nq, seed=4242, cmax=0.8, pert_amp=10.0, dp_noise=0.10, device="cpu")
-    q0, dp, mfx, mfy, cx, cy = (P.q.numpy(), P.dp.numpy(), P.mfx.numpy(), P.mfy.numpy(), P.cx.numpy(),
-                                P.cy.numpy())
+    n, npz, nq = smp["n"], smp["npz"], smp["nq"]
+    q0, dp, mfx, mfy, cx, cy = (smp[k] for k in ("q", "dp", "mfx", "mfy", "cx", "cy"))
     sl = slice(3, 3 + n)
 
     def one_step():
-        q1, dp_last, ns = O.tracer_2d_cube(q0, dp, mfx, mfy, cx, cy, P.geoms, P.topo, hord=8, q_split=q_split)
+        q1, dp_last, ns = O.tracer_2d_cube(q0, dp, mfx, mfy, cx, cy, smp["geoms"], smp["topo"], hord=8,
+                                           q_split=q_split)
         fr = 1.0 / ns
         dpf = dp_last.copy()
-        for t, g in enumerate(P.geoms):
+        for t, g in enumerate(smp["geoms"]):
             mx, my = mfx[t] * fr, mfy[t] * fr
             dpf[t][:, sl, sl] = dp_last[t][:, sl, sl] + (mx[..., :-1] - mx[..., 1:] + my[..., :-1, :] -
                                                          my[..., 1:, :]) * g.rarea[sl, sl]
         dpi = dpf[:, :, sl, sl].transpose(1, 0, 2, 3).reshape(npz, -1)
-        pe1 = np.concatenate([np.full((1, dpi.shape[1]), P.ak[0]), P.ak[0] + np.cumsum(dpi, axis=0)])
-        pe2 = P.ak[:, None] + P.bk[:, None] * pe1[-1][None]
-        for iq in range(nq):
-            O.remap_columns(pe1, q1[:, iq][:, :, sl, sl].transpose(1, 0, 2, 3).reshape(npz, -1), pe2, kord=9)
+        pe1 = np.concatenate([np.full((1, dpi.shape[1]), smp["ak"][0]), smp["ak"][0] + np.cumsum(dpi, axis=0)])
+        pe2 = smp["ak"][:, None] + smp["bk"][:, None] * pe1[-1][None]
+        return np.stack([O.remap_columns(pe1, q1[:, iq][:, :, sl, sl].transpose(1, 0, 2, 3).reshape(npz, -1), pe2,
+                                         kord=9).reshape(npz, 6, n, n) for iq in range(nq)])
 
     for _ in range(warmup):
         one_step()
     t0 = time.perf_counter()
-    done = 0
-    while True:
-        one_step()
-        done += 1
-        el = time.perf_counter() - t0
-        if (steps is not None and done >= steps) or (steps is None and el >= seconds):
-            break
-    upd = 6 * n * n * npz * nq * done
-    return upd / el, {"sample": f"6xC{n} L{npz} {nq} tracers, n_split={q_split}, {done} steps",
-                      "seconds": el, "threads": os.cpu_count()}
+    for _ in range(steps):
+        out = one_step()
+    el = time.perf_counter() - t0
+    upd = 6 * n * n * npz * nq * steps
+    return upd / el, out, {"sample": f"6xC{n} L{npz}, tracers 0..{nq - 1} of the workload's seeded fields, "
+                                     f"n_split={q_split}, {steps} steps", "seconds": el, "threads": os.cpu_count()}
+
+
+def rel_l2_vs_oracle(x, ref, n):
+    """Per-tracer relative L2 of a GPU result x (6, ntr, npz, nd, nd) against the oracle's (ntr, npz, 6, n, n)."""
+    import numpy as np
+    s = slice(3, 3 + n)
+    out = []
+    for iq in range(ref.shape[0]):
+        g = np.asarray(x[:, iq, :, s, s], dtype=np.float64).transpose(1, 0, 2, 3)
+        out.append(float(np.linalg.norm(g - ref[iq]) / np.linalg.norm(ref[iq])))
+    return out
 
 
 # ------------------------------------------------------------------- main --
@@ -396,7 +421,10 @@ def run_reference(a, world, rank):
         return
     import oracle
     oracle.build()
-    rate, info = cpu_oracle_rate(a.n, a.npz, CPU_SAMPLE_NQ, a.q_split, 0.0, steps=a.steps, warmup=a.warmup)
+    P = headline_problem(a, nq=CPU_SAMPLE_NQ)
+    smp = oracle_sample(P, CPU_SAMPLE_NQ)
+    del P
+    rate, _, info = cpu_oracle_rate(smp, a.q_split, steps=a.steps, warmup=a.warmup)
     cfg = workload(a)
     cores = os.cpu_count()
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
@@ -466,7 +494,6 @@ def main():
 
     import __graft_entry__
     __graft_entry__.build()
-    from fv3atm_gb300 import synth as S
 
     units = 6 * a.n * a.n * a.npz * a.nq  # tracer-cell-levels per step
     # Pinned host arrays of the end-to-end leg, allocated first, as a model
@@ -480,7 +507,7 @@ def main():
     pinned = {} if a.no_e2e else {k: torch.empty(v, dtype=torch.float32, pin_memory=True)
                                   for k, v in e2e_shapes.items()}
     t_gen = time.perf_counter()
-    P = S.make_problem(a.n, a.npz, a.nq, seed=2000 + rank, cmax=0.8, pert_amp=10.0, dp_noise=0.10, device="cuda")
+    P = headline_problem(a, rank)
     torch.cuda.synchronize()
     t_gen = time.perf_counter() - t_gen
     stream = torch.cuda.Stream()
@@ -495,11 +522,13 @@ def main():
     st.step(a.q_split, use_graph=False)
     st.sync()
     m1 = st.mass("Q_REMAPPED")
-    mq = None
-    if not a.no_fp64:  # kept for the comparison with the FP64 leg, which runs last
-        mq = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, device="cuda")
-        st.download_device("Q_REMAPPED", mq.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
-        torch.cuda.synchronize()
+    # one step from the initial fields, kept for the comparisons with the FP64 leg and the oracle
+    mq = torch.empty(st.field_shape("Q_REMAPPED"), dtype=torch.float32, device="cuda")
+    st.download_device("Q_REMAPPED", mq.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    mq_sample = mq[:, :CPU_SAMPLE_NQ].cpu().numpy()
+    if a.no_fp64:
+        del mq
     q32 = P.q.to(torch.float32).contiguous()
     st.upload_device("Q", q32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
@@ -616,6 +645,7 @@ def main():
     # leave host-to-device copies from pinned memory several times slower for
     # the rest of the process on this host, which would distort the e2e leg.
     err = None
+    fp64_sample = None
     if not a.no_fp64:
         st = build_state(P, "fp64", a.nq, a.npz, a.n, 0)
         st.step(a.q_split, use_graph=False)
@@ -624,6 +654,7 @@ def main():
         st.download_device("Q_REMAPPED", ref_q.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         err = rel_err_per_tracer(mq, ref_q, a.n)
+        fp64_sample = ref_q[:, :CPU_SAMPLE_NQ].cpu().numpy()
         del mq, ref_q
         torch.cuda.empty_cache()
         ms64, kern64 = timed_steps(st, a, world, max(1, a.steps), max(1, min(a.warmup, 3)), stream)
@@ -635,10 +666,18 @@ def main():
 
     # ---------------------------------------------------------- CPU oracle
     cpu = None
+    vs_oracle = None
     if rank == 0 and world == 1 and not a.no_cpu:
-        rate, info = cpu_oracle_rate(a.n, a.npz, CPU_SAMPLE_NQ, a.q_split, 0.0, steps=CPU_SAMPLE_STEPS, warmup=0)
+        smp = oracle_sample(P, CPU_SAMPLE_NQ)
+        rate, ref, info = cpu_oracle_rate(smp, a.q_split, steps=CPU_SAMPLE_STEPS, warmup=0)
         cpu = {"value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port", "cpu_model": cpu_model(),
                "sample": info["sample"] + f", {info['seconds']:.1f} s (C++ FP64 oracle, OpenMP)"}
+        # the same tracers after one step of the GPU legs, against the FP64 oracle
+        vs_oracle = {"tracers": list(range(CPU_SAMPLE_NQ)),
+                     "mixed_rel_l2_vs_oracle_per_tracer": rel_l2_vs_oracle(mq_sample, ref, a.n),
+                     "fp64_rel_l2_vs_oracle_per_tracer": (rel_l2_vs_oracle(fp64_sample, ref, a.n)
+                                                          if fp64_sample is not None else None)}
+        del smp, ref
 
     if rank != 0:
         return
@@ -666,6 +705,8 @@ def main():
         "fp64": out.get("fp64"),
         "mixed_over_fp64": (value / out["fp64"]["value"]) if "fp64" in out else None,
         "mixed_rel_l2_vs_fp64_per_tracer": err,
+        "mixed_rel_l2_vs_oracle_per_tracer": vs_oracle["mixed_rel_l2_vs_oracle_per_tracer"] if vs_oracle else None,
+        "fp64_rel_l2_vs_oracle_per_tracer": vs_oracle["fp64_rel_l2_vs_oracle_per_tracer"] if vs_oracle else None,
         "mixed_mass_rel_change_one_step": [float(abs(x - y) / abs(y)) for x, y in zip(m1, m0)],
         "e2e": e2e,
         "ensemble": ens,

@@ -32,8 +32,9 @@
 // Layers 2..km-3: Lin (2004) kord 4 constraint (edge deviations at most
 // |2 dm| with the sign of dm); the two layers at each end: CW84.
 //
-// Both: for iv >= 0 a layer whose edges or interior minimum fall below the
-// floor is flattened.
+// Both: for iv >= 0, where a layer's edges or interior minimum fall below the
+// floor, its deviations are scaled so that the minimum reaches the floor
+// (Zhang & Shu 2010; the mean is kept and the result is continuous in q).
 #pragma once
 
 #include "fv3g_internal.cuh"
@@ -70,33 +71,45 @@ template <typename T> __device__ __forceinline__ void cw84_sel(T& bl, T& br) {
   br = flat ? T(0) : nbr;
 }
 
-// kord 9: the limited value of raw interface a at u (0..km)
-template <typename T, class QF>
-__device__ __forceinline__ T k9_interface(T a, int u, int km, int iv, T floor_v, QF q) {
-  if (u <= 0) return clamp2(a, q(0), q(1));
-  if (u >= km) return iv == -2 ? a : clamp2(a, q(km - 2), q(km - 1));
-  const T qa = q(u - 1), qb = q(u);
+// kord 9: the limited value of raw interface a at u (0..km), given the
+// means of layers u-2, u-1, u, u+1 (read only where they exist: the top
+// interface reads layers 0, 1 as qb, qp1, the bottom one km-2, km-1 as qm2, qa)
+template <typename T>
+__device__ __forceinline__ T k9_interface(T a, int u, int km, int iv, T floor_v, T qm2, T qa, T qb, T qp1) {
+  if (u <= 0) return clamp2(a, qb, qp1);
+  if (u >= km) return iv == -2 ? a : clamp2(a, qm2, qa);
   const T dc = qb - qa;
-  const T dl = u > 1 ? qa - q(u - 2) : dc;
-  const T dr = u < km - 1 ? q(u + 1) - qb : dc;
+  const T dl = u > 1 ? qa - qm2 : dc;
+  const T dr = u < km - 1 ? qp1 - qb : dc;
   const T lo = tmin(qa, qb), hi = tmax(qa, qb);
   const bool mono = same_sign(dl, dr);
   const bool near_max = !mono && dl > T(0);
   const T below = tmin(a, hi);
-  const T r = mono ? tmin(tmax(a, lo), hi) : (near_max ? tmax(a, lo) : (iv >= 0 ? tmax(below, floor_v) : below));
-  return r;
+  return mono ? tmin(tmax(a, lo), hi) : (near_max ? tmax(a, lo) : (iv >= 0 ? tmax(below, floor_v) : below));
 }
 
-// kord 4: half-increment slope of layer k (0 in the end layers)
-template <typename T, class QF, class HF>
-__device__ __forceinline__ T ppm_slope(int k, int km, QF q, HF h) {
-  if (k < 1 || k > km - 2) return T(0);
-  const T d0 = h(k - 1), d1 = h(k), d2 = h(k + 1);
-  const T qm = q(k - 1), q0 = q(k), qp = q(k + 1);
+// the same through a layer functor q(k): the end interfaces take their
+// layers from the column ends
+template <typename T, class QF>
+__device__ __forceinline__ T k9_interface_f(T a, int u, int km, int iv, T floor_v, QF q) {
+  if (u <= 0) return k9_interface(a, 0, km, iv, floor_v, T(0), T(0), q(0), q(1));
+  if (u >= km) return k9_interface(a, km, km, iv, floor_v, q(km - 2), q(km - 1), T(0), T(0));
+  return k9_interface(a, u, km, iv, floor_v, u > 1 ? q(u - 2) : T(0), q(u - 1), q(u), u < km - 1 ? q(u + 1) : T(0));
+}
+
+// kord 4: half-increment slope of layer k in 1..km-2 from the means and
+// thicknesses of layers k-1, k, k+1
+template <typename T>
+__device__ __forceinline__ T ppm_slope(T qm, T q0, T qp, T d0, T d1, T d2) {
   const T dq = d1 / (d0 + d1 + d2) * ((T(2) * d0 + d1) / (d2 + d1) * (qp - q0) + (d1 + T(2) * d2) / (d0 + d1) * (q0 - qm));
   const T mx = tmax(tmax(qm, q0), qp) - q0;
   const T mn = q0 - tmin(tmin(qm, q0), qp);
   return sign_of(tmin(tmin(T(0.5) * tabs(dq), mx), mn), dq);
+}
+template <typename T, class QF, class HF>
+__device__ __forceinline__ T ppm_slope_f(int k, int km, QF q, HF h) {
+  if (k < 1 || k > km - 2) return T(0);
+  return ppm_slope(q(k - 1), q(k), q(k + 1), h(k - 1), h(k), h(k + 1));
 }
 
 // interface between an end layer (q0, h0) and the next (q1, h1) from the
@@ -107,6 +120,19 @@ __device__ __forceinline__ T quad3_interface(T q0, T q1, T q2, T h0, T h1, T h2)
   const T w2 = -h0 * h1 / ((h0 + h1 + h2) * (h1 + h2));
   const T w1 = T(1) - w0 - w2;
   return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+// kord 4: CW84 eq. 1.6 at interface u in 2..km-2 (between layers j = u-1 and
+// u: means q0, q1) from the thicknesses of layers u-2..u+1 and the slopes
+// dml, dmr of layers u-1, u
+template <typename T>
+__device__ __forceinline__ T ppm_interface_inner(T q0, T q1, T dml, T dmr, T hm, T h0, T h1, T h2) {
+  const T s01 = h0 + h1, sall = hm + h0 + h1 + h2;
+  const T c0 = h0 / s01;
+  const T c1 = T(2) * h1 * h0 / s01 * ((hm + h0) / (T(2) * h0 + h1) - (h2 + h1) / (T(2) * h1 + h0)) / sall;
+  const T c2 = h0 * (hm + h0) / (T(2) * h0 + h1) / sall;
+  const T c3 = h1 * (h1 + h2) / (h0 + T(2) * h1) / sall;
+  return q0 + (c0 + c1) * (q1 - q0) - (T(2) * c2) * dmr + (T(2) * c3) * dml;
 }
 
 // kord 4: interface u (0..km); dml, dmr: the slopes of layers u-1 and u
@@ -125,27 +151,20 @@ __device__ __forceinline__ T ppm_interface(int u, int km, int iv, T qs, T dml, T
                         q(km - 2), q(km - 1));
     return u == km - 1 ? b1 : (iv == -2 ? qs : T(2) * q(km - 1) - b1);
   }
-  const int j = u - 1;  // CW84 eq. 1.6 between layers j and j+1
-  const T hm = h(j - 1), h0 = h(j), h1 = h(j + 1), h2 = h(j + 2);
-  const T s01 = h0 + h1, sall = hm + h0 + h1 + h2;
-  const T c0 = h0 / s01;
-  const T c1 = T(2) * h1 * h0 / s01 * ((hm + h0) / (T(2) * h0 + h1) - (h2 + h1) / (T(2) * h1 + h0)) / sall;
-  const T c2 = h0 * (hm + h0) / (T(2) * h0 + h1) / sall;
-  const T c3 = h1 * (h1 + h2) / (h0 + T(2) * h1) / sall;
-  return q(j) + (c0 + c1) * (q(j + 1) - q(j)) - (T(2) * c2) * dmr + (T(2) * c3) * dml;
+  return ppm_interface_inner(q(u - 1), q(u), dml, dmr, h(u - 2), h(u - 1), h(u), h(u + 1));
 }
 
-// Parabola of layer k from its limited-or-raw edges aL, aR (see the header):
-// kord 9 takes aL, aR after k9_interface; kord 4 takes the PPM interfaces and
-// the layer's slope dmk.
-template <typename T, int KORD, class QF>
-__device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qk, T aL, T aR, T dmk, int iv, T floor_v, QF q) {
+// Parabola of layer k (see the header) from its edges aL, aR (kord 9: after
+// k9_interface; kord 4: the PPM interfaces and the layer's slope dmk) and
+// the means of layers k-2..k+2 (read only for interior layers).
+template <typename T, int KORD>
+__device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qm2, T qm1, T qk, T qp1, T qp2, T aL, T aR,
+                                                    T dmk, int iv, T floor_v) {
   T bl = aL - qk, br = aR - qk;
   const bool end = k < 2 || k > km - 3;
   if (end) {
     cw84_sel(bl, br);
   } else if (KORD == 9) {
-    const T qm2 = q(k - 2), qm1 = q(k - 1), qp1 = q(k + 1), qp2 = q(k + 2);
     const T Dm = qm1 - qm2, D0 = qk - qm1, D1 = qp1 - qk, D2 = qp2 - qp1;
     const bool flat = opposite(D0, D1) && (opposite(Dm, D0) || opposite(D1, D2));
     const bool nonmono = T(3) * tabs(bl + br) > tabs(br - bl);
@@ -161,16 +180,35 @@ __device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qk, T aL, T
     bl = -sign_of(tmin(ax, tabs(bl)), xt);
     br = sign_of(tmin(ax, tabs(br)), xt);
   }
-  if (iv >= 0) {  // keep the reconstruction at or above the floor: flatten
+  if (iv >= 0) {
+    // Positivity (Zhang & Shu 2010 scaling, continuous in q): when an edge or
+    // the interior minimum q + s6/12 + da^2/(4 s6) (s6 < -|da|) lies below the
+    // floor, the deviations are scaled by (q - floor)/(q - min) (0 when q is
+    // below the floor).  The interior test is multiplied through by 12 s6:
+    // 12 s6 (q - floor) + s6^2 + 3 da^2 > 0.  Layers that need it are rare, so
+    // the divisions sit in a branch.
     const T s6 = T(-3) * (bl + br), da = br - bl;
     const bool inner = -s6 > tabs(da);
-    const T s6s = inner ? s6 : T(-1);
-    const T fmin = qk + s6s / T(12) + da * da / (T(4) * s6s);
-    const bool low = (qk + bl < floor_v) || (qk + br < floor_v) || (inner && fmin < floor_v);
-    bl = low ? T(0) : bl;
-    br = low ? T(0) : br;
+    const bool low = (qk + bl < floor_v) || (qk + br < floor_v) ||
+                     (inner && T(12) * s6 * (qk - floor_v) + s6 * s6 + T(3) * da * da > T(0));
+    if (low) {
+      T pmin = tmin(qk + bl, qk + br);
+      if (inner) pmin = tmin(pmin, qk + s6 / T(12) + da * da / (T(4) * s6));
+      const T lam = qk > floor_v ? (qk - floor_v) / (qk - pmin) : T(0);
+      bl = lam * bl;
+      br = lam * br;
+    }
   }
   return Profile<T>{qk, qk + bl, qk + br, T(-3) * (bl + br)};
+}
+
+// the same through a layer functor q(k)
+template <typename T, int KORD, class QF>
+__device__ __forceinline__ Profile<T> layer_profile_f(int k, int km, T qk, T aL, T aR, T dmk, int iv, T floor_v,
+                                                      QF q) {
+  const bool inner = k >= 2 && k <= km - 3;
+  return layer_profile<T, KORD>(k, km, inner ? q(k - 2) : qk, inner ? q(k - 1) : qk, qk, inner ? q(k + 1) : qk,
+                                inner ? q(k + 2) : qk, aL, aR, dmk, iv, floor_v);
 }
 
 }  // namespace fv3g

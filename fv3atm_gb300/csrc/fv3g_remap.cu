@@ -159,14 +159,14 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
       }
       // back substitution on the raw values; each interface is limited on its own
       T av = (rhs - SC(s_cp, km) * ap) * SC(s_rd, km);
-      SC(s_a, km) = k9_interface(av, km, km, a.iv, floor_v, qf);
+      SC(s_a, km) = k9_interface_f(av, km, km, a.iv, floor_v, qf);
       for (int k = km - 1; k >= 0; --k) {
         av = SC(s_a, k) - SC(s_cp, k) * av;
-        SC(s_a, k) = k9_interface(av, k, km, a.iv, floor_v, qf);
+        SC(s_a, k) = k9_interface_f(av, k, km, a.iv, floor_v, qf);
       }
     } else {
       // kord 4: the layer slopes (kept in s_d), then the PPM interfaces
-      for (int k = 0; k < km; ++k) SC(s_d, k) = ppm_slope<T>(k, km, qf, hf);
+      for (int k = 0; k < km; ++k) SC(s_d, k) = ppm_slope_f<T>(k, km, qf, hf);
       for (int u = 0; u <= km; ++u)
         SC(s_a, u) = ppm_interface<T>(u, km, a.iv, qsv, u >= 1 ? SC(s_d, u - 1) : T(0), u < km ? SC(s_d, u) : T(0),
                                       qf, hf);
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
     Profile<T> P{};
     auto prof = [&](int k) -> const Profile<T>& {
       if (k != kc) {
-        P = layer_profile<T, KORD>(k, km, q1[k * a.sQk], SC(s_a, k), SC(s_a, k + 1), KORD == 9 ? T(0) : SC(s_d, k),
+        P = layer_profile_f<T, KORD>(k, km, q1[k * a.sQk], SC(s_a, k), SC(s_a, k + 1), KORD == 9 ? T(0) : SC(s_d, k),
                                    a.iv, floor_v, qf);
         kc = k;
       }
@@ -613,6 +613,10 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
     scan_muls_fwd(alf, mf, lane);
     scan_muls_bwd(alb, mb, lane);
   }
+  // kord 4: thicknesses of layers u0-2 .. u0+NPL+1 (clamped into the column)
+  T hw[NPL + 4];
+#pragma unroll
+  for (int i = 0; i < NPL + 4; ++i) hw[i] = KORD == 9 ? T(1) : S.dp[pk<T>(min(max(u0 - 2 + i, 0), km - 1))];
   constexpr int FP = fields_per_pass<T>();
   for (int f0 = 0; f0 < a.nfield; f0 += FP) {
     __syncthreads();  // every warp is done with the previous pass, whose slots are refilled now
@@ -631,11 +635,16 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
       q2[h] = a.q_out + qo + f * a.sQqo;
       store[h] = real && f0 + h < a.nfield;
     }
-    T qv[FP][NPL], st[FP][NPL];
+    // w[h][i]: mean of layer u0 - 2 + i (clamped into the column), the lane's
+    // layers and two on either side; qv: the lane's own layers (0 past km)
+    T qv[FP][NPL], st[FP][NPL], w[FP][NPL + 4];
 #pragma unroll
-    for (int h = 0; h < FP; ++h)
+    for (int h = 0; h < FP; ++h) {
 #pragma unroll
-      for (int j = 0; j < NPL; ++j) qv[h][j] = (u0 + j < km) ? Q[h][pk<T>(u0 + j)] : T(0);
+      for (int i = 0; i < NPL + 4; ++i) w[h][i] = Q[h][pk<T>(min(max(u0 - 2 + i, 0), km - 1))];
+#pragma unroll
+      for (int j = 0; j < NPL; ++j) qv[h][j] = (u0 + j < km) ? w[h][j + 2] : T(0);
+    }
     // -------------------------------------------- interface values a[0..km]
     // st[h][j]: the limited interface u0 + j (kord 9) or the PPM one (kord 4);
     // the interface after the lane's last layer is the next lane's first
@@ -685,43 +694,55 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
       affine_enter_bwd_m<T, FP>(mb, be, av, lane);
 #pragma unroll
       for (int h = 0; h < FP; ++h) {
-        const T* Qh = Q[h];
-        auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
 #pragma unroll
         for (int j = NPL - 1; j >= 0; --j) {
           av[h] = y[h][j] - cpb[j] * av[h];
-          st[h][j] = k9_interface(av[h], min(u0 + j, km), km, a.iv, floor_v, qf);
+          st[h][j] = k9_interface(av[h], min(u0 + j, km), km, a.iv, floor_v, w[h][j], w[h][j + 1], w[h][j + 2],
+                                  w[h][j + 3]);
         }
         st_end[h] = __shfl_down_sync(0xffffffffu, st[h][0], 1);
       }
     } else {
 #pragma unroll
       for (int h = 0; h < FP; ++h) {
+        // slopes of layers u0-1 .. u0+NPL, then interfaces u0 .. u0+NPL
+        T dmw[NPL + 2];
+#pragma unroll
+        for (int i = 0; i < NPL + 2; ++i) {
+          const int k = u0 - 1 + i;
+          const T m = ppm_slope(w[h][i], w[h][i + 1], w[h][i + 2], hw[i], hw[i + 1], hw[i + 2]);
+          dmw[i] = (k >= 1 && k <= km - 2) ? m : T(0);
+        }
         const T* Qh = Q[h];
         auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
         auto hf = [&S, km](int k) -> T { return S.dp[pk<T>(min(max(k, 0), km - 1))]; };
-        T dml = ppm_slope<T>(u0 - 1, km, qf, hf);
+        T ai[NPL + 1];
+#pragma unroll
+        for (int j = 0; j <= NPL; ++j) {
+          const int u = min(u0 + j, km);
+          if (km > 2 && u >= 2 && u <= km - 2)
+            ai[j] = ppm_interface_inner(w[h][j + 1], w[h][j + 2], dmw[j], dmw[j + 1], hw[j], hw[j + 1], hw[j + 2],
+                                        hw[j + 3]);
+          else
+            ai[j] = ppm_interface<T>(u, km, a.iv, qsv, dmw[j], dmw[j + 1], qf, hf);
+        }
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
-          const T dmr = ppm_slope<T>(u0 + j, km, qf, hf);
-          st[h][j] = ppm_interface<T>(min(u0 + j, km), km, a.iv, qsv, dml, dmr, qf, hf);
-          dmv[h][j] = dmr;
-          dml = dmr;
+          st[h][j] = ai[j];
+          dmv[h][j] = dmw[j + 1];
         }
-        st_end[h] = ppm_interface<T>(min(u0 + NPL, km), km, a.iv, qsv, dml, ppm_slope<T>(u0 + NPL, km, qf, hf), qf,
-                                     hf);
+        st_end[h] = ai[NPL];
       }
     }
     // ------------------------------------------ sub-grid parabolas of layers
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
-      const T* Qh = Q[h];
-      auto qf = [Qh, km](int k) -> T { return Qh[pk<T>(min(max(k, 0), km - 1))]; };
 #pragma unroll
       for (int j = 0; j < NPL; ++j) {
         const int u = u0 + j;
-        const Profile<T> p = layer_profile<T, KORD>(u, km, qv[h][j], st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h],
-                                                    dmv[h][j], a.iv, floor_v, qf);
+        const Profile<T> p = layer_profile<T, KORD>(u, km, w[h][j], w[h][j + 1], qv[h][j], w[h][j + 3], w[h][j + 4],
+                                                    st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h], dmv[h][j],
+                                                    a.iv, floor_v);
         if (u < km) {
           S.pl[h][pk<T>(u)] = p.l;
           S.pr[h][pk<T>(u)] = p.r;

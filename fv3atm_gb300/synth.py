@@ -299,8 +299,9 @@ def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, c
         for t, g in enumerate(geoms):
             base = bell(g.centers, centers[iq]) if kind == "bell" else gaussian(g.centers, centers[iq])
             q[t, iq] = torch.as_tensor(base, device=dev)[None] * vert[:, None, None]
-    if noise > 0.0:
-        q += noise * torch.empty_like(q).uniform_(-1.0, 1.0, generator=gen)
+    if noise > 0.0:  # drawn tracer by tracer: the first tracers do not depend on nq
+        for iq in range(nq):
+            q[:, iq] += noise * torch.empty_like(q[:, iq]).uniform_(-1.0, 1.0, generator=gen)
         q.clamp_(min=0.0)
     if T == 6:
         fill_cube_halo(q.view(6, nq * npz, nd, nd), n, ng, topo)
@@ -312,19 +313,28 @@ def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, c
 def fill_courant_halo(cx, cy, n: int, ng: int, topo: np.ndarray) -> None:
     """Courant numbers of the halo faces of six tiles from the faces they stand for (grid.face_source), as a
     halo update of the winds gives them: cx (6, npz, nd, n+1) on the halo rows, cy (6, npz, n+1, nd) on the
-    halo columns."""
+    halo columns.  The sources are interior or tile-edge faces, which this does not change."""
+    import torch
     o = ng - 1
+    halo = list(range(1 - ng, 1)) + list(range(n + 1, n + ng + 1))
+    # (destination array, t, row, col) <- (source array, t, row, col, sign), grouped by the pair of arrays
+    groups = {}
     for t in range(6):
-        for j in list(range(1 - ng, 1)) + list(range(n + 1, n + ng + 1)):
+        for j in halo:
             for i in range(1, n + 2):
                 tt, fk, fi, fj, sign = G.face_source(topo, n, t, "x", i, j)
-                src = cx[tt, :, fj + o, fi - 1] if fk == "x" else cy[tt, :, fj - 1, fi + o]
-                cx[t, :, j + o, i - 1] = sign * src
-        for i in list(range(1 - ng, 1)) + list(range(n + 1, n + ng + 1)):
+                src = (fj + o, fi - 1) if fk == "x" else (fj - 1, fi + o)
+                groups.setdefault(("x", fk), []).append((t, j + o, i - 1, tt, *src, sign))
+        for i in halo:
             for j in range(1, n + 2):
                 tt, fk, fi, fj, sign = G.face_source(topo, n, t, "y", i, j)
-                src = cx[tt, :, fj + o, fi - 1] if fk == "x" else cy[tt, :, fj - 1, fi + o]
-                cy[t, :, j - 1, i + o] = sign * src
+                src = (fj + o, fi - 1) if fk == "x" else (fj - 1, fi + o)
+                groups.setdefault(("y", fk), []).append((t, j - 1, i + o, tt, *src, sign))
+    arrays = {"x": cx, "y": cy}
+    for (dk, sk), rows in groups.items():
+        idx = torch.as_tensor(np.array(rows, dtype=np.int64), device=cx.device)
+        src = arrays[sk][idx[:, 3], :, idx[:, 4], idx[:, 5]] * idx[:, 6:7].to(cx.dtype)
+        arrays[dk][idx[:, 0], :, idx[:, 1], idx[:, 2]] = src
 
 
 def _sync_edges(xf, yf, n: int, topo: np.ndarray, row_off: int) -> None:

@@ -577,8 +577,9 @@ void flux_update(double* qk, const double* dp1k, const Level& L, const double* f
 // of Lin (2004): each edge deviation at most |2 dm| with the sign of dm; the
 // two layers at each end take CW84.
 //
-// Both families, iv >= 0: a layer whose edges or interior minimum fall below
-// the floor (0, or q_min when iv == 1) is flattened (its mean is kept).
+// Both families, iv >= 0: where a layer's edges or interior minimum fall below
+// the floor (0, or q_min when iv == 1), its deviations from the mean are scaled
+// so that the minimum reaches the floor (Zhang & Shu 2010; mean kept).
 template <class T>
 void cs_interfaces(const T* q, const double* dp, int km, int iv, double qs, T* a) {
   std::vector<T> rhs(km + 1);
@@ -719,14 +720,28 @@ void column_profile_t(const T* q, const double* dp, int km, int iv, int kord, do
       bl = -tsign(tmin(tabs(xt), tabs(bl)), xt);
       br = tsign(tmin(tabs(xt), tabs(br)), xt);
     }
-    if (iv >= 0) {  // keep the reconstruction at or above the floor: flatten
-      const double l = val(q[k]) + val(bl), r = val(q[k]) + val(br);
+    if (iv >= 0) {
+      // Positivity (Zhang & Shu 2010 scaling): when the reconstruction's
+      // minimum -- an edge, or the interior minimum q + s6/12 + da^2/(4 s6) of
+      // a parabola with s6 < -|da| -- lies below the floor, the deviations are
+      // scaled by (q - floor)/(q - min) so that the minimum reaches the floor
+      // (by 0 when the mean itself is below it).  Mean-preserving and
+      // continuous in q.  The interior test is taken multiplied through by
+      // 12 s6: 12 s6 (q - floor) + s6^2 + 3 da^2 > 0.
+      const double qv = val(q[k]);
       const double s6 = -3.0 * (val(bl) + val(br)), da = val(br) - val(bl);
-      bool low = l < floor_v || r < floor_v;
-      if (!low && -s6 > std::fabs(da)) low = val(q[k]) + s6 / 12.0 + da * da / (4.0 * s6) < floor_v;
+      const bool inner = -s6 > std::fabs(da);
+      const bool low = qv + val(bl) < floor_v || qv + val(br) < floor_v ||
+                       (inner && 12.0 * s6 * (qv - floor_v) + s6 * s6 + 3.0 * da * da > 0.0);
       if (low) {
-        bl = T(0.0);
-        br = T(0.0);
+        T pmin = tmin(q[k] + bl, q[k] + br);
+        if (inner) {
+          const T s6t = T(-3.0) * (bl + br), dat = br - bl;
+          pmin = tmin(pmin, q[k] + s6t / T(12.0) + dat * dat / (T(4.0) * s6t));
+        }
+        const T lam = qv > floor_v ? (q[k] - T(floor_v)) / (q[k] - pmin) : T(0.0);
+        bl = lam * bl;
+        br = lam * br;
       }
     }
     aL[k] = q[k] + bl;

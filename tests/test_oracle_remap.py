@@ -71,6 +71,21 @@ def test_kord9_lets_a_smooth_peak_pass_its_mean():
     assert np.array_equal(q2, q)
 
 
+@pytest.mark.parametrize("kord", [9, 4])
+def test_positivity_limiter_is_continuous(kord):
+    """The iv >= 0 floor scales a layer's deviations instead of switching the layer to a flat profile, so the
+    remap is continuous in q: a perturbation of 1e-10 (relative) moves no value by more than 1e-8 of the range,
+    on columns with many local minima next to the floor (a switch there moved single values by O(1))."""
+    for seed in range(6):
+        pe1, pe2, rng = _column(seed=40 + seed)
+        q = np.maximum(rng.uniform(-0.3, 1.0, 127), 0.0) ** 2
+        q2 = O.remap_column(pe1, q, pe2, iv=0, kord=kord)
+        qp = q * (1.0 + 1e-10 * rng.standard_normal(127))
+        q2p = O.remap_column(pe1, qp, pe2, iv=0, kord=kord)
+        assert np.abs(q2p - q2).max() <= 1e-8 * q.max()
+        assert q2.min() >= -1e-15
+
+
 def _profile_np(q, dp, iv=0, kord=9, qs=0.0, q_min=0.0):
     """An independent numpy restatement of the column reconstruction (the same published constraints as the
     oracle's column_profile_t, written loop by loop) used to check the C++ oracle."""
@@ -161,13 +176,14 @@ def _profile_np(q, dp, iv=0, kord=9, qs=0.0, q_min=0.0):
             xt = 2 * dm[k]
             bl = -np.copysign(min(abs(xt), abs(bl)), xt)
             br = np.copysign(min(abs(xt), abs(br)), xt)
-        if iv >= 0:
+        if iv >= 0:  # scale the deviations so that the minimum reaches the floor
             s6, da = -3 * (bl + br), br - bl
-            low = q[k] + bl < floor or q[k] + br < floor
-            if not low and -s6 > abs(da):
-                low = q[k] + s6 / 12 + da * da / (4 * s6) < floor
-            if low:
-                bl = br = 0.0
+            pmin = min(q[k] + bl, q[k] + br)
+            if -s6 > abs(da):
+                pmin = min(pmin, q[k] + s6 / 12 + da * da / (4 * s6))  # the parabola's interior minimum
+            if pmin < floor:
+                lam = (q[k] - floor) / (q[k] - pmin) if q[k] > floor else 0.0
+                bl, br = lam * bl, lam * br
         out[k] = (q[k], q[k] + bl, q[k] + br, -3 * (bl + br))
     return out
 
