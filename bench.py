@@ -518,6 +518,7 @@ def main():
     st = build_state(P, "mixed", a.nq, a.npz, a.n, a.warps)
     warps = a.warps if a.warps > 0 else st.autotune()
     ring_warps = st.widths()[1]
+    pairs = st.tracer_pairs()
     m0 = st.mass("Q")
     st.step(a.q_split, use_graph=False)
     st.sync()
@@ -689,11 +690,11 @@ def main():
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 stencils; f64 pe/overlap schedule/mass sums", "data": "synthetic (seeded; no public dataset)",
         "config": {**workload(a), "precision": "mixed", "replicas": world, "warps_per_cta": warps,
-                   "warps_per_cta_edge_ring": ring_warps},
+                   "warps_per_cta_edge_ring": ring_warps, "tracers_per_warp": 2 if pairs else 1},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_substep<float,8> (fused fv_tp_2d + flux-form update), interior + edge-ring launch "
-                               "pair of one substep",
+                     "kernel": ("k_substep_pair (two tracers per warp)" if pairs else "k_substep<float,8>") +
+                               " (fused fv_tp_2d + flux-form update), interior + edge-ring launch pair of one substep",
                      "alg_bytes_per_substep": ab["substep"], "avg_substep_ms": sub_avg,
                      "launches_per_substep": sub_n / (a.steps * a.q_split), "peak_kind": peak_kind},
         "step_hbm": {"alg_bytes_per_update": ab["per_update"], "achieved_gbs": step_gbs, "frac": step_gbs / peak},

@@ -292,6 +292,15 @@ class CubeState:
         _lib.call("fv3g_state_nsplt", self._h, C.byref(n))
         return n.value
 
+    def set_tracer_pairs(self, on: bool) -> None:
+        """FP32 states with hord 8: advance the tracers two per warp (True) or one per warp (False)."""
+        _lib.call("fv3g_state_set_tracer_pairs", self._h, int(bool(on)))
+
+    def tracer_pairs(self) -> bool:
+        on = C.c_int(0)
+        _lib.call("fv3g_state_tracer_pairs", self._h, C.byref(on))
+        return bool(on.value)
+
     def widths(self) -> tuple:
         """(interior, edge-ring) advection CTA widths in warps."""
         w, r = C.c_int(0), C.c_int(0)

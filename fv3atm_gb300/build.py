@@ -13,6 +13,10 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfv3g.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "549,177"]
+# The column remap runs two fields per pass in unrolled copies of the same code; without automatic
+# multiply-add contraction (explicit fmaf stays fused) both copies round alike, so a field's result does not
+# depend on which slot of a pass it took (tracer groups of the pipelined host step remap bit for bit alike).
+FILE_FLAGS = {"fv3g_remap.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -43,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

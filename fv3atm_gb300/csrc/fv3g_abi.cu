@@ -127,6 +127,7 @@ struct fv3g_state {
   void* del6u = nullptr; void* del6v = nullptr;  // tracer-damping metrics
   int del6_tiles = 0;                            // tiles whose damping metrics were set
   int warps_ring = 0;                            // edge-ring CTA width (0: warps_per_cta), set by autotune
+  int pairs = 0;                                 // FP32 hord 8: tracers two per warp (k_substep_pair)
   double da_min = 0.0;
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
@@ -226,6 +227,9 @@ void build_topo(Topo& tp) {
     }
 }
 
+// Paired advection (two tracers per warp) exists for FP32 states with hord 8.
+bool pairs_allowed(const fv3g_state* st) { return !st->fp64 && st->d.hord == 8; }
+
 template <typename T>
 AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   AdvArgs<T> a{};
@@ -262,6 +266,7 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
   a.warps_ring = st->warps_ring;
   a.err = st->err;
+  a.pairs = pairs_allowed(st) ? st->pairs : 0;
   return a;
 }
 
@@ -783,9 +788,11 @@ int fv3g_state_nsplt(fv3g_state* st, int* nsplt) {
 // unchanged.
 int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
-  const int cand[] = {4, 5, 6, 8, 10};
-  const int saved_w = st->d.warps_per_cta, saved_r = st->warps_ring, q_cur = st->q_cur, dp_start = st->dp_start,
-            dp_end = st->dp_end;
+  // candidate widths per mode: one tracer per warp, and (FP32 hord 8) two
+  static const int cand[2][7] = {{4, 5, 6, 8, 10, 0, 0}, {3, 4, 5, 6, 8, 10, 12}};
+  const int nmode = pairs_allowed(st) ? 2 : 1;
+  const int saved_w = st->d.warps_per_cta, saved_r = st->warps_ring, saved_p = st->pairs, q_cur = st->q_cur,
+            dp_start = st->dp_start, dp_end = st->dp_end;
   const bool remapped = st->remapped, timing = st->timing;
   st->timing = false;
   cudaEvent_t e0, e1;
@@ -814,22 +821,29 @@ int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
     }
     return 0;
   };
-  int best = 0, best_r = 0;
+  int best = 0, best_r = 0, best_mode = 0;
   float best_ms = 0.f;
   st->warps_ring = 0;
-  for (int w : cand) {
-    st->d.warps_per_cta = w;
-    float ms;
-    if ((rc = time_one(ms))) break;
-    if (ms < 0.f) continue;
-    if (best == 0 || ms < best_ms) {
-      best = w;
-      best_ms = ms;
+  for (int mode = 0; mode < nmode && !rc; ++mode) {
+    st->pairs = mode;
+    for (int w : cand[mode]) {
+      if (w == 0) break;
+      st->d.warps_per_cta = w;
+      float ms;
+      if ((rc = time_one(ms))) break;
+      if (ms < 0.f) continue;
+      if (best == 0 || ms < best_ms) {
+        best = w;
+        best_mode = mode;
+        best_ms = ms;
+      }
     }
   }
   if (!rc && best > 0) {
+    st->pairs = best_mode;
     st->d.warps_per_cta = best;
-    for (int w : cand) {
+    for (int w : cand[best_mode]) {
+      if (w == 0) break;
       if (w == best) continue;
       st->warps_ring = w;
       float ms;
@@ -850,15 +864,37 @@ int fv3g_state_autotune(fv3g_state* st, int* warps_out) {
   if (rc || best == 0) {
     st->d.warps_per_cta = saved_w;
     st->warps_ring = saved_r;
+    st->pairs = saved_p;
     return rc ? rc : set_error(FV3G_E_ARG, "no advection CTA width fits this precision");
   }
   st->d.warps_per_cta = best;
   st->warps_ring = best_r;
+  st->pairs = best_mode;
   if (st->gexec) {  // the captured step was built for the old width
     cudaGraphExecDestroy(st->gexec);
     st->gexec = nullptr;
   }
   if (warps_out) *warps_out = best;
+  return 0;
+}
+
+int fv3g_state_set_tracer_pairs(fv3g_state* st, int on) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (on && !pairs_allowed(st))
+    return set_error(FV3G_E_UNSUPPORTED, "tracer pairs exist for FP32 states with hord 8 only");
+  if (on && st->d.warps_per_cta > PAIR_WIDTH_MAX)
+    return set_error(FV3G_E_ARG, "tracer pairs take at most %d warps per CTA", PAIR_WIDTH_MAX);
+  st->pairs = on ? 1 : 0;
+  if (st->gexec) {
+    cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+  }
+  return 0;
+}
+
+int fv3g_state_tracer_pairs(fv3g_state* st, int* on) {
+  if (!st || !on) return set_error(FV3G_E_ARG, "null argument");
+  *on = pairs_allowed(st) ? st->pairs : 0;
   return 0;
 }
 

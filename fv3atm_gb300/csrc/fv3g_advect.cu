@@ -260,6 +260,9 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
     if (prc) return prc;
   }
   if (hord == 1 && !(a.lim_fac > 0.0)) return set_error(FV3G_E_ARG, "hord 1 needs lim_fac > 0 (got %g)", a.lim_fac);
+  if constexpr (std::is_same<T, float>::value) {
+    if (a.pairs && hord == 8 && !flux_mode) return launch_substep_pair(a, warps, s);
+  }
   switch (hord) {
     case 8: return launch_substep_hord<T, 8>(a, flux_mode, warps, s);
     case 5: return launch_substep_hord<T, 5>(a, flux_mode, warps, s);

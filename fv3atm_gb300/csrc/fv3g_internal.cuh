@@ -97,6 +97,7 @@ struct AdvArgs {
   int nord;
   int damp_mass;    // 1: field q, flux weighted by damp times the face mean of dp1; 0: field damp q
   int* err;         // optional sticky error word: FV3G_E_DELP when a compute cell's dp2 is not positive
+  int pairs;        // FP32, hord 8: advance the tracers two per warp (k_substep_pair)
 };
 
 // First error of a batched step into its sticky word (later ones are dropped).
@@ -235,6 +236,8 @@ int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGe
                      cudaStream_t s);
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s);
+int launch_substep_pair(const AdvArgs<float>& a, int warps, cudaStream_t s);
+constexpr int PAIR_WIDTH_MAX = 12;  // warps (tracer pairs) per CTA of the paired substep
 template <typename T>
 int launch_edge_fix(const AdvArgs<T>& a, int n, cudaStream_t s);
 // Unscaled Courant numbers and mass fluxes to read instead of scaling in place.

@@ -154,17 +154,42 @@ __device__ __forceinline__ T ppm_interface(int u, int km, int iv, T qs, T dml, T
   return ppm_interface_inner(q(u - 1), q(u), dml, dmr, h(u - 2), h(u - 1), h(u), h(u + 1));
 }
 
-// Parabola of layer k (see the header) from its edges aL, aR (kord 9: after
-// k9_interface; kord 4: the PPM interfaces and the layer's slope dmk) and
-// the means of layers k-2..k+2 (read only for interior layers).
+// a / b for the positivity scaling: FP32 columns take the fast reciprocal
+// form (2 ulp; the scaling is continuous, so this moves results by rounding
+// only), FP64 and tangent-linear columns the exact division
+template <typename T> __device__ __forceinline__ T pos_div(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float pos_div<float>(float a, float b) { return __fdividef(a, b); }
+
+// Positivity for iv >= 0 (Zhang & Shu 2010 scaling, continuous in q): when an
+// edge or the interior minimum q + s6/12 + da^2/(4 s6) (s6 < -|da|) lies
+// below the floor, the deviations are scaled by (q - floor)/(q - min) (0 when
+// q is below the floor).  The interior test is multiplied through by 12 s6:
+// 12 s6 (q - floor) + s6^2 + 3 da^2 > 0.  Layers that need it are rare, so the
+// divisions sit in a branch.  FP32 columns scale by a factor smaller by
+// 2^-21, which keeps the fast division's result at or above the floor.
+template <typename T>
+__device__ __forceinline__ void positivity(T qk, T floor_v, T& bl, T& br) {
+  const T s6 = T(-3) * (bl + br), da = br - bl;
+  const bool inner = -s6 > tabs(da);
+  const bool low = (qk + bl < floor_v) || (qk + br < floor_v) ||
+                   (inner && T(12) * s6 * (qk - floor_v) + s6 * s6 + T(3) * da * da > T(0));
+  if (low) {
+    T pmin = tmin(qk + bl, qk + br);
+    if (inner) pmin = tmin(pmin, qk + pos_div(s6, T(12)) + pos_div(da * da, T(4) * s6));
+    T lam = qk > floor_v ? pos_div(qk - floor_v, qk - pmin) : T(0);
+    if (Single<T>::value) lam = lam * T(1.0 - 1.0 / (1 << 21));
+    bl = lam * bl;
+    br = lam * br;
+  }
+}
+
+// Constraint of an interior layer k (2 <= k <= km-3; see the header) on its
+// edge deviations bl = aL - q, br = aR - q (kord 9: edges after k9_interface;
+// kord 4: the PPM interfaces and the layer's slope dmk), with the means of
+// layers k-2..k+2.
 template <typename T, int KORD>
-__device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qm2, T qm1, T qk, T qp1, T qp2, T aL, T aR,
-                                                    T dmk, int iv, T floor_v) {
-  T bl = aL - qk, br = aR - qk;
-  const bool end = k < 2 || k > km - 3;
-  if (end) {
-    cw84_sel(bl, br);
-  } else if (KORD == 9) {
+__device__ __forceinline__ void interior_constraint(T qm2, T qm1, T qk, T qp1, T qp2, T dmk, T& bl, T& br) {
+  if (KORD == 9) {
     const T Dm = qm1 - qm2, D0 = qk - qm1, D1 = qp1 - qk, D2 = qp2 - qp1;
     const bool flat = opposite(D0, D1) && (opposite(Dm, D0) || opposite(D1, D2));
     const bool nonmono = T(3) * tabs(bl + br) > tabs(br - bl);
@@ -180,25 +205,18 @@ __device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qm2, T qm1,
     bl = -sign_of(tmin(ax, tabs(bl)), xt);
     br = sign_of(tmin(ax, tabs(br)), xt);
   }
-  if (iv >= 0) {
-    // Positivity (Zhang & Shu 2010 scaling, continuous in q): when an edge or
-    // the interior minimum q + s6/12 + da^2/(4 s6) (s6 < -|da|) lies below the
-    // floor, the deviations are scaled by (q - floor)/(q - min) (0 when q is
-    // below the floor).  The interior test is multiplied through by 12 s6:
-    // 12 s6 (q - floor) + s6^2 + 3 da^2 > 0.  Layers that need it are rare, so
-    // the divisions sit in a branch.
-    const T s6 = T(-3) * (bl + br), da = br - bl;
-    const bool inner = -s6 > tabs(da);
-    const bool low = (qk + bl < floor_v) || (qk + br < floor_v) ||
-                     (inner && T(12) * s6 * (qk - floor_v) + s6 * s6 + T(3) * da * da > T(0));
-    if (low) {
-      T pmin = tmin(qk + bl, qk + br);
-      if (inner) pmin = tmin(pmin, qk + s6 / T(12) + da * da / (T(4) * s6));
-      const T lam = qk > floor_v ? (qk - floor_v) / (qk - pmin) : T(0);
-      bl = lam * bl;
-      br = lam * br;
-    }
-  }
+}
+
+// Parabola of layer k (see the header) from its edges aL, aR and the means of
+// layers k-2..k+2 (read only for interior layers): the two layers at each
+// end take CW84, the others interior_constraint; then the floor.
+template <typename T, int KORD>
+__device__ __forceinline__ Profile<T> layer_profile(int k, int km, T qm2, T qm1, T qk, T qp1, T qp2, T aL, T aR,
+                                                    T dmk, int iv, T floor_v) {
+  T bl = aL - qk, br = aR - qk;
+  if (k < 2 || k > km - 3) cw84_sel(bl, br);
+  else interior_constraint<T, KORD>(qm2, qm1, qk, qp1, qp2, dmk, bl, br);
+  if (iv >= 0) positivity(qk, floor_v, bl, br);
   return Profile<T>{qk, qk + bl, qk + br, T(-3) * (bl + br)};
 }
 

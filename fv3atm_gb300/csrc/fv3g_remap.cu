@@ -533,19 +533,14 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
   }
 
   // ------------------------------------------- LU of the interface system
-  // Row u of the system: rhs_u = wa q[ia] + wb q[ib] + wc qs, forward step
+  // Row u of the system: rhs_u = wa q_a + wb q_b + wc qs with layers a, b =
+  // u-1, u (top row: 0, 1; bottom row: km-1, km-2), forward step
   // y_u = (rhs_u - mco_u y_{u-1}) rd_u, back step a_u = y_u - cpb_u a_{u+1};
   // rows above km have rd = 0.  kord 4 has no system: its interfaces are an
   // explicit stencil.
   T wa[NPL], wb[NPL], wc[NPL], mco[NPL], rdv[NPL], cpb[NPL];
-  int ia[NPL], ib[NPL];
 #pragma unroll
-  for (int j = 0; j < NPL; ++j) {
-    const int u = u0 + j;
-    ia[j] = min(u == 0 ? 0 : u - 1, km - 1);
-    ib[j] = max(min(u == 0 ? 1 : (u == km ? km - 2 : u), km - 1), 0);
-    wa[j] = wb[j] = wc[j] = mco[j] = rdv[j] = cpb[j] = T(0);
-  }
+  for (int j = 0; j < NPL; ++j) wa[j] = wb[j] = wc[j] = mco[j] = rdv[j] = cpb[j] = T(0);
   if (KORD == 9 && km > 1) {
     const T g = S.dp[pk<T>(1)] / S.dp[pk<T>(0)];
     T dd[NPL];
@@ -667,7 +662,12 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
         be[h] = T(0);
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
-          rhs[h][j] = wa[j] * Q[h][pk<T>(ia[j])] + wb[j] * Q[h][pk<T>(ib[j])] + wc[j] * qsv;
+          // the two layers of row u (ia, ib) from the window: u-1 and u inside the
+          // column, 0 and 1 at the top row, km-1 and km-2 at the bottom one
+          const int u = u0 + j;
+          const T qa = u == 0 ? w[h][j + 2] : w[h][j + 1];
+          const T qb = u == 0 ? w[h][j + 3] : (u == km ? w[h][j] : w[h][j + 2]);
+          rhs[h][j] = wa[j] * qa + wb[j] * qb + wc[j] * qsv;
           be[h] = ajv[j] * be[h] + rhs[h][j] * rdv[j];
           dmv[h][j] = T(0);
         }
@@ -737,16 +737,34 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
     // ------------------------------------------ sub-grid parabolas of layers
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
+      // every layer as an interior one (uniform across the warp) ...
 #pragma unroll
       for (int j = 0; j < NPL; ++j) {
         const int u = u0 + j;
-        const Profile<T> p = layer_profile<T, KORD>(u, km, w[h][j], w[h][j + 1], qv[h][j], w[h][j + 3], w[h][j + 4],
-                                                    st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h], dmv[h][j],
-                                                    a.iv, floor_v);
+        const T qk = qv[h][j];
+        T bl = st[h][j] - qk, br = (j + 1 < NPL ? st[h][j + 1] : st_end[h]) - qk;
+        interior_constraint<T, KORD>(w[h][j], w[h][j + 1], qk, w[h][j + 3], w[h][j + 4], dmv[h][j], bl, br);
+        if (a.iv >= 0) positivity(qk, floor_v, bl, br);
         if (u < km) {
-          S.pl[h][pk<T>(u)] = p.l;
-          S.pr[h][pk<T>(u)] = p.r;
-          S.p6[h][pk<T>(u)] = p.s6;
+          S.pl[h][pk<T>(u)] = qk + bl;
+          S.pr[h][pk<T>(u)] = qk + br;
+          S.p6[h][pk<T>(u)] = T(-3) * (bl + br);
+        }
+      }
+      // ... then the two layers at each end of the column again, with CW84
+      // (only the lanes that hold them)
+      if (u0 < 2 || u0 + NPL > km - 2) {
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+          const int u = u0 + j;
+          if (u < km && (u < 2 || u > km - 3)) {
+            const Profile<T> p = layer_profile<T, KORD>(u, km, qv[h][j], qv[h][j], qv[h][j], qv[h][j], qv[h][j],
+                                                        st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h], T(0), a.iv,
+                                                        floor_v);
+            S.pl[h][pk<T>(u)] = p.l;
+            S.pr[h][pk<T>(u)] = p.r;
+            S.p6[h][pk<T>(u)] = p.s6;
+          }
         }
       }
     }
@@ -816,9 +834,14 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
         for (int j = 0; j < NPL; ++j) {
           const int t = u0 + j;
           const FF mass = ff_add(cm[j + 1], ff_neg(cm[j]));
-          // a division, not a product with the rounded reciprocal: that rounding is shared by every tracer
-          // of the layer and biased the global mass (+5e-10 per step at C384 L127 x20)
-          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T((mass.hi + mass.lo) / (float)dpk[j]);
+          // the quotient mass / dp, not mass times the rounded reciprocal (that rounding is shared by every
+          // tracer of the layer and biased the global mass, +5e-10 per step at C384 L127 x20): the
+          // reciprocal's product corrected by one Newton step on the exact residual (fma), which gives the
+          // rounded quotient but for rare ties, unbiased
+          const float mm = mass.hi + mass.lo, d = (float)dpk[j], r = (float)rdpk[j];
+          const float q0 = mm * r;
+          const float qq = fmaf(fmaf(-q0, d, mm), r, q0);
+          if (store[h] && t < kn) q2[h][(long long)t * a.sQk] = T(qq);
         }
       } else {
 #pragma unroll

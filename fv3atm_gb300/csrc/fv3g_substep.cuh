@@ -28,7 +28,9 @@
 #pragma once
 
 #include <cstdio>
+#include <type_traits>
 
+#include "fv3g_pair.cuh"
 #include "fv3g_stencil.cuh"
 
 namespace fv3g {
@@ -88,7 +90,8 @@ size_t substep_smem_bytes(int warps, bool edges, bool two_edges) {
 // ------------------------------------------------------- PPM line stream ---
 // Deviations (bl, br) of the four cells e-2..e+1 around a cube-face edge at
 // window face e, computed once per line from shared memory and kept there
-// (o[c*32] = bl of cell e-2+c, o[(4+c)*32] = br; lane-strided).  `east`: the
+// (o[c*OS] = bl of cell e-2+c, o[(4+c)*OS] = br; lane-strided, OS = 32 values
+// or, for one value of a pair of tracers, 64).  `east`: the
 // tile interior lies below face e (the high edge of the tile).  The edge value
 // is the mean of the two one-sided, dxa-weighted linear extrapolations.
 //   hord 8: the edge value is clamped to the two cells beside it; the next
@@ -125,7 +128,7 @@ __device__ __forceinline__ T generic_br(int c, EX&& x) {
   return T(7.0 / 12.0) * (x(c) + x(c + 1)) - T(1.0 / 12.0) * (x(c - 1) + x(c + 2)) - x(c);
 }
 
-template <typename T, int HORD, class EX, class ED>
+template <typename T, int HORD, int OS = 32, class EX, class ED>
 __device__ __noinline__ void edge_devs(int e, bool east, EX x, ED ed, T* o) {
   if (e == NO_EDGE) return;
   bool need[4];
@@ -180,7 +183,7 @@ __device__ __noinline__ void edge_devs(int e, bool east, EX x, ED ed, T* o) {
     if (need[0]) b[0] = generic_bl<T, HORD>(e - 2, x);
     if (need[3]) r[3] = generic_br<T, HORD>(e + 1, x);
   }
-  for (int c = 0; c < 4; ++c) { o[c * 32] = b[c]; o[(4 + c) * 32] = r[c]; }
+  for (int c = 0; c < 4; ++c) { o[c * OS] = b[c]; o[(4 + c) * OS] = r[c]; }
 }
 
 // A line of 32 window cells x[0..31] marched with a rolling register window;
@@ -263,6 +266,70 @@ struct Line {
       psm = sm;
     }
     const T fl = c > T(0) ? fl_l : fl_r;
+    xa = xb;
+    xb = xc;
+    xc = x;
+    alb = alc;
+    pbr = br;
+    pb0 = b0;
+    return fl;
+  }
+};
+
+// Two FP32 hord-8 lines marched in lockstep as packed pairs (two tracers of
+// one line, or two lines of one tracer that see the same faces), value for
+// value the march of Line<float, 8>:
+// before step m the state holds x[m-3..m-1] (xa, xb, xc), the slope of cell
+// m-2 (dmb, as magnitude mb and sign sb) and its interface al (alb), and the
+// right deviation and b0 of cell m-3; step(x[m]) finalises cell m-2 and
+// returns the flux through face m-2 (valid for m >= 5).
+struct PairLine {
+  F2 xa, xb, xc, dmb, mb, sb, alb, pbr, pb0;
+
+  __device__ __forceinline__ void init() {
+    xa = xb = xc = dmb = mb = alb = pbr = pb0 = bc(0.f);
+    sb = bc(1.f);
+  }
+
+  // ed: the pair's edge-deviation slots (lane-strided pairs); or, for two
+  // lines with separate slots, edx for the first value and edy for the second
+  template <bool EDGES>
+  __device__ __forceinline__ F2 step(int m, F2 x, float c, const F2* ed, const EdgeSel& es) {
+    return step2<EDGES, true>(m, x, c, ed, nullptr, nullptr, es);
+  }
+  template <bool EDGES, bool PAIRED_SLOTS>
+  __device__ __forceinline__ F2 step2(int m, F2 x, float c, const F2* ed, const float* edx, const float* edy,
+                                      const EdgeSel& es) {
+    // monotonized central slope of cell m-1 (half increments), |dm| and sign
+    const F2 xt = mul2(sub2(x, xb), bc(0.25f));
+    const F2 mag = min3_2(abs2(xt), sub2(max3_2(xb, xc, x), xc), sub2(xc, min3_2(xb, xc, x)));
+    const F2 sg = sign2(xt);
+    const F2 dmc = mul2(mag, sg);
+    const F2 alc = fma2(sub2(dmb, dmc), bc(1.f / 3.f), mul2(bc(0.5f), add2(xb, xc)));  // al[m-1]
+    // cell m-2: edge deviations at most |2 dm| with the sign of dm (Lin 2004)
+    const F2 two = add2(mb, mb);
+    F2 bl = mul2(min2(two, abs2(sub2(alb, xb))), neg2(sb));
+    F2 br = mul2(min2(two, abs2(sub2(alc, xb))), sb);
+    dmb = dmc;
+    mb = mag;
+    sb = sg;
+    if (EDGES && ((es.mask >> m) & 1u)) {  // cell m-2 is cell e-2+d of an edge
+      const int dA = m - es.eA;
+      const int slot = (unsigned)dA < 4u ? dA : es.sb + (m - es.eB);
+      if (PAIRED_SLOTS) {
+        bl = ed[slot * 32];
+        br = ed[(slot + 4) * 32];
+      } else {
+        bl = F2{edx[slot * 32], edy[slot * 32]};
+        br = F2{edx[(slot + 4) * 32], edy[(slot + 4) * 32]};
+      }
+    }
+    const F2 b0 = add2(bl, br);
+    const float a = fabsf(c);
+    const float w1 = 1.f - a, w2 = a * w1;
+    const F2 fl_l = fma2(bc(-w2), pb0, fma2(bc(w1), pbr, xa));  // upwind cell on the left (c > 0)
+    const F2 fl_r = fma2(bc(-w2), b0, fma2(bc(w1), bl, xb));
+    const F2 fl = c > 0.f ? fl_l : fl_r;
     xa = xb;
     xb = xc;
     xc = x;
@@ -374,40 +441,69 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       }
     }
     const bool efw = EDGES && a.cube && a.eflux != nullptr && outer && ro < nj;
-    Line<T, HORD> li, lo;
-    li.init(T(a.lim_fac));
-    lo.init(T(a.lim_fac));
+    if constexpr (std::is_same<T, float>::value && HORD == 8 && !FLUXES) {
+      // FP32 hord 8: the inner line (q) and the outer one (q_i) of this row see
+      // the same faces, so they march as one packed pair (x: inner, y: outer)
+      PairLine lp;
+      lp.init();
+      auto pstep = [&](int m, float c) {
+        return lp.template step2<EDGES, false>(m, F2{qrow[m], qirow[m]}, c, nullptr, ed0, ed1, esx);
+      };
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      li.template step<EDGES>(m, qrow[m], T(0), ed0, esx);
-      lo.template step<EDGES>(m, qirow[m], T(0), ed1, esx);
-    }
-    // face 3
-    T c = L.cx[r][0];
-    T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, esx);
-    T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, esx);
-    T fxx_prev = L.xf[r][0] * fx2;
-    T F_prev = (fo + fx2) * L.mx[ro][0];
-    if (FLUXES && outer) qirow[0] = F_prev;
-    if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
+      for (int m = 0; m < 5; ++m) pstep(m, 0.f);
+      F2 fr = pstep(5, L.cx[r][0]);  // face 3: (inner flux fx2, outer flux fo)
+      float fxx_prev = L.xf[r][0] * fr.x;
+      float F_prev = (fr.y + fr.x) * L.mx[ro][0];
+      if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
 #pragma unroll 2
-    for (int m = 6; m < WIN; ++m) {
-      const int f = m - 2;
-      const T xcol = li.xa;  // q at window column f-1 of this row
-      c = L.cx[r][f - 3];
-      fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, esx);
-      fo = lo.template step<EDGES>(m, qirow[m], c, ed1, esx);
-      const T fxx = L.xf[r][f - 3] * fx2;
-      // q_j of window column f-1 (interior column f-4); column m-6 of this row is consumed
-      qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
-      fxx_prev = fxx;
-      const T F = (fo + fx2) * L.mx[ro][f - 3];
-      if (outer) {
-        if (FLUXES) qirow[f - 3] = F;  // column f-3 was consumed at step f-3
-        else qirow[f - 4] = xcol * L.dpa[ro][f - 4] + (F_prev - F);  // q dp1/rarea + x divergence
+      for (int m = 6; m < WIN; ++m) {
+        const int f = m - 2;
+        const float xcol = lp.xa.x;  // q at window column f-1 of this row
+        fr = pstep(m, L.cx[r][f - 3]);
+        const float fxx = L.xf[r][f - 3] * fr.x;
+        qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
+        fxx_prev = fxx;
+        const float F = (fr.y + fr.x) * L.mx[ro][f - 3];
+        if (outer) qirow[f - 4] = xcol * L.dpa[ro][f - 4] + (F_prev - F);
+        if (efw && i0 + f - 3 == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
+        F_prev = F;
       }
-      if (efw && i0 + f - 3 == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
-      F_prev = F;
+    } else {
+      Line<T, HORD> li, lo;
+      li.init(T(a.lim_fac));
+      lo.init(T(a.lim_fac));
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        li.template step<EDGES>(m, qrow[m], T(0), ed0, esx);
+        lo.template step<EDGES>(m, qirow[m], T(0), ed1, esx);
+      }
+      // face 3
+      T c = L.cx[r][0];
+      T fx2 = li.template step<EDGES>(5, qrow[5], c, ed0, esx);
+      T fo = lo.template step<EDGES>(5, qirow[5], c, ed1, esx);
+      T fxx_prev = L.xf[r][0] * fx2;
+      T F_prev = (fo + fx2) * L.mx[ro][0];
+      if (FLUXES && outer) qirow[0] = F_prev;
+      if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
+#pragma unroll 2
+      for (int m = 6; m < WIN; ++m) {
+        const int f = m - 2;
+        const T xcol = li.xa;  // q at window column f-1 of this row
+        c = L.cx[r][f - 3];
+        fx2 = li.template step<EDGES>(m, qrow[m], c, ed0, esx);
+        fo = lo.template step<EDGES>(m, qirow[m], c, ed1, esx);
+        const T fxx = L.xf[r][f - 3] * fx2;
+        // q_j of window column f-1 (interior column f-4); column m-6 of this row is consumed
+        qrow[f - 4] = (xcol * L.area[r][f - 1] + fxx_prev - fxx) * L.rrx[r][f - 4];
+        fxx_prev = fxx;
+        const T F = (fo + fx2) * L.mx[ro][f - 3];
+        if (outer) {
+          if (FLUXES) qirow[f - 3] = F;  // column f-3 was consumed at step f-3
+          else qirow[f - 4] = xcol * L.dpa[ro][f - 4] + (F_prev - F);  // q dp1/rarea + x divergence
+        }
+        if (efw && i0 + f - 3 == a.npx) a.eflux[efo + efe + iq * (long long)n + (j0 + ro - 1)] = F;
+        F_prev = F;
+      }
     }
   }
   __syncwarp();
@@ -465,17 +561,19 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
 // instantiations: the edge code path costs registers the interior one does
 // not need.  Interior CTAs cover the rectangle [bx0, bx0+nbxi) x [by0,
 // by0+nbyi) of CTA tiles; edge CTAs enumerate the ring around it row by row.
-template <typename T, int HORD, bool FLUXES, bool EDGES>
-__device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap& bm) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
-  const bool two = EDGES && edge_slots16<T>(a.is, a.ie, a.js, a.je);
-  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES, two);
-  SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
-  T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
+// CTA tile of a substep launch: interior CTAs cover the rectangle [bx0,
+// bx0+nbxi) x [by0, by0+nbyi) of CTA tiles; edge CTAs enumerate the ring
+// around it row by row.  Returns the tile's first cell (i0, j0) and size.
+struct TileCtx {
+  int t, k, i0, j0, ni, nj, exA, exB, eyA, eyB;
+  bool corner_block;
+};
 
-  const int t = blockIdx.z, k = blockIdx.y;
+template <typename T, bool EDGES>
+__device__ __forceinline__ TileCtx tile_of(const AdvArgs<T>& a, const BlockMap& bm) {
+  TileCtx c;
+  c.t = blockIdx.z;
+  c.k = blockIdx.y;
   int bx, by;
   {
     const int e = blockIdx.x;
@@ -498,18 +596,28 @@ __device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap
       }
     }
   }
-  const int i0 = a.is + bx * TW, j0 = a.js + by * TW;
-  const int ni = min(TW, a.ie - i0 + 1), nj = min(TW, a.je - j0 + 1);
-  const PlaneGeom& pg = a.pg;
-  const int n = a.npx - 1;
-
+  c.i0 = a.is + bx * TW;
+  c.j0 = a.js + by * TW;
+  c.ni = min(TW, a.ie - c.i0 + 1);
+  c.nj = min(TW, a.je - c.j0 + 1);
   // window faces of cube-face edges (x: west/east, y: south/north)
-  const int exA = EDGES ? window_edge_lo(a.is, i0, a.nested) : NO_EDGE;
-  const int exB = EDGES ? window_edge_hi(a.ie, a.npx, i0, a.nested) : NO_EDGE;
-  const int eyA = EDGES ? window_edge_lo(a.js, j0, a.nested) : NO_EDGE;
-  const int eyB = EDGES ? window_edge_hi(a.je, a.npy, j0, a.nested) : NO_EDGE;
+  c.exA = EDGES ? window_edge_lo(a.is, c.i0, a.nested) : NO_EDGE;
+  c.exB = EDGES ? window_edge_hi(a.ie, a.npx, c.i0, a.nested) : NO_EDGE;
+  c.eyA = EDGES ? window_edge_lo(a.js, c.j0, a.nested) : NO_EDGE;
+  c.eyB = EDGES ? window_edge_hi(a.je, a.npy, c.j0, a.nested) : NO_EDGE;
+  c.corner_block = !a.nested && a.corners != 0 && ((c.i0 - 3 < 1) || (c.i0 + 28 > a.npx - 1)) &&
+                   ((c.j0 - 3 < 1) || (c.j0 + 28 > a.npy - 1));
+  return c;
+}
 
-  // ---------------------------------------------- per-level staging -------
+// Per-level fields of a CTA tile into shared memory (Courant numbers, area
+// and mass fluxes, 1/ra_x, 1/ra_y, dp ratios; edge metrics for edge CTAs);
+// writes dp2 of the tile's cells.  Ends with a CTA barrier.
+template <typename T, bool EDGES>
+__device__ __forceinline__ void stage_level(const AdvArgs<T>& a, SmemLevel<T>& L, const TileCtx& tc) {
+  const PlaneGeom& pg = a.pg;
+  const int t = tc.t, k = tc.k, i0 = tc.i0, j0 = tc.j0, ni = tc.ni, nj = tc.nj;
+  const int exA = tc.exA, exB = tc.exB, eyA = tc.eyA, eyB = tc.eyB;
   {
     const long long fo = t * a.sFt + k * a.sFk;
     const T* cx = a.cx + fo;
@@ -578,9 +686,23 @@ __device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap
     }
   }
   __syncthreads();
+}
 
-  const bool corner_block = !a.nested && a.corners != 0 &&
-                            ((i0 - 3 < 1) || (i0 + 28 > a.npx - 1)) && ((j0 - 3 < 1) || (j0 + 28 > a.npy - 1));
+template <typename T, int HORD, bool FLUXES, bool EDGES>
+__device__ __forceinline__ void substep_body(const AdvArgs<T>& a, const BlockMap& bm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemLevel<T>& L = *reinterpret_cast<SmemLevel<T>*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, W = blockDim.x >> 5;
+  const bool two = EDGES && edge_slots16<T>(a.is, a.ie, a.js, a.je);
+  unsigned char* wbase = smem_raw + sizeof(SmemLevel<T>) + warp * warp_smem_bytes<T>(EDGES, two);
+  SmemWarp<T>& S = *reinterpret_cast<SmemWarp<T>*>(wbase);
+  T* eds = reinterpret_cast<T*>(wbase + sizeof(SmemWarp<T>));
+  const TileCtx tc = tile_of<T, EDGES>(a, bm);
+  stage_level<T, EDGES>(a, L, tc);
+  const int t = tc.t, k = tc.k, i0 = tc.i0, j0 = tc.j0, ni = tc.ni, nj = tc.nj;
+  const int exA = tc.exA, exB = tc.exB, eyA = tc.eyA, eyB = tc.eyB;
+  const int n = a.npx - 1;
+  const bool corner_block = tc.corner_block;
   // edge-flux index (((t*4 + e)*npz + k)*nq + iq)*n + s = efo + e*efe + iq*n + s
   const long long efe = (long long)a.npz * a.nq * n;
   const long long efo = (((long long)t * 4) * a.npz + k) * a.nq * n;

@@ -370,10 +370,18 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
                    const void* cy, const void* mfx, const void* mfy, void* q_out, int host_f32,
                    int groups, void* stream);
 /* Choose the advection CTA width (warps per CTA) by timing one substep of
- * the loaded fields at each candidate width; the fastest is kept for the
- * state (warps_out may be NULL).  Side-effect free on the state's fields.
- * Call it outside stream capture, after the inputs are uploaded. */
+ * the loaded fields at each candidate width -- for FP32 states with hord 8
+ * both with one tracer per warp and with two (fv3g_state_set_tracer_pairs)
+ * -- and keep the fastest for the state (warps_out may be NULL).
+ * Side-effect free on the state's fields.  Call it outside stream capture,
+ * after the inputs are uploaded. */
 int fv3g_state_autotune(fv3g_state* st, int* warps_out);
+/* FP32 states with hord 8: advance the tracers two per warp (on = 1; packed
+ * FP32 pair arithmetic, up to 12 warps per CTA) or one per warp (0, the
+ * default).  Results agree to FP32 rounding.  FV3G_E_UNSUPPORTED for other
+ * states when on = 1. */
+int fv3g_state_set_tracer_pairs(fv3g_state* st, int on);
+int fv3g_state_tracer_pairs(fv3g_state* st, int* on);
 /* The advection CTA widths in use: interior CTAs and the CTAs whose window
  * holds a cube-face edge (the autotuner may run those narrower). */
 int fv3g_state_widths(fv3g_state* st, int* warps, int* warps_ring);

@@ -10,6 +10,7 @@ import pytest
 import oracle as O
 from fv3atm_gb300 import api
 from fv3atm_gb300 import synth as S
+from fv3atm_gb300._lib import Fv3gError
 
 from ._helpers import (area_fluxes, cube_mass, final_dp, interior, ra_xy, rel_l2, remap_reference)
 
@@ -79,6 +80,40 @@ def test_cube_edge_sync_option_matches_oracle(cuda, cube_prob, precision, tol, h
         m1 = cube_mass(q, dpf, P.geoms, P.n)
         assert np.all(np.abs(m1 - m0) <= 1e-13 * np.abs(m0)), (m1 - m0) / m0
     st.close()
+
+
+@pytest.mark.parametrize("n,nq,warps,edge_sync", [(60, 3, 0, False), (12, 2, 0, False), (28, 4, 1, False),
+                                                  (30, 5, 2, True), (53, 2, 12, False), (29, 25, 4, True)])
+def test_tracer_pairs_match_oracle_and_single_tracers(cuda, n, nq, warps, edge_sync):
+    """FP32 hord 8 with two tracers per warp (packed pair arithmetic): against the FP64 oracle within the mixed
+    tolerance and against the one-tracer-per-warp kernel within FP32 rounding -- odd tracer counts (the last
+    pair holds one tracer), windows that hold both cube edges (n <= 28) or an edge at window face 30/31, several
+    pairs per warp, and the tile-edge reconciliation (edge fluxes written per tracer of a pair)."""
+    P = S.make_problem(n, 3, nq, seed=71, cmax=0.8)
+    q_ref, _, _ = O.tracer_2d_cube(P.q, P.dp, P.mfx, P.mfy, P.cx, P.cy, P.geoms, P.topo, hord=8, q_split=2,
+                                   sync_edges=edge_sync)
+    out = {}
+    for pairs in (False, True):
+        st = api.CubeState(n, 3, nq, precision="mixed", hord=8, warps_per_cta=warps, edge_sync=edge_sync)
+        st.load_problem(P)
+        st.set_tracer_pairs(pairs)
+        assert st.tracer_pairs() == pairs
+        st.tracer_2d(2)
+        out[pairs] = st.download("Q")
+        st.close()
+    for iq in range(nq):
+        assert rel_l2(interior(out[True][:, iq], n), interior(q_ref[:, iq], n)) <= MIXED_TOL, iq
+        assert rel_l2(interior(out[True][:, iq], n), interior(out[False][:, iq], n)) <= 1e-6, iq
+
+
+def test_tracer_pairs_only_for_fp32_hord8(cuda):
+    P = S.make_problem(14, 2, 2, seed=3)
+    for prec, hord in (("fp64", 8), ("mixed", 5)):
+        st = api.CubeState(14, 2, 2, precision=prec, hord=hord)
+        with pytest.raises(Fv3gError, match="tracer pairs"):
+            st.set_tracer_pairs(True)
+        assert not st.tracer_pairs()
+        st.close()
 
 
 @pytest.mark.parametrize("warps", [1, 3])
@@ -734,11 +769,15 @@ def test_autotune_picks_a_width_and_leaves_results_unchanged(cuda, cube_prob):
     st = api.CubeState(P.n, P.npz, P.nq, precision="mixed")
     st.load_problem(P)
     w = st.autotune()
-    assert w in (4, 5, 6, 8, 10)
+    assert w in (3, 4, 5, 6, 8, 10, 12)
     assert st.widths()[0] == w and st.widths()[1] <= 8  # FP32 edge-ring CTAs are capped at 8 warps
     st.step(3)
     got = st.download("Q_REMAPPED")
-    want = _run_cube(P, "mixed", remap=True, graph=True, warps=4).download("Q_REMAPPED")
+    ref = api.CubeState(P.n, P.npz, P.nq, precision="mixed", warps_per_cta=4)
+    ref.load_problem(P)
+    ref.set_tracer_pairs(st.tracer_pairs())  # the mode the tuner chose, at another width
+    ref.step(3)
+    want = ref.download("Q_REMAPPED")
     assert np.array_equal(got, want)  # every tracer's arithmetic is independent of the CTA width
 
 
