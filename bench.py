@@ -547,6 +547,25 @@ def main():
     step_gbs = ab["step"] * a.steps / (ms / 1e3) / 1e9
     launches = sum(v[1] for v in kern.values())
 
+    # ------------------------------------------------------ mass-fixer leg
+    # the same state with the global mass fixer on: one step's mass change
+    # from the initial fields, then the cost of the fixer in timed steps
+    st.set_mass_fix(True)
+    q32 = P.q.to(torch.float32).contiguous()
+    st.upload_device("Q", q32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    del q32
+    fm0 = st.mass("Q")
+    st.step(a.q_split, use_graph=False)
+    st.sync()
+    fm1 = st.mass("Q_REMAPPED")
+    ms_fix, kern_fix = timed_steps(st, a, world, a.steps, min(a.warmup, 3), stream)
+    st.set_mass_fix(False)
+    mass_fix = {"rel_change_one_step": [float(abs(x - y) / abs(y)) for x, y in zip(fm1, fm0)],
+                "ms_per_step": ms_fix / a.steps, "overhead_ms_per_step": (ms_fix - ms) / a.steps,
+                "remap_ms_per_step": kern_fix.get("remap", (0.0, 0))[0] / a.steps,
+                "kernels": "per remap: k_mass_partial + reduce before (step-start mass) and after, k_mass_fix"}
+
     # --------------------------------------------------------------- e2e leg
     e2e = None
     if not a.no_e2e:
@@ -709,6 +728,7 @@ def main():
         "mixed_rel_l2_vs_oracle_per_tracer": vs_oracle["mixed_rel_l2_vs_oracle_per_tracer"] if vs_oracle else None,
         "fp64_rel_l2_vs_oracle_per_tracer": vs_oracle["fp64_rel_l2_vs_oracle_per_tracer"] if vs_oracle else None,
         "mixed_mass_rel_change_one_step": [float(abs(x - y) / abs(y)) for x, y in zip(m1, m0)],
+        "mixed_mass_fix": mass_fix,
         "e2e": e2e,
         "ensemble": ens,
         "cpu_baseline": cpu,

@@ -28,7 +28,7 @@ EXPORTS = (
     "fv3g_ensemble_step", "fv3g_ensemble_destroy", "fv3g_fillz", "fv3g_pressure_vars", "fv3g_fillz_batched",
     "fv3g_tracer_2d_nested", "fv3g_nc_open", "fv3g_nc_close", "fv3g_nc_nvars", "fv3g_nc_var_info", "fv3g_nc_checksum",
     "fv3g_nc_read", "fv3g_state_read_restart", "fv3g_state_write_restart", "fv3g_state_nsplt",
-    "fv3g_state_set_tracer_pairs", "fv3g_state_tracer_pairs",
+    "fv3g_state_set_tracer_pairs", "fv3g_state_tracer_pairs", "fv3g_state_set_mass_fix",
 )
 
 
@@ -52,7 +52,7 @@ class StateDesc(C.Structure):
     _fields_ = [("n", C.c_int), ("ntiles", C.c_int), ("npz", C.c_int), ("nq", C.c_int), ("precision", C.c_int),
                 ("hord", C.c_int), ("kord", C.c_int), ("iv", C.c_int), ("q_min", C.c_double),
                 ("warps_per_cta", C.c_int), ("nord_tr", C.c_int), ("trdm", C.c_double), ("lim_fac", C.c_double),
-                ("fill", C.c_int), ("edge_sync", C.c_int)]
+                ("fill", C.c_int), ("edge_sync", C.c_int), ("mass_fix", C.c_int)]
 
 
 class NestBC(C.Structure):

@@ -203,14 +203,15 @@ class CubeState:
 
     def __init__(self, n: int, npz: int, nq: int, *, precision: str = "fp64", hord: int = 8, kord: int = 9,
                  iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0, ntiles: int = 6, nord_tr: int = 0,
-                 trdm: float = 0.0, lim_fac: float = 1.0, fill: bool = False, edge_sync: bool = False):
+                 trdm: float = 0.0, lim_fac: float = 1.0, fill: bool = False, edge_sync: bool = False,
+                 mass_fix: bool = False):
         L = _lib.load()
         self.n, self.npz, self.nq, self.ntiles = n, npz, nq, ntiles
         self.nd = n + 6
         self.precision = precision
         prec = _lib.FV3G_FP64 if precision == "fp64" else _lib.FV3G_MIXED
         desc = StateDesc(n, ntiles, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta, nord_tr, trdm, lim_fac,
-                         int(fill), int(edge_sync))
+                         int(fill), int(edge_sync), int(mass_fix))
         self._h = C.c_void_p()
         _lib.check(L.fv3g_state_create(C.byref(desc), C.byref(self._h)), "fv3g_state_create")
         self._grids = []
@@ -295,6 +296,10 @@ class CubeState:
     def set_tracer_pairs(self, on: bool) -> None:
         """FP32 states with hord 8: advance the tracers two per warp (True) or one per warp (False)."""
         _lib.call("fv3g_state_set_tracer_pairs", self._h, int(bool(on)))
+
+    def set_mass_fix(self, on: bool) -> None:
+        """Restore each tracer's global mass after every step (True) or leave it as transported (False)."""
+        _lib.call("fv3g_state_set_mass_fix", self._h, int(bool(on)))
 
     def tracer_pairs(self) -> bool:
         on = C.c_int(0)

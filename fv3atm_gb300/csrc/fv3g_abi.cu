@@ -132,6 +132,8 @@ struct fv3g_state {
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
   double* partials = nullptr; double* mass_out = nullptr;
+  double* mass0 = nullptr;  // mass fixer: each tracer's mass at the step's start, then scratch (6 nq)
+  int* emax = nullptr;      // mass fixer: each tracer's largest biased exponent at the step's start
   unsigned long long* cmax = nullptr;  // bits of the Courant maximum (q_split 0)
   int last_nsplt = 0;                  // substeps of the last tracer_2d
   int* err = nullptr;
@@ -454,6 +456,56 @@ int tracer_2d_t(fv3g_state* st, int nsplt, cudaStream_t s) {
   return substeps_t<T>(st, nsplt, 0, st->nq, s);
 }
 
+// Global-mass arguments of tracers [g0, g0+ng) of field q on thickness dp.
+template <typename T>
+MassArgs<T> mass_args(const fv3g_state* st, const void* q, const void* dp, int g0) {
+  MassArgs<T> m{};
+  m.sQk = st->plane;
+  m.sQq = st->plane * st->npz;
+  m.sQt = m.sQq * st->nq;
+  m.q = (const T*)q + (long long)g0 * m.sQq;
+  m.dp = (const T*)dp;
+  m.sFk = st->plane;
+  m.sFt = st->plane * st->npz;
+  m.area = (const T*)st->area;
+  m.sMt = st->plane;
+  m.pg = st->pg;
+  m.i1 = 1; m.j1 = 1; m.ni = st->n; m.nj = st->n;
+  m.npz = st->npz;
+  m.ntiles = st->nt;
+  m.partials = st->partials;
+  return m;
+}
+
+// Mass fixer (desc.mass_fix), around the remap of tracers [g0, g0+ng): the
+// step-start mass from the home buffer and the Lagrangian thickness before
+// the remap overwrites it (with each tracer's largest exponent), then after
+// the remap the remapped mass with its small-value class and the correction
+// of each tracer back to its step-start mass.  Scratch: mass0 holds the
+// step-start masses [0, nq), the remapped masses [nq, 4nq) (three per
+// tracer, by group) and the first pass's moved masses [4nq, 6nq) (two per
+// tracer, by group).
+template <typename T>
+int mass_fix_pre(fv3g_state* st, cudaStream_t s, int g0, int ng) {
+  MassArgs<T> m = mass_args<T>(st, st->q[0], st->dp[0], g0);
+  if (!st->fp64) {
+    FV3G_CUDA(cudaMemsetAsync(st->emax + g0, 0, sizeof(int) * ng, s));
+    m.emax_out = st->emax + g0;
+  }
+  return launch_mass<T>(m, ng, st->mass0 + g0, s);
+}
+template <typename T>
+int mass_fix_post(fv3g_state* st, cudaStream_t s, int g0, int ng) {
+  const MassArgs<T> m = mass_args<T>(st, st->q[0], st->dp_eul, g0);
+  MassArgs<T> mc = m;
+  if (!st->fp64) mc.cls_emax = st->emax + g0;
+  double* m1c = st->mass0 + st->nq + 3 * g0;
+  double* dm = st->mass0 + 4 * st->nq + 2 * g0;
+  CHECK(launch_mass<T>(mc, ng, m1c, s));
+  return launch_mass_fix<T>(m, (T*)st->q[0] + (long long)g0 * m.sQq, ng, g0, st->mass0 + g0, m1c, dm,
+                            st->fp64 ? nullptr : st->emax + g0, s);
+}
+
 // Remap of tracers [g0, g0+ng) of tiles [t0, t0+ntl) from the Lagrangian
 // levels onto ak + bk ps.
 template <typename T>
@@ -484,11 +536,15 @@ int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1, int t0 = 0,
   r.km = st->npz; r.kn = st->npz;
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
+  const bool whole = t0 == 0 && ntl == st->nt;  // every tile of the tracers: the mass fixer applies here
+  if (st->d.mass_fix && whole) CHECK(mass_fix_pre<T>(st, s, g0, ng));
   CHECK(launch_remap<T>(r, st->d.kord, s));
   if (st->d.fill)  // Lagrangian_to_Eulerian's fillz of the remapped tracers
     CHECK(launch_fillz_planes<T>(r.q_out, r.dp_out, st->n, ntl, st->npz, ng, r.sQt, r.sQq, r.sQk, r.sFt, r.sFk,
                                  st->pg, s));
-  CHECK(mark(st, K_REMAP, s, st->d.fill ? 2 : 1));
+  if (st->d.mass_fix && whole) CHECK(mass_fix_post<T>(st, s, g0, ng));
+  // mass fixer: two mass sums (2 launches each), then 3 fixer launches (FP32) or 1 (FP64)
+  CHECK(mark(st, K_REMAP, s, (st->d.fill ? 2 : 1) + (st->d.mass_fix && whole ? (st->fp64 ? 5 : 7) : 0)));
   if (t0 + ntl == st->nt) {  // the last tile range of the field: the state now holds the remapped field
     st->q_cur = 0;
     st->remapped = true;
@@ -629,8 +685,10 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
     rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
   if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
-  if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * 2 * MASS_BLOCKS * d.nq);
+  if (!rc) rc = dalloc(st, (void**)&st->partials, sizeof(double) * MASS_PARTIALS_PER_TRACER * d.nq);
   if (!rc) rc = dalloc(st, (void**)&st->mass_out, sizeof(double) * d.nq);
+  if (!rc) rc = dalloc(st, (void**)&st->mass0, sizeof(double) * 6 * d.nq);
+  if (!rc) rc = dalloc(st, (void**)&st->emax, sizeof(int) * d.nq);
   if (!rc) rc = dalloc(st, (void**)&st->cmax, sizeof(unsigned long long));
   if (!rc) rc = dalloc(st, (void**)&st->err, sizeof(int));
   if (!rc) {
@@ -895,6 +953,16 @@ int fv3g_state_set_tracer_pairs(fv3g_state* st, int on) {
 int fv3g_state_tracer_pairs(fv3g_state* st, int* on) {
   if (!st || !on) return set_error(FV3G_E_ARG, "null argument");
   *on = pairs_allowed(st) ? st->pairs : 0;
+  return 0;
+}
+
+int fv3g_state_set_mass_fix(fv3g_state* st, int on) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  st->d.mass_fix = on ? 1 : 0;
+  if (st->gexec) {  // the captured step holds the old kernel list
+    cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+  }
   return 0;
 }
 
@@ -1250,7 +1318,15 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
     FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + g], 0));
     CHECK(st->fp64 ? substeps_t<double>(st, q_split, g0, ng, cs) : substeps_t<float>(st, q_split, g0, ng, cs));
     // the remap runs tile by tile, each tile's download starting as soon as it is remapped, so only the
-    // last tile of the last group waits for its download at the end
+    // last tile of the last group waits for its download at the end; with the mass fixer the group's
+    // tiles are remapped first and corrected together, then downloaded
+    if (st->d.mass_fix) {
+      CHECK(st->fp64 ? remap_t<double>(st, cs, g0, ng) : remap_t<float>(st, cs, g0, ng));
+      FV3G_CUDA(cudaEventRecord(st->pev[2 + G + (size_t)g * st->nt], cs));
+      FV3G_CUDA(cudaStreamWaitEvent(ds, st->pev[2 + G + (size_t)g * st->nt], 0));
+      CHECK(q_group_copy(st, g0, ng, q_out, true, ds, kCopyCtas));
+      continue;
+    }
     for (int t = 0; t < st->nt; ++t) {
       CHECK(st->fp64 ? remap_t<double>(st, cs, g0, ng, t, 1) : remap_t<float>(st, cs, g0, ng, t, 1));
       cudaEvent_t done = st->pev[2 + G + (size_t)g * st->nt + t];

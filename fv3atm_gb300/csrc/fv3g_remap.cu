@@ -20,6 +20,7 @@
 #include <cfloat>
 #include <mutex>
 
+#include "fv3g_ff.cuh"
 #include "fv3g_internal.cuh"
 #include "fv3g_profile.cuh"
 #include "fv3g_remap.cuh"
@@ -259,26 +260,6 @@ struct ColSmem {
   float mh[FP][pk<float>(32 * NPL) + 1];  // FP32 fields: cumulative layer mass at every source interface,
   float ml[FP][pk<float>(32 * NPL) + 1];  // as an unevaluated sum hi + lo (float-float)
 };
-
-// Float-float arithmetic (an unevaluated sum of two floats, ~48-bit
-// significand): the error-free transformations TwoSum (Knuth) and TwoProd
-// (with fma), then one renormalisation.
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  float e = (a.hi - (s - bb)) + (b.hi - bb);
-  e += a.lo + b.lo;
-  const float h = s + e;
-  return FF{h, e - (h - s)};
-}
-__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
-__device__ __forceinline__ FF ff_prod(float a, float b) {
-  const float p = a * b;
-  return FF{p, fmaf(a, b, -p)};
-}
 
 // Fields reach shared memory through a ring of RING slots, filled by
 // cp.async RING-1 fields ahead.  Each slot holds the CTA's 8 columns,

@@ -300,6 +300,10 @@ typedef struct {
                      downwind tile's edge cell is corrected); 0 (upstream behaviour) keeps each tile's own
                      value.  With halos that hold the neighbours' cells, metrics and winds the two values
                      already agree to round-off; the option removes that round-off from the global mass. */
+  int mass_fix;   /* 1: after every remap of all tiles, restore each tracer's global mass sum(q delp area) to its
+                     value at the step's start (the transport conserves it; FP32 storage rounds it by ~1e-10 per
+                     step): FP64 states scale q by (1 + eps); FP32 states move a dithered few values by one unit
+                     in the last place, unbiased, leaving ~1e-13 (the stored FP32 mass is summed exactly) */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */
@@ -382,6 +386,9 @@ int fv3g_state_autotune(fv3g_state* st, int* warps_out);
  * states when on = 1. */
 int fv3g_state_set_tracer_pairs(fv3g_state* st, int on);
 int fv3g_state_tracer_pairs(fv3g_state* st, int* on);
+/* Switch the mass fixer (fv3g_state_desc.mass_fix) on (1) or off (0) for
+ * the following steps. */
+int fv3g_state_set_mass_fix(fv3g_state* st, int on);
 /* The advection CTA widths in use: interior CTAs and the CTAs whose window
  * holds a cube-face edge (the autotuner may run those narrower). */
 int fv3g_state_widths(fv3g_state* st, int* warps, int* warps_ring);

@@ -116,6 +116,43 @@ def test_tracer_pairs_only_for_fp32_hord8(cuda):
         st.close()
 
 
+@pytest.mark.parametrize("precision,bound", [("mixed", 1e-12), ("fp64", 1e-14)])
+def test_mass_fix_restores_global_mass_every_step(cuda, precision, bound):
+    """mass_fix = 1: after each step every tracer's global mass sum(q delp area) equals its value at the step's
+    start to the bound (the FP32 state's mass summed exactly; the FP32 fixer's floor is ~2^-24 of the largest
+    values' share of the mass, then 2^-10 of that in its second pass), over several steps; the fixed state stays
+    within 1e-8 of the unfixed one, and the host-array step (tracer groups) fixes bit for bit alike."""
+    import torch
+    P = S.make_problem(192, 64, 4, seed=83, cmax=0.8)
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision, mass_fix=True)
+    st.load_problem(P)
+    plain = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    plain.load_problem(P)
+    for step in range(4):
+        m0 = st.mass("Q")
+        st.step(3)
+        st.sync()
+        m1 = st.mass("Q_REMAPPED")
+        assert np.all(np.abs(m1 - m0) <= bound * np.abs(m0)), (step, (m1 - m0) / m0)
+        if step == 0:
+            plain.step(3)
+            a, b = st.download("Q_REMAPPED"), plain.download("Q_REMAPPED")
+            for iq in range(P.nq):
+                assert rel_l2(interior(a[:, iq], P.n), interior(b[:, iq], P.n)) <= 1e-8
+            want = a
+        # the next step starts from the remapped (and fixed) field
+        st.upload("Q", st.download("Q_REMAPPED"))
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
+    host = {k: torch.as_tensor(v).to(dt).contiguous().pin_memory() for k, v in src.items()}
+    out = torch.zeros(st.field_shape("Q_REMAPPED"), dtype=dt).pin_memory()
+    st.step_host(3, host["Q"].data_ptr(), {k: h.data_ptr() for k, h in host.items()}, out.data_ptr(),
+                 precision == "mixed", 2)
+    assert np.array_equal(out.numpy().astype(np.float64), want)
+    st.close()
+    plain.close()
+
+
 @pytest.mark.parametrize("warps", [1, 3])
 def test_cube_warps_per_cta_do_not_change_results(cuda, cube_prob, warps):
     P = cube_prob
