@@ -302,8 +302,10 @@ typedef struct {
                      already agree to round-off; the option removes that round-off from the global mass. */
   int mass_fix;   /* 1: after every remap of all tiles, restore each tracer's global mass sum(q delp area) to its
                      value at the step's start (the transport conserves it; FP32 storage rounds it by ~1e-10 per
-                     step): FP64 states scale q by (1 + eps); FP32 states move a dithered few values by one unit
-                     in the last place, unbiased, leaving ~1e-13 (the stored FP32 mass is summed exactly) */
+                     step): FP64 states scale q by (1 + eps); FP32 states move a dithered few values (in a fixed
+                     1/16 of the rows) by one unit in the last place, unbiased, then a few small values to take
+                     the residual to ~1e-14 (the stored FP32 mass is summed exactly).  Switchable per step with
+                     fv3g_state_set_mass_fix. */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */
