@@ -315,6 +315,17 @@ class CubeState:
     def step(self, q_split: int, use_graph: bool = True, stream=None) -> None:
         _lib.call("fv3g_step", self._h, q_split, int(use_graph), _stream(stream))
 
+    def step_tl(self, q_split: int, dq_in: int, dq_out: int, parts: int = 3, stream=None) -> None:
+        """fv3g_state_step_tl: dq_out = J dq_in for the step about the state's inputs (FP64 six-tile state);
+        device pointers (ints) of Q-shaped FP64 arrays; parts 1 tracer_2d, 2 remap, 3 both."""
+        _lib.call("fv3g_state_step_tl", self._h, q_split, parts, C.c_void_p(dq_in), C.c_void_p(dq_out),
+                  _stream(stream))
+
+    def step_ad(self, q_split: int, q_ad_out: int, q_ad_in: int, parts: int = 3, stream=None) -> None:
+        """fv3g_state_step_ad: q_ad_in = J^T q_ad_out (hand-written reverse sweeps; kord 4)."""
+        _lib.call("fv3g_state_step_ad", self._h, q_split, parts, C.c_void_p(q_ad_out), C.c_void_p(q_ad_in),
+                  _stream(stream))
+
     def step_host(self, q_split: int, q_in: int, fields: dict, q_out: int, host_f32: bool, groups: int = 0,
                   stream=None) -> None:
         """fv3g_step_host: host pointers (ints) of Q, of fields["DELP"/"CX"/"CY"/"MFX"/"MFY"] and of the output;

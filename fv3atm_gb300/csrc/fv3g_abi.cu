@@ -17,6 +17,7 @@
 #include <new>
 #include <vector>
 
+#include "fv3g_adjoint.cuh"
 #include "fv3g_internal.cuh"
 #include "fv3g_mass.cuh"
 #include "fv3g_remap.cuh"
@@ -574,6 +575,117 @@ int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaS
   return 0;
 }
 
+// ------------------------------------------ tangent-linear and adjoint ---
+// Device allocations of one tangent-linear / adjoint call, freed at its end.
+struct CallBufs {
+  std::vector<void*> p;
+  ~CallBufs() {
+    for (void* x : p) cudaFree(x);
+  }
+  template <typename T>
+  int take(T** out, size_t count) {
+    void* v = nullptr;
+    const cudaError_t e = cudaMalloc(&v, count * sizeof(T) + 256);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(FV3G_E_NOMEM, "tangent-linear / adjoint buffers: %zu bytes: %s", count * sizeof(T),
+                       cudaGetErrorString(e));
+    }
+    p.push_back(v);
+    *out = (T*)v;
+    return 0;
+  }
+};
+
+// The trajectory of a linearised step: the forward substeps of the state's
+// inputs run with the production kernels, each substep's input (halo strips
+// filled) and layer thickness kept as a checkpoint.
+struct LinStep {
+  int nsplt = 0;
+  std::vector<double*> q;   // nsplt + 1 q-shaped checkpoints (the last: the remap's input)
+  std::vector<double*> dp;  // nsplt + 1 per-level thicknesses
+  LinArgs a{};
+  LinTraj tr{};
+  LinWork w{};
+  long long qn = 0, fn = 0;  // elements of a q-shaped / per-level array
+};
+
+int lin_check(fv3g_state* st) {
+  if (!st->fp64) return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint step needs an FP64 state");
+  if (st->nt != 6) return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint step needs the six-tile state");
+  if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  if (st->d.trdm > 1e-4 || st->d.fill || st->d.edge_sync || st->d.mass_fix)
+    return set_error(FV3G_E_UNSUPPORTED,
+                     "the tangent-linear / adjoint step covers trdm 0, fill 0, edge_sync 0 and mass_fix 0");
+  if (st->d.hord != 1 && st->d.hord != 5 && st->d.hord != 8)
+    return set_error(FV3G_E_UNSUPPORTED, "hord %d not implemented (1, 5 and 8 are)", st->d.hord);
+  return 0;
+}
+
+int lin_forward(fv3g_state* st, int q_split, cudaStream_t s, CallBufs& B, LinStep& L) {
+  CHECK(lin_check(st));
+  if (q_split < 0) {  // no substeps: the remap alone, of the home field on DELP
+    L.nsplt = 0;
+  } else {
+    CHECK(resolve_nsplt(st, q_split, s, &L.nsplt));
+    CHECK(prologue_t<double>(st, L.nsplt, s));
+  }
+  L.qn = (long long)st->nt * st->nq * st->npz * st->plane;
+  L.fn = (long long)st->nt * st->npz * st->plane;
+  L.q.assign(L.nsplt + 1, nullptr);
+  L.dp.assign(L.nsplt + 1, nullptr);
+  for (int i = 0; i <= L.nsplt; ++i) {
+    CHECK(B.take(&L.q[i], L.qn));
+    CHECK(B.take(&L.dp[i], L.fn));
+  }
+  FV3G_CUDA(cudaMemcpyAsync(L.q[0], st->q[0], sizeof(double) * L.qn, cudaMemcpyDeviceToDevice, s));
+  FV3G_CUDA(cudaMemcpyAsync(L.dp[0], st->dp[0], sizeof(double) * L.fn, cudaMemcpyDeviceToDevice, s));
+  const int warps = std::min(st->nq, st->d.warps_per_cta > 0 ? st->d.warps_per_cta : 5);
+  for (int it = 0; it < L.nsplt; ++it) {
+    CHECK(launch_cube_halo<double>(L.q[it], st->plane * st->npz * st->nq, st->plane, st->nq * st->npz, st->pg, st->n,
+                                   st->topo, s));
+    AdvArgs<double> a = adv_args<double>(st, 0, 0, 0, 0);
+    a.q_in = L.q[it];
+    a.q_out = L.q[it + 1];
+    a.dp1 = L.dp[it];
+    a.dp2 = L.dp[it + 1];
+    a.eflux = nullptr;
+    a.warps_ring = std::min(a.warps_ring, st->nq);
+    CHECK(launch_substep<double>(a, st->d.hord, false, warps, s));
+  }
+  if (L.nsplt > 0) st->last_nsplt = L.nsplt;
+  // the linearised substep's arguments and buffers
+  LinArgs& a = L.a;
+  a.pg = st->pg;
+  a.P = st->plane;
+  a.n = st->n; a.nt = st->nt; a.nq = st->nq; a.npz = st->npz;
+  a.hord = st->d.hord;
+  a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
+  a.topo = st->topo;
+  a.cx = (const double*)st->cxs; a.cy = (const double*)st->cys;
+  a.xfx = (const double*)st->xfx; a.yfx = (const double*)st->yfx;
+  a.mfx = (const double*)st->mfxs; a.mfy = (const double*)st->mfys;
+  a.area = (const double*)st->area; a.rarea = (const double*)st->rarea;
+  a.dxa = (const double*)st->dxa; a.dya = (const double*)st->dya;
+  double** tq[] = {&L.tr.qc1, &L.tr.qc2, &L.tr.qi, &L.tr.qj, &L.tr.fx2, &L.tr.fy2,
+                   &L.w.a1, &L.w.a2, &L.w.ai, &L.w.aj, &L.w.gx, &L.w.gy, &L.w.fx2, &L.w.fy2};
+  for (double** b : tq) CHECK(B.take(b, L.qn));
+  for (double** b : {&L.tr.wxi, &L.tr.wyi, &L.tr.wxo, &L.tr.wyo}) CHECK(B.take(b, 6 * L.qn));
+  return 0;
+}
+
+// Copy between a caller's q-shaped device array ((nt nq npz) planes of nd x
+// nd, i fastest) and state-layout planes.
+int lin_user_copy(fv3g_state* st, double* planes, const double* user, bool to_user, cudaStream_t s) {
+  const size_t nd = (size_t)st->nd, es = sizeof(double);
+  const size_t hplane = nd * nd * es, dplane = (size_t)st->plane * es, pitch = (size_t)st->pg.pitch * es;
+  const long long np = (long long)st->nt * st->nq * st->npz;
+  if (to_user)
+    return copy_planes(const_cast<double*>(user), nd * es, hplane, planes, pitch, dplane, nd * es, nd, np,
+                       cudaMemcpyDeviceToDevice, s);
+  return copy_planes(planes, pitch, dplane, user, nd * es, hplane, nd * es, nd, np, cudaMemcpyDeviceToDevice, s);
+}
+
 }  // namespace
 
 int fv3g::state_field_view(fv3g_state* st, int field, bool loading, StateFieldView* v) {
@@ -830,6 +942,109 @@ int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
   CHECK(resolve_nsplt(st, q_split, s, &nsplt));
   st->last_nsplt = nsplt;
   return st->fp64 ? tracer_2d_t<double>(st, nsplt, s) : tracer_2d_t<float>(st, nsplt, s);
+}
+
+int fv3g_state_step_tl(fv3g_state* st, int q_split, int parts, const double* dq_in, double* dq_out, void* stream) {
+  if (!st || !dq_in || !dq_out) return set_error(FV3G_E_ARG, "null argument");
+  if (parts < 1 || parts > 3) return set_error(FV3G_E_ARG, "parts must be 1 (tracer_2d), 2 (remap) or 3 (both)");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CallBufs B;
+  LinStep L;
+  CHECK(lin_forward(st, (parts & 1) ? q_split : -1, s, B, L));
+  if ((parts & 2) && st->d.kord != 4 && st->d.kord != 9)
+    return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented", st->d.kord);
+  double *dq0, *dq1;
+  CHECK(B.take(&dq0, L.qn));
+  CHECK(B.take(&dq1, L.qn));
+  CHECK(lin_user_copy(st, dq0, dq_in, false, s));
+  for (int it = 0; it < L.nsplt; ++it) {
+    CHECK(launch_cube_halo<double>(dq0, st->plane * st->npz * st->nq, st->plane, st->nq * st->npz, st->pg, st->n,
+                                   st->topo, s));
+    L.a.dp1 = L.dp[it];
+    L.a.dp2 = L.dp[it + 1];
+    CHECK(lin_trajectory(L.a, L.q[it], L.tr, s));
+    CHECK(lin_substep_tl(L.a, L.tr, L.w, dq0, dq1, s));
+    std::swap(dq0, dq1);
+  }
+  if (!(parts & 2)) {  // tracer_2d alone: the tangent on the Lagrangian levels
+    CHECK(lin_user_copy(st, dq0, dq_out, true, s));
+    FV3G_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  }
+  // the remap on (value, tangent) planes: the production kernel's tangent-linear instance
+  using D2 = Dual<double>;
+  D2 *qd, *qo, *dpd, *scr;
+  unsigned char* sched;
+  const long long ncol = (long long)st->nt * st->n * st->n;
+  CHECK(B.take(&qd, L.qn));
+  CHECK(B.take(&qo, L.qn));
+  CHECK(B.take(&dpd, L.fn));
+  CHECK(B.take(&scr, (size_t)6 * (KMAX + 1) * ncol));
+  CHECK(B.take(&sched, (size_t)(KMAX + 1) * ncol));
+  CHECK(lin_pack_dual(qd, L.q[L.nsplt], dq0, L.qn, s));
+  CHECK(lin_pack_dual(qo, L.q[L.nsplt], nullptr, L.qn, s));
+  CHECK(lin_pack_dual(dpd, L.dp[L.nsplt], nullptr, L.fn, s));
+  RemapArgs<D2> r{};
+  r.q_in = qd;
+  r.q_out = qo;
+  r.sQk = st->plane;
+  r.sQq = st->plane * st->npz;
+  r.sQt = r.sQq * st->nq;
+  r.sQqo = r.sQq;
+  r.nfield = st->nq;
+  r.dp = dpd;
+  r.sFk = st->plane;
+  r.sFt = st->plane * st->npz;
+  r.ak = st->ak;
+  r.bk = st->bk;
+  r.pg = st->pg;
+  r.i1 = 1; r.j1 = 1; r.ni = st->n; r.nj = st->n;
+  r.ncol = ncol;
+  r.km = st->npz; r.kn = st->npz;
+  r.iv = st->d.iv;
+  r.q_min = st->d.q_min;
+  r.scratch = scr;
+  r.sched = sched;
+  CHECK(launch_remap_tl(r, st->d.kord, s));
+  FV3G_CUDA(cudaMemsetAsync(dq1, 0, sizeof(double) * L.qn, s));
+  CHECK(lin_unpack_tangent(qo, dq1, L.qn, s));
+  CHECK(lin_user_copy(st, dq1, dq_out, true, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));  // the call's buffers are freed on return
+  return 0;
+}
+
+int fv3g_state_step_ad(fv3g_state* st, int q_split, int parts, const double* q_ad_out, double* q_ad_in,
+                       void* stream) {
+  if (!st || !q_ad_out || !q_ad_in) return set_error(FV3G_E_ARG, "null argument");
+  if (parts < 1 || parts > 3) return set_error(FV3G_E_ARG, "parts must be 1 (tracer_2d), 2 (remap) or 3 (both)");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CallBufs B;
+  LinStep L;
+  CHECK(lin_forward(st, (parts & 1) ? q_split : -1, s, B, L));
+  if ((parts & 2) && st->d.kord != 4)
+    return set_error(FV3G_E_UNSUPPORTED, "the adjoint step's remap is kord 4 (got %d)", st->d.kord);
+  double *g, *a0, *a1;
+  CHECK(B.take(&g, L.qn));
+  CHECK(B.take(&a0, L.qn));
+  CHECK(B.take(&a1, L.qn));
+  FV3G_CUDA(cudaMemsetAsync(a0, 0, sizeof(double) * L.qn, s));
+  if (parts & 2) {
+    CHECK(lin_user_copy(st, g, q_ad_out, false, s));
+    CHECK(lin_remap_ad(L.q[L.nsplt], L.dp[L.nsplt], st->ak, st->bk, g, a0, st->pg, st->plane, st->n, st->nt, st->nq,
+                       st->npz, st->npz, st->d.iv, st->d.q_min, st->d.kord, s));
+  } else {
+    CHECK(lin_user_copy(st, a0, q_ad_out, false, s));
+  }
+  for (int it = L.nsplt - 1; it >= 0; --it) {
+    L.a.dp1 = L.dp[it];
+    L.a.dp2 = L.dp[it + 1];
+    CHECK(lin_trajectory(L.a, L.q[it], L.tr, s));
+    CHECK(lin_substep_ad(L.a, L.tr, L.w, a0, a1, s));
+    std::swap(a0, a1);
+  }
+  CHECK(lin_user_copy(st, a0, q_ad_in, true, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));
+  return 0;
 }
 
 int fv3g_state_nsplt(fv3g_state* st, int* nsplt) {

@@ -345,6 +345,29 @@ int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream);
 int fv3g_state_nsplt(fv3g_state* st, int* nsplt);
 /* Remap every tracer from the Lagrangian levels of DELP_OUT to ak + bk*ps. */
 int fv3g_remap_batched(fv3g_state* st, void* stream);
+/* Tangent-linear and adjoint of one step (tracer_2d with q_split substeps,
+ * then the remap; parts = 1: tracer_2d alone (output on the Lagrangian
+ * levels), 2: the remap alone (of the home field on DELP), 3: both) of an
+ * FP64 six-tile state about its current inputs (the
+ * home tracer field Q, DELP, CX, CY, MFX, MFY and the levels), with the
+ * winds and thicknesses frozen and every limiter branch frozen at the
+ * trajectory (trdm 0, fill 0, edge_sync 0, mass_fix 0; hord 1, 5 or 8).
+ * Each call runs the forward substeps and keeps every substep's input as a
+ * checkpoint, from which the linearised substeps recompute their trajectory.
+ * Arrays are device pointers in the layout of FV3G_FIELD_Q (nt*nq*npz planes
+ * of nd x nd, i fastest); only interior cells are read, and halo cells of the
+ * outputs are zero.
+ *   fv3g_state_step_tl: dq_out = J dq_in (kord 4 or 9: the remap runs as the
+ *     remap kernel on value/tangent pairs).
+ *   fv3g_state_step_ad: q_ad_in = J^T q_ad_out (hand-written reverse sweeps:
+ *     the substeps' PPM stencils, copy_corners and the cube halo transposed,
+ *     and the kord-4 column remap; kord 9 returns FV3G_E_UNSUPPORTED).
+ * Replace: the tangent-linear / adjoint of tracer_2d (fv_tracer2d.F90) and of
+ * the tracer remap of Lagrangian_to_Eulerian (fv_mapz.F90). */
+int fv3g_state_step_tl(fv3g_state* st, int q_split, int parts, const double* dq_in, double* dq_out,
+                       void* stream);
+int fv3g_state_step_ad(fv3g_state* st, int q_split, int parts, const double* q_ad_out, double* q_ad_in,
+                       void* stream);
 /* tracer_2d + remap; with use_graph the step is captured once as a CUDA graph
  * and replayed on later calls with the same substep count (q_split 0: the
  * count is derived first, as in fv3g_tracer_2d_batched). */
