@@ -656,12 +656,8 @@ int lin_forward(fv3g_state* st, int q_split, cudaStream_t s, CallBufs& B, LinSte
   if (L.nsplt > 0) st->last_nsplt = L.nsplt;
   // the linearised substep's arguments and buffers
   LinArgs& a = L.a;
-  a.pg = st->pg;
-  a.P = st->plane;
-  a.n = st->n; a.nt = st->nt; a.nq = st->nq; a.npz = st->npz;
-  a.hord = st->d.hord;
-  a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
-  a.topo = st->topo;
+  a = lin_state_args(st->pg, st->plane, st->n, st->nt, st->nq, st->npz, st->d.hord,
+                     st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0, st->topo);
   a.cx = (const double*)st->cxs; a.cy = (const double*)st->cys;
   a.xfx = (const double*)st->xfx; a.yfx = (const double*)st->yfx;
   a.mfx = (const double*)st->mfxs; a.mfy = (const double*)st->mfys;

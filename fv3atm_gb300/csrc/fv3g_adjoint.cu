@@ -47,13 +47,34 @@ __device__ T ppm_face(int hord, double lim_fac, int f, const XF& X, const DF& DX
   T bl[2], br[2];  // deviations of cells f-1 and f
   bool smt[2] = {true, true};
   if (hord == 8) {
+    // the forms of the substep kernel, so that exact ties (flat lines) take
+    // its one-sided derivatives: its line march (clamped slopes, copysign)
+    // away from cube-face edges, the generic cell values of its edge windows
+    // (cells e-2 .. e+1 of an edge e) beside them
     auto DM = [&](int m) -> T { return vl_slope(X(m - 1), X(m), X(m + 1)); };
     auto AL = [&](int g) -> T { return T(0.5) * (X(g - 1) + X(g)) + (DM(g - 1) - DM(g)) * T(1.0 / 3.0); };
+    auto DMC = [&](int m) -> T {
+      const T xm = X(m - 1), x0 = X(m), xp = X(m + 1);
+      const T xt = T(0.25) * (xp - xm);
+      return copysign_t(tmin3(tabs(xt), tmax3(xm, x0, xp) - x0, x0 - tmin3(xm, x0, xp)), xt);
+    };
+    auto ALC = [&](int g) -> T { return T(0.5) * (X(g - 1) + X(g)) + (DMC(g - 1) - DMC(g)) * T(1.0 / 3.0); };
+    auto window = [&](int m) {
+      return (eLo != NO_EDGE && m >= eLo - 2 && m <= eLo + 1) || (eHi != NO_EDGE && m >= eHi - 2 && m <= eHi + 1);
+    };
     for (int h = 0; h < 2; ++h) {
       const int m = f - 1 + h;
-      const T xt = T(2) * DM(m);
-      bl[h] = -tsign(tmin(tabs(xt), tabs(AL(m) - X(m))), xt);
-      br[h] = tsign(tmin(tabs(xt), tabs(AL(m + 1) - X(m))), xt);
+      if (window(m)) {
+        const T xt = T(2) * DM(m);
+        bl[h] = -tsign(tmin(tabs(xt), tabs(AL(m) - X(m))), xt);
+        br[h] = tsign(tmin(tabs(xt), tabs(AL(m + 1) - X(m))), xt);
+      } else {
+        const T dmm = DMC(m);
+        const T xt = dmm + dmm;
+        const T axt = tabs(xt);
+        bl[h] = copysign_t(tmin(axt, tabs(ALC(m) - X(m))), -xt);
+        br[h] = copysign_t(tmin(axt, tabs(ALC(m + 1) - X(m))), xt);
+      }
     }
     auto setl = [&](int m, T v) { if (in(m)) bl[m - f + 1] = v; };
     auto setr = [&](int m, T v) { if (in(m)) br[m - f + 1] = v; };
@@ -126,12 +147,9 @@ __device__ T ppm_face(int hord, double lim_fac, int f, const XF& X, const DF& DX
     }
   }
   const bool high = hord == 8 || smt[0] || smt[1];
-  if (c > 0.0) {
-    const T b0 = bl[0] + br[0];
-    return high ? X(f - 1) + T(1.0 - c) * (br[0] - T(c) * b0) : X(f - 1);
-  }
-  const T b0 = bl[1] + br[1];
-  return high ? X(f) + T(1.0 + c) * (bl[1] + T(c) * b0) : X(f);
+  const double ac = fabs(c), w1 = 1.0 - ac, w2 = ac * w1;
+  if (c > 0.0) return high ? (X(f - 1) + T(w1) * br[0]) - T(w2) * (bl[0] + br[0]) : X(f - 1);
+  return high ? (X(f) + T(w1) * bl[1]) - T(w2) * (bl[1] + br[1]) : X(f);
 }
 
 // The six weights of face f's flux on cells f-3..f+2 (one forward-mode pass
@@ -165,7 +183,7 @@ __device__ __forceinline__ bool cell_of(const LinArgs& a, Cell& c) {
   c.pl = blockIdx.y;
   c.i = a.pg.isd + (int)(c.p % a.pg.pitch);
   c.j = a.pg.jsd + (int)(c.p / a.pg.pitch);
-  if (c.i > a.n + NG || c.j > a.n + NG) return false;  // plane padding: never read
+  if (c.i > a.ied || c.j > a.jed) return false;  // plane padding: never read
   const int per_tile = a.nq * a.npz;
   c.t = c.pl / per_tile;
   c.k = c.pl % a.npz;
@@ -175,11 +193,41 @@ __device__ __forceinline__ bool cell_of(const LinArgs& a, Cell& c) {
   return true;
 }
 
+__device__ __forceinline__ bool in_rng(int v, int lo, int hi) { return v >= lo && v <= hi; }
 __device__ __forceinline__ bool inside_data(const LinArgs& a, int i, int j) {
-  return i >= 1 - NG && i <= a.n + NG && j >= 1 - NG && j <= a.n + NG;
+  return in_rng(i, a.isd, a.ied) && in_rng(j, a.jsd, a.jed);
 }
-__device__ __forceinline__ bool corner_cell(int n, int i, int j) {
-  return (i < 1 || i > n) && (j < 1 || j > n);
+// a cell of a copy_corners block that the sweeps fill
+__device__ __forceinline__ bool corner_cell(const LinArgs& a, int i, int j) {
+  const bool oi = i < 1 || i > a.npx - 1, oj = j < 1 || j > a.npy - 1;
+  if (!(oi && oj)) return false;
+  const int bit = (i < 1 ? 0 : 1) + (j < 1 ? 0 : 2);
+  return (a.corners >> bit) & 1;
+}
+
+__device__ __forceinline__ double ra_y(const LinArgs& a, const Cell& c, int i, int j) {
+  const PlaneGeom& pg = a.pg;
+  if (a.ra_y) return a.ra_y[c.lev + pg.at(i, j)];
+  return a.area[c.met + pg.at(i, j)] + a.yfx[c.lev + pg.at(i, j)] - a.yfx[c.lev + pg.at(i, j + 1)];
+}
+__device__ __forceinline__ double ra_x(const LinArgs& a, const Cell& c, int i, int j) {
+  const PlaneGeom& pg = a.pg;
+  if (a.ra_x) return a.ra_x[c.lev + pg.at(i, j)];
+  return a.area[c.met + pg.at(i, j)] + a.xfx[c.lev + pg.at(i, j)] - a.xfx[c.lev + pg.at(i + 1, j)];
+}
+
+// face ranges of the four sweeps
+__device__ __forceinline__ bool yi_face(const LinArgs& a, int i, int j) {  // inner y: every column
+  return in_rng(j, a.js, a.je + 1) && in_rng(i, a.isd, a.ied);
+}
+__device__ __forceinline__ bool xi_face(const LinArgs& a, int i, int j) {  // inner x: every row
+  return in_rng(i, a.is, a.ie + 1) && in_rng(j, a.jsd, a.jed);
+}
+__device__ __forceinline__ bool xo_face(const LinArgs& a, int i, int j) {  // outer x: compute rows
+  return in_rng(i, a.is, a.ie + 1) && in_rng(j, a.js, a.je);
+}
+__device__ __forceinline__ bool yo_face(const LinArgs& a, int i, int j) {  // outer y: compute columns
+  return in_rng(j, a.js, a.je + 1) && in_rng(i, a.is, a.ie);
 }
 
 // ---------------------------------------------------------- trajectory ---
@@ -189,43 +237,41 @@ __global__ void k_lin_corners(const LinArgs a, const double* q, double* c1, doub
   Cell c;
   if (!cell_of(a, c)) return;
   const double* qp = q + c.q0;
-  if (inside_data(a, c.i, c.j) && corner_cell(a.n, c.i, c.j)) {
+  if (corner_cell(a, c.i, c.j)) {
     int i1 = c.i, j1 = c.j, i2 = c.i, j2 = c.j;
-    corner_rotate(i1, j1, a.n + 1, a.n + 1, 1);
-    corner_rotate(i2, j2, a.n + 1, a.n + 1, 2);
-    c1[c.q0 + c.p] = qp[a.pg.at(i1, j1)];
-    c2[c.q0 + c.p] = qp[a.pg.at(i2, j2)];
+    corner_rotate(i1, j1, a.npx, a.npy, 1);
+    corner_rotate(i2, j2, a.npx, a.npy, 2);
+    c1[c.q0 + c.p] = inside_data(a, i1, j1) ? qp[a.pg.at(i1, j1)] : 0.0;
+    c2[c.q0 + c.p] = inside_data(a, i2, j2) ? qp[a.pg.at(i2, j2)] : 0.0;
   } else {
     c1[c.q0 + c.p] = qp[c.p];
     c2[c.q0 + c.p] = qp[c.p];
   }
 }
 
-// Inner sweeps: y faces (i, f) for every column of the data domain on the
-// dir-2 copy, x faces (f, j) for every row on the dir-1 copy: weights and
-// flux values.
+// Inner sweeps: y faces for every column of the data domain on the dir-2
+// copy, x faces for every row on the dir-1 copy: weights and flux values.
 __global__ void k_lin_inner(const LinArgs a, const LinTraj tr) {
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n;
   const PlaneGeom& pg = a.pg;
   double fy = 0.0, fx = 0.0;
-  if (c.j >= 1 && c.j <= n + 1 && c.i >= 1 - NG && c.i <= n + NG) {
+  if (yi_face(a, c.i, c.j)) {
     const double* line = tr.qc2 + c.q0;
     const int i = c.i;
     auto xv = [&](int m) { return line[pg.at(i, m)]; };
     auto dx = [&](int m) { return a.dya[c.met + pg.at(i, m)]; };
-    fy = face_weights(a.hord, a.lim_fac, c.j, xv, dx, a.cy[c.lev + c.p], 1, n + 1, tr.wyi + c.q0 + c.p, ws);
+    fy = face_weights(a.hord, a.lim_fac, c.j, xv, dx, a.cy[c.lev + c.p], a.es, a.en, tr.wyi + c.q0 + c.p, ws);
   } else {
     for (int s = 0; s < 6; ++s) tr.wyi[s * ws + c.q0 + c.p] = 0.0;
   }
-  if (c.i >= 1 && c.i <= n + 1 && c.j >= 1 - NG && c.j <= n + NG) {
+  if (xi_face(a, c.i, c.j)) {
     const double* line = tr.qc1 + c.q0;
     const int j = c.j;
     auto xv = [&](int m) { return line[pg.at(m, j)]; };
     auto dx = [&](int m) { return a.dxa[c.met + pg.at(m, j)]; };
-    fx = face_weights(a.hord, a.lim_fac, c.i, xv, dx, a.cx[c.lev + c.p], 1, n + 1, tr.wxi + c.q0 + c.p, ws);
+    fx = face_weights(a.hord, a.lim_fac, c.i, xv, dx, a.cx[c.lev + c.p], a.ew, a.ee, tr.wxi + c.q0 + c.p, ws);
   } else {
     for (int s = 0; s < 6; ++s) tr.wxi[s * ws + c.q0 + c.p] = 0.0;
   }
@@ -233,31 +279,22 @@ __global__ void k_lin_inner(const LinArgs a, const LinTraj tr) {
   tr.fx2[c.q0 + c.p] = fx;
 }
 
-__device__ __forceinline__ double ra_y(const LinArgs& a, const Cell& c, int i, int j) {
-  const PlaneGeom& pg = a.pg;
-  return a.area[c.met + pg.at(i, j)] + a.yfx[c.lev + pg.at(i, j)] - a.yfx[c.lev + pg.at(i, j + 1)];
-}
-__device__ __forceinline__ double ra_x(const LinArgs& a, const Cell& c, int i, int j) {
-  const PlaneGeom& pg = a.pg;
-  return a.area[c.met + pg.at(i, j)] + a.xfx[c.lev + pg.at(i, j)] - a.xfx[c.lev + pg.at(i + 1, j)];
-}
-
-// Inner updates: q_i = (q area + yfx fy2 - yfx' fy2') / ra_y on rows 1..n of
-// every column, q_j likewise along x on columns 1..n of every row.  The same
-// form maps the tangents.
+// Inner updates: q_i = (q area + yfx fy2 - yfx' fy2') / ra_y on the compute
+// rows of every column, q_j likewise along x on the compute columns of every
+// row.  The same form maps the tangents.
 __global__ void k_lin_mid(const LinArgs a, const double* c1, const double* c2, const double* fx2, const double* fy2,
                           double* qi, double* qj) {
   Cell c;
   if (!cell_of(a, c)) return;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
   double vi = 0.0, vj = 0.0;
-  if (j >= 1 && j <= n && i >= 1 - NG && i <= n + NG) {
+  if (in_rng(j, a.js, a.je)) {
     const double y0 = a.yfx[c.lev + pg.at(i, j)], y1 = a.yfx[c.lev + pg.at(i, j + 1)];
     vi = (c2[c.q0 + c.p] * a.area[c.met + c.p] + y0 * fy2[c.q0 + pg.at(i, j)] - y1 * fy2[c.q0 + pg.at(i, j + 1)]) /
          ra_y(a, c, i, j);
   }
-  if (i >= 1 && i <= n && j >= 1 - NG && j <= n + NG) {
+  if (in_rng(i, a.is, a.ie)) {
     const double x0 = a.xfx[c.lev + pg.at(i, j)], x1 = a.xfx[c.lev + pg.at(i + 1, j)];
     vj = (c1[c.q0 + c.p] * a.area[c.met + c.p] + x0 * fx2[c.q0 + pg.at(i, j)] - x1 * fx2[c.q0 + pg.at(i + 1, j)]) /
          ra_x(a, c, i, j);
@@ -266,29 +303,28 @@ __global__ void k_lin_mid(const LinArgs a, const double* c1, const double* c2, c
   qj[c.q0 + c.p] = vj;
 }
 
-// Outer sweeps: x faces (f, j), rows 1..n, on q_i; y faces (i, f), columns
-// 1..n, on q_j: weights.
+// Outer sweeps: x faces of the compute rows on q_i, y faces of the compute
+// columns on q_j: weights.
 __global__ void k_lin_outer(const LinArgs a, const LinTraj tr) {
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n;
   const PlaneGeom& pg = a.pg;
-  if (c.i >= 1 && c.i <= n + 1 && c.j >= 1 && c.j <= n) {
+  if (xo_face(a, c.i, c.j)) {
     const double* line = tr.qi + c.q0;
     const int j = c.j;
     auto xv = [&](int m) { return line[pg.at(m, j)]; };
     auto dx = [&](int m) { return a.dxa[c.met + pg.at(m, j)]; };
-    face_weights(a.hord, a.lim_fac, c.i, xv, dx, a.cx[c.lev + c.p], 1, n + 1, tr.wxo + c.q0 + c.p, ws);
+    face_weights(a.hord, a.lim_fac, c.i, xv, dx, a.cx[c.lev + c.p], a.ew, a.ee, tr.wxo + c.q0 + c.p, ws);
   } else {
     for (int s = 0; s < 6; ++s) tr.wxo[s * ws + c.q0 + c.p] = 0.0;
   }
-  if (c.j >= 1 && c.j <= n + 1 && c.i >= 1 && c.i <= n) {
+  if (yo_face(a, c.i, c.j)) {
     const double* line = tr.qj + c.q0;
     const int i = c.i;
     auto xv = [&](int m) { return line[pg.at(i, m)]; };
     auto dx = [&](int m) { return a.dya[c.met + pg.at(i, m)]; };
-    face_weights(a.hord, a.lim_fac, c.j, xv, dx, a.cy[c.lev + c.p], 1, n + 1, tr.wyo + c.q0 + c.p, ws);
+    face_weights(a.hord, a.lim_fac, c.j, xv, dx, a.cy[c.lev + c.p], a.es, a.en, tr.wyo + c.q0 + c.p, ws);
   } else {
     for (int s = 0; s < 6; ++s) tr.wyo[s * ws + c.q0 + c.p] = 0.0;
   }
@@ -301,27 +337,26 @@ __global__ void k_tl_inner(const LinArgs a, const LinTraj tr, const double* t1, 
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n;
   const PlaneGeom& pg = a.pg;
   double fy = 0.0, fx = 0.0;
-  if (c.j >= 1 && c.j <= n + 1 && c.i >= 1 - NG && c.i <= n + NG)
+  if (yi_face(a, c.i, c.j))
     for (int s = 0; s < 6; ++s) fy += tr.wyi[s * ws + c.q0 + c.p] * t2[c.q0 + pg.at(c.i, c.j - 3 + s)];
-  if (c.i >= 1 && c.i <= n + 1 && c.j >= 1 - NG && c.j <= n + NG)
+  if (xi_face(a, c.i, c.j))
     for (int s = 0; s < 6; ++s) fx += tr.wxi[s * ws + c.q0 + c.p] * t1[c.q0 + pg.at(c.i - 3 + s, c.j)];
   fy2[c.q0 + c.p] = fy;
   fx2[c.q0 + c.p] = fx;
 }
 
-// The substep's update of an interior cell from the outer-sweep flux
-// tangents (computed here for the cell's four faces) and the inner ones.
+// The substep's update of a compute cell from the outer-sweep flux tangents
+// (computed here for the cell's four faces) and the inner ones.
 __global__ void k_tl_update(const LinArgs a, const LinTraj tr, const double* dq, const double* ti, const double* tj,
                             const double* fx2, const double* fy2, double* out) {
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
-  if (i < 1 || i > n || j < 1 || j > n) {
+  if (!in_rng(i, a.is, a.ie) || !in_rng(j, a.js, a.je)) {
     out[c.q0 + c.p] = 0.0;
     return;
   }
@@ -342,43 +377,52 @@ __global__ void k_tl_update(const LinArgs a, const LinTraj tr, const double* dq,
 }
 
 // ------------------------------------------------------------- adjoint ---
-// Outer-sweep flux adjoints: with t = q_ad rarea / dp2 on interior cells,
-// FX_ad(f) = t(f) - t(f-1), and both x sweeps' fluxes enter FX with 0.5 mfx.
+// Outer-sweep flux adjoints of the substep: with t = q_ad rarea / dp2 on the
+// compute cells, FX_ad(f) = t(f) - t(f-1), and both x sweeps' fluxes enter
+// FX with 0.5 mfx.
 __global__ void k_ad_faces(const LinArgs a, const double* qa, double* gx, double* gy) {
   Cell c;
   if (!cell_of(a, c)) return;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
   auto tt = [&](int ii, int jj) -> double {
-    if (ii < 1 || ii > n || jj < 1 || jj > n) return 0.0;
+    if (!in_rng(ii, a.is, a.ie) || !in_rng(jj, a.js, a.je)) return 0.0;
     const long long p = pg.at(ii, jj);
     return qa[c.q0 + p] * a.rarea[c.met + p] / a.dp2[c.lev + p];
   };
   double vx = 0.0, vy = 0.0;
-  if (i >= 1 && i <= n + 1 && j >= 1 && j <= n) vx = 0.5 * a.mfx[c.lev + c.p] * (tt(i, j) - tt(i - 1, j));
-  if (j >= 1 && j <= n + 1 && i >= 1 && i <= n) vy = 0.5 * a.mfy[c.lev + c.p] * (tt(i, j) - tt(i, j - 1));
+  if (xo_face(a, i, j)) vx = 0.5 * a.mfx[c.lev + c.p] * (tt(i, j) - tt(i - 1, j));
+  if (yo_face(a, i, j)) vy = 0.5 * a.mfy[c.lev + c.p] * (tt(i, j) - tt(i, j - 1));
   gx[c.q0 + c.p] = vx;
   gy[c.q0 + c.p] = vy;
 }
 
-// Outer sweeps transposed: the adjoints of q_i (rows 1..n, every column) and
-// of q_j (columns 1..n, every row), each cell summing the faces whose
+// The same from fv_tp_2d's flux adjoints: g = 0.5 w flux_ad.
+__global__ void k_ad_flux_in(const LinArgs a, const double* fxa, const double* fya, double* gx, double* gy) {
+  Cell c;
+  if (!cell_of(a, c)) return;
+  gx[c.q0 + c.p] = xo_face(a, c.i, c.j) ? 0.5 * a.mfx[c.lev + c.p] * fxa[c.q0 + c.p] : 0.0;
+  gy[c.q0 + c.p] = yo_face(a, c.i, c.j) ? 0.5 * a.mfy[c.lev + c.p] * fya[c.q0 + c.p] : 0.0;
+}
+
+// Outer sweeps transposed: the adjoints of q_i (compute rows, every column)
+// and of q_j (compute columns, every row), each cell summing the faces whose
 // stencils hold it.
 __global__ void k_ad_outer(const LinArgs a, const LinTraj tr, const double* gx, const double* gy, double* ai,
                            double* aj) {
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
   double vi = 0.0, vj = 0.0;
-  if (j >= 1 && j <= n && i >= 1 - NG && i <= n + NG)
-    for (int f = max(1, i - 2); f <= min(n + 1, i + 3); ++f) {
+  if (in_rng(j, a.js, a.je))
+    for (int f = max(a.is, i - 2); f <= min(a.ie + 1, i + 3); ++f) {
       const long long pf = pg.at(f, j);
       vi += tr.wxo[(i - f + 3) * ws + c.q0 + pf] * gx[c.q0 + pf];
     }
-  if (i >= 1 && i <= n && j >= 1 - NG && j <= n + NG)
-    for (int f = max(1, j - 2); f <= min(n + 1, j + 3); ++f) {
+  if (in_rng(i, a.is, a.ie))
+    for (int f = max(a.js, j - 2); f <= min(a.je + 1, j + 3); ++f) {
       const long long pf = pg.at(i, f);
       vj += tr.wyo[(j - f + 3) * ws + c.q0 + pf] * gy[c.q0 + pf];
     }
@@ -392,20 +436,20 @@ __global__ void k_ad_mid(const LinArgs a, const double* ai, const double* aj, co
                          double* fx2, double* fy2) {
   Cell c;
   if (!cell_of(a, c)) return;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
   double vy = 0.0, vx = 0.0;
-  if (j >= 1 && j <= n + 1 && i >= 1 - NG && i <= n + NG) {
+  if (yi_face(a, i, j)) {
     double s = 0.0;
-    if (j <= n) s += ai[c.q0 + pg.at(i, j)] / ra_y(a, c, i, j);
-    if (j >= 2) s -= ai[c.q0 + pg.at(i, j - 1)] / ra_y(a, c, i, j - 1);
-    vy = a.yfx[c.lev + c.p] * s + ((i >= 1 && i <= n) ? gy[c.q0 + c.p] : 0.0);
+    if (j <= a.je) s += ai[c.q0 + pg.at(i, j)] / ra_y(a, c, i, j);
+    if (j - 1 >= a.js) s -= ai[c.q0 + pg.at(i, j - 1)] / ra_y(a, c, i, j - 1);
+    vy = a.yfx[c.lev + c.p] * s + (in_rng(i, a.is, a.ie) ? gy[c.q0 + c.p] : 0.0);
   }
-  if (i >= 1 && i <= n + 1 && j >= 1 - NG && j <= n + NG) {
+  if (xi_face(a, i, j)) {
     double s = 0.0;
-    if (i <= n) s += aj[c.q0 + pg.at(i, j)] / ra_x(a, c, i, j);
-    if (i >= 2) s -= aj[c.q0 + pg.at(i - 1, j)] / ra_x(a, c, i - 1, j);
-    vx = a.xfx[c.lev + c.p] * s + ((j >= 1 && j <= n) ? gx[c.q0 + c.p] : 0.0);
+    if (i <= a.ie) s += aj[c.q0 + pg.at(i, j)] / ra_x(a, c, i, j);
+    if (i - 1 >= a.is) s -= aj[c.q0 + pg.at(i - 1, j)] / ra_x(a, c, i - 1, j);
+    vx = a.xfx[c.lev + c.p] * s + (in_rng(j, a.js, a.je) ? gx[c.q0 + c.p] : 0.0);
   }
   fy2[c.q0 + c.p] = vy;
   fx2[c.q0 + c.p] = vx;
@@ -418,58 +462,58 @@ __global__ void k_ad_inner(const LinArgs a, const LinTraj tr, const double* ai, 
   Cell c;
   if (!cell_of(a, c)) return;
   const long long ws = (long long)a.nt * a.nq * a.npz * a.P;
-  const int n = a.n, i = c.i, j = c.j;
+  const int i = c.i, j = c.j;
   const PlaneGeom& pg = a.pg;
   double v1 = 0.0, v2 = 0.0;
-  if (inside_data(a, i, j)) {
-    if (j >= 1 && j <= n) v2 = ai[c.q0 + c.p] * a.area[c.met + c.p] / ra_y(a, c, i, j);
-    for (int f = max(1, j - 2); f <= min(n + 1, j + 3); ++f) {
-      const long long pf = pg.at(i, f);
-      v2 += tr.wyi[(j - f + 3) * ws + c.q0 + pf] * fy2[c.q0 + pf];
-    }
-    if (i >= 1 && i <= n) v1 = aj[c.q0 + c.p] * a.area[c.met + c.p] / ra_x(a, c, i, j);
-    for (int f = max(1, i - 2); f <= min(n + 1, i + 3); ++f) {
-      const long long pf = pg.at(f, j);
-      v1 += tr.wxi[(i - f + 3) * ws + c.q0 + pf] * fx2[c.q0 + pf];
-    }
+  if (in_rng(j, a.js, a.je)) v2 = ai[c.q0 + c.p] * a.area[c.met + c.p] / ra_y(a, c, i, j);
+  for (int f = max(a.js, j - 2); f <= min(a.je + 1, j + 3); ++f) {
+    const long long pf = pg.at(i, f);
+    v2 += tr.wyi[(j - f + 3) * ws + c.q0 + pf] * fy2[c.q0 + pf];
+  }
+  if (in_rng(i, a.is, a.ie)) v1 = aj[c.q0 + c.p] * a.area[c.met + c.p] / ra_x(a, c, i, j);
+  for (int f = max(a.is, i - 2); f <= min(a.ie + 1, i + 3); ++f) {
+    const long long pf = pg.at(f, j);
+    v1 += tr.wxi[(i - f + 3) * ws + c.q0 + pf] * fx2[c.q0 + pf];
   }
   a1[c.q0 + c.p] = v1;
   a2[c.q0 + c.p] = v2;
 }
 
-// The input's adjoint before the corner and halo transposes: the direct
-// term dp1/dp2 on interior cells plus both copies' adjoints off the corner
-// blocks.
-__global__ void k_ad_collect(const LinArgs a, const double* qa, const double* a1, const double* a2, double* out) {
+// The input's adjoint before the corner (and halo) transposes: the substep's
+// direct term dp1/dp2 on the compute cells (qa, when given) plus both
+// copies' adjoints off the filled corner blocks; added to out when acc.
+__global__ void k_ad_collect(const LinArgs a, const double* qa, const double* a1, const double* a2, double* out,
+                             int acc) {
   Cell c;
   if (!cell_of(a, c)) return;
-  const int n = a.n, i = c.i, j = c.j;
   double v = 0.0;
-  if (i >= 1 && i <= n && j >= 1 && j <= n) v = qa[c.q0 + c.p] * a.dp1[c.lev + c.p] / a.dp2[c.lev + c.p];
-  if (inside_data(a, i, j) && !corner_cell(n, i, j)) v += a1[c.q0 + c.p] + a2[c.q0 + c.p];
-  out[c.q0 + c.p] = v;
+  if (qa && in_rng(c.i, a.is, a.ie) && in_rng(c.j, a.js, a.je))
+    v = qa[c.q0 + c.p] * a.dp1[c.lev + c.p] / a.dp2[c.lev + c.p];
+  if (!corner_cell(a, c.i, c.j)) v += a1[c.q0 + c.p] + a2[c.q0 + c.p];
+  out[c.q0 + c.p] = acc ? out[c.q0 + c.p] + v : v;
 }
 
-// copy_corners transposed: each corner-block cell's adjoint moves to the
-// halo-strip cell it was rotated from (one thread per plane and corner; the
-// strips a corner reads are its own, so no two threads meet).
+// copy_corners transposed: each filled corner-block cell's adjoint moves to
+// the halo-strip cell it was rotated from (one thread per plane and corner;
+// the 72 rotation targets of a plane are distinct, so no two threads meet).
 __global__ void k_ad_corners(const LinArgs a, const double* a1, const double* a2, double* out) {
   const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nplanes = (long long)a.nt * a.nq * a.npz;
   if (id >= nplanes * 4) return;
   const long long q0 = (id / 4) * a.P;
   const int corner = (int)(id % 4);
-  const int n = a.n;
-  const int ib = (corner & 1) ? n + 1 : 1 - NG, jb = (corner & 2) ? n + 1 : 1 - NG;
+  if (!((a.corners >> corner) & 1)) return;
+  const int ib = (corner & 1) ? a.npx : 1 - NG, jb = (corner & 2) ? a.npy : 1 - NG;
   for (int dj = 0; dj < NG; ++dj)
     for (int di = 0; di < NG; ++di) {
       const int i = ib + di, j = jb + dj;
+      if (!inside_data(a, i, j)) continue;
       const long long p = a.pg.at(i, j);
       int i1 = i, j1 = j, i2 = i, j2 = j;
-      corner_rotate(i1, j1, n + 1, n + 1, 1);
-      corner_rotate(i2, j2, n + 1, n + 1, 2);
-      out[q0 + a.pg.at(i1, j1)] += a1[q0 + p];
-      out[q0 + a.pg.at(i2, j2)] += a2[q0 + p];
+      corner_rotate(i1, j1, a.npx, a.npy, 1);
+      corner_rotate(i2, j2, a.npx, a.npy, 2);
+      if (inside_data(a, i1, j1)) out[q0 + a.pg.at(i1, j1)] += a1[q0 + p];
+      if (inside_data(a, i2, j2)) out[q0 + a.pg.at(i2, j2)] += a2[q0 + p];
     }
 }
 
@@ -508,6 +552,26 @@ __global__ void k_ad_halo(const LinArgs a, const double* in, double* out) {
     v += in[((long long)u * per_tile + within) * a.P + a.pg.at(hi, hj)];
   }
   out[c.q0 + c.p] = v;
+}
+
+// del-2 damping fluxes transposed (fluxes d6 (q(m-1) - q(m)) through the
+// compute faces): q_ad(m) += d6(m+1) F_ad(m+1) - d6(m) F_ad(m) along x and y.
+__global__ void k_ad_damp(const LinArgs a, const double* fxa, const double* fya, const double* d6x,
+                          const double* d6y, double* out) {
+  Cell c;
+  if (!cell_of(a, c)) return;
+  const int i = c.i, j = c.j;
+  const PlaneGeom& pg = a.pg;
+  double v = 0.0;
+  if (d6x && in_rng(j, a.js, a.je)) {
+    if (xo_face(a, i + 1, j)) v += d6x[pg.at(i + 1, j)] * fxa[c.q0 + pg.at(i + 1, j)];
+    if (xo_face(a, i, j)) v -= d6x[pg.at(i, j)] * fxa[c.q0 + pg.at(i, j)];
+  }
+  if (d6y && in_rng(i, a.is, a.ie)) {
+    if (yo_face(a, i, j + 1)) v += d6y[pg.at(i, j + 1)] * fya[c.q0 + pg.at(i, j + 1)];
+    if (yo_face(a, i, j)) v -= d6y[pg.at(i, j)] * fya[c.q0 + pg.at(i, j)];
+  }
+  out[c.q0 + c.p] += v;
 }
 
 dim3 plane_grid(const LinArgs& a) {
@@ -757,12 +821,44 @@ int lin_substep_ad(const LinArgs& a, const LinTraj& tr, const LinWork& w, const 
   k_ad_mid<<<g, 128, 0, s>>>(a, w.ai, w.aj, w.gx, w.gy, w.fx2, w.fy2);
   k_ad_inner<<<g, 128, 0, s>>>(a, tr, w.ai, w.aj, w.fx2, w.fy2, w.a1, w.a2);
   // the collected adjoint goes through gx (free after k_ad_mid) before the halo transpose
-  k_ad_collect<<<g, 128, 0, s>>>(a, q_ad_out, w.a1, w.a2, w.gx);
+  k_ad_collect<<<g, 128, 0, s>>>(a, q_ad_out, w.a1, w.a2, w.gx, 0);
   const long long nc = (long long)a.nt * a.nq * a.npz * 4;
   k_ad_corners<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(a, w.a1, w.a2, w.gx);
   k_ad_halo<<<g, 128, 0, s>>>(a, w.gx, q_ad_in);
   FV3G_CUDA(cudaGetLastError());
   return 0;
+}
+
+int lin_fluxes_ad(const LinArgs& a, const LinTraj& tr, const LinWork& w, const double* fx_ad, const double* fy_ad,
+                  const double* d6x, const double* d6y, double* q_ad, cudaStream_t s) {
+  const dim3 g = plane_grid(a);
+  k_ad_flux_in<<<g, 128, 0, s>>>(a, fx_ad, fy_ad, w.gx, w.gy);
+  k_ad_outer<<<g, 128, 0, s>>>(a, tr, w.gx, w.gy, w.ai, w.aj);
+  k_ad_mid<<<g, 128, 0, s>>>(a, w.ai, w.aj, w.gx, w.gy, w.fx2, w.fy2);
+  k_ad_inner<<<g, 128, 0, s>>>(a, tr, w.ai, w.aj, w.fx2, w.fy2, w.a1, w.a2);
+  k_ad_collect<<<g, 128, 0, s>>>(a, nullptr, w.a1, w.a2, q_ad, 1);
+  const long long nc = (long long)a.nt * a.nq * a.npz * 4;
+  k_ad_corners<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(a, w.a1, w.a2, q_ad);
+  if (d6x || d6y) k_ad_damp<<<g, 128, 0, s>>>(a, fx_ad, fy_ad, d6x, d6y, q_ad);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+
+LinArgs lin_state_args(const PlaneGeom& pg, long long P, int n, int nt, int nq, int npz, int hord, double lim_fac,
+                       const Topo& topo) {
+  LinArgs a{};
+  a.pg = pg;
+  a.P = P;
+  a.is = 1; a.ie = n; a.js = 1; a.je = n;
+  a.isd = 1 - NG; a.ied = n + NG; a.jsd = 1 - NG; a.jed = n + NG;
+  a.npx = n + 1; a.npy = n + 1;
+  a.ew = 1; a.ee = n + 1; a.es = 1; a.en = n + 1;
+  a.corners = 15;
+  a.n = n; a.nt = nt; a.nq = nq; a.npz = npz;
+  a.hord = hord;
+  a.lim_fac = lim_fac;
+  a.topo = topo;
+  return a;
 }
 
 int lin_remap_ad(const double* q, const double* dp, const double* ak, const double* bk, const double* q2_ad,

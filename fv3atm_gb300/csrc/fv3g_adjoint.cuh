@@ -27,12 +27,18 @@ namespace fv3g {
 struct LinArgs {
   PlaneGeom pg;
   long long P;  // elements per plane
-  int n, nt, nq, npz;
+  int is, ie, js, je;      // compute domain (tile indices)
+  int isd, ied, jsd, jed;  // data domain
+  int npx, npy;            // tile cells + 1 per direction
+  int ew, ee, es, en;      // cube-face edge faces of the x lines (ew, ee) and y lines (es, en), or NO_EDGE
+  int corners;             // copy_corners blocks filled: bit 0 sw, 1 se, 2 nw, 3 ne (0 on nested tiles)
+  int n, nt, nq, npz;      // six-tile state: tile size (halo transpose), tiles, tracers, levels
   int hord;
   double lim_fac;
   Topo topo;
   // frozen inputs of the substep (per-level planes, scaled by 1/nsplt)
-  const double *cx, *cy, *xfx, *yfx, *mfx, *mfy;
+  const double *cx, *cy, *xfx, *yfx, *mfx, *mfy;  // mfx / mfy: the weights of the face fluxes (times 0.5)
+  const double *ra_x, *ra_y;  // optional; else area + xfx(i) - xfx(i+1), area + yfx(j) - yfx(j+1)
   const double *dp1, *dp2;  // layer thickness at the substep's start and end
   const double *area, *rarea, *dxa, *dya;
 };
@@ -53,6 +59,10 @@ struct LinWork {
   double *fx2, *fy2;  // tangents / adjoints of the inner-sweep fluxes
 };
 
+// the arguments of the six-tile state's substeps (n cells per tile edge)
+LinArgs lin_state_args(const PlaneGeom& pg, long long P, int n, int nt, int nq, int npz, int hord, double lim_fac,
+                       const Topo& topo);
+
 // trajectory of the substep whose halo-filled input is q
 int lin_trajectory(const LinArgs& a, const double* q, const LinTraj& tr, cudaStream_t s);
 // tangent-linear substep: dq (halo strips filled) -> dq_out (interior cells)
@@ -62,6 +72,14 @@ int lin_substep_tl(const LinArgs& a, const LinTraj& tr, const LinWork& w, const 
 // q_ad_in (interior cells of its input; halo cells zero)
 int lin_substep_ad(const LinArgs& a, const LinTraj& tr, const LinWork& w, const double* q_ad_out, double* q_ad_in,
                    cudaStream_t s);
+
+// fv_tp_2d's adjoint from its flux adjoints (one plane; fluxes 0.5 (outer +
+// inner) times a.mfx / a.mfy): q_ad (data domain) += J^T (fx_ad, fy_ad).
+// d6x / d6y (may be null): del-2 damping flux weights, the damping flux
+// through a face being d6 times the difference of the two cells beside it
+// (x: q(i-1) - q(i); y: q(j-1) - q(j)).
+int lin_fluxes_ad(const LinArgs& a, const LinTraj& tr, const LinWork& w, const double* fx_ad, const double* fy_ad,
+                  const double* d6x, const double* d6y, double* q_ad, cudaStream_t s);
 
 // Adjoint of the kord-4 remap of every interior column of the state: q_ad
 // (the source field's adjoint, q-shaped) = J^T q2_ad at the trajectory q

@@ -2,22 +2,19 @@
 // fv3g_fv_tp_2d_tl / fv3g_fv_tp_2d_ad (fv_tp_2d of tp_core.F90) and
 // fv3g_map1_ppm_tl / fv3g_map1_ppm_ad (map1_ppm of fv_mapz.F90), with the
 // Courant numbers, mass fluxes and pressures frozen and every limiter branch
-// frozen at the trajectory (hord 5 and the unlimited parts have none).
+// frozen at the trajectory.
 //
-// The tangent-linear model is the forward kernel instantiated on Dual<double>
-// (value, tangent) planes.  The adjoint is assembled from tangent-linear runs
-// in which the inputs are coloured so that every Jacobian entry is recovered
-// exactly, then contracted with the output adjoints:
-//   * fv_tp_2d: the fluxes depend on the x-sweep input (q with the dir-1
-//     corner fill) through boxes of 6x1 (fx) and 7x6 (fy) cells, and on the
-//     y-sweep input (dir-2 fill) through 6x7 (fx) and 1x6 (fy) boxes.  With
-//     the corner fills taken out of the kernel (they are applied to the
-//     trajectory and transposed afterwards), colouring the x input with
-//     periods (7, 6) and the y input with (6, 7) gives each cell of a box its
-//     own colour: 42 colours per input, run as 42 tracer planes of one launch.
-//   * map1_ppm: a column's output depends on every source layer (the
-//     interface values solve a tridiagonal system), so the km unit directions
-//     run as km fields of one launch.
+// The tangent-linear models are the forward kernels instantiated on
+// Dual<double> (value, tangent) planes.  The adjoints are hand-written
+// reverse sweeps (fv3g_adjoint.cu):
+//   * fv_tp_2d: the face weights of the four PPM sweeps on the trajectory,
+//     then the transposed stencils gathered cell by cell, the inner updates
+//     transposed, and the copy_corners fills transposed (del-2 damping, nord
+//     0, transposed as its two-cell face differences);
+//   * map1_ppm, kord 4: the column reversed (integration over the overlaps,
+//     the layer parabolas, the PPM interfaces and slopes).  kord 9, whose
+//     interfaces solve a tridiagonal system per column, runs the km unit
+//     directions as km fields of one tangent-linear launch.
 // Adjoint convention (as generated adjoint code): input adjoints are
 // incremented, output adjoints are consumed and set to zero.
 #include <cuda_runtime.h>
@@ -25,6 +22,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "fv3g_adjoint.cuh"
 #include "fv3g_hostio.cuh"
 #include "fv3g_remap.cuh"
 
@@ -42,76 +40,6 @@ __global__ void k_unpack_dual(const D2* in, double* v, double* d, long long n) {
     if (v) v[i] = in[i].v;
     if (d) d[i] = in[i].d;
   }
-}
-
-// ncolor planes of the trajectory; with tangent_on, tangent 1 on the cells of
-// the plane's colour ((i - ilo) mod px) + px ((j - jlo) mod py), else 0.
-__global__ void k_color_planes(D2* out, const double* traj, PlaneGeom pg, int ilo, int ihi, int jlo, int jhi, int px,
-                               int py, int ncolor, int tangent_on) {
-  const long long P = pg.plane();
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < P * ncolor;
-       id += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(id / P);
-    const long long p = id - (long long)c * P;
-    const int i = pg.isd + (int)(p % pg.pitch), j = pg.jsd + (int)(p / pg.pitch);
-    double d = 0.0;
-    if (tangent_on && i >= ilo && i <= ihi && j >= jlo && j <= jhi)
-      d = ((i - ilo) % px) + px * ((j - jlo) % py) == c ? 1.0 : 0.0;
-    out[id] = D2(traj[p], d);
-  }
-}
-
-struct FaceBox {  // faces (fi, fj) in [i+a0, i+a1] x [j+b0, j+b1] hold cell (i, j) in their stencil box
-  int a0, a1, b0, b1;
-};
-
-// g(i, j) = sum over the faces whose box holds (i, j) of d flux / d q(i, j)
-// (the tangent of the cell's colour plane) times the flux adjoint.
-__global__ void k_gather_adjoint(double* g, const D2* fx, const D2* fy, const double* fxa, const double* fya,
-                                 PlaneGeom pg, int ilo, int ihi, int jlo, int jhi, int px, int py, FaceBox bx,
-                                 FaceBox by, int is, int ie, int js, int je) {
-  const long long P = pg.plane();
-  const int ni = ihi - ilo + 1, nj = jhi - jlo + 1;
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < (long long)ni * nj;
-       id += (long long)gridDim.x * blockDim.x) {
-    const int i = ilo + (int)(id % ni), j = jlo + (int)(id / ni);
-    const int c = ((i - ilo) % px) + px * ((j - jlo) % py);
-    const D2* fxc = fx + (long long)c * P;
-    const D2* fyc = fy + (long long)c * P;
-    double s = 0.0;
-    for (int fj = max(j + bx.b0, js); fj <= min(j + bx.b1, je); ++fj)
-      for (int fi = max(i + bx.a0, is); fi <= min(i + bx.a1, ie + 1); ++fi) {
-        const long long p = pg.at(fi, fj);
-        s += fxc[p].d * fxa[p];
-      }
-    for (int fj = max(j + by.b0, js); fj <= min(j + by.b1, je + 1); ++fj)
-      for (int fi = max(i + by.a0, is); fi <= min(i + by.a1, ie); ++fi) {
-        const long long p = pg.at(fi, fj);
-        s += fyc[p].d * fya[p];
-      }
-    g[pg.at(i, j)] += s;
-  }
-}
-
-// Transpose of the copy_corners fill of direction dir: the adjoint of every
-// cube-corner halo cell moves to the strip cell it was copied from.
-__global__ void k_corners_adjoint(double* g, PlaneGeom pg, int npx, int npy, int corners, int dir) {
-  const int id = threadIdx.x;
-  if (id >= 36) return;
-  const int c = id / 9, a = (id % 9) / 3 + 1, b = id % 3 + 1;
-  if (!(corners & (1 << c))) return;
-  const int su = (c & 1) ? 1 : -1, sv = (c & 2) ? 1 : -1;
-  const int cx2 = su < 0 ? 1 : 2 * npx - 1, cy2 = sv < 0 ? 1 : 2 * npy - 1;
-  const int U = su * (2 * a - 1), V = sv * (2 * b - 1);
-  const bool plus = (dir == 1) ? (su == -sv) : (su == sv);
-  const int U2 = plus ? -V : V, V2 = plus ? U : -U;
-  const int i = (U + cx2) / 2, j = (V + cy2) / 2, is = (U2 + cx2) / 2, js = (V2 + cy2) / 2;
-  if (i < pg.isd || j < pg.jsd || is < pg.isd || js < pg.jsd || i >= pg.isd + pg.pitch || is >= pg.isd + pg.pitch ||
-      j >= pg.jsd + pg.rows || js >= pg.jsd + pg.rows)
-    return;
-  // corner cells and their sources are disjoint, and each source has one corner cell
-  g[pg.at(is, js)] += g[pg.at(i, j)];
-  g[pg.at(i, j)] = 0.0;
 }
 
 unsigned grid_1d(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 4096); }
@@ -319,7 +247,36 @@ int fv3g_map1_ppm_ad(int km, const double* pe1, const double* q1, double* q1_ad,
   const int ncol = i2 - i1 + 1;
   const size_t nib = (size_t)(iend - ibeg + 1), plane = nib * (size_t)(jend - jbeg + 1);
   const size_t row = (size_t)(j - jbeg) * nib;
-  // field f: the trajectory with the unit tangent of source layer f
+  if (kord == 4 && km >= 3) {  // the hand-written reverse of the column remap
+    std::vector<double> h1((size_t)km * ncol), h2((size_t)kn * ncol), ha((size_t)km * ncol, 0.0);
+    std::vector<double> hq(qs ? (size_t)ncol : 0);
+    for (int k = 0; k < km; ++k)
+      for (int c = 0; c < ncol; ++c) h1[(size_t)k * ncol + c] = q1[(size_t)(i1 + c - ibeg) + row + k * plane];
+    for (int k = 0; k < kn; ++k)
+      for (int c = 0; c < ncol; ++c) h2[(size_t)k * ncol + c] = q2_ad[(size_t)(i1 + c - ibeg) + row + k * plane];
+    CHECK(g_ctx.begin(padded((size_t)km * ncol, 8) * 2 + padded((size_t)kn * ncol, 8) +
+                      padded((size_t)(km + 1) * ncol, 8) + padded((size_t)(kn + 1) * ncol, 8) + padded(ncol, 8)));
+    cudaStream_t s = g_ctx.stream;
+    double *d1 = g_ctx.take<double>((size_t)km * ncol), *da = g_ctx.take<double>((size_t)km * ncol);
+    double *d2 = g_ctx.take<double>((size_t)kn * ncol), *p1 = g_ctx.take<double>((size_t)(km + 1) * ncol);
+    double *p2 = g_ctx.take<double>((size_t)(kn + 1) * ncol), *dq = g_ctx.take<double>(ncol);
+    FV3G_CUDA(cudaMemcpyAsync(d1, h1.data(), sizeof(double) * h1.size(), cudaMemcpyHostToDevice, s));
+    FV3G_CUDA(cudaMemcpyAsync(d2, h2.data(), sizeof(double) * h2.size(), cudaMemcpyHostToDevice, s));
+    FV3G_CUDA(cudaMemcpyAsync(p1, pe1, sizeof(double) * (km + 1) * ncol, cudaMemcpyHostToDevice, s));
+    FV3G_CUDA(cudaMemcpyAsync(p2, pe2, sizeof(double) * (kn + 1) * ncol, cudaMemcpyHostToDevice, s));
+    if (qs) FV3G_CUDA(cudaMemcpyAsync(dq, qs, sizeof(double) * ncol, cudaMemcpyHostToDevice, s));
+    FV3G_CUDA(cudaMemsetAsync(da, 0, sizeof(double) * km * ncol, s));
+    CHECK(lin_remap_ad_rows(d1, p1, p2, qs ? dq : nullptr, d2, da, ncol, km, kn, iv, kord, s));
+    FV3G_CUDA(cudaMemcpyAsync(ha.data(), da, sizeof(double) * ha.size(), cudaMemcpyDeviceToHost, s));
+    FV3G_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < km; ++k)
+      for (int c = 0; c < ncol; ++c) q1_ad[(size_t)(i1 + c - ibeg) + row + k * plane] += ha[(size_t)k * ncol + c];
+    for (int t = 0; t < kn; ++t)
+      for (int c = 0; c < ncol; ++c) q2_ad[(size_t)(i1 + c - ibeg) + row + t * plane] = 0.0;
+    return 0;
+  }
+  // kord 9 (whose interfaces solve a tridiagonal system per column): field f
+  // carries the unit tangent of source layer f through the tangent-linear remap
   std::vector<D2> h1((size_t)km * km * ncol);
   for (int f = 0; f < km; ++f)
     for (int k = 0; k < km; ++k)
@@ -409,75 +366,93 @@ int fv3g_fv_tp_2d_ad(const double* q, double* q_ad, const double* crx, const dou
   CHECK(check_tp_damping(damping, nord, grid));
   if (!q || !q_ad || !crx || !cry || !xfx || !yfx || !ra_x || !ra_y || !fx_ad || !fy_ad)
     return set_error(FV3G_E_ARG, "null array argument");
-  constexpr int NC = 42;  // colours per input: 7 x 6
   const PlaneGeom pg = plane_for(bd);
   const size_t P = (size_t)pg.plane();
-  CHECK(g_ctx.begin(7 * padded(P, 8) + 14 * padded(P, 16) + 4 * padded(P * NC, 16)));
-  cudaStream_t s = g_ctx.stream;
-  double *stage = g_ctx.take<double>(P), *qx = g_ctx.take<double>(P), *qy = g_ctx.take<double>(P);
-  double *fxa = g_ctx.take<double>(P), *fya = g_ctx.take<double>(P), *gx = g_ctx.take<double>(P);
-  double* gy = g_ctx.take<double>(P);
-  FrozenTp f;
-  D2** slots[] = {&f.cx, &f.cy, &f.xf, &f.yf, &f.rx, &f.ry, &f.mx, &f.my, &f.dxa, &f.dya, &f.area};
-  for (D2** sl : slots) *sl = g_ctx.take<D2>(P);
-  D2 *in_x = g_ctx.take<D2>(P * NC), *in_y = g_ctx.take<D2>(P * NC), *fl = g_ctx.take<D2>(P * NC * 2);
-  D2 *d6u = g_ctx.take<D2>(P), *d6v = g_ctx.take<D2>(P), *dms = g_ctx.take<D2>(P);
-  FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
-  CHECK(upload_frozen(f, stage, pg, bd, crx, cry, xfx, yfx, ra_x, ra_y, mfx, mfy, grid, s));
   const int is = bd->is, ie = bd->ie, js = bd->js, je = bd->je, isd = bd->isd, ied = bd->ied, jsd = bd->jsd,
             jed = bd->jed;
-  CHECK(h2d_planes(qx, pg, q, isd, ied, jsd, jed, 1, s));
-  CHECK(h2d_planes(qy, pg, q, isd, ied, jsd, jed, 1, s));
-  CHECK(h2d_planes(fxa, pg, fx_ad, is, ie + 1, js, je, 1, s));
-  CHECK(h2d_planes(fya, pg, fy_ad, is, ie, js, je + 1, 1, s));
-  // trajectories of the two sweep directions: the copy_corners fills
-  const int corners = grid->nested ? 0 : corner_mask(grid);
-  if (corners) {
-    k_corners<<<1, 64, 0, s>>>(qx, pg, npx, npy, corners, 1, 1);
-    k_corners<<<1, 64, 0, s>>>(qy, pg, npx, npy, corners, 2, 1);
-    FV3G_CUDA(cudaGetLastError());
+  CHECK(g_ctx.begin(60 * padded(P, 8)));
+  cudaStream_t s = g_ctx.stream;
+  // frozen planes and the trajectory of the call
+  double *qv = g_ctx.take<double>(P), *cx = g_ctx.take<double>(P), *cy = g_ctx.take<double>(P);
+  double *xf = g_ctx.take<double>(P), *yf = g_ctx.take<double>(P), *rx = g_ctx.take<double>(P);
+  double *ry = g_ctx.take<double>(P), *wx = g_ctx.take<double>(P), *wy = g_ctx.take<double>(P);
+  double *dxa = g_ctx.take<double>(P), *dya = g_ctx.take<double>(P), *area = g_ctx.take<double>(P);
+  double *fxa = g_ctx.take<double>(P), *fya = g_ctx.take<double>(P), *qa = g_ctx.take<double>(P);
+  double *d6x = g_ctx.take<double>(P), *d6y = g_ctx.take<double>(P);
+  LinTraj tr{};
+  LinWork w{};
+  double** one[] = {&tr.qc1, &tr.qc2, &tr.qi, &tr.qj, &tr.fx2, &tr.fy2, &w.a1, &w.a2,
+                    &w.ai, &w.aj, &w.gx, &w.gy, &w.fx2, &w.fy2};
+  for (double** b : one) *b = g_ctx.take<double>(P);
+  for (double** b : {&tr.wxi, &tr.wyi, &tr.wxo, &tr.wyo}) *b = g_ctx.take<double>(6 * P);
+  FV3G_CUDA(cudaMemsetAsync(g_ctx.arena, 0, g_ctx.used, s));
+  struct Item {
+    double* dst;
+    const double* src;
+    int ilo, ihi, jlo, jhi;
+  } items[] = {{qv, q, isd, ied, jsd, jed},
+               {cx, crx, is, ie + 1, jsd, jed},
+               {cy, cry, isd, ied, js, je + 1},
+               {xf, xfx, is, ie + 1, jsd, jed},
+               {yf, yfx, isd, ied, js, je + 1},
+               {rx, ra_x, is, ie, jsd, jed},
+               {ry, ra_y, isd, ied, js, je},
+               // without mass fluxes the area fluxes weight the result, as upstream
+               {wx, mfx ? mfx : xfx, is, ie + 1, mfx ? js : jsd, mfx ? je : jed},
+               {wy, mfy ? mfy : yfx, mfy ? is : isd, mfy ? ie : ied, js, je + 1},
+               {dxa, grid->dxa, isd, ied, jsd, jed},
+               {dya, grid->dya, isd, ied, jsd, jed},
+               {area, grid->area, isd, ied, jsd, jed},
+               {fxa, fx_ad, is, ie + 1, js, je},
+               {fya, fy_ad, is, ie, js, je + 1}};
+  for (const Item& it : items) CHECK(h2d_planes(it.dst, pg, it.src, it.ilo, it.ihi, it.jlo, it.jhi, 1, s));
+  if (damping) {
+    // del-2 damping flux weights: d6 (difference across the face), times the
+    // face mean of mass with mass fluxes, else times the damping coefficient
+    const double damp = damp_coefficient(damp_c, grid->da_min, 0);
+    const int nid = ied - isd + 1, njd = jed - jsd + 1;
+    std::vector<double> hx((size_t)(ie - is + 2) * (je - js + 1)), hy((size_t)(ie - is + 1) * (je - js + 2));
+    auto M = [&](int i, int j) { return mass[(size_t)(j - jsd) * nid + (i - isd)]; };
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie + 1; ++i) {
+        const double d6 = grid->del6_v[(size_t)(j - jsd) * (nid + 1) + (i - isd)];
+        hx[(size_t)(j - js) * (ie - is + 2) + (i - is)] = d6 * (mfx ? 0.5 * damp * (M(i - 1, j) + M(i, j)) : damp);
+      }
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie; ++i) {
+        const double d6 = grid->del6_u[(size_t)(j - jsd) * nid + (i - isd)];
+        hy[(size_t)(j - js) * (ie - is + 1) + (i - is)] = d6 * (mfx ? 0.5 * damp * (M(i, j - 1) + M(i, j)) : damp);
+      }
+    (void)njd;
+    CHECK(h2d_planes(d6x, pg, hx.data(), is, ie + 1, js, je, 1, s));
+    CHECK(h2d_planes(d6y, pg, hy.data(), is, ie, js, je + 1, 1, s));
   }
-  AdvArgs<D2> a = tp_args(f, pg, bd, npx, npy, NC);
-  a.q_in = in_y;
-  a.q_in_x = in_x;
-  a.corners = 0;  // fills are in the trajectories; their transposes follow
-  a.nested = grid->nested;
+  LinArgs a{};
+  a.pg = pg;
+  a.P = (long long)P;
+  a.is = is; a.ie = ie; a.js = js; a.je = je;
+  a.isd = isd; a.ied = ied; a.jsd = jsd; a.jed = jed;
+  a.npx = npx; a.npy = npy;
+  a.ew = (!grid->nested && is == 1) ? 1 : NO_EDGE;
+  a.ee = (!grid->nested && ie + 1 == npx) ? npx : NO_EDGE;
+  a.es = (!grid->nested && js == 1) ? 1 : NO_EDGE;
+  a.en = (!grid->nested && je + 1 == npy) ? npy : NO_EDGE;
+  a.corners = grid->nested ? 0 : corner_mask(grid);
+  a.nt = 1; a.nq = 1; a.npz = 1;
+  a.hord = hord;
   a.lim_fac = lim_fac;
-  a.fx_out = fl;
-  a.fy_out = fl + P * NC;
-  // the del-2 damping reads the y-sweep input's strip and interior cells (the two cells beside each face),
-  // inside the boxes the gather below reads for that input
-  AdvArgs<D2> ad = a;
-  if (damping) CHECK(damping_args(ad, d6u, d6v, dms, stage, pg, bd, grid, mfx, mass, damp_c, s));
-  for (int pass = 0; pass < 2; ++pass) {  // 0: x-sweep input, 1: y-sweep input
-    const int px = pass == 0 ? 7 : 6, py = pass == 0 ? 6 : 7;
-    const long long n = (long long)P * NC;
-    k_color_planes<<<grid_1d(n), 256, 0, s>>>(in_x, qx, pg, isd, ied, jsd, jed, px, py, NC, pass == 0);
-    k_color_planes<<<grid_1d(n), 256, 0, s>>>(in_y, qy, pg, isd, ied, jsd, jed, px, py, NC, pass == 1);
-    FV3G_CUDA(cudaGetLastError());
-    FV3G_CUDA(cudaMemsetAsync(fl, 0, sizeof(D2) * P * NC * 2, s));
-    CHECK(launch_substep_tl(a, hord, s));
-    if (damping) CHECK(launch_damp_tl(ad, s));
-    // face boxes holding a cell: x input fx [i-2, i+3] x {j}, fy [i-3, i+3] x [j-2, j+3];
-    // y input fx [i-2, i+3] x [j-3, j+3], fy {i} x [j-2, j+3]
-    const FaceBox bxf = pass == 0 ? FaceBox{-2, 3, 0, 0} : FaceBox{-2, 3, -3, 3};
-    const FaceBox byf = pass == 0 ? FaceBox{-3, 3, -2, 3} : FaceBox{0, 0, -2, 3};
-    k_gather_adjoint<<<grid_1d((long long)(ied - isd + 1) * (jed - jsd + 1)), 256, 0, s>>>(
-        pass == 0 ? gx : gy, fl, fl + P * NC, fxa, fya, pg, isd, ied, jsd, jed, px, py, bxf, byf, is, ie, js, je);
-    FV3G_CUDA(cudaGetLastError());
-  }
-  if (corners) {
-    k_corners_adjoint<<<1, 64, 0, s>>>(gx, pg, npx, npy, corners, 1);
-    k_corners_adjoint<<<1, 64, 0, s>>>(gy, pg, npx, npy, corners, 2);
-    FV3G_CUDA(cudaGetLastError());
-  }
-  // q_ad += gx + gy on the host (the data domain of the caller's array)
+  a.cx = cx; a.cy = cy; a.xfx = xf; a.yfx = yf;
+  a.mfx = wx; a.mfy = wy;
+  a.ra_x = rx; a.ra_y = ry;
+  a.area = area; a.dxa = dxa; a.dya = dya;
+  CHECK(lin_trajectory(a, qv, tr, s));
+  CHECK(lin_fluxes_ad(a, tr, w, fxa, fya, damping ? d6x : nullptr, damping ? d6y : nullptr, qa, s));
+  // q_ad += J^T (fx_ad, fy_ad) over the caller's data domain; the flux adjoints are consumed
   const int ni = ied - isd + 1, nj = jed - jsd + 1;
-  std::vector<double> hx((size_t)ni * nj), hy((size_t)ni * nj);
-  CHECK(d2h_planes(hx.data(), gx, pg, isd, ied, jsd, jed, 1, s));
-  CHECK(d2h_planes(hy.data(), gy, pg, isd, ied, jsd, jed, 1, s));
+  std::vector<double> h((size_t)ni * nj);
+  CHECK(d2h_planes(h.data(), qa, pg, isd, ied, jsd, jed, 1, s));
   FV3G_CUDA(cudaStreamSynchronize(s));
-  for (size_t e = 0; e < hx.size(); ++e) q_ad[e] += hx[e] + hy[e];
+  for (size_t e = 0; e < h.size(); ++e) q_ad[e] += h[e];
   std::fill(fx_ad, fx_ad + (size_t)(ie - is + 2) * (je - js + 1), 0.0);
   std::fill(fy_ad, fy_ad + (size_t)(ie - is + 1) * (je - js + 2), 0.0);
   return 0;
