@@ -233,55 +233,79 @@ ENSEMBLE = [(48, 32)] * 16 + [(96, 64)] * 10 + [(192, 127)] * 6
 
 
 def ensemble_leg(a, stream):
-    """All members advanced by one CUDA graph per step (fv3g_ensemble_step), mixed precision, each member's
-    CTA width autotuned for its size; per-member error of one step against the FP64 path (each member against
-    the oracle: tests/test_gpu_configs.py)."""
+    """The uneven ensemble (16 x C48 L32, 10 x C96 L64, 6 x C192 L127 single tiles, 4 tracers each), mixed
+    precision.  Headline form: the members of each size as one state of independent tiles (one launch per
+    phase for all of them), the three states on three streams of one CUDA graph per step
+    (fv3g_ensemble_step), each state's CTA width autotuned; per-member error of one step against the FP64
+    path (each member against the oracle: tests/test_gpu_configs.py).  Also timed: one state per member in
+    the same graph form (per_member_states)."""
     import numpy as np
     import torch
     from fv3atm_gb300 import api
     from fv3atm_gb300 import synth as S
-    probs, states, widths = [], [], []
-    units = 0
-    for k, (n, npz) in enumerate(ENSEMBLE):
-        P = S.make_problem(n, npz, 4, ntiles=1, seed=5000 + k, cmax=0.7)
-        st = api.CubeState(n, npz, 4, precision="mixed", ntiles=1)
-        st.load_problem(P)
-        widths.append(st.autotune())
-        probs.append(P)
-        states.append(st)
-        units += n * n * npz * 4
-    ens = api.Ensemble(states)
+    probs = [S.make_problem(n, npz, 4, ntiles=1, seed=5000 + k, cmax=0.7) for k, (n, npz) in enumerate(ENSEMBLE)]
+    units = sum(n * n * npz * 4 for n, npz in ENSEMBLE)
     s = stream.cuda_stream
-    # accuracy: one ensemble step from the initial fields against the FP64 path
-    ens.step(2, stream=s)
+
+    def timed(ens):
+        for _ in range(max(1, min(a.warmup, 3))):
+            ens.step(2, stream=s)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            ens.step(2, stream=s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / a.steps
+
+    # one state of independent tiles per size
+    sizes = sorted(set(ENSEMBLE))
+    batches, widths = [], {}
+    for n, npz in sizes:
+        B = S.stack_tiles([P for P, sz in zip(probs, ENSEMBLE) if sz == (n, npz)])
+        st = api.CubeState(n, npz, 4, precision="mixed", ntiles=B.ntiles, independent_tiles=True)
+        st.load_problem(B)
+        widths[f"C{n}L{npz}x{B.ntiles}"] = st.autotune()
+        batches.append((st, B))
+    ens = api.Ensemble([st for st, _ in batches])
+    ens.step(2, stream=s)  # accuracy: one step from the initial fields against the FP64 path
     torch.cuda.synchronize()
     errs = []
-    for P, st in zip(probs, states):
-        ref = api.CubeState(P.n, P.npz, 4, precision="fp64", ntiles=1)
-        ref.load_problem(P)
+    for st, B in batches:
+        ref = api.CubeState(B.n, B.npz, 4, precision="fp64", ntiles=B.ntiles, independent_tiles=True)
+        ref.load_problem(B)
         ref.step(2)
         g, r = st.download("Q_REMAPPED"), ref.download("Q_REMAPPED")
-        sl = (slice(None), slice(None), slice(None), slice(3, 3 + P.n), slice(3, 3 + P.n))
-        errs.append(float(np.linalg.norm((g - r)[sl]) / np.linalg.norm(r[sl])))
+        for t in range(B.ntiles):
+            sl = (t, slice(None), slice(None), slice(3, 3 + B.n), slice(3, 3 + B.n))
+            errs.append(float(np.linalg.norm((g - r)[sl]) / np.linalg.norm(r[sl])))
         ref.close()
-    for _ in range(max(1, min(a.warmup, 3))):
-        ens.step(2, stream=s)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(a.steps):
-        ens.step(2, stream=s)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / a.steps
+    for st, B in batches:  # back to the initial fields
+        st.upload("Q", B.q.numpy())
+    ms = timed(ens)
+    ens.close()
+    for st, _ in batches:
+        st.close()
+    # one state per member, the same graph form
+    states = []
+    for P in probs:
+        st = api.CubeState(P.n, P.npz, 4, precision="mixed", ntiles=1)
+        st.load_problem(P)
+        st.autotune()
+        states.append(st)
+    ens = api.Ensemble(states)
+    ms_members = timed(ens)
     ens.close()
     for st in states:
         st.close()
     return {"value": units / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "members": len(ENSEMBLE),
             "rel_l2_vs_fp64_max": max(errs), "rel_l2_vs_fp64_mean": sum(errs) / len(errs),
-            "warps_per_cta_by_member": widths,
+            "warps_per_cta_by_size": widths,
+            "per_member_states": {"value": units / (ms_members / 1e3), "ms_per_step": ms_members},
             "config": "16 x C48 L32 + 10 x C96 L64 + 6 x C192 L127 single tiles (prescribed halo ring), 4 tracers, "
-                      "n_split 2, hord 8, kord 9, mixed precision, one graph per ensemble step"}
+                      "n_split 2, hord 8, kord 9, mixed precision; the members of each size as one state of "
+                      "independent tiles, one graph per ensemble step"}
 
 
 def build_state(P, precision, nq, npz, n, warps=0):

@@ -52,7 +52,8 @@ class StateDesc(C.Structure):
     _fields_ = [("n", C.c_int), ("ntiles", C.c_int), ("npz", C.c_int), ("nq", C.c_int), ("precision", C.c_int),
                 ("hord", C.c_int), ("kord", C.c_int), ("iv", C.c_int), ("q_min", C.c_double),
                 ("warps_per_cta", C.c_int), ("nord_tr", C.c_int), ("trdm", C.c_double), ("lim_fac", C.c_double),
-                ("fill", C.c_int), ("edge_sync", C.c_int), ("mass_fix", C.c_int)]
+                ("fill", C.c_int), ("edge_sync", C.c_int), ("mass_fix", C.c_int),
+                ("independent_tiles", C.c_int)]
 
 
 class NestBC(C.Structure):

@@ -198,20 +198,21 @@ def _stream(stream):
 
 
 class CubeState:
-    """ntiles (6: the cube; 1: one face with a prescribed halo ring) x npz levels x nq tracers
-    resident in HBM (fv3g_state)."""
+    """ntiles (6: the cube; 1: one face with a prescribed halo ring; with independent_tiles, a batch of such
+    single faces of one size, advanced with one launch per phase) x npz levels x nq tracers resident in HBM
+    (fv3g_state)."""
 
     def __init__(self, n: int, npz: int, nq: int, *, precision: str = "fp64", hord: int = 8, kord: int = 9,
                  iv: int = 0, q_min: float = 0.0, warps_per_cta: int = 0, ntiles: int = 6, nord_tr: int = 0,
                  trdm: float = 0.0, lim_fac: float = 1.0, fill: bool = False, edge_sync: bool = False,
-                 mass_fix: bool = False):
+                 mass_fix: bool = False, independent_tiles: bool = False):
         L = _lib.load()
         self.n, self.npz, self.nq, self.ntiles = n, npz, nq, ntiles
         self.nd = n + 6
         self.precision = precision
         prec = _lib.FV3G_FP64 if precision == "fp64" else _lib.FV3G_MIXED
         desc = StateDesc(n, ntiles, npz, nq, prec, hord, kord, iv, q_min, warps_per_cta, nord_tr, trdm, lim_fac,
-                         int(fill), int(edge_sync), int(mass_fix))
+                         int(fill), int(edge_sync), int(mass_fix), int(independent_tiles))
         self._h = C.c_void_p()
         _lib.check(L.fv3g_state_create(C.byref(desc), C.byref(self._h)), "fv3g_state_create")
         self._grids = []

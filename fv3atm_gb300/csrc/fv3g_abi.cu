@@ -113,7 +113,8 @@ struct fv3g_state {
   fv3g_state_desc d{};
   bool fp64 = true;
   int n = 0, nd = 0, npz = 0, nq = 0;
-  int nt = 6;  // tiles: 6 (cube, halos from the neighbours) or 1 (one face, halo ring prescribed by the caller)
+  int nt = 6;  // tiles: the cube's 6, or single faces whose halo ring the caller prescribes (1, or a batch)
+  bool cube = true;  // the tiles are the six faces of the cube (halos from the neighbours)
   PlaneGeom pg{};
   long long plane = 0;
   size_t esz = 8;
@@ -126,7 +127,7 @@ struct fv3g_state {
   void* area = nullptr; void* rarea = nullptr; void* dxa = nullptr; void* dya = nullptr;
   void* dx = nullptr; void* dy = nullptr; void* sin4 = nullptr;
   void* del6u = nullptr; void* del6v = nullptr;  // tracer-damping metrics
-  int del6_tiles = 0;                            // tiles whose damping metrics were set
+  std::vector<char> del6_set;                    // per tile: its damping metrics were set
   int warps_ring = 0;                            // edge-ring CTA width (0: warps_per_cta), set by autotune
   int pairs = 0;                                 // FP32 hord 8: tracers two per warp (k_substep_pair)
   double da_min = 0.0;
@@ -263,13 +264,14 @@ AdvArgs<T> adv_args(fv3g_state* st, int src, int dst, int dp_in, int dp_out) {
   a.npz = st->npz;
   a.corners = 15;
   a.nested = 0;
-  a.cube = st->nt == 6 ? 1 : 0;
+  a.cube = st->cube ? 1 : 0;
   a.topo = st->topo;
   a.eflux = (T*)st->eflux;
   a.lim_fac = st->d.lim_fac > 0.0 ? st->d.lim_fac : 1.0;
   a.warps_ring = st->warps_ring;
   a.err = st->err;
   a.pairs = pairs_allowed(st) ? st->pairs : 0;
+  a.ntiles = st->nt;
   return a;
 }
 
@@ -352,7 +354,7 @@ int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t 
 // fluxes, shared by every tracer.
 template <typename T>
 int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s) {
-  if (st->d.trdm > 1e-4 && (st->del6_tiles != (1 << st->nt) - 1 || !(st->da_min > 0.0)))
+  if (st->d.trdm > 1e-4 && (std::count(st->del6_set.begin(), st->del6_set.end(), 1) != st->nt || !(st->da_min > 0.0)))
     return set_error(FV3G_E_ARG, "tracer damping (trdm > 1e-4) needs every tile's grid with del6_u, del6_v, da_min");
   // scaled copies of cx, cy, mfx, mfy (read from the inputs, written scaled) and the area fluxes
   const T frac = (nsplt == 1) ? T(1) : T(1.0 / nsplt);
@@ -386,11 +388,12 @@ int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
     a.q_out += gofs;
     a.nq = ng;
     a.warps_ring = std::min(a.warps_ring, ng);
-    if (st->nt == 6) {
+    if (st->cube) {
       CHECK(launch_cube_halo<T>((T*)st->q[src] + gofs, a.sQt, st->plane, ng * st->npz, st->pg, st->n, st->topo, s));
       CHECK(mark(st, K_HALO, s));
     } else if (src != 0) {  // the prescribed ring of the home buffer, held over the step
       CHECK(launch_copy_halo_ring<T>((T*)st->q[src] + gofs, (const T*)st->q[0] + gofs, st->plane, ng * st->npz,
+                                     a.sQt, st->nt,
                                      st->pg, st->n, s));
       CHECK(mark(st, K_HALO, s));
     }
@@ -409,7 +412,7 @@ int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
       const int nint = bm.nbxi * bm.nbyi;
       CHECK(mark(st, K_SUBSTEP, s, (nint > 0) + (bm.nbx * bm.nby > nint) + (damp ? 1 : 0)));
     }
-    if (st->nt == 6 && st->eflux != nullptr) {
+    if (st->cube && st->eflux != nullptr) {
       CHECK(launch_edge_fix<T>(a, st->n, s));
       CHECK(mark(st, K_EDGEFIX, s));
     }
@@ -612,7 +615,7 @@ struct LinStep {
 
 int lin_check(fv3g_state* st) {
   if (!st->fp64) return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint step needs an FP64 state");
-  if (st->nt != 6) return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint step needs the six-tile state");
+  if (!st->cube) return set_error(FV3G_E_UNSUPPORTED, "the tangent-linear / adjoint step needs the six-tile cube");
   if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
   if (st->d.trdm > 1e-4 || st->d.fill || st->d.edge_sync || st->d.mass_fix)
     return set_error(FV3G_E_UNSUPPORTED,
@@ -733,8 +736,10 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   if (!desc || !out) return set_error(FV3G_E_ARG, "null argument");
   *out = nullptr;
   const fv3g_state_desc& d = *desc;
-  if (d.ntiles != 6 && d.ntiles != 1)
-    return set_error(FV3G_E_UNSUPPORTED, "batched state supports ntiles 6 (cube) or 1 (one face, prescribed halo)");
+  if (d.independent_tiles ? (d.ntiles < 1 || d.ntiles > 1024) : (d.ntiles != 6 && d.ntiles != 1))
+    return set_error(FV3G_E_UNSUPPORTED,
+                     "batched state supports ntiles 6 (cube), 1 (one face, prescribed halo) or, with "
+                     "independent_tiles, 1..1024 single faces (got %d)", d.ntiles);
   if (d.n < 12 || d.npz < 2 || d.npz > KMAX || d.nq < 1)
     return set_error(FV3G_E_ARG, "bad sizes n=%d npz=%d nq=%d (n>=12, 2<=npz<=%d, nq>=1)", d.n, d.npz, d.nq, KMAX);
   if (d.precision != FV3G_FP64 && d.precision != FV3G_MIXED) return set_error(FV3G_E_ARG, "bad precision %d", d.precision);
@@ -756,6 +761,8 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   st->npz = d.npz;
   st->nq = d.nq;
   st->nt = d.ntiles;
+  st->cube = !d.independent_tiles && d.ntiles == 6;
+  st->del6_set.assign(d.ntiles, 0);
   st->pg.pitch = ((st->nd + 1 + 7) / 8) * 8;
   st->pg.rows = st->nd + 1;
   st->pg.isd = 1 - NG;
@@ -789,7 +796,7 @@ int fv3g_state_create(const fv3g_state_desc* desc, fv3g_state** out) {
   for (void** m : metrics)
     if (!rc) rc = dalloc(st, m, P * nt);
   if (!rc) rc = dalloc(st, &st->sin4, P * nt * 4);
-  if (!rc && nt == 6 && d.edge_sync)
+  if (!rc && st->cube && d.edge_sync)
     rc = dalloc(st, &st->eflux, st->esz * 6 * 4 * (size_t)d.npz * d.nq * d.n);
   if (!rc) rc = dalloc(st, (void**)&st->ak, sizeof(double) * (KMAX + 1));
   if (!rc) rc = dalloc(st, (void**)&st->bk, sizeof(double) * (KMAX + 1));
@@ -848,7 +855,7 @@ int fv3g_state_set_grid(fv3g_state* st, int tile, const fv3g_grid* g) {
       int rc = st->fp64 ? upload_t<double>(st, fs, m.src, st->stream) : upload_t<float>(st, fs, m.src, st->stream);
       if (rc) return rc;
     }
-    st->del6_tiles |= 1 << tile;
+    st->del6_set[tile] = 1;
   }
   if (g->da_min > 0.0) st->da_min = g->da_min;
   if (!g->sin_sg) return set_error(FV3G_E_ARG, "null sin_sg");

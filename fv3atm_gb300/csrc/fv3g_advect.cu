@@ -298,12 +298,14 @@ int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s) 
 }
 
 // Halo ring (the NG-deep strips and the corner blocks) of every plane copied
-// from src to dst: the prescribed halo of a single-tile state, held over the
-// substeps of a step.
+// from src to dst: the prescribed halo of single tiles, held over the
+// substeps of a step.  nplanes planes per tile, ntiles tiles sQt apart.
 template <typename T>
-__global__ void k_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n) {
+__global__ void k_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, long long sQt, int ntiles,
+                                 PlaneGeom pg, int n) {
   const int nd = n + 2 * NG, ring = nd * nd - n * n;
-  for (int pl = blockIdx.y; pl < nplanes; pl += gridDim.y)
+  const long long tot = (long long)nplanes * ntiles;
+  for (long long tp = blockIdx.y; tp < tot; tp += gridDim.y)
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ring; c += gridDim.x * blockDim.x) {
       int i, j;
       if (c < NG * nd) {  // rows below the tile
@@ -319,16 +321,18 @@ __global__ void k_copy_halo_ring(T* dst, const T* src, long long splane, int npl
         const int k = r % (2 * NG);
         i = k < NG ? 1 - NG + k : n + 1 + (k - NG);
       }
-      const long long p = pl * splane + pg.at(i, j);
+      const long long p = (tp / nplanes) * sQt + (tp % nplanes) * splane + pg.at(i, j);
       dst[p] = src[p];
     }
 }
 
 template <typename T>
-int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n, cudaStream_t s) {
+int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, long long sQt, int ntiles,
+                          PlaneGeom pg, int n, cudaStream_t s) {
   const int nd = n + 2 * NG, ring = nd * nd - n * n;
-  dim3 grid((unsigned)std::min((ring + 255) / 256, 16), (unsigned)std::min(nplanes, 65535));
-  k_copy_halo_ring<T><<<grid, 256, 0, s>>>(dst, src, splane, nplanes, pg, n);
+  const long long tot = (long long)nplanes * ntiles;
+  dim3 grid((unsigned)std::min((ring + 255) / 256, 16), (unsigned)std::min<long long>(tot, 65535));
+  k_copy_halo_ring<T><<<grid, 256, 0, s>>>(dst, src, splane, nplanes, sQt, ntiles, pg, n);
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }
@@ -369,7 +373,7 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
   template int launch_substep<T>(const AdvArgs<T>&, int, bool, int, cudaStream_t);                          \
   template int launch_edge_fix<T>(const AdvArgs<T>&, int, cudaStream_t);                                     \
   template int launch_cube_halo<T>(T*, long long, long long, int, PlaneGeom, int, const Topo&, cudaStream_t);   \
-  template int launch_copy_halo_ring<T>(T*, const T*, long long, int, PlaneGeom, int, cudaStream_t);             \
+  template int launch_copy_halo_ring<T>(T*, const T*, long long, int, long long, int, PlaneGeom, int, cudaStream_t);             \
   template int launch_area_flux<T>(T*, T*, T*, T*, T*, T*, const T*, const T*, const T*, const T*, const T*, \
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \
                                    int, T, cudaStream_t, AreaFluxSrc<T>);                                    \

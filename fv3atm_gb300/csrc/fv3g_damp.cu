@@ -173,7 +173,7 @@ int launch_damp(const AdvArgs<T>& a, bool flux_mode, cudaStream_t s) {
   if (flux_mode && (!a.fx_out || !a.fy_out)) return set_error(FV3G_E_ARG, "flux-mode damping needs flux planes");
   if (!flux_mode && (!a.q_out || !a.dp2)) return set_error(FV3G_E_ARG, "damping of q needs q_out and dp2");
   const int nbx = (a.ie - a.is + TW) / TW, nby = (a.je - a.js + TW) / TW;
-  const dim3 grid((unsigned)(nbx * nby), (unsigned)a.npz, a.cube ? 6u : 1u);
+  const dim3 grid((unsigned)(nbx * nby), (unsigned)a.npz, (unsigned)adv_tiles(a));
   constexpr size_t smem = sizeof(SmemDamp<T>);
   switch (a.nord * 2 + (flux_mode ? 1 : 0)) {
     case 0: k_damp<T, 0, false><<<grid, 256, smem, s>>>(a, nbx); break;

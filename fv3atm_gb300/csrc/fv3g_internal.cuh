@@ -98,7 +98,14 @@ struct AdvArgs {
   int damp_mass;    // 1: field q, flux weighted by damp times the face mean of dp1; 0: field damp q
   int* err;         // optional sticky error word: FV3G_E_DELP when a compute cell's dp2 is not positive
   int pairs;        // FP32, hord 8: advance the tracers two per warp (k_substep_pair)
+  int ntiles;       // tiles the launches cover (0: 6 for the cube, else 1)
 };
+
+// tiles a substep launch covers
+template <typename T>
+__host__ __device__ __forceinline__ int adv_tiles(const AdvArgs<T>& a) {
+  return a.ntiles > 0 ? a.ntiles : (a.cube ? 6 : 1);
+}
 
 // First error of a batched step into its sticky word (later ones are dropped).
 __device__ __forceinline__ void raise_error(int* err, int code) {
@@ -229,7 +236,8 @@ double damp_coefficient(double damp_c, double da_min, int nord);
 
 // Host launchers (fv3g_advect.cu)
 template <typename T>
-int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, PlaneGeom pg, int n, cudaStream_t s);
+int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, long long sQt, int ntiles,
+                          PlaneGeom pg, int n, cudaStream_t s);
 int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s);
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,

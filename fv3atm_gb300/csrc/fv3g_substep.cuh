@@ -610,80 +610,124 @@ __device__ __forceinline__ TileCtx tile_of(const AdvArgs<T>& a, const BlockMap& 
   return c;
 }
 
+// One element of a plane field (clamped into the plane, as ld_field) into
+// shared memory: FP32 and FP64 values by an asynchronous copy (cp.async, no
+// register round trip, many in flight per thread), other types by a load.
+template <typename T>
+__device__ __forceinline__ void stage_ld(T* dst, const T* base, const PlaneGeom& pg, int i, int j) {
+  i = min(max(i, pg.isd), pg.isd + pg.pitch - 1);
+  j = min(max(j, pg.jsd), pg.jsd + pg.rows - 1);
+  const T* src = base + pg.at(i, j);
+  if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+  } else {
+    *dst = *src;
+  }
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Per-level fields of a CTA tile into shared memory (Courant numbers, area
 // and mass fluxes, 1/ra_x, 1/ra_y, dp ratios; edge metrics for edge CTAs);
 // writes dp2 of the tile's cells.  Ends with a CTA barrier.
+// Phase 1 copies every raw window asynchronously (the windows of dp1 and
+// rarea into dpa and ub, a caller's ra_x / ra_y into rrx / rry); phase 2
+// forms the derived values from shared memory with the same arithmetic as
+// the field expressions; phase 3 halves the mass fluxes.
 template <typename T, bool EDGES>
 __device__ __forceinline__ void stage_level(const AdvArgs<T>& a, SmemLevel<T>& L, const TileCtx& tc) {
   const PlaneGeom& pg = a.pg;
   const int t = tc.t, k = tc.k, i0 = tc.i0, j0 = tc.j0, ni = tc.ni, nj = tc.nj;
   const int exA = tc.exA, exB = tc.exB, eyA = tc.eyA, eyB = tc.eyB;
-  {
-    const long long fo = t * a.sFt + k * a.sFk;
-    const T* cx = a.cx + fo;
-    const T* cy = a.cy + fo;
-    const T* xf = a.xfx + fo;
-    const T* yf = a.yfx + fo;
-    const T* mx = a.mfx + fo;
-    const T* my = a.mfy + fo;
-    const T* area = a.area + t * a.sMt;
-    const T* rarea = a.rarea + t * a.sMt;
-    for (int e = threadIdx.x; e < NF * WIN; e += blockDim.x) {
-      const int f = e / WIN, w = e % WIN;
-      L.cy[f][w] = ld_field(cy, pg, i0 - 3 + w, j0 + f);
-      L.yf[f][w] = ld_field(yf, pg, i0 - 3 + w, j0 + f);
-    }
-    for (int e = threadIdx.x; e < WIN * NF; e += blockDim.x) {
-      const int r = e / NF, f = e % NF;
-      L.cx[r][f] = ld_field(cx, pg, i0 + f, j0 - 3 + r);
-      L.xf[r][f] = ld_field(xf, pg, i0 + f, j0 - 3 + r);
-    }
-    for (int e = threadIdx.x; e < TW * NF; e += blockDim.x) {
-      const int r = e / NF, f = e % NF;
-      L.mx[r][f] = T(0.5) * ld_field(mx, pg, i0 + f, j0 + r);
-      const int ff = e / TW, c = e % TW;
-      L.my[ff][c] = T(0.5) * ld_field(my, pg, i0 + c, j0 + ff);
-    }
-    for (int e = threadIdx.x; e < WIN * WIN; e += blockDim.x) {
-      const int r = e / WIN, w = e % WIN;
-      L.area[r][w] = ld_field(area, pg, i0 - 3 + w, j0 - 3 + r);
-    }
+  const long long fo = t * a.sFt + k * a.sFk;
+  const T* cx = a.cx + fo;
+  const T* cy = a.cy + fo;
+  const T* xf = a.xfx + fo;
+  const T* yf = a.yfx + fo;
+  const T* mx = a.mfx + fo;
+  const T* my = a.mfy + fo;
+  const T* area = a.area + t * a.sMt;
+  const T* rarea = a.rarea + t * a.sMt;
+  const T* dp1 = a.dp1 ? a.dp1 + fo : nullptr;
+  T* dp2o = a.dp2 ? a.dp2 + fo : nullptr;
+  // ---- phase 1: raw windows
+  for (int e = threadIdx.x; e < NF * WIN; e += blockDim.x) {
+    const int f = e / WIN, w = e % WIN;
+    stage_ld(&L.cy[f][w], cy, pg, i0 - 3 + w, j0 + f);
+    stage_ld(&L.yf[f][w], yf, pg, i0 - 3 + w, j0 + f);
+  }
+  for (int e = threadIdx.x; e < WIN * NF; e += blockDim.x) {
+    const int r = e / NF, f = e % NF;
+    stage_ld(&L.cx[r][f], cx, pg, i0 + f, j0 - 3 + r);
+    stage_ld(&L.xf[r][f], xf, pg, i0 + f, j0 - 3 + r);
+  }
+  for (int e = threadIdx.x; e < TW * NF; e += blockDim.x) {
+    const int r = e / NF, f = e % NF;
+    stage_ld(&L.mx[r][f], mx, pg, i0 + f, j0 + r);
+    const int ff = e / TW, c = e % TW;
+    stage_ld(&L.my[ff][c], my, pg, i0 + c, j0 + ff);
+  }
+  for (int e = threadIdx.x; e < WIN * WIN; e += blockDim.x) {
+    const int r = e / WIN, w = e % WIN;
+    stage_ld(&L.area[r][w], area, pg, i0 - 3 + w, j0 - 3 + r);
+  }
+  if (a.ra_x || a.ra_y) {
     for (int e = threadIdx.x; e < WIN * TW; e += blockDim.x) {
       const int r = e / TW, c = e % TW;
-      const int i = i0 + c, j = j0 - 3 + r;
-      L.rrx[r][c] = T(1) / (a.ra_x ? ld_field(a.ra_x, pg, i, j)
-                                   : ld_field(area, pg, i, j) + ld_field(xf, pg, i, j) - ld_field(xf, pg, i + 1, j));
+      if (a.ra_x) stage_ld(&L.rrx[r][c], a.ra_x, pg, i0 + c, j0 - 3 + r);
       const int r2 = e / WIN, w = e % WIN;
-      const int i2 = i0 - 3 + w, j2 = j0 + r2;
-      L.rry[r2][w] = T(1) / (a.ra_y ? ld_field(a.ra_y, pg, i2, j2)
-                                    : ld_field(area, pg, i2, j2) + ld_field(yf, pg, i2, j2) - ld_field(yf, pg, i2, j2 + 1));
+      if (a.ra_y) stage_ld(&L.rry[r2][w], a.ra_y, pg, i0 - 3 + w, j0 + r2);
     }
-    const T* dp1 = a.dp1 ? a.dp1 + fo : nullptr;
-    T* dp2o = a.dp2 ? a.dp2 + fo : nullptr;
-    for (int e = threadIdx.x; dp1 != nullptr && e < TW * TW; e += blockDim.x) {
+  }
+  if (dp1 != nullptr) {
+    for (int e = threadIdx.x; e < TW * TW; e += blockDim.x) {
       const int r = e / TW, c = e % TW;
-      const int i = i0 + c, j = j0 + r;
-      const T ra = ld_field(rarea, pg, i, j);
-      const T d1 = ld_field(dp1, pg, i, j);
-      const T d2 = d1 + (ld_field(mx, pg, i, j) - ld_field(mx, pg, i + 1, j) + ld_field(my, pg, i, j) -
-                         ld_field(my, pg, i, j + 1)) * ra;
+      stage_ld(&L.dpa[r][c], dp1, pg, i0 + c, j0 + r);
+      stage_ld(&L.ub[r][c], rarea, pg, i0 + c, j0 + r);
+    }
+  }
+  if (EDGES) {  // metrics of the one-sided edge values: dxa across x edges, dya across y edges
+    const T* dxa = a.dxa + t * a.sMt;
+    const T* dya = a.dya + t * a.sMt;
+    for (int e = threadIdx.x; e < 2 * 4 * WIN; e += blockDim.x) {
+      const int side = e / (4 * WIN), m = (e / WIN) % 4, w = e % WIN;
+      const int ex = side ? exB : exA, ey = side ? eyB : eyA;
+      if (ex == NO_EDGE) L.edx[side][m][w] = T(1);
+      else stage_ld(&L.edx[side][m][w], dxa, pg, i0 - 3 + ex - 2 + m, j0 - 3 + w);
+      if (ey == NO_EDGE) L.edy[side][m][w] = T(1);
+      else stage_ld(&L.edy[side][m][w], dya, pg, i0 - 3 + w, j0 - 3 + ey - 2 + m);
+    }
+  }
+  stage_wait();
+  __syncthreads();
+  // ---- phase 2: derived values
+  for (int e = threadIdx.x; e < WIN * TW; e += blockDim.x) {
+    const int r = e / TW, c = e % TW;
+    L.rrx[r][c] = T(1) / (a.ra_x ? L.rrx[r][c] : L.area[r][c + 3] + L.xf[r][c] - L.xf[r][c + 1]);
+    const int r2 = e / WIN, w = e % WIN;
+    L.rry[r2][w] = T(1) / (a.ra_y ? L.rry[r2][w] : L.area[r2 + 3][w] + L.yf[r2][w] - L.yf[r2 + 1][w]);
+  }
+  if (dp1 != nullptr) {
+    for (int e = threadIdx.x; e < TW * TW; e += blockDim.x) {
+      const int r = e / TW, c = e % TW;
+      const T d1 = L.dpa[r][c], ra = L.ub[r][c];
+      const T d2 = d1 + (L.mx[r][c] - L.mx[r][c + 1] + L.my[r][c] - L.my[r + 1][c]) * ra;
       L.dpa[r][c] = d1 / ra;
       L.ub[r][c] = ra / d2;
       if (r < nj && c < ni) {
-        if (dp2o != nullptr) dp2o[pg.at(i, j)] = d2;
+        if (dp2o != nullptr) dp2o[pg.at(i0 + c, j0 + r)] = d2;
         if (!(d2 > T(0))) raise_error(a.err, FV3G_E_DELP);
       }
     }
-    if (EDGES) {  // metrics of the one-sided edge values: dxa across x edges, dya across y edges
-      const T* dxa = a.dxa + t * a.sMt;
-      const T* dya = a.dya + t * a.sMt;
-      for (int e = threadIdx.x; e < 2 * 4 * WIN; e += blockDim.x) {
-        const int side = e / (4 * WIN), m = (e / WIN) % 4, w = e % WIN;
-        const int ex = side ? exB : exA, ey = side ? eyB : eyA;
-        L.edx[side][m][w] = ex == NO_EDGE ? T(1) : ld_field(dxa, pg, i0 - 3 + ex - 2 + m, j0 - 3 + w);
-        L.edy[side][m][w] = ey == NO_EDGE ? T(1) : ld_field(dya, pg, i0 - 3 + w, j0 - 3 + ey - 2 + m);
-      }
-    }
+  }
+  __syncthreads();
+  // ---- phase 3: 0.5 mfx, 0.5 mfy
+  for (int e = threadIdx.x; e < TW * NF; e += blockDim.x) {
+    const int r = e / NF, f = e % NF;
+    L.mx[r][f] = T(0.5) * L.mx[r][f];
+    const int ff = e / TW, c = e % TW;
+    L.my[ff][c] = T(0.5) * L.my[ff][c];
   }
   __syncthreads();
 }
@@ -726,7 +770,7 @@ template <typename T, int HORD, bool FLUXES>
 static int launch_one(const AdvArgs<T>& a, int warps, cudaStream_t s) {
   const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
   const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
-  const int nt = a.cube ? 6 : 1;
+  const int nt = adv_tiles(a);
   // edge-ring CTAs may run narrower (and at most ring_max_warps wide)
   const int wr = std::min(a.warps_ring > 0 ? a.warps_ring : warps, ring_max_warps((int)sizeof(T)));
   const bool two = edge_slots16<T>(a.is, a.ie, a.js, a.je);

@@ -271,7 +271,7 @@ int launch_substep_pair(const AdvArgs<float>& a, int warps, cudaStream_t s) {
   const int wr = std::min(std::min(a.warps_ring > 0 ? a.warps_ring : warps, PAIR_RING_MAX_WARPS), npairs);
   const BlockMap bm = block_map(a.is, a.ie, a.js, a.je, a.npx, a.npy, a.nested);
   const int nint = bm.nbxi * bm.nbyi, nring = bm.nbx * bm.nby - nint;
-  const int nt = a.cube ? 6 : 1;
+  const int nt = adv_tiles(a);
   const bool two = windows_hold_two_edges(a.is, a.ie, a.js, a.je);
   if (nint > 0) {
     k_substep_pair<false><<<dim3(nint, a.npz, nt), 32 * w, pair_smem_bytes(w, false, false), s>>>(a, bm);

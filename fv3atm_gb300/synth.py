@@ -196,6 +196,20 @@ def fill_cube_halo(x, n: int, ng: int, topo: np.ndarray):
     return x
 
 
+def stack_tiles(probs: list) -> "Problem":
+    """Single-tile problems of one size (n, npz, nq) as one problem of len(probs) independent tiles (the
+    layout of a state with independent_tiles): each tile keeps its grid, fields and halo ring."""
+    import torch
+    p0 = probs[0]
+    for p in probs:
+        if (p.n, p.npz, p.nq, p.ntiles) != (p0.n, p0.npz, p0.nq, 1):
+            raise ValueError("stack_tiles takes single-tile problems of one size")
+    cat = lambda name: torch.cat([torch.as_tensor(getattr(p, name)) for p in probs], dim=0)
+    return Problem(n=p0.n, ng=p0.ng, npz=p0.npz, nq=p0.nq, ntiles=len(probs), geoms=[p.geoms[0] for p in probs],
+                   topo=p0.topo, ak=p0.ak, bk=p0.bk, dt=p0.dt, q=cat("q"), dp=cat("dp"), cx=cat("cx"), cy=cat("cy"),
+                   mfx=cat("mfx"), mfy=cat("mfy"), meta=dict(members=[p.meta for p in probs]))
+
+
 def make_problem(n: int, npz: int, nq: int, *, ntiles: int = 6, seed: int = 0, cmax: float = 0.8,
                  u0: float = 40.0, pert_amp: float = 10.0, lmax: int = 20, dp_noise: float = 0.10,
                  ps_range: tuple = (95000.0, 103000.0), tracer_kind: str = "mixed", noise: float = 0.01,

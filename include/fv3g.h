@@ -283,7 +283,8 @@ typedef struct fv3g_state fv3g_state;
 typedef struct {
   int n;          /* cells per tile edge (C_n) */
   int ntiles;     /* 6: the cube, halos from the neighbouring tiles; 1: one cube face whose halo ring
-                     (strips and corner blocks of Q) is uploaded by the caller and held over the step */
+                     (strips and corner blocks of Q) is uploaded by the caller and held over the step;
+                     with independent_tiles, any count of such single faces (members of one size) */
   int npz;        /* Lagrangian levels */
   int nq;         /* tracers */
   int precision;  /* FV3G_FP64 or FV3G_MIXED */
@@ -306,6 +307,9 @@ typedef struct {
                      1/16 of the rows) by one unit in the last place, unbiased, then a few small values to take
                      the residual to ~1e-14 (the stored FP32 mass is summed exactly).  Switchable per step with
                      fv3g_state_set_mass_fix. */
+  int independent_tiles; /* 1: the ntiles tiles are independent single faces (ensemble members of one size and
+                     level count, each with its own grid, fields and prescribed halo ring), advanced together:
+                     one launch per phase for all of them; 0: ntiles 6 is the cube, 1 one face */
 } fv3g_state_desc;
 
 /* Which field an upload/download addresses. */

@@ -116,6 +116,40 @@ def test_tracer_pairs_only_for_fp32_hord8(cuda):
         st.close()
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_independent_tiles_match_single_members(cuda, precision):
+    """A state of independent tiles (members of one size, each with its own grid, fields and prescribed halo
+    ring; one launch per phase for all of them) gives every member bit for bit what the member's own
+    single-tile state gives, over two steps; an ensemble of such batches steps alike."""
+    probs = [S.make_problem(32, 12, 3, ntiles=1, seed=700 + k, cmax=0.7) for k in range(3)]
+    B = S.stack_tiles(probs)
+    batch = api.CubeState(32, 12, 3, precision=precision, ntiles=3, independent_tiles=True, warps_per_cta=3)
+    batch.load_problem(B)
+    singles = []
+    for P in probs:
+        st = api.CubeState(32, 12, 3, precision=precision, ntiles=1, warps_per_cta=3)
+        st.load_problem(P)
+        singles.append(st)
+    for step in range(2):
+        batch.step(2)
+        for st in singles:
+            st.step(2)
+    out = batch.download("Q_REMAPPED")
+    for t, st in enumerate(singles):
+        assert np.array_equal(out[t], st.download("Q_REMAPPED")[0]), t
+    other = api.CubeState(32, 12, 3, precision=precision, ntiles=3, independent_tiles=True, warps_per_cta=3)
+    other.load_problem(B)
+    ens = api.Ensemble([other])
+    ens.step(2)
+    ens.step(2)
+    import torch
+    torch.cuda.synchronize()
+    assert np.array_equal(other.download("Q_REMAPPED"), out)
+    ens.close()
+    for st in singles + [batch, other]:
+        st.close()
+
+
 @pytest.mark.parametrize("precision,bound", [("mixed", 1e-12), ("fp64", 1e-14)])
 def test_mass_fix_restores_global_mass_every_step(cuda, precision, bound):
     """mass_fix = 1: after each step every tracer's global mass sum(q delp area) equals its value at the step's
