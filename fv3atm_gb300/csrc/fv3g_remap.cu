@@ -716,36 +716,27 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
       }
     }
     // ------------------------------------------ sub-grid parabolas of layers
+    // every layer takes both the interior constraint and CW84 and keeps the
+    // one its position calls for (the two layers at each end of the column:
+    // CW84), uniform across the warp, then the floor
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
-      // every layer as an interior one (uniform across the warp) ...
 #pragma unroll
       for (int j = 0; j < NPL; ++j) {
         const int u = u0 + j;
         const T qk = qv[h][j];
         T bl = st[h][j] - qk, br = (j + 1 < NPL ? st[h][j + 1] : st_end[h]) - qk;
+        T ble = bl, bre = br;
+        cw84_sel(ble, bre);
         interior_constraint<T, KORD>(w[h][j], w[h][j + 1], qk, w[h][j + 3], w[h][j + 4], dmv[h][j], bl, br);
+        const bool end = u < 2 || u > km - 3;
+        bl = end ? ble : bl;
+        br = end ? bre : br;
         if (a.iv >= 0) positivity(qk, floor_v, bl, br);
         if (u < km) {
           S.pl[h][pk<T>(u)] = qk + bl;
           S.pr[h][pk<T>(u)] = qk + br;
           S.p6[h][pk<T>(u)] = T(-3) * (bl + br);
-        }
-      }
-      // ... then the two layers at each end of the column again, with CW84
-      // (only the lanes that hold them)
-      if (u0 < 2 || u0 + NPL > km - 2) {
-#pragma unroll
-        for (int j = 0; j < NPL; ++j) {
-          const int u = u0 + j;
-          if (u < km && (u < 2 || u > km - 3)) {
-            const Profile<T> p = layer_profile<T, KORD>(u, km, qv[h][j], qv[h][j], qv[h][j], qv[h][j], qv[h][j],
-                                                        st[h][j], j + 1 < NPL ? st[h][j + 1] : st_end[h], T(0), a.iv,
-                                                        floor_v);
-            S.pl[h][pk<T>(u)] = p.l;
-            S.pr[h][pk<T>(u)] = p.r;
-            S.p6[h][pk<T>(u)] = p.s6;
-          }
         }
       }
     }
@@ -794,9 +785,11 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
 #pragma unroll
     for (int h = 0; h < FP; ++h) {
       if (Single<T>::value) {
-        FF cm[NPL + 1];  // cumulative mass at this lane's target interfaces
+        // cumulative mass at this lane's target interfaces; the last one is the
+        // next lane's first (32 NPL > kn, so lane 31's last is never used)
+        FF cm[NPL + 1];
 #pragma unroll
-        for (int j = 0; j <= NPL; ++j) {
+        for (int j = 0; j < NPL; ++j) {
           const int L = Ls[j];
           const float X = (float)Xs[j];
           const int il = pk<float>(L), iu = pk<float>(L + 1);
@@ -811,6 +804,7 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
           }
           cm[j] = c;
         }
+        cm[NPL] = FF{__shfl_down_sync(0xffffffffu, cm[0].hi, 1), __shfl_down_sync(0xffffffffu, cm[0].lo, 1)};
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
           const int t = u0 + j;
