@@ -173,6 +173,12 @@ def map1_ppm_ad(km, pe1, q1, q1_ad, qs, kn, pe2, q2_ad, i1, i2, j, ibeg, iend, j
               iend, jbeg, jend, iv, kord)
 
 
+def map1_q2(km, pe1, q1, kn, pe2, q2, dp2, i1, i2, iv, kord, j, ibeg, iend, jbeg, jend, q_min=0.0) -> None:
+    """map1_q2: row j of q1 onto pe2 with the target thicknesses dp2 (i1:i2, kn); q2 (kn, i2-i1+1) C order."""
+    _lib.call("fv3g_map1_q2", km, _p(pe1), _p(q1), kn, _p(pe2), _p(q2), _p(dp2), i1, i2, iv, kord, j, ibeg, iend, jbeg,
+              jend, C.c_double(q_min))
+
+
 def fillz(im, km, nq, q, dp) -> None:
     """q (nq, km, im) (Fortran q(im, km, nq)) filled in place; dp (km, im)."""
     _lib.call("fv3g_fillz", im, km, nq, _p(q), _p(dp))
@@ -326,6 +332,13 @@ class CubeState:
         """fv3g_state_step_ad: q_ad_in = J^T q_ad_out (hand-written reverse sweeps; kord 4)."""
         _lib.call("fv3g_state_step_ad", self._h, q_split, parts, C.c_void_p(q_ad_out), C.c_void_p(q_ad_in),
                   _stream(stream))
+
+    def remap_fields(self, fields_in: int, fields_out: int, nfield: int, kind: int = 0, iv: int = 1, kord: int = 9,
+                     q_min: float = 0.0, log_p: bool = False, stream=None) -> None:
+        """fv3g_state_remap_fields: device pointers (ints) of (ntiles, nfield, npz, nd, nd) arrays of the state's
+        element type; kind 0 cells, 1 u faces, 2 v faces."""
+        _lib.call("fv3g_state_remap_fields", self._h, C.c_void_p(fields_in), C.c_void_p(fields_out), nfield, kind, iv,
+                  kord, C.c_double(q_min), int(bool(log_p)), _stream(stream))
 
     def step_host(self, q_split: int, q_in: int, fields: dict, q_out: int, host_f32: bool, groups: int = 0,
                   stream=None) -> None:

@@ -685,6 +685,47 @@ int lin_user_copy(fv3g_state* st, double* planes, const double* user, bool to_us
   return copy_planes(planes, pitch, dplane, user, nd * es, hplane, nd * es, nd, np, cudaMemcpyDeviceToDevice, s);
 }
 
+template <typename T>
+int remap_fields_t(fv3g_state* st, const void* in, void* out, int nfield, int kind, int iv, int kord,
+                          double q_min, int log_p, cudaStream_t s) {
+  const int n = st->n, nd = st->nd, km = st->npz;
+  const int ni = kind == 2 ? n + 1 : n, nj = kind == 1 ? n + 1 : n;
+  const long long nc = (long long)st->nt * ni * nj;
+  T* dpl = (T*)st->dp[st->dp_end];  // the Lagrangian thickness of the last tracer_2d (DELP before any)
+  if (kind != 0)  // the faces read the columns beside them: the halo strips of the thickness
+    CHECK(launch_cube_halo<T>(dpl, st->plane * km, st->plane, km, st->pg, n, st->topo, s));
+  CallBufs B;
+  double *pe1, *pe2;
+  CHECK(B.take(&pe1, (size_t)(km + 1) * nc));
+  CHECK(B.take(&pe2, (size_t)(km + 1) * nc));
+  CHECK(launch_field_pressures<T>(dpl, st->plane * km, st->plane, st->pg, st->nt, km, ni, nj, kind, log_p, st->ak,
+                                  st->bk, pe1, pe2, s));
+  RemapArgs<T> r{};
+  PlaneGeom up{};  // the caller's planes: nd x nd, i fastest
+  up.pitch = nd;
+  up.rows = nd;
+  up.isd = 1 - NG;
+  up.jsd = 1 - NG;
+  r.q_in = (const T*)in;
+  r.q_out = (T*)out;
+  r.sQk = (long long)nd * nd;
+  r.sQq = r.sQk * km;
+  r.sQt = r.sQq * nfield;
+  r.sQqo = r.sQq;
+  r.nfield = nfield;
+  r.pe1 = pe1;
+  r.pe2 = pe2;
+  r.pg = up;
+  r.i1 = 1; r.j1 = 1; r.ni = ni; r.nj = nj;
+  r.ncol = nc;
+  r.km = km; r.kn = km;
+  r.iv = iv;
+  r.q_min = q_min;
+  CHECK(launch_remap<T>(r, kord, s));
+  FV3G_CUDA(cudaStreamSynchronize(s));  // the pressure buffers are freed on return
+  return 0;
+}
+
 }  // namespace
 
 int fv3g::state_field_view(fv3g_state* st, int field, bool loading, StateFieldView* v) {
@@ -1048,6 +1089,21 @@ int fv3g_state_step_ad(fv3g_state* st, int q_split, int parts, const double* q_a
   CHECK(lin_user_copy(st, a0, q_ad_in, true, s));
   FV3G_CUDA(cudaStreamSynchronize(s));
   return 0;
+}
+
+int fv3g_state_remap_fields(fv3g_state* st, const void* fields_in, void* fields_out, int nfield, int kind, int iv,
+                            int kord, double q_min, int log_p, void* stream) {
+  if (!st || !fields_in || !fields_out) return set_error(FV3G_E_ARG, "null argument");
+  if (nfield < 1) return set_error(FV3G_E_ARG, "nfield must be positive");
+  if (kind < 0 || kind > 2) return set_error(FV3G_E_ARG, "kind must be 0 (cells), 1 (u faces) or 2 (v faces)");
+  if (kind != 0 && !st->cube)
+    return set_error(FV3G_E_UNSUPPORTED, "face fields need the six-tile cube (the faces read the neighbouring tiles)");
+  if (iv < -1 || iv > 1) return set_error(FV3G_E_ARG, "iv %d outside -1..1", iv);
+  if (kord != 4 && kord != 9) return set_error(FV3G_E_UNSUPPORTED, "kord %d not implemented (4 and 9 are)", kord);
+  if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
+  cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  return st->fp64 ? remap_fields_t<double>(st, fields_in, fields_out, nfield, kind, iv, kord, q_min, log_p, s)
+                  : remap_fields_t<float>(st, fields_in, fields_out, nfield, kind, iv, kord, q_min, log_p, s);
 }
 
 int fv3g_state_nsplt(fv3g_state* st, int* nsplt) {

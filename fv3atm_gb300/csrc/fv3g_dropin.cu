@@ -508,9 +508,11 @@ int fv3g_tracer_2d_1L(double* q, double* dp1, double* mfx, double* mfy, double* 
                         lim_fac, halo_fn, halo_ctx, nsplt_out, true);
 }
 
+// dp2 (optional, map1_q2): (i1:i2, kn) target thicknesses dividing the overlap
+// masses, and q2 then the 2-D (i1:i2, kn) row
 static int map_common(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
                       double* q2, int i1, int i2, int j1, int j2, int ibeg, int iend, int jbeg, int jend, int nq,
-                      int iv, int kord, double q_min) {
+                      int iv, int kord, double q_min, const double* dp2 = nullptr) {
   if (!pe1 || !q1 || !pe2 || !q2) return set_error(FV3G_E_ARG, "null array argument");
   if (km < 1 || km > KMAX || kn < 1 || kn > KMAX)
     return set_error(FV3G_E_ARG, "remap supports 1..%d layers (km=%d, kn=%d)", KMAX, km, kn);
@@ -529,13 +531,15 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   pg.rows = nj;
   const size_t P = (size_t)ni * nj;
   CHECK(g_ctx.begin(padded(P * km * nq, 8) + padded(P * kn * nq, 8) + padded(P * (km + 1), 8) +
-                    padded(P * (kn + 1), 8) + padded(P, 8) + 1024));
+                    padded(P * (kn + 1), 8) + padded(P, 8) + padded(P * kn, 8) + 1024));
   cudaStream_t s = g_ctx.stream;
   double* d1 = g_ctx.take<double>(P * km * nq);
   double* d2 = g_ctx.take<double>(P * kn * nq);
   double* dpe1 = g_ctx.take<double>(P * (km + 1));
   double* dpe2 = g_ctx.take<double>(P * (kn + 1));
   double* dqs = g_ctx.take<double>(P);
+  double* ddp2 = g_ctx.take<double>(P * kn);
+  if (dp2) FV3G_CUDA(cudaMemcpyAsync(ddp2, dp2, sizeof(double) * P * kn, cudaMemcpyHostToDevice, s));
   const int nib = iend - ibeg + 1, njb = jend - jbeg + 1;
   // q1(ibeg:iend, jbeg:jend, km*nq): the (i1:i2, j1:j2) block of every plane
   {
@@ -559,12 +563,15 @@ static int map_common(int km, const double* pe1, const double* q1, const double*
   r.pe1 = dpe1;
   r.pe2 = dpe2;
   r.qs = qs ? dqs : nullptr;
+  r.dp2 = dp2 ? ddp2 : nullptr;
   r.pg = pg;
   r.i1 = i1; r.j1 = j1; r.ni = ni; r.nj = nj;
   r.ncol = ncol;
   r.km = km; r.kn = kn; r.iv = iv; r.q_min = q_min;
   CHECK(launch_remap<double>(r, kord, s));
-  {
+  if (dp2) {  // the 2-D (i1:i2, kn) row of map1_q2
+    FV3G_CUDA(cudaMemcpyAsync(q2, d2, sizeof(double) * P * kn, cudaMemcpyDeviceToHost, s));
+  } else {
     CHECK(copy_planes(q2 + (i1 - ibeg) + (size_t)(j1 - jbeg) * nib, (size_t)nib * 8, (size_t)nib * njb * 8, d2,
                       (size_t)ni * 8, (size_t)ni * nj * 8, (size_t)ni * 8, nj, (long long)kn * nq,
                       cudaMemcpyDeviceToHost, s));
@@ -582,6 +589,15 @@ int fv3g_map_scalar(int km, const double* pe1, const double* q1, const double* q
 int fv3g_map1_ppm(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
                   double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord) {
   return map_common(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, j, ibeg, iend, jbeg, jend, 1, iv, kord, 0.0);
+}
+
+int fv3g_map1_q2(int km, const double* pe1, const double* q1, int kn, const double* pe2, double* q2,
+                 const double* dp2, int i1, int i2, int iv, int kord, int j, int ibeg, int iend, int jbeg, int jend,
+                 double q_min) {
+  if (!dp2) return set_error(FV3G_E_ARG, "null array argument");
+  if (iv == -2) return set_error(FV3G_E_ARG, "map1_q2 takes iv -1..1 (no surface values)");
+  return map_common(km, pe1, q1, nullptr, kn, pe2, q2, i1, i2, j, j, ibeg, iend, jbeg, jend, 1, iv, kord, q_min,
+                    dp2);
 }
 
 int fv3g_map_scalar_3d(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,

@@ -213,8 +213,8 @@ __global__ void __launch_bounds__(128) k_remap_scratch(const RemapArgs<T> a) {
           const Profile<T>& p = prof(Lb);
           mass = mass + (dpb * Xb) * pmean(p.l, p.r, p.s6, T(0), Xb);
         }
-        // target thickness from the FP64 interface pressures
-        const T dpk = T(pe2_at(k2 + 1) - pe2_at(k2));
+        // target thickness from the FP64 interface pressures (or the caller's)
+        const T dpk = a.dp2 ? T(a.dp2[(long long)k2 * nc + col]) : T(pe2_at(k2 + 1) - pe2_at(k2));
         out = mass / dpk;
       }
       q2[k2 * a.sQk] = out;
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(32 * RCOL, sizeof(T) == 4 ? 2 : 1) k_remap_war
 #pragma unroll
   for (int j = 0; j < NPL; ++j) {
     const int t = u0 + j;
-    dpk[j] = (t < kn) ? T(p2v[j + 1] - p2v[j]) : T(1);
+    dpk[j] = (t < kn) ? (a.dp2 ? T(a.dp2[(long long)t * nc + col]) : T(p2v[j + 1] - p2v[j])) : T(1);
     if (real && t < kn && a.dp_out != nullptr) a.dp_out[fo + (long long)t * a.sFk] = dpk[j];
   }
 
@@ -899,6 +899,56 @@ int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s) {
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }
+
+// Interface pressures of the columns of a field kind (0: cells; 1: y faces
+// (i, j) between cells (i, j-1) and (i, j), the u winds; 2: x faces between
+// (i-1, j) and (i, j), the v winds) from the Lagrangian thickness planes dp
+// ([tile][level], halo cells filled for the faces): pe1 = ptop + the running
+// sum of dp (the mean of the two columns beside a face), pe2 = ak + bk ps with
+// the same ps; with log_p both in ln p.  [k][col] layout, col = (t nj + cj) ni
+// + ci over the kind's columns ci < ni, cj < nj.
+template <typename T>
+__global__ void k_field_pressures(const T* dp, long long sFt, long long sFk, PlaneGeom pg, int nt, int km, int ni,
+                                  int nj, int kind, int log_p, const double* ak, const double* bk, double* pe1,
+                                  double* pe2) {
+  const long long nc = (long long)nt * ni * nj;
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= nc) return;
+  const int ci = (int)(col % ni);
+  const long long rest = col / ni;
+  const int cj = (int)(rest % nj), t = (int)(rest / nj);
+  const int i = 1 + ci, j = 1 + cj;
+  const T* da = dp + t * sFt + pg.at(i, j);
+  const T* db = dp + t * sFt + (kind == 1 ? pg.at(i, j - 1) : kind == 2 ? pg.at(i - 1, j) : pg.at(i, j));
+  double pa = ak[0], pb = ak[0];
+  pe1[col] = log_p ? log(pa) : pa;
+  for (int k = 0; k < km; ++k) {
+    pa += (double)da[(long long)k * sFk];
+    pb += (double)db[(long long)k * sFk];
+    const double p = kind == 0 ? pa : 0.5 * (pa + pb);
+    pe1[(long long)(k + 1) * nc + col] = log_p ? log(p) : p;
+  }
+  const double ps = kind == 0 ? pa : 0.5 * (pa + pb);
+  for (int k = 0; k <= km; ++k) {
+    const double p = ak[k] + bk[k] * ps;
+    pe2[(long long)k * nc + col] = log_p ? log(p) : p;
+  }
+}
+
+template <typename T>
+int launch_field_pressures(const T* dp, long long sFt, long long sFk, PlaneGeom pg, int nt, int km, int ni, int nj,
+                           int kind, int log_p, const double* ak, const double* bk, double* pe1, double* pe2,
+                           cudaStream_t s) {
+  const long long nc = (long long)nt * ni * nj;
+  k_field_pressures<T><<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(dp, sFt, sFk, pg, nt, km, ni, nj, kind, log_p, ak,
+                                                                   bk, pe1, pe2);
+  FV3G_CUDA(cudaGetLastError());
+  return 0;
+}
+template int launch_field_pressures<float>(const float*, long long, long long, PlaneGeom, int, int, int, int, int,
+                                           int, const double*, const double*, double*, double*, cudaStream_t);
+template int launch_field_pressures<double>(const double*, long long, long long, PlaneGeom, int, int, int, int, int,
+                                            int, const double*, const double*, double*, double*, cudaStream_t);
 
 // Tangent-linear remap: the thread-per-column kernel on value/tangent pairs
 // (scratch supplied by the caller, remap_scratch_bytes(ncol, 16)).

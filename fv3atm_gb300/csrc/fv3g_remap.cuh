@@ -22,6 +22,7 @@ struct RemapArgs {
   const double* pe1;  // drop-in mode: [k][col] interface pressures (null in batched mode)
   const double* pe2;
   const double* qs;  // [col] surface value for iv == -2 (may be null)
+  const double* dp2;  // [k][col] target thicknesses dividing the overlap masses (map1_q2); null: pe2 differences
   PlaneGeom pg;
   int i1, j1, ni, nj;  // column block: i1..i1+ni-1, j1..j1+nj-1 on every tile
   long long ncol;      // ntiles * ni * nj
@@ -39,5 +40,10 @@ int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s);
 size_t remap_scratch_bytes(long long ncol, size_t elem_bytes);  // scratch + schedule of the scratch kernel
 int prepare_remap_kernels();
 int launch_remap_tl(const RemapArgs<Dual<double>>& a, int kord, cudaStream_t s);
+// interface pressures of the columns of a field kind (cells, u or v faces) for the remap of extra fields
+template <typename T>
+int launch_field_pressures(const T* dp, long long sFt, long long sFk, PlaneGeom pg, int nt, int km, int ni, int nj,
+                           int kind, int log_p, const double* ak, const double* bk, double* pe1, double* pe2,
+                           cudaStream_t s);
 
 }  // namespace fv3g

@@ -188,6 +188,16 @@ int fv3g_map_scalar(int km, const double* pe1, const double* q1, const double* q
                     const double* pe2, double* q2, int i1, int i2, int j, int ibeg, int iend,
                     int jbeg, int jend, int iv, int kord, double q_min);
 
+/* map1_q2 (fv_mapz.F90): the map1_ppm reconstruction of row j of q1 onto the
+ * target interfaces pe2, with the target thicknesses dp2 (i1:i2, kn) given:
+ * a target layer spanning several source layers takes its overlap mass
+ * divided by dp2; q2 is the 2-D row (i1:i2, kn).  q_min: the floor of iv 1.
+ * Replaces: map1_q2(km, pe1, q1, kn, pe2, q2, dp2, i1, i2, iv, kord, j, ibeg,
+ *           iend, jbeg, jend, q_min). */
+int fv3g_map1_q2(int km, const double* pe1, const double* q1, int kn, const double* pe2, double* q2,
+                 const double* dp2, int i1, int i2, int iv, int kord, int j, int ibeg, int iend, int jbeg, int jend,
+                 double q_min);
+
 /* map1_ppm (fv_mapz.F90): as map_scalar without the floor argument.
  * Replaces: map1_ppm(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend,
  *           jbeg, jend, iv, kord). */
@@ -349,6 +359,20 @@ int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream);
 int fv3g_state_nsplt(fv3g_state* st, int* nsplt);
 /* Remap every tracer from the Lagrangian levels of DELP_OUT to ak + bk*ps. */
 int fv3g_remap_batched(fv3g_state* st, void* stream);
+/* The remap of Lagrangian_to_Eulerian for fields beside the tracers (pt and
+ * the winds), from the Lagrangian levels of the last tracer_2d (DELP_OUT) onto
+ * ak + bk ps: nfield fields in device arrays of the state's element type in
+ * the layout of FV3G_FIELD_Q ((ntiles, nfield, npz) planes of nd x nd); only
+ * the kind's columns are read and written.
+ *   kind 0: cell-centred fields (pt with iv 1 and q_min its floor, kord_tm);
+ *     log_p 1 remaps in ln p, as pt is remapped on peln;
+ *   kind 1: u winds on the y faces (i = 1..n, j = 1..n+1), kind 2: v winds on
+ *     the x faces (i = 1..n+1, j = 1..n), each face column's pressures the
+ *     mean of the two cells beside it (iv -1, kord_mt); six-tile cube only.
+ * Replaces: the pt, u and v remaps of Lagrangian_to_Eulerian (fv_mapz.F90:
+ *   map_scalar on peln for pt, map1_ppm with pe0 / pe3 for u and v). */
+int fv3g_state_remap_fields(fv3g_state* st, const void* fields_in, void* fields_out, int nfield, int kind, int iv,
+                            int kord, double q_min, int log_p, void* stream);
 /* Tangent-linear and adjoint of one step (tracer_2d with q_split substeps,
  * then the remap; parts = 1: tracer_2d alone (output on the Lagrangian
  * levels), 2: the remap alone (of the home field on DELP), 3: both) of an

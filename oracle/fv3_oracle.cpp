@@ -756,9 +756,11 @@ template <class T> inline T pmean(const T& l, const T& r, const T& s6, double x1
 }
 
 // Conservative remap of one column (merge of the two sorted interface lists).
+// dp2 (optional): the target thicknesses that divide the overlap masses
+// (map1_q2), else pe2 differences.
 template <class T>
 void remap_column_t(int km, const double* pe1, const T* q1, double qs, int kn, const double* pe2, T* q2,
-                    int iv, int kord, double q_min) {
+                    int iv, int kord, double q_min, const double* dp2 = nullptr) {
   std::vector<double> dp(km);
   for (int k = 0; k < km; ++k) dp[k] = pe1[k + 1] - pe1[k];
   std::vector<T> aL(km), aR(km), a6(km);
@@ -796,7 +798,7 @@ void remap_column_t(int km, const double* pe1, const T* q1, double qs, int kn, c
     } else if (bot > pe1[km]) {  // below the source column: constant extension
       mass = mass + q1[km - 1] * T(bot - pe1[km]);
     }
-    q2[k2] = mass / T(bot - top);
+    q2[k2] = mass / T(dp2 ? dp2[k2] : bot - top);
     k1 = std::min(m, km - 1);
   }
 }
@@ -1213,6 +1215,26 @@ void orc_map_scalar(int km, const double* pe1, const double* q1, const double* q
 void orc_map1_ppm(int km, const double* pe1, const double* q1, const double* qs, int kn, const double* pe2,
                   double* q2, int i1, int i2, int j, int ibeg, int iend, int jbeg, int jend, int iv, int kord) {
   map_row(km, pe1, q1, qs, kn, pe2, q2, i1, i2, j, ibeg, iend, jbeg, jend, iv, kord, 0.0);
+}
+
+// map1_q2 (fv_mapz.F90): the remap of columns with the target thicknesses
+// dp2 (kn, ncol) given for the division of the overlap masses.
+void orc_remap_columns_dp2(int ncol, int km, const double* pe1, const double* q1, const double* qs, int kn,
+                           const double* pe2, const double* dp2, double* q2, int iv, int kord, double q_min) {
+#pragma omp parallel
+  {
+    std::vector<double> p1(km + 1), p2(kn + 1), c1(km), c2(kn), d2(kn);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncol; ++c) {
+      for (int k = 0; k <= km; ++k) p1[k] = pe1[c + (size_t)k * ncol];
+      for (int k = 0; k <= kn; ++k) p2[k] = pe2[c + (size_t)k * ncol];
+      for (int k = 0; k < km; ++k) c1[k] = q1[c + (size_t)k * ncol];
+      for (int k = 0; k < kn; ++k) d2[k] = dp2[c + (size_t)k * ncol];
+      remap_column_t<double>(km, p1.data(), c1.data(), qs ? qs[c] : 0.0, kn, p2.data(), c2.data(), iv, kord, q_min,
+                             d2.data());
+      for (int k = 0; k < kn; ++k) q2[c + (size_t)k * ncol] = c2[k];
+    }
+  }
 }
 
 void orc_remap_columns(int ncol, int km, const double* pe1, const double* q1, const double* qs, int kn,

@@ -276,13 +276,19 @@ def remap_column(pe1, q1, pe2, iv=0, kord=9, qs=0.0, q_min=0.0) -> np.ndarray:
     return q2
 
 
-def remap_columns(pe1, q1, pe2, iv=0, kord=9, qs=None, q_min=0.0) -> np.ndarray:
-    """pe1 (km+1, ncol), q1 (km, ncol), pe2 (kn+1, ncol) -> q2 (kn, ncol)."""
+def remap_columns(pe1, q1, pe2, iv=0, kord=9, qs=None, q_min=0.0, dp2=None) -> np.ndarray:
+    """pe1 (km+1, ncol), q1 (km, ncol), pe2 (kn+1, ncol) -> q2 (kn, ncol); dp2 (kn, ncol): the target
+    thicknesses dividing the overlap masses (map1_q2), else the pe2 differences."""
     pe1, q1, pe2 = _f64(pe1), _f64(q1), _f64(pe2)
     km, ncol = q1.shape
     kn = pe2.shape[0] - 1
     q2 = np.zeros((kn, ncol))
     qsa = _f64(qs) if qs is not None else None
+    if dp2 is not None:
+        d2 = _f64(dp2)
+        lib().orc_remap_columns_dp2(ncol, km, _p(pe1), _p(q1), _p(qsa) if qsa is not None else None, kn, _p(pe2),
+                                    _p(d2), _p(q2), iv, kord, C.c_double(q_min))
+        return q2
     lib().orc_remap_columns(ncol, km, _p(pe1), _p(q1), _p(qsa) if qsa is not None else None, kn, _p(pe2), _p(q2),
                             iv, kord, C.c_double(q_min))
     return q2

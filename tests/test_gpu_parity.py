@@ -900,3 +900,65 @@ def test_state_fillz_conserves_column_mass(cuda):
         assert np.all(np.abs(m1 - m0) <= 1e-12 * np.abs(interior(before[:, iq], n) * dpe).sum(1))
         pos = m0 > 0
         assert np.all(interior(after[:, iq], n).transpose(0, 2, 3, 1)[pos] >= 0.0)
+
+
+@pytest.mark.parametrize("kord,iv", [(9, 0), (9, -1), (4, 1), (4, -1)])
+def test_map1_q2_matches_oracle(cuda, kord, iv):
+    """fv3g_map1_q2: row j of q1 onto pe2 with the target thicknesses dp2 given (2-D output row) equals the
+    oracle's remap with the same dp2."""
+    rng = np.random.default_rng(90 + kord)
+    km, kn, ni, nj, j = 48, 40, 9, 3, 2
+    pe1 = np.zeros((km + 1, ni))
+    pe1[0] = 50.0
+    pe1[1:] = 50.0 + np.cumsum(rng.uniform(300.0, 900.0, (km, ni)), axis=0)
+    pe2 = np.linspace(0.0, 1.0, kn + 1)[:, None] * (pe1[-1] - pe1[0]) + pe1[0]
+    pe2[-1] = pe1[-1]
+    dp2 = np.diff(pe2, axis=0) * rng.uniform(0.97, 1.03, (kn, ni))
+    q1 = rng.uniform(0.2, 1.4, (km, nj, ni))  # Fortran q1(ibeg:iend, jbeg:jend, km)
+    q2 = np.zeros((kn, ni))
+    api.map1_q2(km, pe1, q1, kn, pe2, q2, dp2, 1, ni, iv, kord, j, 1, ni, 1, nj, 0.1 if iv == 1 else 0.0)
+    want = O.remap_columns(pe1, q1[:, j - 1, :], pe2, iv=iv, kord=kord, q_min=0.1 if iv == 1 else 0.0, dp2=dp2)
+    assert rel_l2(q2, want) <= 1e-12
+
+
+@pytest.mark.parametrize("kind,iv,log_p", [(0, 1, False), (0, 1, True), (1, -1, False), (2, -1, False)])
+def test_state_remap_fields_match_oracle(cuda, kind, iv, log_p):
+    """fv3g_state_remap_fields after a tracer_2d: cell fields (pt, optionally in ln p) and u / v winds on the
+    faces (pressures the mean of the two cells beside a face, across tile edges from the neighbouring tiles)
+    equal the oracle's column remap on the same pressures."""
+    import torch
+    P = S.make_problem(24, 10, 2, seed=47, cmax=0.6)
+    st = api.CubeState(24, 10, 2, precision="fp64", kord=9)
+    st.load_problem(P)
+    st.tracer_2d(2)
+    st.sync()
+    n, nd, km = 24, 30, 10
+    dp = torch.as_tensor(st.download("DELP_OUT"))
+    S.fill_cube_halo(dp, n, 3, P.topo)  # the faces' neighbouring columns
+    dp = dp.numpy()
+    rng = np.random.default_rng(48 + kind)
+    f = rng.uniform(250.0, 320.0, (6, 3, km, nd, nd)) if kind == 0 else rng.uniform(-30.0, 30.0, (6, 3, km, nd, nd))
+    fin = torch.as_tensor(f, device="cuda")
+    fout = torch.zeros_like(fin)
+    st.remap_fields(fin.data_ptr(), fout.data_ptr(), 3, kind=kind, iv=iv, kord=9, q_min=1.0, log_p=log_p)
+    torch.cuda.synchronize()
+    got = fout.cpu().numpy()
+    ak, bk = np.asarray(P.ak, np.float64), np.asarray(P.bk, np.float64)
+    ni, nj = (n + 1, n) if kind == 2 else (n, n + 1) if kind == 1 else (n, n)
+    for t in range(6):
+        for (ci, cj) in [(0, 0), (ni - 1, nj - 1), (ni // 2, 3), (1, nj - 2)]:
+            i, jj = 1 + ci + 2, 1 + cj + 2  # array indices (halo 3: tile index 1 is array index 3)
+            pa = ak[0] + np.concatenate([[0.0], np.cumsum(dp[t, :, jj + 0, i + 0])])
+            if kind == 0:
+                p = pa
+            else:
+                ib, jb = (i, jj - 1) if kind == 1 else (i - 1, jj)
+                p = 0.5 * (pa + ak[0] + np.concatenate([[0.0], np.cumsum(dp[t, :, jb, ib])]))
+            p2 = ak + bk * p[-1]
+            if log_p:
+                p, p2 = np.log(p), np.log(p2)
+            for fi in range(3):
+                want = O.remap_columns(p[:, None], f[t, fi, :, jj, i][:, None], p2[:, None], iv=iv, kord=9,
+                                       q_min=1.0)[:, 0]
+                assert rel_l2(got[t, fi, :, jj, i], want) <= 1e-12, (t, ci, cj, fi)
+    st.close()

@@ -260,3 +260,28 @@ def test_map_scalar_row_matches_columns():
     for i in range(1, 8):
         ref = O.remap_column(pe1[:, j, i], q1[:, j, i], pe2[:, j, i], kord=9)
         assert np.array_equal(out[:, j, i], ref)
+
+
+@pytest.mark.parametrize("kord", [4, 9])
+def test_map1_q2_divides_the_overlap_mass_by_dp2(kord):
+    """map1_q2 (dp2 given): with dp2 the pe2 differences it is the plain remap; with dp2 doubled, a target
+    layer spanning several source layers halves (its overlap mass over dp2) and one inside a single source
+    layer keeps its mean."""
+    rng = np.random.default_rng(31)
+    km, kn, ncol = 40, 25, 12
+    pe1 = np.zeros((km + 1, ncol))
+    pe1[0] = 100.0
+    pe1[1:] = 100.0 + np.cumsum(rng.uniform(200.0, 800.0, (km, ncol)), axis=0)
+    pe2 = np.linspace(0.0, 1.0, kn + 1)[:, None] * (pe1[-1] - pe1[0]) + pe1[0]
+    pe2[-1] = pe1[-1]
+    q1 = rng.uniform(0.5, 1.5, (km, ncol))
+    plain = O.remap_columns(pe1, q1, pe2, iv=0, kord=kord)
+    assert np.allclose(O.remap_columns(pe1, q1, pe2, iv=0, kord=kord, dp2=np.diff(pe2, axis=0)), plain, rtol=0,
+                       atol=1e-15)
+    doubled = O.remap_columns(pe1, q1, pe2, iv=0, kord=kord, dp2=2.0 * np.diff(pe2, axis=0))
+    for c in range(ncol):
+        for k2 in range(kn):
+            spans = np.searchsorted(pe1[:, c], pe2[k2, c], side="right") != np.searchsorted(pe1[:, c],
+                                                                                           pe2[k2 + 1, c], side="left")
+            want = 0.5 * plain[k2, c] if spans else plain[k2, c]
+            assert doubled[k2, c] == pytest.approx(want, rel=1e-14), (c, k2)
