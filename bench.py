@@ -670,9 +670,12 @@ def main():
         e2e = {"value": world * units * a.steps / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": ems / a.steps,
                "host_dtype": "f32 (as a 32BIT build of the model holds its tracers)",
-               "path": "fv3g_step_host (per-level inputs, then tracer groups: upload g+1 | advect + remap g | "
-                       "download g-1)",
-               "groups": a.groups if a.groups > 0 else max(1, a.nq // warps),
+               "path": "fv3g_step_host (the first tracer group in level blocks: upload block b+1 | advect block b; "
+                       "later groups: upload g+1 | advect + remap g | download g-1; remap tile by tile with "
+                       "each tile's download)",
+               # the library's default: one group when the first group streams in level blocks (cube, fixed
+               # q_split, at least 16 levels), else groups of one CTA width of tracers
+               "groups": a.groups if a.groups > 0 else (1 if a.q_split > 0 and a.npz >= 16 else max(1, a.nq // warps)),
                "sequential": {"value": world * units * a.steps / (ems_seq / 1e3), "ms_per_step": ems_seq / a.steps,
                               "phases": phase, "link_h2d_gbs_plain_copy": link_h2d,
                               "path": "fv3g_upload_async x6 -> fv3g_step (graph) -> fv3g_download_async"}}

@@ -351,34 +351,44 @@ int download_t(fv3g_state* st, const FieldShape& fs, double* host, cudaStream_t 
 }
 
 // Prologue of tracer_2d: scaled work copies of cx, cy, mfx, mfy and the area
-// fluxes, shared by every tracer.
+// fluxes, shared by every tracer; levels [k0, k0+nk) (nk < 0: every level).
 template <typename T>
-int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s) {
+int prologue_t(fv3g_state* st, int nsplt, cudaStream_t s, int k0 = 0, int nk = -1) {
+  if (nk < 0) nk = st->npz;
+  const long long lo = (long long)k0 * st->plane;  // first level's offset in every per-level field
   if (st->d.trdm > 1e-4 && (std::count(st->del6_set.begin(), st->del6_set.end(), 1) != st->nt || !(st->da_min > 0.0)))
     return set_error(FV3G_E_ARG, "tracer damping (trdm > 1e-4) needs every tile's grid with del6_u, del6_v, da_min");
   // scaled copies of cx, cy, mfx, mfy (read from the inputs, written scaled) and the area fluxes
   const T frac = (nsplt == 1) ? T(1) : T(1.0 / nsplt);
   AreaFluxSrc<T> src;
-  src.cx = (const T*)st->cx;
-  src.cy = (const T*)st->cy;
-  src.mfx = (const T*)st->mfx;
-  src.mfy = (const T*)st->mfy;
+  src.cx = (const T*)st->cx + lo;
+  src.cy = (const T*)st->cy + lo;
+  src.mfx = (const T*)st->mfx + lo;
+  src.mfy = (const T*)st->mfy + lo;
   src.err = st->err;
-  CHECK(launch_area_flux<T>((T*)st->cxs, (T*)st->cys, (T*)st->xfx, (T*)st->yfx, (T*)st->mfxs, (T*)st->mfys,
-                            (const T*)st->dxa, (const T*)st->dya, (const T*)st->dx, (const T*)st->dy,
-                            (const T*)st->sin4, st->plane * st->npz, st->plane, st->plane, st->plane, st->pg, 1,
-                            st->n, 1, st->n, st->nt, st->npz, frac, s, src));
+  CHECK(launch_area_flux<T>((T*)st->cxs + lo, (T*)st->cys + lo, (T*)st->xfx + lo, (T*)st->yfx + lo,
+                            (T*)st->mfxs + lo, (T*)st->mfys + lo, (const T*)st->dxa, (const T*)st->dya,
+                            (const T*)st->dx, (const T*)st->dy, (const T*)st->sin4, st->plane * st->npz, st->plane,
+                            st->plane, st->plane, st->pg, 1, st->n, 1, st->n, st->nt, nk, frac, s, src));
   CHECK(mark(st, K_PROLOGUE, s, 1));
   return 0;
 }
 
 // The substeps of tracer_2d for tracers [g0, g0+ng) (every tracer is
 // advected independently; the layer thicknesses they write are the same).
+// Levels [k0, k0+nk) (nk < 0: every level); the level range needs the cube
+// without edge reconciliation.
 template <typename T>
-int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
+int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s, int k0 = 0, int nk = -1) {
+  if (nk < 0) nk = st->npz;
+  const bool part = nk < st->npz;
+  if (part && (!st->cube || st->eflux != nullptr))
+    return set_error(FV3G_E_ARG, "a level range of the substeps needs the cube without edge reconciliation");
   // a CTA advances one tracer per warp: no wider than the group
   const int warps = std::min(ng, st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10));
-  const long long gofs = (long long)g0 * st->plane * st->npz;  // element offset of the group in a tile
+  // element offset of the group and the first level in a tile
+  const long long gofs = (long long)g0 * st->plane * st->npz + (long long)k0 * st->plane;
+  const long long lo = (long long)k0 * st->plane;  // first level's offset in the per-level fields
   int src = 0, dpi = 0;
   for (int it = 0; it < nsplt; ++it) {
     const int dst = (src == 1) ? 2 : 1;
@@ -386,10 +396,17 @@ int substeps_t(fv3g_state* st, int nsplt, int g0, int ng, cudaStream_t s) {
     AdvArgs<T> a = adv_args<T>(st, src, dst, dpi, dpo);
     a.q_in += gofs;
     a.q_out += gofs;
+    if (part) {
+      a.cx += lo; a.cy += lo; a.xfx += lo; a.yfx += lo; a.mfx += lo; a.mfy += lo;
+      a.dp1 += lo;
+      a.dp2 += lo;
+      a.npz = nk;
+    }
     a.nq = ng;
     a.warps_ring = std::min(a.warps_ring, ng);
     if (st->cube) {
-      CHECK(launch_cube_halo<T>((T*)st->q[src] + gofs, a.sQt, st->plane, ng * st->npz, st->pg, st->n, st->topo, s));
+      CHECK(launch_cube_halo<T>((T*)st->q[src] + gofs, a.sQt, st->plane, ng * nk, st->pg, st->n, st->topo, s, nk,
+                                (long long)st->plane * st->npz));
       CHECK(mark(st, K_HALO, s));
     } else if (src != 0) {  // the prescribed ring of the home buffer, held over the step
       CHECK(launch_copy_halo_ring<T>((T*)st->q[src] + gofs, (const T*)st->q[0] + gofs, st->plane, ng * st->npz,
@@ -558,22 +575,44 @@ int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1, int t0 = 0,
 
 // Copy tracers [g0, g0+ng) of tiles [t0, t1) between a host (ntiles, nq,
 // npz, nd, nd) array of the state's element type and the planes of q[0].
+// Levels [k0, k0+nk) only when nk >= 0 (one copy per tile and tracer).
 int q_group_copy(fv3g_state* st, int g0, int ng, void* host, bool to_host, cudaStream_t s, int max_ctas, int t0 = 0,
-                 int t1 = -1) {
+                 int t1 = -1, int k0 = 0, int nk = -1) {
   const size_t es = st->esz, nd = (size_t)st->nd;
   const size_t hplane = nd * nd * es, dplane = (size_t)st->plane * es;
   if (t1 < 0) t1 = st->nt;
-  for (int t = t0; t < t1; ++t) {
-    const long long p0 = ((long long)t * st->nq + g0) * st->npz;  // first plane of the group in tile t
-    char* dev = (char*)st->q[0] + p0 * dplane;
-    char* h = (char*)host + p0 * hplane;
-    const size_t pitch = (size_t)st->pg.pitch * es;
-    if (to_host)
-      CHECK(copy_planes(h, nd * es, hplane, dev, pitch, dplane, nd * es, nd, (long long)ng * st->npz,
-                        cudaMemcpyDeviceToHost, s, max_ctas));
-    else
-      CHECK(copy_planes(dev, pitch, dplane, h, nd * es, hplane, nd * es, nd, (long long)ng * st->npz,
-                        cudaMemcpyHostToDevice, s, max_ctas));
+  const bool part = nk >= 0 && nk < st->npz;
+  for (int t = t0; t < t1; ++t)
+    for (int r = 0; r < (part ? ng : 1); ++r) {
+      // first plane of the group (or of tracer g0+r's level range) in tile t, and the planes copied
+      const long long p0 = ((long long)t * st->nq + g0 + r) * st->npz + (part ? k0 : 0);
+      const long long np = part ? nk : (long long)ng * st->npz;
+      char* dev = (char*)st->q[0] + p0 * dplane;
+      char* h = (char*)host + p0 * hplane;
+      const size_t pitch = (size_t)st->pg.pitch * es;
+      if (to_host)
+        CHECK(copy_planes(h, nd * es, hplane, dev, pitch, dplane, nd * es, nd, np, cudaMemcpyDeviceToHost, s,
+                          max_ctas));
+      else
+        CHECK(copy_planes(dev, pitch, dplane, h, nd * es, hplane, nd * es, nd, np, cudaMemcpyHostToDevice, s,
+                          max_ctas));
+    }
+  return 0;
+}
+
+// Levels [k0, k0+nk) of every tile of a per-level input field from a host
+// array in the field's layout.
+int level_field_copy(fv3g_state* st, int field, const void* host, cudaStream_t s, int k0, int nk, int max_ctas) {
+  FieldShape fs{};
+  CHECK(field_shape(st, field, fs, true));
+  const size_t es = st->esz;
+  const size_t dpl = (size_t)st->plane * es, hpl = (size_t)fs.ni * fs.nj * es;
+  for (int t = 0; t < st->nt; ++t) {
+    const long long p0 = (long long)t * st->npz + k0;
+    char* dev = (char*)fs.dev + p0 * dpl + ((size_t)fs.joff * st->pg.pitch + fs.ioff) * es;
+    const char* h = (const char*)host + p0 * hpl;
+    CHECK(copy_planes(dev, (size_t)st->pg.pitch * es, dpl, h, (size_t)fs.ni * es, hpl, (size_t)fs.ni * es, fs.nj, nk,
+                      cudaMemcpyHostToDevice, s, max_ctas));
   }
   return 0;
 }
@@ -1534,7 +1573,13 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
   if (!st->levels_set) return set_error(FV3G_E_ARG, "fv3g_state_set_levels has not been called");
   const int warps = st->d.warps_per_cta > 0 ? st->d.warps_per_cta : (st->fp64 ? 5 : 10);
-  int G = groups > 0 ? groups : std::max(1, st->nq / warps);
+  // The first group streams in level blocks (a cube state with a fixed q_split and neither edge reconciliation
+  // nor the mass fixer): each block's per-level inputs and tracers upload, then its prologue and substeps run
+  // while the next block uploads, so the advection starts after one block instead of after every input.
+  // Then one group is the default (measured at C384 L127 x20: 177 ms, two groups 180 ms); else groups of
+  // one CTA width of tracers.
+  const bool stream_lev = st->cube && !st->d.edge_sync && !st->d.mass_fix && q_split > 0 && st->npz >= 16;
+  int G = groups > 0 ? groups : (stream_lev ? 1 : std::max(1, st->nq / warps));
   G = std::min(G, st->nq);
   // The copy streams run at the highest priority: a compute kernel's grid is
   // far larger than the GPU, and without priority the copy kernels' CTAs
@@ -1546,7 +1591,9 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
     if (!st->up) FV3G_CUDA(cudaStreamCreateWithPriority(&st->up, cudaStreamNonBlocking, greatest));
     if (!st->down) FV3G_CUDA(cudaStreamCreateWithPriority(&st->down, cudaStreamNonBlocking, greatest));
   }
-  const size_t need = 2 + (size_t)G * (1 + st->nt);  // start, levels, per group: uploaded, each tile remapped
+  const int NB = stream_lev ? 8 : 0;
+  // start, levels, per group: uploaded, each tile remapped; per level block of the first group: uploaded
+  const size_t need = 2 + (size_t)G * (1 + st->nt) + NB;
   while (st->pev.size() < need + 1) {
     cudaEvent_t e;
     FV3G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1565,32 +1612,65 @@ int fv3g_step_host(fv3g_state* st, int q_split, const void* q_in, const void* de
   constexpr int kCopyCtas = 152;  // one copy CTA per SM beside the compute kernels
   const int lev_fields[] = {FV3G_FIELD_DELP, FV3G_FIELD_CX, FV3G_FIELD_CY, FV3G_FIELD_MFX, FV3G_FIELD_MFY};
   const void* lev_src[] = {delp, cx, cy, mfx, mfy};
-  for (int f = 0; f < 5; ++f) {
-    FieldShape fs{};
-    CHECK(field_shape(st, lev_fields[f], fs, true));
-    CHECK(plane_copy(st, fs, (void*)lev_src[f], false, cudaMemcpyHostToDevice, us));
-  }
-  FV3G_CUDA(cudaEventRecord(ev_lev, us));
-  // q_split 0: the count from the uploaded Courant numbers (the host waits for the per-level uploads)
-  if (q_split == 0) CHECK(resolve_nsplt(st, 0, us, &q_split));
-  st->last_nsplt = q_split;
   auto group = [&](int g, int& g0, int& ng) {
     g0 = (int)((long long)st->nq * g / G);
     ng = (int)((long long)st->nq * (g + 1) / G) - g0;
   };
-  for (int g = 0; g < G; ++g) {
+  auto block = [&](int b, int& k0, int& nk) {
+    k0 = (int)((long long)st->npz * b / NB);
+    nk = (int)((long long)st->npz * (b + 1) / NB) - k0;
+  };
+  cudaEvent_t* ev_block = st->pev.data() + 2 + (size_t)G * (1 + st->nt);
+  if (stream_lev) {
+    int g0, ng;
+    group(0, g0, ng);
+    for (int b = 0; b < NB; ++b) {
+      int k0, nk;
+      block(b, k0, nk);
+      const int ctas = b == 0 ? 0 : kCopyCtas;  // the first block alone at full width
+      for (int f = 0; f < 5; ++f) CHECK(level_field_copy(st, lev_fields[f], lev_src[f], us, k0, nk, ctas));
+      CHECK(q_group_copy(st, g0, ng, (void*)q_in, false, us, ctas, 0, -1, k0, nk));
+      FV3G_CUDA(cudaEventRecord(ev_block[b], us));
+    }
+  } else {
+    for (int f = 0; f < 5; ++f) {
+      FieldShape fs{};
+      CHECK(field_shape(st, lev_fields[f], fs, true));
+      CHECK(plane_copy(st, fs, (void*)lev_src[f], false, cudaMemcpyHostToDevice, us));
+    }
+    FV3G_CUDA(cudaEventRecord(ev_lev, us));
+    // q_split 0: the count from the uploaded Courant numbers (the host waits for the per-level uploads)
+    if (q_split == 0) CHECK(resolve_nsplt(st, 0, us, &q_split));
+  }
+  st->last_nsplt = q_split;
+  for (int g = stream_lev ? 1 : 0; g < G; ++g) {
     int g0, ng;
     group(g, g0, ng);
     CHECK(q_group_copy(st, g0, ng, (void*)q_in, false, us, g == 0 ? 0 : kCopyCtas));
     FV3G_CUDA(cudaEventRecord(st->pev[2 + g], us));
   }
-  FV3G_CUDA(cudaStreamWaitEvent(cs, ev_lev, 0));
-  CHECK(st->fp64 ? prologue_t<double>(st, q_split, cs) : prologue_t<float>(st, q_split, cs));
+  if (stream_lev) {
+    int g0, ng;
+    group(0, g0, ng);
+    for (int b = 0; b < NB; ++b) {
+      int k0, nk;
+      block(b, k0, nk);
+      FV3G_CUDA(cudaStreamWaitEvent(cs, ev_block[b], 0));
+      CHECK(st->fp64 ? prologue_t<double>(st, q_split, cs, k0, nk) : prologue_t<float>(st, q_split, cs, k0, nk));
+      CHECK(st->fp64 ? substeps_t<double>(st, q_split, g0, ng, cs, k0, nk)
+                     : substeps_t<float>(st, q_split, g0, ng, cs, k0, nk));
+    }
+  } else {
+    FV3G_CUDA(cudaStreamWaitEvent(cs, ev_lev, 0));
+    CHECK(st->fp64 ? prologue_t<double>(st, q_split, cs) : prologue_t<float>(st, q_split, cs));
+  }
   for (int g = 0; g < G; ++g) {
     int g0, ng;
     group(g, g0, ng);
-    FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + g], 0));
-    CHECK(st->fp64 ? substeps_t<double>(st, q_split, g0, ng, cs) : substeps_t<float>(st, q_split, g0, ng, cs));
+    if (!(stream_lev && g == 0)) {
+      FV3G_CUDA(cudaStreamWaitEvent(cs, st->pev[2 + g], 0));
+      CHECK(st->fp64 ? substeps_t<double>(st, q_split, g0, ng, cs) : substeps_t<float>(st, q_split, g0, ng, cs));
+    }
     // the remap runs tile by tile, each tile's download starting as soon as it is remapped, so only the
     // last tile of the last group waits for its download at the end; with the mass fixer the group's
     // tiles are remapped first and corrected together, then downloaded

@@ -48,16 +48,18 @@ __device__ __forceinline__ T edge_correction(const AdvArgs<T>& a, int n, int t, 
 // its own storage order into shared memory and the halo strip written in
 // its own, so rows are coalesced and column strips move NG cells per row.
 template <typename T>
-__global__ void __launch_bounds__(256) k_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg,
-                                                   int n, Topo topo) {
+__global__ void __launch_bounds__(256) k_cube_halo(T* q, long long sQt, long long splane, int nplanes, int nlev,
+                                                   long long sQq, PlaneGeom pg, int n, Topo topo) {
   extern __shared__ __align__(16) unsigned char halo_raw[];
   T* strip = reinterpret_cast<T*>(halo_raw);  // [depth][position along the source edge]
   const int e = blockIdx.y, t = blockIdx.z;
   const int nt = topo.nbr[t][e], ne = topo.nedge[t][e], rev = topo.rev[t][e];
   const int cells = NG * n;
   for (int pl = blockIdx.x; pl < nplanes; pl += gridDim.x) {
-    const T* src = q + nt * sQt + pl * splane;
-    T* dst = q + t * sQt + pl * splane;
+    // planes of a tile: nlev levels of each tracer, tracers sQq apart
+    const long long off = (long long)(pl / nlev) * sQq + (long long)(pl % nlev) * splane;
+    const T* src = q + nt * sQt + off;
+    T* dst = q + t * sQt + off;
     for (int c = threadIdx.x; c < cells; c += blockDim.x) {
       int d, sp, i, j;
       if (ne == ES || ne == EN) {  // source rows: positions along i are contiguous
@@ -273,11 +275,11 @@ int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cud
 
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
-                     cudaStream_t s) {
+                     cudaStream_t s, int nlev, long long sQq) {
   const size_t smem = (size_t)NG * n * sizeof(T);
   if (smem > 48 * 1024) return set_error(FV3G_E_ARG, "tile size %d too large for the halo kernel", n);
   dim3 grid((unsigned)std::min(nplanes, 65535), 4, 6);
-  k_cube_halo<T><<<grid, 256, smem, s>>>(q, sQt, splane, nplanes, pg, n, topo);
+  k_cube_halo<T><<<grid, 256, smem, s>>>(q, sQt, splane, nplanes, nlev > 0 ? nlev : nplanes, sQq, pg, n, topo);
   FV3G_CUDA(cudaGetLastError());
   return 0;
 }
@@ -372,7 +374,8 @@ int launch_max_courant(const T* cx, const T* cy, long long sFt, long long sFk, P
 #define FV3G_INST(T)                                                                                          \
   template int launch_substep<T>(const AdvArgs<T>&, int, bool, int, cudaStream_t);                          \
   template int launch_edge_fix<T>(const AdvArgs<T>&, int, cudaStream_t);                                     \
-  template int launch_cube_halo<T>(T*, long long, long long, int, PlaneGeom, int, const Topo&, cudaStream_t);   \
+  template int launch_cube_halo<T>(T*, long long, long long, int, PlaneGeom, int, const Topo&, cudaStream_t, int,  \
+                                   long long);                                                                 \
   template int launch_copy_halo_ring<T>(T*, const T*, long long, int, long long, int, PlaneGeom, int, cudaStream_t);             \
   template int launch_area_flux<T>(T*, T*, T*, T*, T*, T*, const T*, const T*, const T*, const T*, const T*, \
                                    long long, long long, long long, long long, PlaneGeom, int, int, int, int, int, \

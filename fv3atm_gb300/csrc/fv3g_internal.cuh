@@ -241,7 +241,7 @@ int launch_copy_halo_ring(T* dst, const T* src, long long splane, int nplanes, l
 int launch_substep_tl(const AdvArgs<Dual<double>>& a, int hord, cudaStream_t s);
 template <typename T>
 int launch_cube_halo(T* q, long long sQt, long long splane, int nplanes, PlaneGeom pg, int n, const Topo& topo,
-                     cudaStream_t s);
+                     cudaStream_t s, int nlev = 0, long long sQq = 0);  // nlev > 0: planes of nlev levels, sQq apart
 template <typename T>
 int launch_substep(const AdvArgs<T>& a, int hord, bool flux_mode, int warps, cudaStream_t s);
 int launch_substep_pair(const AdvArgs<float>& a, int warps, cudaStream_t s);

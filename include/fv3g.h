@@ -412,10 +412,14 @@ int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32,
 int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, void* stream);
 int fv3g_stream_sync(fv3g_state* st, void* stream);
 /* One tracer_2d + remap step from host arrays to host arrays with the
- * transfers overlapped with the compute: the per-level inputs are uploaded
- * first, then the tracers move in `groups` groups (0: nq / warps_per_cta), and
- * group g is advected and remapped while group g+1 uploads and group g-1
- * downloads.  q_in, q_out: (ntiles, nq, npz, nd, nd); delp, cx, cy, mfx, mfy:
+ * transfers overlapped with the compute: the tracers move in `groups` groups,
+ * and group g is advected and remapped while group g+1 uploads and group g-1
+ * downloads; the remap runs tile by tile, each tile's download starting as
+ * soon as it is remapped.  On the six-tile cube with q_split given, at least
+ * 16 levels, edge_sync 0 and mass_fix 0 the first group's per-level inputs and
+ * tracers stream in 8 level blocks, each block advected as soon as it has
+ * arrived (groups 0: one group there, else nq / warps_per_cta groups after
+ * the per-level inputs).  q_in, q_out: (ntiles, nq, npz, nd, nd); delp, cx, cy, mfx, mfy:
  * the FV3G_FIELD_* shapes; element type float (host_f32 = 1, MIXED states) or
  * double (FP64 states); page-locked host memory for full bandwidth.  With a
  * stream the work is ordered after the stream's prior work and the call

@@ -670,6 +670,29 @@ def test_step_host_pipelined_equals_device_step(cuda, cube_prob, precision, grou
     st.close()
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("groups", [1, 3])
+def test_step_host_level_blocks_equal_device_step(cuda, precision, groups):
+    """With 16 levels or more the first tracer group streams in level blocks (its per-level inputs and tracers
+    upload block by block while the earlier blocks advect): the result is the device step's, bit for bit."""
+    import torch
+    P = S.make_problem(40, 20, 5, seed=13, cmax=0.8)
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    st.load_problem(P)
+    st.step(2)
+    want = st.download("Q_REMAPPED")
+    src = {"Q": P.q, "DELP": P.dp, "CX": P.cx, "CY": P.cy, "MFX": P.mfx, "MFY": P.mfy}
+    host = {k: torch.as_tensor(v).to(dt).contiguous().pin_memory() for k, v in src.items()}
+    out = torch.zeros(st.field_shape("Q_REMAPPED"), dtype=dt).pin_memory()
+    for _ in range(2):
+        out.zero_()
+        st.step_host(2, host["Q"].data_ptr(), {k: h.data_ptr() for k, h in host.items()}, out.data_ptr(),
+                     precision == "mixed", groups)
+        assert np.array_equal(out.numpy().astype(np.float64), want)
+    st.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
 def test_batched_q_split_zero_derives_the_substep_count(cuda, precision, tol):
     """q_split 0 on the batched path (fv_core_nml's default): nsplt = int(1 + max |Courant|) as tracer_2d
