@@ -29,6 +29,7 @@ EXPORTS = (
     "fv3g_tracer_2d_nested", "fv3g_nc_open", "fv3g_nc_close", "fv3g_nc_nvars", "fv3g_nc_var_info", "fv3g_nc_checksum",
     "fv3g_nc_read", "fv3g_state_read_restart", "fv3g_state_write_restart", "fv3g_state_nsplt",
     "fv3g_state_set_tracer_pairs", "fv3g_state_tracer_pairs", "fv3g_state_set_mass_fix", "fv3g_state_step_tl", "fv3g_state_step_ad", "fv3g_map1_q2", "fv3g_state_remap_fields",
+    "fv3g_state_set_remap_form", "fv3g_state_remap_form",
 )
 
 

@@ -308,6 +308,15 @@ class CubeState:
         """Restore each tracer's global mass after every step (True) or leave it as transported (False)."""
         _lib.call("fv3g_state_set_mass_fix", self._h, int(bool(on)))
 
+    def set_remap_form(self, form: int) -> None:
+        """Remap kernel: 0 warp per column (default), 1 thread per column for FP32 kord-9 states of 16+ levels."""
+        _lib.call("fv3g_state_set_remap_form", self._h, int(form))
+
+    def remap_form(self) -> int:
+        f = C.c_int(0)
+        _lib.call("fv3g_state_remap_form", self._h, C.byref(f))
+        return f.value
+
     def tracer_pairs(self) -> bool:
         on = C.c_int(0)
         _lib.call("fv3g_state_tracer_pairs", self._h, C.byref(on))

@@ -16,7 +16,7 @@ FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppres
 # The column remap runs two fields per pass in unrolled copies of the same code; without automatic
 # multiply-add contraction (explicit fmaf stays fused) both copies round alike, so a field's result does not
 # depend on which slot of a pass it took (tracer groups of the pipelined host step remap bit for bit alike).
-FILE_FLAGS = {"fv3g_remap.cu": ["-fmad=false"]}
+FILE_FLAGS = {"fv3g_remap.cu": ["-fmad=false"], "fv3g_remap_col.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:

@@ -130,6 +130,7 @@ struct fv3g_state {
   std::vector<char> del6_set;                    // per tile: its damping metrics were set
   int warps_ring = 0;                            // edge-ring CTA width (0: warps_per_cta), set by autotune
   int pairs = 0;                                 // FP32 hord 8: tracers two per warp (k_substep_pair)
+  int remap_form = 0;                            // 0: warp-per-column remap; 1: thread-per-column FP32 where it applies
   double da_min = 0.0;
   void* eflux = nullptr;
   double* ak = nullptr; double* bk = nullptr;
@@ -557,6 +558,7 @@ int remap_t(fv3g_state* st, cudaStream_t s, int g0 = 0, int ng = -1, int t0 = 0,
   r.km = st->npz; r.kn = st->npz;
   r.iv = st->d.iv;
   r.q_min = st->d.q_min;
+  r.form = st->remap_form;
   const bool whole = t0 == 0 && ntl == st->nt;  // every tile of the tracers: the mass fixer applies here
   if (st->d.mass_fix && whole) CHECK(mass_fix_pre<T>(st, s, g0, ng));
   CHECK(launch_remap<T>(r, st->d.kord, s));
@@ -1266,6 +1268,23 @@ int fv3g_state_set_tracer_pairs(fv3g_state* st, int on) {
 int fv3g_state_tracer_pairs(fv3g_state* st, int* on) {
   if (!st || !on) return set_error(FV3G_E_ARG, "null argument");
   *on = pairs_allowed(st) ? st->pairs : 0;
+  return 0;
+}
+
+int fv3g_state_set_remap_form(fv3g_state* st, int form) {
+  if (!st) return set_error(FV3G_E_ARG, "null state");
+  if (form != 0 && form != 1) return set_error(FV3G_E_ARG, "remap form %d (0: warp per column, 1: thread per column)", form);
+  st->remap_form = form;
+  if (st->gexec) {  // the captured step holds the old kernel
+    cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+  }
+  return 0;
+}
+
+int fv3g_state_remap_form(fv3g_state* st, int* form) {
+  if (!st || !form) return set_error(FV3G_E_ARG, "null argument");
+  *form = st->remap_form;
   return 0;
 }
 

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <mutex>
+#include <type_traits>
 
 #include "fv3g_ff.cuh"
 #include "fv3g_internal.cuh"
@@ -887,6 +888,12 @@ int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s) {
   {
     const int prc = prepare_remap_kernels();
     if (prc) return prc;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    if (a.form == 1 && remap_col_applies(a, kord)) {
+      FV3G_CUDA(launch_remap_col(a, s));
+      return 0;
+    }
   }
   if (a.scratch != nullptr) {
     const unsigned nb = (unsigned)((a.ncol + 127) / 128);

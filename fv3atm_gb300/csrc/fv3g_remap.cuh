@@ -33,11 +33,18 @@ struct RemapArgs {
   // (KMAX+1) * ncol schedule bytes.
   T* scratch;
   unsigned char* sched;
+  // 0: the warp-per-column kernel; 1: the FP32 thread-per-column kernel
+  // wherever it applies (batched kord 9, iv -1..1, at least 16 layers), else
+  // the warp kernel
+  int form;
 };
 
 template <typename T>
 int launch_remap(const RemapArgs<T>& a, int kord, cudaStream_t s);
-size_t remap_scratch_bytes(long long ncol, size_t elem_bytes);  // scratch + schedule of the scratch kernel
+size_t remap_scratch_bytes(long long ncol, size_t elem_bytes);
+// the FP32 thread-per-column kernel of the batched remap (fv3g_remap_col.cu)
+bool remap_col_applies(const RemapArgs<float>& a, int kord);
+cudaError_t launch_remap_col(const RemapArgs<float>& a, cudaStream_t s);  // scratch + schedule of the scratch kernel
 int prepare_remap_kernels();
 int launch_remap_tl(const RemapArgs<Dual<double>>& a, int kord, cudaStream_t s);
 // interface pressures of the columns of a field kind (cells, u or v faces) for the remap of extra fields
