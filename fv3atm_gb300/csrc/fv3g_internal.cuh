@@ -134,12 +134,15 @@ __host__ __device__ __forceinline__ int window_edge_hi(int ie, int npx, int i0, 
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T tabs(T a) { return a < T(0) ? -a : a; }
-// FP32: one min / max instruction, and |x| an operand modifier, where the
-// compare-and-select forms above take two or three dependent instructions;
-// the results differ only for NaN and in the sign of a zero
+// FP32 and FP64: one min / max instruction, and |x| an operand modifier,
+// where the compare-and-select forms above take two or three dependent
+// instructions; the results differ only for NaN and in the sign of a zero
 __device__ __forceinline__ float tmin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float tmax(float a, float b) { return fmaxf(a, b); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
+__device__ __forceinline__ double tmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ double tmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ double tabs(double a) { return fabs(a); }
 // |a| with the sign of b, b == 0 counted positive
 template <typename T> __device__ __forceinline__ T tsign(T a, T b) {
   T m = tabs(a);
