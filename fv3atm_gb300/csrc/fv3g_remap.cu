@@ -2,20 +2,23 @@
 // with the cs_profile reconstruction of fv_mapz.F90, GFDL_atmos_cubed_sphere,
 // absent submodule .gitmodules:1-4).
 //
-// One thread per column; consecutive threads own consecutive i, so every
-// level of every field is read and written as a coalesced row.  Per column,
-// once for all fields:
-//   * the Lagrangian interface pressures pe1 (FP64 running sum of delp) and
-//     the target interfaces pe2 = ak + bk*ps (FP64);
-//   * the overlap schedule: for every target interface, the source layer that
-//     contains it and its fractional position (FP64 differences, stored in T);
-//   * the LU factors of the tridiagonal interface system (they depend on the
-//     layer thicknesses only).
-// Per field: the interface values (kord 9: forward/back substitution of the
-// C1 system; kord 4: the explicit PPM stencil), the kord constraints
-// (fv3g_profile.cuh), and the integration of the sub-grid parabolas over the
-// overlaps.  Column-constant arrays and the interface values live in a
-// scratch buffer laid out [level][column] (coalesced, L2-resident).
+// Two kernels share the schemes of fv3g_profile.cuh:
+//   * k_remap_warp, the batched and drop-in remap: one warp per column, lane l
+//     owning interfaces / layers l*NPL .. l*NPL+NPL-1, the column's constants
+//     (interface pressures, overlap schedule, LU factors of the interface
+//     system) in registers for all its fields, the recurrences as warp scans
+//     (see the comment above the kernel);
+//   * k_remap_scratch, one thread per column with its column arrays in a
+//     caller-owned scratch buffer laid out [level][column], for the
+//     allocation-free entry and the tangent-linear remap.
+// Per column, once for all fields: the Lagrangian interface pressures pe1
+// (FP64 running sum of delp), the target interfaces pe2 = ak + bk*ps (FP64),
+// the overlap schedule (for every target interface the source layer that
+// holds it and its fractional position) and the LU factors of the C1 system.
+// Per field: the interface values (kord 9: forward and back substitution;
+// kord 4: the explicit PPM stencil), the kord constraints, and the
+// integration of the sub-grid parabolas over the overlaps.  The FP32
+// thread-per-column form of the batched remap is fv3g_remap_col.cu.
 #include <algorithm>
 #include <cfloat>
 #include <mutex>
