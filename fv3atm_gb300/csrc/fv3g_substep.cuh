@@ -455,7 +455,9 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
       float fxx_prev = L.xf[r][0] * fr.x;
       float F_prev = (fr.y + fr.x) * L.mx[ro][0];
       if (efw && i0 == 1) a.eflux[efo + iq * (long long)n + (j0 + ro - 1)] = -F_prev;
-#pragma unroll 2
+      // interior CTAs unroll the march fully (the line's rolling state then needs no register moves:
+      // 76 registers against 86); the edge-ring CTAs, at their 128-register cap, by two
+#pragma unroll(EDGES ? 2 : WIN)
       for (int m = 6; m < WIN; ++m) {
         const int f = m - 2;
         const float xcol = lp.xa.x;  // q at window column f-1 of this row
