@@ -340,6 +340,28 @@ struct PairLine {
   }
 };
 
+// One element from global into shared memory by an asynchronous copy (FP32,
+// FP64; other types by a plain load); stage_ld takes it from a plane with its
+// indices clamped into the plane; stage_wait waits for all of the thread's
+// copies.
+template <typename T>
+__device__ __forceinline__ void copy_async(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+  } else {
+    *dst = *src;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void stage_ld(T* dst, const T* base, const PlaneGeom& pg, int i, int j) {
+  i = min(max(i, pg.isd), pg.isd + pg.pitch - 1);
+  j = min(max(j, pg.jsd), pg.jsd + pg.rows - 1);
+  copy_async(dst, base + pg.at(i, j));
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ------------------------------------------------------------ the kernel ---
 // One tracer of one CTA tile through the three stages (see file header).
 template <typename T, int HORD, bool FLUXES, bool EDGES>
@@ -367,11 +389,14 @@ __device__ __forceinline__ void advance_tracer(const AdvArgs<T>& a, SmemLevel<T>
     const int ic = min(max(i0 - 3 + lane, pg.isd), pg.isd + pg.pitch - 1);
     const T* src = base + t * a.sQt + iq * a.sQq + k * a.sQk + (ic - pg.isd);
     const int jhi = pg.jsd + pg.rows - 1;
+    // every row in flight (asynchronous copies wait for nothing in the loop and hold no registers), then
+    // one wait for them all: the corner cells written next must land after the copies
 #pragma unroll 8
     for (int r = 0; r < WIN; ++r) {
       const int jr = min(max(j0 - 3 + r, pg.jsd), jhi);
-      S.q[r][lane] = src[(long long)(jr - pg.jsd) * pg.pitch];
+      copy_async(&S.q[r][lane], src + (long long)(jr - pg.jsd) * pg.pitch);
     }
+    stage_wait();
   };
   load_window(a.q_in);
   if (corner_block) corner_cells(2);
@@ -615,20 +640,6 @@ __device__ __forceinline__ TileCtx tile_of(const AdvArgs<T>& a, const BlockMap& 
 // One element of a plane field (clamped into the plane, as ld_field) into
 // shared memory: FP32 and FP64 values by an asynchronous copy (cp.async, no
 // register round trip, many in flight per thread), other types by a load.
-template <typename T>
-__device__ __forceinline__ void stage_ld(T* dst, const T* base, const PlaneGeom& pg, int i, int j) {
-  i = min(max(i, pg.isd), pg.isd + pg.pitch - 1);
-  j = min(max(j, pg.jsd), pg.jsd + pg.rows - 1);
-  const T* src = base + pg.at(i, j);
-  if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
-  } else {
-    *dst = *src;
-  }
-}
-__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Per-level fields of a CTA tile into shared memory (Courant numbers, area
 // and mass fluxes, 1/ra_x, 1/ra_y, dp ratios; edge metrics for edge CTAs);
