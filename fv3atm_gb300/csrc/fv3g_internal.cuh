@@ -150,6 +150,20 @@ template <typename T> __device__ __forceinline__ T tsign(T a, T b) {
 }
 __device__ __forceinline__ float copysign_t(float a, float b) { return copysignf(a, b); }
 __device__ __forceinline__ double copysign_t(double a, double b) { return copysign(a, b); }
+// One element from global into shared memory by an asynchronous copy (FP32,
+// FP64; other element types by a plain load); stage_wait waits for all of the
+// thread's copies.
+template <typename T>
+__device__ __forceinline__ void copy_async(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
+  } else {
+    *dst = *src;
+  }
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 // three-input min / max (one instruction for f32 on sm_100 and later)
 __device__ __forceinline__ float tmax3(float a, float b, float c) {
   float r;

@@ -340,27 +340,14 @@ struct PairLine {
   }
 };
 
-// One element from global into shared memory by an asynchronous copy (FP32,
-// FP64; other types by a plain load); stage_ld takes it from a plane with its
-// indices clamped into the plane; stage_wait waits for all of the thread's
-// copies.
-template <typename T>
-__device__ __forceinline__ void copy_async(T* dst, const T* src) {
-  if constexpr (sizeof(T) == 4 || sizeof(T) == 8) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src));
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src));
-  } else {
-    *dst = *src;
-  }
-}
+// One element of a plane, its indices clamped into the plane, into shared
+// memory by an asynchronous copy (copy_async).
 template <typename T>
 __device__ __forceinline__ void stage_ld(T* dst, const T* base, const PlaneGeom& pg, int i, int j) {
   i = min(max(i, pg.isd), pg.isd + pg.pitch - 1);
   j = min(max(j, pg.jsd), pg.jsd + pg.rows - 1);
   copy_async(dst, base + pg.at(i, j));
 }
-__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // ------------------------------------------------------------ the kernel ---
 // One tracer of one CTA tile through the three stages (see file header).
