@@ -144,6 +144,7 @@ struct fv3g_state {
   cudaStream_t stream = nullptr;
   cudaStream_t up = nullptr, down = nullptr;  // fv3g_step_host: upload and download streams
   std::vector<cudaEvent_t> pev;               // fv3g_step_host: its events
+  cudaEvent_t xev = nullptr;                  // orders copies on a caller's stream with the state's stream
   int q_cur = 0;      // buffer holding the latest tracer field
   int dp_start = 0;   // buffer holding dp at the start of the last substep
   int dp_end = 0;     // buffer holding dp at the end of the last substep
@@ -906,6 +907,7 @@ int fv3g_state_destroy(fv3g_state* st) {
   if (st->gexec) cudaGraphExecDestroy(st->gexec);
   for (cudaEvent_t e : st->ev) cudaEventDestroy(e);
   for (cudaEvent_t e : st->pev) cudaEventDestroy(e);
+  if (st->xev) cudaEventDestroy(st->xev);
   if (st->up) cudaStreamDestroy(st->up);
   if (st->down) cudaStreamDestroy(st->down);
   for (void* p : st->allocs) cudaFree(p);
@@ -983,12 +985,32 @@ int fv3g_download(fv3g_state* st, int field, double* host) {
   return st->fp64 ? download_t<double>(st, fs, host, st->stream) : download_t<float>(st, fs, host, st->stream);
 }
 
+// A copy on a caller's stream s other than the state's: after the work already
+// queued on the state's stream (which may still read or write the field) and
+// before the work queued there after it (which reads the uploaded field or
+// overwrites the downloaded one).
+static int xfer_begin(fv3g_state* st, cudaStream_t s) {
+  if (s == st->stream) return 0;
+  if (!st->xev) FV3G_CUDA(cudaEventCreateWithFlags(&st->xev, cudaEventDisableTiming));
+  FV3G_CUDA(cudaEventRecord(st->xev, st->stream));
+  FV3G_CUDA(cudaStreamWaitEvent(s, st->xev, 0));
+  return 0;
+}
+static int xfer_end(fv3g_state* st, cudaStream_t s) {
+  if (s == st->stream) return 0;
+  FV3G_CUDA(cudaEventRecord(st->xev, s));
+  FV3G_CUDA(cudaStreamWaitEvent(st->stream, st->xev, 0));
+  return 0;
+}
+
 int fv3g_upload_device(fv3g_state* st, int field, const void* dptr, void* stream) {
   if (!st || !dptr) return set_error(FV3G_E_ARG, "null argument");
   FieldShape fs{};
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CHECK(xfer_begin(st, s));
   CHECK(plane_copy(st, fs, const_cast<void*>(dptr), false, cudaMemcpyDeviceToDevice, s));
+  CHECK(xfer_end(st, s));
   if (field == FV3G_FIELD_Q) {
     st->q_cur = 0;
     st->remapped = false;
@@ -1001,7 +1023,9 @@ int fv3g_download_device(fv3g_state* st, int field, void* dptr, void* stream) {
   FieldShape fs{};
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CHECK(xfer_begin(st, s));
   CHECK(plane_copy(st, fs, dptr, true, cudaMemcpyDeviceToDevice, s));
+  CHECK(xfer_end(st, s));
   return 0;
 }
 
@@ -1556,13 +1580,14 @@ int fv3g_upload_async(fv3g_state* st, int field, const void* host, int host_f32,
   FieldShape fs{};
   CHECK(field_shape(st, field, fs, true));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  if ((host_f32 != 0) != !st->fp64 && host_f32) return set_error(FV3G_E_UNSUPPORTED, "FP32 host data into an FP64 state");
+  CHECK(xfer_begin(st, s));
   if ((host_f32 != 0) == !st->fp64) {  // same element type: one pitched copy
     CHECK(plane_copy(st, fs, (void*)host, false, cudaMemcpyHostToDevice, s));
-  } else if (!host_f32) {
-    CHECK(upload_t<float>(st, fs, (const double*)host, s));
   } else {
-    return set_error(FV3G_E_UNSUPPORTED, "FP32 host data into an FP64 state");
+    CHECK(upload_t<float>(st, fs, (const double*)host, s));
   }
+  CHECK(xfer_end(st, s));
   if (field == FV3G_FIELD_Q) {
     st->q_cur = 0;
     st->remapped = false;
@@ -1576,7 +1601,9 @@ int fv3g_download_async(fv3g_state* st, int field, void* host, int host_f32, voi
   CHECK(field_shape(st, field, fs, false));
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   if ((host_f32 != 0) != !st->fp64) return set_error(FV3G_E_UNSUPPORTED, "host type must match the state precision");
+  CHECK(xfer_begin(st, s));
   CHECK(plane_copy(st, fs, host, true, cudaMemcpyDeviceToHost, s));
+  CHECK(xfer_end(st, s));
   return 0;
 }
 

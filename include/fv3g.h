@@ -343,7 +343,10 @@ int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk); /
 /* Host <-> device copies (FP64 host data; converted to FP32 in MIXED mode).
  * Every `stream` argument of this header: NULL selects the state's own
  * (non-blocking) stream; any other handle is used as given, including
- * cudaStreamLegacy ((void*)1) for the legacy default stream. */
+ * cudaStreamLegacy ((void*)1) for the legacy default stream.  A copy
+ * (fv3g_upload_device / _download_device / _upload_async / _download_async)
+ * on a stream other than the state's is ordered after the work already
+ * queued on the state's stream and before the work queued there after it. */
 int fv3g_upload(fv3g_state* st, int field, const double* host);
 int fv3g_download(fv3g_state* st, int field, double* host);
 /* Raw device copies with the state's storage type (float in MIXED). */
