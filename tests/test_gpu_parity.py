@@ -797,6 +797,35 @@ def test_device_upload_after_conversion_on_default_stream(cuda):
         assert float(torch.linalg.vector_norm(b - a) / torch.linalg.vector_norm(a)) <= MIXED_TOL, iq
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_upload_on_a_delayed_stream_is_ordered_before_the_state_work(cuda, precision):
+    """An upload on another stream, held back there by a bounded spin, is still read by the state's next
+    step on its own stream: the step runs after the copy.  The transport is homogeneous in q and doubling
+    is exact, so uploading 2 q must give exactly twice the step of q (the step of the old q if unordered)."""
+    import torch
+    P = S.make_problem(30, 5, 2, seed=31, cmax=0.8)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    st = api.CubeState(P.n, P.npz, P.nq, precision=precision)
+    try:
+        st.load_problem(P)
+        st.tracer_2d(2)
+        ref = st.download("Q")
+        st.upload("Q", P.q.numpy())
+        q2 = (2 * torch.as_tensor(P.q.numpy())).to(dt).cuda().contiguous()
+        side = torch.cuda.Stream()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            torch.cuda._sleep(20_000_000)  # a bounded spin of ~10 ms ahead of the copy on that stream
+        st.upload_device("Q", q2.data_ptr(), stream=side.cuda_stream)
+        st.tracer_2d(2)
+        got = st.download("Q")
+        torch.cuda.synchronize()
+        s = slice(3, 3 + P.n)
+        assert np.array_equal(got[..., s, s], 2 * ref[..., s, s])
+    finally:
+        st.close()
+
+
 # ------------------------------------------------------- committed fixtures
 def test_cube_matches_committed_golden_fixture(cuda):
     from .test_golden import load_cube
