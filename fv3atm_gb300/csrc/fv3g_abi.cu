@@ -985,19 +985,27 @@ int fv3g_download(fv3g_state* st, int field, double* host) {
   return st->fp64 ? download_t<double>(st, fs, host, st->stream) : download_t<float>(st, fs, host, st->stream);
 }
 
-// A copy on a caller's stream s other than the state's: after the work already
-// queued on the state's stream (which may still read or write the field) and
-// before the work queued there after it (which reads the uploaded field or
-// overwrites the downloaded one).
+// Work on a caller's stream s other than the state's (a copy, a step, a mass
+// sum): after the work already queued on the state's stream (which may still
+// read or write the same fields) and before the work queued there after it.
+// A stream under capture is left to whoever builds the graph.
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus c = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &c) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return c != cudaStreamCaptureStatusNone;
+}
 static int xfer_begin(fv3g_state* st, cudaStream_t s) {
-  if (s == st->stream) return 0;
+  if (s == st->stream || capturing(s)) return 0;
   if (!st->xev) FV3G_CUDA(cudaEventCreateWithFlags(&st->xev, cudaEventDisableTiming));
   FV3G_CUDA(cudaEventRecord(st->xev, st->stream));
   FV3G_CUDA(cudaStreamWaitEvent(s, st->xev, 0));
   return 0;
 }
 static int xfer_end(fv3g_state* st, cudaStream_t s) {
-  if (s == st->stream) return 0;
+  if (s == st->stream || capturing(s)) return 0;
   FV3G_CUDA(cudaEventRecord(st->xev, s));
   FV3G_CUDA(cudaStreamWaitEvent(st->stream, st->xev, 0));
   return 0;
@@ -1047,10 +1055,12 @@ int fv3g_field_info(fv3g_state* st, int field, void** dptr, long long* strides4,
 int fv3g_tracer_2d_batched(fv3g_state* st, int q_split, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CHECK(xfer_begin(st, s));
   int nsplt = q_split;
   CHECK(resolve_nsplt(st, q_split, s, &nsplt));
   st->last_nsplt = nsplt;
-  return st->fp64 ? tracer_2d_t<double>(st, nsplt, s) : tracer_2d_t<float>(st, nsplt, s);
+  CHECK(st->fp64 ? tracer_2d_t<double>(st, nsplt, s) : tracer_2d_t<float>(st, nsplt, s));
+  return xfer_end(st, s);
 }
 
 int fv3g_state_step_tl(fv3g_state* st, int q_split, int parts, const double* dq_in, double* dq_out, void* stream) {
@@ -1425,10 +1435,12 @@ int fv3g_ensemble_step(fv3g_ensemble* e, int q_split, void* stream) {
     e->g_qsplit = q_split;
   }
   cudaStream_t s = stream ? (cudaStream_t)stream : e->ms[0];
+  for (fv3g_state* st : e->m) CHECK(xfer_begin(st, s));
   FV3G_CUDA(cudaGraphLaunch(e->gexec, s));
   for (fv3g_state* st : e->m) {
     st->q_cur = 0;
     st->remapped = true;
+    CHECK(xfer_end(st, s));
   }
   return 0;
 }
@@ -1441,22 +1453,28 @@ int fv3g_fillz_batched(fv3g_state* st, void* stream) {
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
   const long long sQk = st->plane, sQq = st->plane * st->npz, sQt = sQq * st->nq;
   const long long sFk = st->plane, sFt = st->plane * st->npz;
+  CHECK(xfer_begin(st, s));
   if (st->fp64)
-    return launch_fillz_planes<double>((double*)st->q[0], (const double*)st->dp_eul, st->n, st->nt, st->npz, st->nq,
-                                       sQt, sQq, sQk, sFt, sFk, st->pg, s);
-  return launch_fillz_planes<float>((float*)st->q[0], (const float*)st->dp_eul, st->n, st->nt, st->npz, st->nq, sQt,
-                                    sQq, sQk, sFt, sFk, st->pg, s);
+    CHECK(launch_fillz_planes<double>((double*)st->q[0], (const double*)st->dp_eul, st->n, st->nt, st->npz, st->nq,
+                                      sQt, sQq, sQk, sFt, sFk, st->pg, s));
+  else
+    CHECK(launch_fillz_planes<float>((float*)st->q[0], (const float*)st->dp_eul, st->n, st->nt, st->npz, st->nq,
+                                     sQt, sQq, sQk, sFt, sFk, st->pg, s));
+  return xfer_end(st, s);
 }
 
 int fv3g_remap_batched(fv3g_state* st, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
-  return st->fp64 ? remap_t<double>(st, s) : remap_t<float>(st, s);
+  CHECK(xfer_begin(st, s));
+  CHECK(st->fp64 ? remap_t<double>(st, s) : remap_t<float>(st, s));
+  return xfer_end(st, s);
 }
 
 int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
   if (!st) return set_error(FV3G_E_ARG, "null state");
   cudaStream_t s = stream ? (cudaStream_t)stream : st->stream;
+  CHECK(xfer_begin(st, s));
   if (q_split == 0) {  // the count first (one read of the Courant maximum), then the step for that count
     CHECK(resolve_nsplt(st, 0, s, &q_split));
   }
@@ -1493,7 +1511,7 @@ int fv3g_step(fv3g_state* st, int q_split, int use_graph, void* stream) {
   st->q_cur = 0;
   st->remapped = true;
   st->last_nsplt = q_split;
-  return 0;
+  return xfer_end(st, s);
 }
 
 int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream) {
@@ -1526,8 +1544,10 @@ int fv3g_mass_sum(fv3g_state* st, int which, double* host_out, void* stream) {
     m.partials = st->partials;
     return launch_mass<T>(m, st->nq, st->mass_out, s);
   };
+  CHECK(xfer_begin(st, s));
   int rc = st->fp64 ? run(double{}) : run(float{});
   if (rc) return rc;
+  CHECK(xfer_end(st, s));
   FV3G_CUDA(cudaMemcpyAsync(host_out, st->mass_out, sizeof(double) * st->nq, cudaMemcpyDeviceToHost, s));
   FV3G_CUDA(cudaStreamSynchronize(s));
   return 0;

@@ -343,10 +343,11 @@ int fv3g_state_set_levels(fv3g_state* st, const double* ak, const double* bk); /
 /* Host <-> device copies (FP64 host data; converted to FP32 in MIXED mode).
  * Every `stream` argument of this header: NULL selects the state's own
  * (non-blocking) stream; any other handle is used as given, including
- * cudaStreamLegacy ((void*)1) for the legacy default stream.  A copy
- * (fv3g_upload_device / _download_device / _upload_async / _download_async)
- * on a stream other than the state's is ordered after the work already
- * queued on the state's stream and before the work queued there after it. */
+ * cudaStreamLegacy ((void*)1) for the legacy default stream.  Work on a
+ * stream other than the state's (copies, steps, remaps, mass sums, the
+ * ensemble step) is ordered after the work already queued on the state's
+ * stream and before the work queued there after it; a stream under capture
+ * is left to the caller that builds the graph. */
 int fv3g_upload(fv3g_state* st, int field, const double* host);
 int fv3g_download(fv3g_state* st, int field, double* host);
 /* Raw device copies with the state's storage type (float in MIXED). */
